@@ -1,0 +1,348 @@
+"""Benchmark of the CQBEM Laplace-domain assembly on GB300.
+
+Workload (default): the mixed-size object set -- 24 objects, icospheres with 162/642/2562 vertices
+drawn with probabilities 0.5/0.35/0.15, scaled to seeded ellipsoids (axes 0.5-2 x 0.1 m), E
+log-uniform in [1e4, 1e6] Pa, nu uniform in [0.2, 0.45], rho 1000, dt = 1/200, BDF2, N in {16, 32}
+(L = N + 1, L/2 + 1 Laplace frequencies), collocation with the 7-point rule.  Synthetic and seeded;
+the reference publishes no dataset or numbers for this path.
+
+One step = every Laplace-domain matrix (G, H, B_trans, B_angular at every frequency) of every
+object.  Metric: complex matrix entries per second, counted as sum over objects of
+(L/2+1) * (2 (3V)^2 + 12 * 3V).
+
+  value : device-resident path -- one multi-frequency launch per (object, kind), outputs complex64
+          kept in HBM; CUDA-event time summed over K steps, L2 flushed between steps.
+  e2e   : the plain drop-in through the C ABI with host buffers -- one call per (object, kind,
+          frequency) into a pinned host buffer in the reference layout (complex128), i.e. the
+          frequency loop of compute_G_matrices with its device-to-host copy, timed end to end.
+  --impl reference : the reference's CPU algorithm (the oracle's reference-mixed restatement,
+          OpenMP on all host cores) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# algorithmic FP32 flops per kernel evaluation (field point x quadrature point x frequency),
+# regular collocation pass: geometry + two complex exponentials + kernel combination
+FLOPS_PER_EVAL = {"G": 130, "H": 240, "B_trans": 60, "B_angular": 150}
+KINDS = ("G", "H", "B_trans", "B_angular")
+
+
+def make_workload(seed: int = 2024, n_objects: int = 24):
+    from surfaceonlydeformables_gb300.meshes import Material, make_icosphere_mesh
+
+    rng = np.random.default_rng(seed)
+    objs = []
+    for k in range(n_objects):
+        level = int(rng.choice([2, 3, 4], p=[0.5, 0.35, 0.15]))
+        axes = rng.uniform(0.5, 2.0, size=3)
+        E = float(np.exp(rng.uniform(np.log(1e4), np.log(1e6))))
+        nu = float(rng.uniform(0.2, 0.45))
+        N = int(rng.choice([16, 32]))
+        mesh = make_icosphere_mesh(level, 0.1, axes=axes, seed=seed + k)
+        objs.append(dict(mesh=mesh, mat=Material(E, nu, 1000.0), N=N, dt=1.0 / 200.0, bdf=2, order=5, subdiv=1))
+    return objs
+
+
+def entries(nV: int, nfreq: int) -> int:
+    return nfreq * (2 * (3 * nV) ** 2 + 12 * 3 * nV)
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measure_fp32_peak(torch, dev) -> float:
+    """cuBLAS SGEMM with TF32 disabled (FP32 CUDA-core pipes), best of 5, TFLOP/s."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device=dev, dtype=torch.float32)
+    b = torch.randn(n, n, device=dev, dtype=torch.float32)
+    for _ in range(2):
+        torch.mm(a, b)
+    best = 0.0
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.mm(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def cpu_sample(objs, threads: int, nfreq: int = 2):
+    """Reference CPU path (oracle, reference-mixed precision) on one 642-vertex object."""
+    from oracle import oracle as O
+
+    O.build()
+    cores = O.set_threads(threads)
+    obj = next((o for o in objs if o["mesh"].nV == 642), objs[0])
+    m, mat = obj["mesh"], obj["mat"]
+    s, R, L = O.cq_frequencies(obj["bdf"], obj["dt"], obj["N"])
+    t0 = time.perf_counter()
+    for kind in KINDS:
+        for sl in s[:nfreq]:
+            O.collocation(kind, m, mat, sl, order=obj["order"], subdiv=obj["subdiv"], mode=O.MIXED)
+    dt = time.perf_counter() - t0
+    ent = entries(m.nV, nfreq)
+    return ent / dt, dt, cores, f"1 object (nV={m.nV}), 4 kinds, {nfreq} of {len(s)} frequencies, all rows"
+
+
+def run_reference(args):
+    objs = make_workload()
+    threads = os.cpu_count() or 1
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    rates = []
+    for it in range(args.warmup + args.steps):
+        r, dt, cores, sample = cpu_sample(objs, threads, nfreq=1)
+        if it >= args.warmup:
+            rates.append((r, dt))
+    value = float(np.mean([r for r, _ in rates]))
+    ms = float(np.mean([d for _, d in rates]) * 1e3)
+    line = {"metric": "CQBEM Laplace-domain entries/s (mixed-size 24-object set)", "value": value,
+            "unit": "entries/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32+fp64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "mixed-size 24-object collocation set (sampled on CPU)", "objects": 24},
+            "cpu_baseline": {"value": value, "unit": "entries/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "entries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from surfaceonlydeformables_gb300 import build as B
+
+    B.build()
+    objs = make_workload()
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    ctx = api.Context(local, stream=stream)
+    meshes = [api.Mesh(ctx, o["mesh"]) for o in objs]
+    freqs = []
+    for o in objs:
+        s, R, Lq = L.cq_frequencies(o["bdf"], o["dt"], o["N"])
+        o["s"], o["R"], o["L"] = s, R, Lq
+    total_entries = sum(entries(o["mesh"].nV, len(o["s"])) for o in objs)
+    # device outputs, complex64, one buffer per (object, kind)
+    outs = []
+    for o, m in zip(objs, meshes):
+        nf = len(o["s"])
+        per = {}
+        for kind in KINDS:
+            shape = (nf,) + api.out_shape(L.KINDS[kind], m.nV)
+            per[kind] = torch.empty(shape, dtype=torch.complex64, device=dev)
+        outs.append(per)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        for o, m, per in zip(objs, meshes, outs):
+            for kind in KINDS:
+                api.assemble_frequencies(ctx, m, kind, o["mat"], o["s"], order=o["order"], subdiv=o["subdiv"],
+                                         out=per[kind], dtype=L.C64)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launches
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()  # evict L2 between steps (untimed)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+    launches = ctx.launches - launches0
+    torch.cuda.synchronize()
+    t_local = float(sum(times))
+    t = torch.tensor([t_local], device=dev)
+    if dist:
+        dist.barrier()
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    t_max = float(t.item())
+    value = world * total_entries * args.steps / t_max
+
+    # ---- end to end: plain per-frequency drop-in with pinned host buffers (reference layout) ----
+    big = max(m.nV for m in meshes)
+    host = torch.empty((3 * big, 3 * big), dtype=torch.complex128, pin_memory=True)
+    e2e_steps = max(1, args.steps // 2)
+
+    def e2e_step():
+        d2h = 0
+        for o, m in zip(objs, meshes):
+            for kind in KINDS:
+                shape = api.out_shape(L.KINDS[kind], m.nV)
+                buf = host.view(-1)[: shape[0] * shape[1]].view(shape).numpy()
+                for sl in o["s"]:
+                    api.assemble(ctx, m, kind, o["mat"], sl, order=o["order"], subdiv=o["subdiv"], out=buf,
+                                 dtype=L.C128)
+                    d2h += buf.nbytes
+        return d2h
+
+    e2e_value, d2h_bytes = None, 0
+    if not args.no_e2e:
+        e2e_step()  # warm the staging buffers
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            d2h_bytes = e2e_step()
+        torch.cuda.synchronize()
+        e2e_t = time.perf_counter() - t0
+        e2e_value = world * total_entries * e2e_steps / e2e_t
+    h2d_bytes = sum(16 * len(o["s"]) + 64 for o in objs) * 4  # per-call frequency constants
+
+    # ---- roofline of the dominant kernel: regular (FP32) H scatter on the largest object ----
+    peak_fp32 = measure_fp32_peak(torch, dev)
+    iL = int(np.argmax([m.nV for m in meshes]))
+    o, m = objs[iL], meshes[iL]
+    rows = {}
+    for kind in KINDS:
+        for part, pname in ((L.PART_REGULAR, "regular"), (L.PART_SINGULAR, "singular")):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = 3
+            e0.record(stream)
+            for _ in range(reps):
+                api.assemble_frequencies(ctx, m, kind, o["mat"], o["s"], order=o["order"], subdiv=o["subdiv"],
+                                         parts=part, out=outs[iL][kind], dtype=L.C64)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            rows[(kind, pname)] = e0.elapsed_time(e1) * 1e-3 / reps
+    dom = max(rows, key=rows.get)
+    nq = 7
+    evals = (m.nV * m.nF - 3 * m.nF) * nq * len(o["s"])
+    kind_dom = "H"
+    flops = evals * FLOPS_PER_EVAL[kind_dom]
+    achieved = flops / rows[(kind_dom, "regular")] / 1e12
+    roofline = {"bound": "fp32", "kernel": f"coll_scatter_kernel<H> (nV={m.nV}, {len(o['s'])} frequencies)",
+                "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s", "frac": achieved / peak_fp32,
+                "peak_source": "measured live: cuBLAS SGEMM 8192^3, TF32 off", "traffic": None,
+                "flops_per_eval": FLOPS_PER_EVAL[kind_dom], "evals_per_launch": evals,
+                "launch_ms": rows[(kind_dom, "regular")] * 1e3,
+                "dominant": f"{dom[0]}/{dom[1]}", "pass_ms": {f"{k}/{p}": v * 1e3 for (k, p), v in rows.items()}}
+
+    # ---- CPU baseline (rank 0, N = 1 only) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        r, dtc, cores, sample = cpu_sample(objs, os.cpu_count() or 1)
+        cpu = {"value": r, "unit": "entries/s", "cores": cores, "kind": "port", "sample": sample,
+               "seconds": dtc}
+    if rank == 0:
+        line = {"metric": "CQBEM Laplace-domain entries/s (mixed-size 24-object set)", "value": value,
+                "unit": "entries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic",
+                "config": {"workload": "mixed-size 24-object collocation assembly (G,H,B_trans,B_angular, all "
+                                       "Laplace frequencies)", "objects": len(objs),
+                           "vertices": [m.nV for m in meshes], "frequencies": [len(o["s"]) for o in objs],
+                           "entries_per_step": total_entries, "quadrature": "7-point (order 5), singular 5x5 FP64",
+                           "l2": "L2 flushed (256 MB write) between timed steps; outputs (~"
+                                 f"{total_entries * 8 / 1e9:.0f} GB complex64) exceed L2",
+                           "parallelism": f"replicas x{world}"},
+                "roofline": roofline, "cpu_baseline": cpu,
+                "e2e": {"value": e2e_value, "unit": "entries/s", "h2d_bytes_per_step": h2d_bytes,
+                        "d2h_bytes_per_step": d2h_bytes, "path": "sod_cqbem_assemble per (object, kind, "
+                        "frequency) into pinned host memory, complex128 reference layout", "steps": e2e_steps},
+                "gpu_launches": int(launches), "clocks": clk.summary()}
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,137 @@
+/*
+ * sod_gb300.h -- C ABI of the GB300 (sm_103a) CQBEM precomputation library.
+ *
+ * Drop-in replacement for the BEM precomputation hot path of SurfaceOnlyDeformables:
+ * Laplace-domain assembly of the elastodynamic CQBEM matrices G (single layer U), H (double
+ * layer P), B_trans and B_angular by collocation or Galerkin quadrature, the FP64-accurate
+ * inverse transform to convolution-quadrature time weights, the elastostatic Kelvin matrices
+ * and the per-step history convolution.
+ *
+ * Conventions shared by every entry point
+ *   - plain pointers and sizes; no C++ or framework types cross this boundary;
+ *   - row-major layouts identical to the reference's Eigen row-major types
+ *     (include/type_declaration.hpp:16-49 of the reference):
+ *       V  double[nV][3]   vertex positions (already centred by the caller)
+ *       F  int32 [nF][3]   triangle vertex indices, outward orientation
+ *       N  double[nF][3]   unit face normals (NULL: computed from V, F)
+ *       U, P              [3nV][3nV] complex (interleaved re, im)
+ *       B_trans           [3nV][3]   complex
+ *       B_angular         [3nV][3][3] complex ([row][j][k], the reference's ind_3d order)
+ *   - output buffers are caller-owned and FULLY overwritten (there is no accumulate-into
+ *     contract, unlike the reference's Galerkin kernels which add into a zeroed buffer);
+ *   - a pointer may be host or device memory; the library detects which
+ *     (cudaPointerGetAttributes) and copies host data through its own device buffers;
+ *   - every call returns an int status (SOD_OK = 0); nothing prints, exits or aborts;
+ *     sod_last_error() returns a thread-local message for the last failure;
+ *   - results do not depend on thread count, launch configuration or batch composition:
+ *     all reductions run in a fixed order (no floating-point atomics).
+ *
+ * The library needs an sm_103a GPU; without one every compute call returns
+ * SOD_ERR_NO_DEVICE.  There is no CPU fallback.
+ */
+#ifndef SOD_GB300_H
+#define SOD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------- */
+enum sod_status {
+    SOD_OK = 0,
+    SOD_ERR_INVALID_ARG = 1, /* bad size, order, kind, null pointer, degenerate input   */
+    SOD_ERR_OOM = 2,         /* device or pinned-host allocation failed                 */
+    SOD_ERR_CUDA = 3,        /* a CUDA runtime call failed                              */
+    SOD_ERR_NO_DEVICE = 4,   /* no usable sm_103a device                                */
+    SOD_ERR_TIMEOUT = 5,     /* a bounded device-side wait expired                      */
+    SOD_ERR_UNSUPPORTED = 6, /* valid request outside the implemented envelope          */
+    SOD_ERR_CAPACITY = 7     /* request exceeds an admission / footprint cap            */
+};
+
+/* ---- enumerations --------------------------------------------------------------------- */
+enum sod_kind { SOD_G = 0, SOD_H = 1, SOD_B_TRANS = 2, SOD_B_ANGULAR = 3 };
+enum sod_method { SOD_COLLOCATION = 0, SOD_GALERKIN = 1 };
+enum sod_dtype { SOD_C128 = 0, SOD_C64 = 1, SOD_F64 = 2, SOD_F32 = 3, SOD_BF16 = 4 };
+/* parts of an assembly to compute (for isolating the FP32 regular and FP64 singular passes) */
+enum sod_parts { SOD_PART_REGULAR = 1, SOD_PART_SINGULAR = 2, SOD_PART_ALL = 3 };
+
+typedef struct sod_context sod_context;
+typedef struct sod_mesh sod_mesh;
+
+/* ---- library / diagnostics -------------------------------------------------------------- */
+int sod_version(void);
+const char *sod_last_error(void);
+/* Host-side quadrature table, {l0,l1,l2,w} rows (w sums to 1), for order 1..5 (Cowper, as
+ * include/integrator.hpp:55-113 of the reference) and 7 (13-point degree-7 rule, not in the
+ * reference).  Returns the number of points via *npts.  Needs no GPU. */
+int sod_triangle_rule(int order, double *out, int *npts);
+/* CQ frequencies s_l = gamma(R zeta^l)/dt for l = 0..L/2, R = (1e-10)^(1/(2N)), L = N+1,
+ * gamma_BDF1(z) = 1-z, gamma_BDF2(z) = 3/2 - 2z + z^2/2.  Replaces the prologue of
+ * compute_G_matrices (src/elastodynamics_cqbem_G.cu:177-182,223).  s_out: (L/2+1) complex.
+ * Needs no GPU. */
+int sod_cq_frequencies(int bdf, double dt, int N, double *s_out, double *R_out, int *L_out);
+
+/* ---- context: device, stream, scratch ----------------------------------------------------- */
+int sod_context_create(int device, sod_context **ctx);
+int sod_context_destroy(sod_context *ctx);
+/* Work is issued on `stream` (a cudaStream_t; NULL = CUDA's default stream).  A new context uses
+ * a non-blocking stream of its own.  A context's scratch buffers are reused call after call in
+ * stream order, so one context must not be driven from two streams at once. */
+int sod_context_set_stream(sod_context *ctx, void *stream);
+int sod_context_synchronize(sod_context *ctx);
+/* Threads per CTA of the collocation scatter kernels (0 = automatic); for the autotuner. */
+int sod_context_set_tuning(sod_context *ctx, int coll_threads, int galerkin_threads);
+/* Count of kernel launches issued by this context since creation (for launch accounting). */
+int64_t sod_context_launch_count(const sod_context *ctx);
+
+/* ---- mesh: device-resident geometry + precomputed topology -------------------------------- */
+/* Uploads V, F (and N, or computes unit face normals), builds vertex stars, face colourings for
+ * the deterministic scatter, and the singular-pair lists.  vmap: vertex_map_inverse of the
+ * reference (NULL when traction discontinuity is off). */
+int sod_mesh_create(sod_context *ctx, const double *V, int nV, const int *F, int nF, const double *N,
+                    const int *vmap, sod_mesh **mesh);
+int sod_mesh_destroy(sod_mesh *mesh);
+
+/* ---- Laplace-domain assembly, one frequency (the drop-in kernels) ------------------------- */
+/* Whole-matrix replacement of the reference's per-row / per-pair kernels for one Laplace
+ * frequency s = (s_re, s_im):
+ *   kind G, collocation : compute_elastodynamic_G_kernel_collocation over all rows
+ *                         (src/elastodynamics_cqbem_G_collocation.cu:18-142; driver G.cu:280-305)
+ *   kind H, collocation : src/elastodynamics_cqbem_H_collocation.cu:18-158 (H.cu:300-327)
+ *   kind B_trans, coll. : src/elastodynamics_cqbem_B_trans_collocation.cu:17-124
+ *   kind B_angular,coll.: src/elastodynamics_cqbem_B_angular_collocation.cu:17-143
+ *   Galerkin (any kind) : non-singular pairs (..._galerkin_non_singular.cu) plus singular pairs
+ *                         (src/elastodynamics_cqbem_galerkin_singular.cpp), i.e. the sum formed at
+ *                         src/elastodynamics_cqbem_G.cu:225-260.
+ * Regular integrals run in FP32, singular ones in FP64.  order: triangle rule (1..5, 7);
+ * subdiv: uniform subdivision (1..4); sorder/ssub: 1-D Gauss order (1..5) and subdivision of the
+ * singular rules (the reference uses order/subdiv for both).
+ * out: complex, dtype SOD_C128 (reference layout) or SOD_C64; shape per kind as above. */
+int sod_cqbem_assemble(sod_context *ctx, const sod_mesh *mesh, int kind, int method, double c1, double c2,
+                       double rho, double s_re, double s_im, int order, int subdiv, int sorder, int ssub,
+                       int parts, void *out, int out_dtype);
+
+/* Same for nfreq frequencies s[2*l], s[2*l+1] in one launch; out holds nfreq consecutive matrices.
+ * Replaces the frequency loop of compute_{G,H,B_trans,B_angular}_matrices
+ * (src/elastodynamics_cqbem_G.cu:221-309 and its H / B_trans / B_angular twins). */
+int sod_cqbem_assemble_frequencies(sod_context *ctx, const sod_mesh *mesh, int kind, int method, double c1,
+                                   double c2, double rho, const double *s, int nfreq, int order, int subdiv,
+                                   int sorder, int ssub, int parts, void *out, int out_dtype);
+
+/* ---- inverse transform to CQ time weights (FP64-accurate) --------------------------------- */
+/* X_n = R^-n / L * sum_{l=0}^{L/2} c_l Re(Xhat_l zeta^-nl),  c_0 = 1, c_l = 2 otherwise except
+ * c_{L/2} = 1 for even L;  n = 0..L-1 (src/elastodynamics_cqbem_G.cu:324-337).
+ * Xhat: nfreq = L/2+1 blocks of M complex (dtype SOD_C128 or SOD_C64), out: L blocks of M reals
+ * (SOD_F64 or SOD_F32).  SOD_F64 output accumulates in FP64 (agrees with an FP64 CPU transform to
+ * <= 1e-10 of the stacked Frobenius norm); SOD_F32 output uses double-float arithmetic on the FP32
+ * pipes (about 2^-48 of the term magnitude before the final FP32 rounding). */
+int sod_cq_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, int64_t M, int nfreq, int L,
+                             double R, void *out, int out_dtype);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SOD_GB300_H */

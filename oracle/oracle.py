@@ -1,0 +1,168 @@
+"""ctypes front end of the CPU oracle (oracle/sod_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline / reference legs.  The product package never imports this module.
+PARITY UNPINNED: see the header of sod_oracle.cpp.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libsod_oracle.so")
+_lib = None
+
+KIND = {"G": 0, "H": 1, "B_trans": 2, "B_angular": 3}
+FP64, MIXED = 0, 1
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with the committed Makefile (g++ -O3 -fopenmp)."""
+    src = os.path.join(_HERE, "sod_oracle.cpp")
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(_LIB_PATH)
+        d, i, l, p = ctypes.c_double, ctypes.c_int, ctypes.c_long, ctypes.c_void_p
+        _lib.oracle_collocation.argtypes = [i, i, p, i, p, i, p, p, d, d, d, d, d, i, i, i, i, p, i, i, p]
+        _lib.oracle_galerkin.argtypes = [i, i, p, i, p, i, p, p, d, d, d, d, d, i, i, i, i, p, i, i, p]
+        _lib.oracle_inverse_transform.argtypes = [i, i, d, p, l, p]
+        _lib.oracle_cq_frequencies.argtypes = [i, d, i, p, p, p]
+        _lib.oracle_c_matrix_collocation.argtypes = [p, i, p, i, p, d, p]
+        _lib.oracle_c_matrix_galerkin.argtypes = [p, i, p, i, p]
+        _lib.oracle_elastostatic.argtypes = [i, i, p, i, p, i, p, d, d, i, i, i, i, p]
+        _lib.oracle_rigid_modes.argtypes = [p, i, p, i, p]
+        _lib.oracle_tri_rule.argtypes = [i, p]
+        _lib.oracle_set_threads.argtypes = [i]
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_threads(n: int) -> int:
+    return lib().oracle_set_threads(int(n))
+
+
+def tri_rule(order: int) -> np.ndarray:
+    out = np.zeros((13, 4))
+    n = lib().oracle_tri_rule(order, _ptr(out))
+    return out[:n]
+
+
+def cq_frequencies(bdf: int, dt: float, N: int):
+    s = np.zeros(2 * (N + 1))
+    R = ctypes.c_double()
+    L = ctypes.c_int()
+    lam = lib().oracle_cq_frequencies(bdf, dt, N, _ptr(s), ctypes.byref(R), ctypes.byref(L))
+    return s[: 2 * lam].view(np.complex128).copy(), R.value, L.value
+
+
+def _ncols(kind: int, nV: int) -> int:
+    return 3 * nV if kind <= 1 else (3 if kind == 2 else 9)
+
+
+def _assemble(fn, kind, mesh, mat, s, order, subdiv, sorder, ssub, rows, parts, mode, vmap):
+    kind = KIND.get(kind, kind)
+    rows_a = None if rows is None else np.ascontiguousarray(rows, dtype=np.int32)
+    nr = mesh.nV if rows_a is None else len(rows_a)
+    out = np.zeros((3 * nr, _ncols(kind, mesh.nV)), dtype=np.complex128)
+    vm = None if vmap is None else np.ascontiguousarray(vmap, dtype=np.int32)
+    rc = fn(kind, mode, _ptr(mesh.V), mesh.nV, _ptr(mesh.F), mesh.nF, _ptr(mesh.N), _ptr(vm),
+            mat.c1, mat.c2, mat.rho, float(np.real(s)), float(np.imag(s)), order, subdiv, sorder, ssub,
+            _ptr(rows_a), nr, parts, _ptr(out))
+    if rc:
+        raise ValueError(f"oracle rejected the arguments (code {rc})")
+    return out
+
+
+def collocation(kind, mesh, mat, s, order=5, subdiv=1, sorder=None, ssub=None, rows=None, parts=3,
+                mode=FP64, vmap=None) -> np.ndarray:
+    """Rows (3 per listed vertex) of U/P (3V cols), B_trans (3 cols) or B_angular (9 cols, [j][k])."""
+    return _assemble(lib().oracle_collocation, kind, mesh, mat, s, order, subdiv,
+                     sorder or order, ssub or subdiv, rows, parts, mode, vmap)
+
+
+def galerkin(kind, mesh, mat, s, order=5, subdiv=1, sorder=5, ssub=1, rows=None, parts=3, mode=FP64,
+             vmap=None) -> np.ndarray:
+    return _assemble(lib().oracle_galerkin, kind, mesh, mat, s, order, subdiv, sorder, ssub, rows, parts,
+                     mode, vmap)
+
+
+def inverse_transform(Xhat: np.ndarray, L: int, R: float) -> np.ndarray:
+    """Xhat: (Lambda, ...) complex -> (L, ...) real time-domain weights."""
+    X = np.ascontiguousarray(Xhat, dtype=np.complex128)
+    M = int(np.prod(X.shape[1:]))
+    out = np.zeros((L,) + X.shape[1:], dtype=np.float64)
+    rc = lib().oracle_inverse_transform(X.shape[0], L, R, _ptr(X), M, _ptr(out))
+    if rc:
+        raise ValueError("inverse transform: nfreq must equal L//2 + 1")
+    return out
+
+
+def c_matrix_collocation(mesh, nu: float) -> np.ndarray:
+    out = np.zeros((3 * mesh.nV, 3))
+    lib().oracle_c_matrix_collocation(_ptr(mesh.V), mesh.nV, _ptr(mesh.F), mesh.nF, _ptr(mesh.N), nu, _ptr(out))
+    return out
+
+
+def c_matrix_galerkin(mesh) -> np.ndarray:
+    out = np.zeros((3 * mesh.nV, 3 * mesh.nV))
+    lib().oracle_c_matrix_galerkin(_ptr(mesh.V), mesh.nV, _ptr(mesh.F), mesh.nF, _ptr(out))
+    return out
+
+
+def elastostatic(kind, mesh, mat, galerkin=False, order=5, subdiv=1, sorder=None, ssub=None) -> np.ndarray:
+    kind = KIND.get(kind, kind)
+    out = np.zeros((3 * mesh.nV, 3 * mesh.nV))
+    rc = lib().oracle_elastostatic(kind, int(galerkin), _ptr(mesh.V), mesh.nV, _ptr(mesh.F), mesh.nF,
+                                   _ptr(mesh.N), mat.nu, mat.mu, order, subdiv, sorder or min(order, 5),
+                                   ssub or subdiv, _ptr(out))
+    if rc:
+        raise ValueError("elastostatic: bad quadrature order")
+    return out
+
+
+def rigid_modes(mesh) -> np.ndarray:
+    T = np.zeros((6, 3 * mesh.nV))
+    lib().oracle_rigid_modes(_ptr(mesh.V), mesh.nV, _ptr(mesh.F), mesh.nF, _ptr(T))
+    return T
+
+
+def b_euler(B_angular_n: np.ndarray) -> np.ndarray:
+    """B_euler(i,j) = B_ang(i,(j+2)%3,(j+1)%3) - B_ang(i,(j+1)%3,(j+2)%3)
+    (src/elastodynamics_cqbem_matrix_collection.cpp:296-301).  B_angular_n: (3V, 3, 3)."""
+    out = np.zeros(B_angular_n.shape[:2])
+    for j in range(3):
+        out[:, j] = B_angular_n[:, (j + 2) % 3, (j + 1) % 3] - B_angular_n[:, (j + 1) % 3, (j + 2) % 3]
+    return out
+
+
+def b_angular_shift(B_ang_n: np.ndarray, B_trans_n: np.ndarray, V: np.ndarray, cm: np.ndarray) -> np.ndarray:
+    """B_ang(3v+i, j, k) += B_trans(3v+i, j) * (x_v - cm)_k  (src/elastodynamics_cqbem_B_angular.cu:326-334)."""
+    d = np.repeat(V - cm[None, :], 3, axis=0)
+    return B_ang_n + B_trans_n[:, :, None] * d[:, None, :]
+
+
+def history_convolution(G, H, p_hist, u_hist, B=None, a_hist=None):
+    """b = sum_{k=1..K} (G_k p_{n-k} - H_k u_{n-k} [+ B_k a_{n-k}])  (src/elastodynamics_cqbem_object.cpp:44-48;
+    H is negated at load, src/elastodynamics_cqbem_matrix_collection.cpp:140).
+    G, H: (N+1, 3V, 3V); p_hist/u_hist: (K, 3V[, R]) with index 0 the most recent step (n-1)."""
+    K = p_hist.shape[0]
+    b = np.zeros(p_hist.shape[1:], dtype=np.float64)
+    for k in range(1, K + 1):
+        b += G[k].astype(np.float64) @ p_hist[k - 1] - H[k].astype(np.float64) @ u_hist[k - 1]
+        if B is not None:
+            b += B[k] @ a_hist[k - 1]
+    return b

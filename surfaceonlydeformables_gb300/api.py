@@ -1,0 +1,135 @@
+"""Thin object layer over the C ABI: Context (device + stream + scratch) and Mesh (device-resident
+geometry), plus the per-frequency assembly and inverse-transform calls."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+from .meshes import Material, SurfaceMesh
+
+
+def _torch():
+    import torch  # deferred: the package itself needs only numpy
+
+    return torch
+
+
+class Context:
+    """A device, a CUDA stream and the library's scratch buffers (sod_context)."""
+
+    def __init__(self, device: int = 0, stream=None):
+        self._h = ctypes.c_void_p()
+        L.check(L.load().sod_context_create(device, ctypes.byref(self._h)))
+        self.device = device
+        if stream is not None:
+            self.set_stream(stream)
+
+    def set_stream(self, stream) -> None:
+        """stream: a torch.cuda.Stream or a raw cudaStream_t integer (0 = CUDA's default stream)."""
+        raw = int(getattr(stream, "cuda_stream", stream) or 0)
+        L.check(L.load().sod_context_set_stream(self._h, ctypes.c_void_p(raw) if raw else None))
+
+    def synchronize(self) -> None:
+        L.check(L.load().sod_context_synchronize(self._h))
+
+    def set_tuning(self, coll_threads: int = 0, galerkin_threads: int = 0) -> None:
+        L.check(L.load().sod_context_set_tuning(self._h, coll_threads, galerkin_threads))
+
+    @property
+    def launches(self) -> int:
+        return int(L.load().sod_context_launch_count(self._h))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if self._h:
+            L.load().sod_context_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Mesh:
+    """Device-resident mesh with precomputed stars, neighbour slots and face colourings."""
+
+    def __init__(self, ctx: Context, mesh: SurfaceMesh, vmap=None):
+        self.ctx = ctx
+        self.host = mesh
+        self.nV, self.nF = mesh.nV, mesh.nF
+        self._vmap = None if vmap is None else np.ascontiguousarray(vmap, dtype=np.int32)
+        self._h = ctypes.c_void_p()
+        L.check(L.load().sod_mesh_create(ctx.handle, L.ptr(mesh.V), mesh.nV, L.ptr(mesh.F), mesh.nF, L.ptr(mesh.N),
+                                         L.ptr(self._vmap), ctypes.byref(self._h)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if self._h:
+            L.load().sod_mesh_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def out_shape(kind: int, nV: int) -> tuple[int, int]:
+    return (3 * nV, 3 * nV) if kind in (L.G, L.H) else ((3 * nV, 3) if kind == L.B_TRANS else (3 * nV, 9))
+
+
+def assemble(ctx: Context, mesh: Mesh, kind, mat: Material, s: complex, order: int = 5, subdiv: int = 1,
+             sorder: int | None = None, ssub: int | None = None, method: int = L.COLLOCATION,
+             parts: int = L.PART_ALL, out=None, dtype: int = L.C128):
+    """Laplace-domain matrix of `kind` at frequency s (drop-in for the reference's per-row kernels).
+
+    out: numpy (host) or torch CUDA tensor of the right shape/dtype; allocated as numpy if None.
+    B_angular comes back as (3V, 9) = [row][j*3+k]."""
+    kind = L.KINDS.get(kind, kind)
+    if out is None:
+        out = np.empty(out_shape(kind, mesh.nV), dtype=np.complex128 if dtype == L.C128 else np.complex64)
+    sorder = sorder or min(order, 5)
+    ssub = ssub or subdiv
+    L.check(L.load().sod_cqbem_assemble(ctx.handle, mesh.handle, kind, method, mat.c1, mat.c2, mat.rho,
+                                        float(np.real(s)), float(np.imag(s)), order, subdiv, sorder, ssub, parts,
+                                        L.ptr(out), dtype))
+    return out
+
+
+def assemble_frequencies(ctx: Context, mesh: Mesh, kind, mat: Material, s, order: int = 5, subdiv: int = 1,
+                         sorder: int | None = None, ssub: int | None = None, method: int = L.COLLOCATION,
+                         parts: int = L.PART_ALL, out=None, dtype: int = L.C128):
+    """All listed Laplace frequencies in one launch: out has shape (len(s),) + out_shape(kind)."""
+    kind = L.KINDS.get(kind, kind)
+    s = np.ascontiguousarray(np.asarray(s, dtype=np.complex128).ravel())
+    if out is None:
+        out = np.empty((len(s),) + out_shape(kind, mesh.nV), dtype=np.complex128 if dtype == L.C128 else np.complex64)
+    sorder = sorder or min(order, 5)
+    ssub = ssub or subdiv
+    L.check(L.load().sod_cqbem_assemble_frequencies(ctx.handle, mesh.handle, kind, method, mat.c1, mat.c2, mat.rho,
+                                                    L.ptr(s.view(np.float64)), len(s), order, subdiv, sorder, ssub,
+                                                    parts, L.ptr(out), dtype))
+    return out
+
+
+def inverse_transform(ctx: Context, Xhat, L_: int, R: float, out=None, out_dtype: int = L.F64):
+    """Time-domain CQ weights from Laplace-domain blocks: Xhat (L/2+1, ...) complex -> (L, ...) real."""
+    in_dtype = L.C128 if str(Xhat.dtype).endswith("complex128") else L.C64
+    nfreq = Xhat.shape[0]
+    M = int(np.prod(Xhat.shape[1:]))
+    if out is None:
+        out = np.empty((L_,) + tuple(Xhat.shape[1:]), dtype=np.float64 if out_dtype == L.F64 else np.float32)
+    L.check(L.load().sod_cq_inverse_transform(ctx.handle, L.ptr(Xhat), in_dtype, M, nfreq, L_, R, L.ptr(out),
+                                              out_dtype))
+    return out

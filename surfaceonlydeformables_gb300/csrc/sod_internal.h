@@ -1,0 +1,168 @@
+// sod_internal.h -- host-side structures shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/sod_gb300.h"
+#include "sod_device.cuh"
+
+namespace sod {
+
+// ---- errors -------------------------------------------------------------------------------
+void set_error(const std::string &msg);
+struct Status {
+    int code = SOD_OK;
+};
+#define SOD_CHECK_CUDA(expr)                                                                      \
+    do {                                                                                          \
+        cudaError_t _e = (expr);                                                                  \
+        if (_e != cudaSuccess) {                                                                  \
+            ::sod::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));               \
+            return _e == cudaErrorMemoryAllocation ? SOD_ERR_OOM : SOD_ERR_CUDA;                 \
+        }                                                                                         \
+    } while (0)
+#define SOD_REQUIRE(cond, msg)                                                                    \
+    do {                                                                                          \
+        if (!(cond)) {                                                                            \
+            ::sod::set_error(msg);                                                                \
+            return SOD_ERR_INVALID_ARG;                                                           \
+        }                                                                                         \
+    } while (0)
+#define SOD_TRY(expr)                                                                             \
+    do {                                                                                          \
+        int _rc = (expr);                                                                         \
+        if (_rc != SOD_OK) return _rc;                                                            \
+    } while (0)
+
+// ---- device buffer (owning) ---------------------------------------------------------------
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    int ensure(size_t n) {  // grow-only
+        if (n <= bytes) return SOD_OK;
+        release();
+        if (n == 0) return SOD_OK;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            return SOD_ERR_OOM;
+        }
+        bytes = n;
+        return SOD_OK;
+    }
+    template <class T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+// ---- quadrature point table passed by value to kernels ----------------------------------------
+constexpr int MAX_TRI_PTS = 13 * 16;  // order-7 rule with subdivision 4
+struct PointTable {
+    int n;
+    float4 p[MAX_TRI_PTS];  // (l0, l1, l2, w): barycentrics w.r.t. the whole face, weight / subdiv^2
+};
+struct PointD {
+    double l0, l1, l2, w;
+};
+struct PointTableD {  // FP64 copy of the same table
+    int n;
+    PointD p[MAX_TRI_PTS];
+};
+struct GaussTable {  // 1-D Gauss-Legendre on [0,1] after subdivision: points and weights
+    int n;
+    double x[20], w[20];
+};
+int make_point_table(int order, int subdiv, PointTable &pt, PointTableD *ptd = nullptr);
+int make_unit_gauss(int order, int subdiv, GaussTable &g);
+const double (*tri_rule_table(int order, int &n))[4];
+const double (*gl_rule_table(int order, int &n))[2];
+
+// ---- context ------------------------------------------------------------------------------
+}  // namespace sod
+
+struct sod_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    std::atomic<int64_t> launches{0};
+    int coll_threads = 0;  // 0 = automatic
+    int gal_threads = 0;
+    int num_sms = 0;
+    size_t smem_optin = 0;
+    // scratch
+    sod::DevBuf sing;      // singular corrections
+    sod::DevBuf kconst;    // per-frequency constants
+    sod::DevBuf staging;   // device staging for host outputs
+    sod::DevBuf staging2;  // device staging for host inputs
+    sod::DevBuf twiddle;   // inverse-transform twiddles
+    void count(int n = 1) { launches += n; }
+};
+
+struct sod_mesh {
+    sod_context *ctx = nullptr;
+    int nV = 0, nF = 0;
+    bool has_vmap = false;
+    std::vector<double> V, N;
+    std::vector<int> F, vmap;
+    // device copies
+    sod::DevBuf dV, dN, dF, dVf, dCanon;
+    // vertex stars: faces incident to each canonical vertex, with the singular corner
+    std::vector<int> star_off, star_face, star_corner;
+    sod::DevBuf dStarOff, dStarFace, dStarCorner;
+    // per field vertex i: distinct vertices touched by its star faces (singular block slots)
+    std::vector<int> nbr_off, nbr_vert, star_slot;  // star_slot: 3 slots per star entry
+    sod::DevBuf dNbrOff, dNbrVert, dStarSlot;
+    // colour-ordered face records for the deterministic scatter, keyed by threads-per-CTA
+    struct Coloured {
+        int ncolors = 0;
+        std::vector<int> off;  // ncolors + 1
+        sod::DevBuf dFaces;    // 4 float4 per face
+        sod::DevBuf dCanonF;   // int4 per face (canonical corner ids) if vmap
+        sod::DevBuf dOff;
+    };
+    std::map<int, std::unique_ptr<Coloured>> coloured;
+    // all faces in natural order (for the reduction kernels and Galerkin)
+    sod::DevBuf dFacesNat, dCanonNat;
+    int coloured_for(int threads, const Coloured **out);
+};
+
+namespace sod {
+// Per-frequency constants travel as a __grid_constant__ kernel parameter (no host->device copy,
+// no stream synchronisation); launches with more frequencies are split into chunks.
+constexpr int MAX_FREQ_PER_LAUNCH = 40;
+struct FreqTable {
+    int n;
+    KConst<float> kf[MAX_FREQ_PER_LAUNCH];
+    KConst<double> kd[MAX_FREQ_PER_LAUNCH];
+};
+struct CollLaunch {
+    const sod_mesh *mesh;
+    int kind;
+    int nfreq;
+    const KConst<double> *kc_host;  // host array, nfreq entries
+    int order, subdiv, sorder, ssub, parts;
+    void *out;  // device
+    int out_dtype;
+    long long freq_stride;  // elements between consecutive frequencies of out
+    cudaStream_t stream;
+};
+int launch_collocation(sod_context *ctx, const CollLaunch &L);
+int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, int64_t M, int nfreq, int L,
+                             double R, void *out, int out_dtype, cudaStream_t stream);
+KConst<double> make_kconst(double c1, double c2, double rho, double sr, double si);
+KConst<float> to_float(const KConst<double> &k);
+}  // namespace sod

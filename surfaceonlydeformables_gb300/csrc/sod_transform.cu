@@ -1,0 +1,195 @@
+// sod_transform.cu -- inverse transform from Laplace frequencies to CQ time weights.
+//
+// X_n = R^-n / L * sum_{l=0}^{L/2} c_l Re(Xhat_l zeta^-nl)  for every matrix entry, n = 0..L-1
+// (reference: src/elastodynamics_cqbem_G.cu:324-337, H.cu:347-371, B_trans.cu:289-304,
+// B_angular.cu:310-325).  The reference re-reads every U_l.mat from disk for each n; here each
+// CTA stages a tile of entries x all frequencies in shared memory once and produces all L outputs.
+//
+// Two kernels:
+//  * FP64 output: native FP64 accumulation (one DFMA per real multiply-add).  Late weights are the
+//    result of heavy cancellation (terms ~R^-n |Xhat|, results far smaller), so only 53-bit
+//    accumulation reproduces the reference's FP64 transform to 1e-10 on real data.
+//  * FP32 output: double-float arithmetic on the FP32 pipes (GB300 has little FP64 throughput):
+//    twiddles split hi+lo, every product hi*x formed exactly with an FMA (TwoProduct), the sum
+//    carried as an unevaluated pair with TwoSum -- about 2^-48 of the term magnitude, far below
+//    the rounding of the FP32 result.
+#include <cmath>
+#include <vector>
+
+#include "sod_internal.h"
+
+namespace sod {
+
+// error-free transformations on FP32
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+struct df {
+    float hi, lo;
+};
+// acc += a * x  where a = (ahi + alo) is a double-float constant and x an FP32 value
+__device__ __forceinline__ void df_mac(df &acc, float ahi, float alo, float x) {
+    const float p = ahi * x;
+    const float pe = fmaf(ahi, x, -p);  // exact: p + pe = ahi * x
+    float s, e;
+    two_sum(acc.hi, p, s, e);
+    acc.lo += e + fmaf(alo, x, pe);
+    acc.hi = s;
+}
+
+template <int TILE>
+__global__ void __launch_bounds__(TILE) inv_transform_df_kernel(const void *__restrict__ Xhat, int in_c128, long long M,
+                                                               int nfreq, int L, const float4 *__restrict__ tw,
+                                                               void *__restrict__ out, int out_f64) {
+    // shared: twiddles [L][nfreq] as float4 (re_hi, re_lo, im_hi, im_lo), entries [nfreq][TILE] hi (+lo)
+    extern __shared__ float4 sm[];
+    float4 *stw = sm;
+    float2 *sx_hi = reinterpret_cast<float2 *>(stw + L * nfreq);
+    float2 *sx_lo = sx_hi + (size_t)nfreq * TILE;
+    for (int t = threadIdx.x; t < L * nfreq; t += TILE) stw[t] = tw[t];
+    const long long e0 = (long long)blockIdx.x * TILE;
+    const long long e = e0 + threadIdx.x;
+    const bool live = e < M;
+    for (int l = 0; l < nfreq; l++) {
+        float2 hi = make_float2(0.f, 0.f), lo = make_float2(0.f, 0.f);
+        if (live) {
+            if (in_c128) {
+                const double2 v = reinterpret_cast<const double2 *>(Xhat)[(long long)l * M + e];
+                hi = make_float2((float)v.x, (float)v.y);
+                lo = make_float2((float)(v.x - (double)hi.x), (float)(v.y - (double)hi.y));
+            } else {
+                hi = reinterpret_cast<const float2 *>(Xhat)[(long long)l * M + e];
+            }
+        }
+        sx_hi[l * TILE + threadIdx.x] = hi;
+        if (in_c128) sx_lo[l * TILE + threadIdx.x] = lo;
+    }
+    __syncthreads();
+    if (!live) return;
+    for (int n = 0; n < L; n++) {
+        df acc = {0.f, 0.f};
+        for (int l = 0; l < nfreq; l++) {
+            const float4 w = stw[n * nfreq + l];
+            const float2 x = sx_hi[l * TILE + threadIdx.x];
+            // Re(x * w) = x.re * w.re - x.im * w.im
+            df_mac(acc, w.x, w.y, x.x);
+            df_mac(acc, -w.z, -w.w, x.y);
+            if (in_c128) {
+                const float2 xl = sx_lo[l * TILE + threadIdx.x];
+                df_mac(acc, w.x, w.y, xl.x);
+                df_mac(acc, -w.z, -w.w, xl.y);
+            }
+        }
+        const double v = (double)acc.hi + (double)acc.lo;
+        if (out_f64)
+            reinterpret_cast<double *>(out)[(long long)n * M + e] = v;
+        else
+            reinterpret_cast<float *>(out)[(long long)n * M + e] = (float)v;
+    }
+}
+
+template <int TILE>
+__global__ void __launch_bounds__(TILE) inv_transform_f64_kernel(const void *__restrict__ Xhat, int in_c128, long long M,
+                                                                int nfreq, int L, const double2 *__restrict__ tw,
+                                                                double *__restrict__ out) {
+    extern __shared__ double2 smd[];
+    double2 *stw = smd;                    // [L][nfreq] twiddles
+    double2 *sx = stw + (size_t)L * nfreq;  // [nfreq][TILE] inputs
+    for (int t = threadIdx.x; t < L * nfreq; t += TILE) stw[t] = tw[t];
+    const long long e = (long long)blockIdx.x * TILE + threadIdx.x;
+    const bool live = e < M;
+    for (int l = 0; l < nfreq; l++) {
+        double2 v = make_double2(0.0, 0.0);
+        if (live) {
+            if (in_c128) {
+                v = reinterpret_cast<const double2 *>(Xhat)[(long long)l * M + e];
+            } else {
+                const float2 f = reinterpret_cast<const float2 *>(Xhat)[(long long)l * M + e];
+                v = make_double2(f.x, f.y);
+            }
+        }
+        sx[l * TILE + threadIdx.x] = v;
+    }
+    __syncthreads();
+    if (!live) return;
+    for (int n = 0; n < L; n++) {
+        double acc = 0.0;
+        for (int l = 0; l < nfreq; l++) {
+            const double2 w = stw[n * nfreq + l];
+            const double2 x = sx[l * TILE + threadIdx.x];
+            acc = fma(x.x, w.x, acc);
+            acc = fma(-x.y, w.y, acc);
+        }
+        out[(long long)n * M + e] = acc;
+    }
+}
+
+// twiddles c_l R^-n / L zeta^-nl for n < L, l < nfreq, generated on the device (no host copy)
+__global__ void twiddle_kernel(int L, int nfreq, double R, double2 *tw64, float4 *tw32) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= L * nfreq) return;
+    const int n = t / nfreq, l = t % nfreq;
+    const bool twice = l != 0 && (l != L / 2 || L % 2 == 1);
+    const double sc = (twice ? 2.0 : 1.0) * pow(R, -(double)n) / (double)L;
+    double sn, cs;
+    sincospi(-2.0 * (double)(((long long)n * l) % L) / (double)L, &sn, &cs);
+    const double re = sc * cs, im = sc * sn;
+    if (tw64) tw64[t] = make_double2(re, im);
+    if (tw32) {
+        const float rh = (float)re, ih = (float)im;
+        tw32[t] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
+    }
+}
+
+int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, int64_t M, int nfreq, int L, double R,
+                             void *out, int out_dtype, cudaStream_t stream) {
+    SOD_REQUIRE(L >= 1 && nfreq == L / 2 + 1, "inverse transform: nfreq must equal L/2 + 1");
+    SOD_REQUIRE(in_dtype == SOD_C128 || in_dtype == SOD_C64, "inverse transform: input must be complex128 or complex64");
+    SOD_REQUIRE(out_dtype == SOD_F64 || out_dtype == SOD_F32, "inverse transform: output must be float64 or float32");
+    SOD_REQUIRE(R > 0.0 && M >= 0, "inverse transform: bad R or M");
+    if (M == 0) return SOD_OK;
+    const int in_c128 = in_dtype == SOD_C128;
+    if (out_dtype == SOD_F64) {
+        const size_t ntw = (size_t)L * nfreq;
+        SOD_TRY(ctx->twiddle.ensure(sizeof(double2) * ntw));
+        twiddle_kernel<<<(unsigned)((ntw + 255) / 256), 256, 0, stream>>>(L, nfreq, R, ctx->twiddle.as<double2>(), nullptr);
+        SOD_CHECK_CUDA(cudaGetLastError());
+        ctx->count();
+        constexpr int TILE = 128;
+        const size_t smem = sizeof(double2) * (ntw + (size_t)nfreq * TILE);
+        if (smem > ctx->smem_optin) {
+            set_error("inverse transform: too many frequencies for the shared-memory tile");
+            return SOD_ERR_UNSUPPORTED;
+        }
+        SOD_CHECK_CUDA(cudaFuncSetAttribute(inv_transform_f64_kernel<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem));
+        const long long blocks = (M + TILE - 1) / TILE;
+        inv_transform_f64_kernel<TILE><<<(unsigned)blocks, TILE, smem, stream>>>(
+            Xhat, in_c128, M, nfreq, L, ctx->twiddle.as<double2>(), reinterpret_cast<double *>(out));
+        SOD_CHECK_CUDA(cudaGetLastError());
+        ctx->count();
+        return SOD_OK;
+    }
+    const size_t ntw = (size_t)L * nfreq;
+    SOD_TRY(ctx->twiddle.ensure(sizeof(float4) * ntw));
+    float4 *dtw = ctx->twiddle.as<float4>();
+    twiddle_kernel<<<(unsigned)((ntw + 255) / 256), 256, 0, stream>>>(L, nfreq, R, nullptr, dtw);
+    SOD_CHECK_CUDA(cudaGetLastError());
+    ctx->count();
+    constexpr int TILE = 128;
+    const size_t smem = sizeof(float4) * ntw + sizeof(float2) * (size_t)nfreq * TILE * (in_c128 ? 2 : 1);
+    if (smem > ctx->smem_optin) {
+        set_error("inverse transform: too many frequencies for the shared-memory tile");
+        return SOD_ERR_UNSUPPORTED;
+    }
+    SOD_CHECK_CUDA(cudaFuncSetAttribute(inv_transform_df_kernel<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const long long blocks = (M + TILE - 1) / TILE;
+    inv_transform_df_kernel<TILE><<<(unsigned)blocks, TILE, smem, stream>>>(Xhat, in_c128, M, nfreq, L, dtw, out, 0);
+    SOD_CHECK_CUDA(cudaGetLastError());
+    ctx->count();
+    return SOD_OK;
+}
+
+}  // namespace sod

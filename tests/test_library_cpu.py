@@ -1,0 +1,67 @@
+"""The C-ABI library builds, loads and exports every symbol include/sod_gb300.h declares; its
+host-only entry points agree with the oracle.  No compute call is made without a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "sod_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(sod_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_header_symbols_all_exported(sodlib):
+    lib = sodlib.load()
+    names = header_symbols()
+    assert len(names) >= 14
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in include/sod_gb300.h but not exported"
+    assert sorted(sodlib.declared_symbols()) == names, "ctypes signatures out of sync with the header"
+
+
+def test_triangle_rules_match_oracle(sodlib, oracle):
+    for order in (1, 2, 3, 4, 5, 7):
+        np.testing.assert_array_equal(sodlib.triangle_rule(order), oracle.tri_rule(order))
+    with pytest.raises(sodlib.SodError) as e:
+        sodlib.triangle_rule(6)
+    assert e.value.code == sodlib.SOD_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("bdf,dt,N", [(2, 0.01, 32), (1, 0.005, 16), (2, 1 / 200, 64), (2, 0.01, 5)])
+def test_cq_frequencies_match_oracle(sodlib, oracle, bdf, dt, N):
+    s_lib, R_lib, L_lib = sodlib.cq_frequencies(bdf, dt, N)
+    s_or, R_or, L_or = oracle.cq_frequencies(bdf, dt, N)
+    assert L_lib == L_or and abs(R_lib - R_or) < 1e-15
+    assert np.max(np.abs(s_lib - s_or) / np.abs(s_or)) < 1e-13
+
+
+def test_bad_arguments_are_rejected(sodlib):
+    lib = sodlib.load()
+    R = ctypes.c_double()
+    L = ctypes.c_int()
+    s = np.zeros(8)
+    assert lib.sod_cq_frequencies(3, 0.01, 4, sodlib.ptr(s), ctypes.byref(R), ctypes.byref(L)) == sodlib.SOD_ERR_INVALID_ARG
+    assert b"BDF" in lib.sod_last_error()
+    assert lib.sod_cq_frequencies(2, -1.0, 4, sodlib.ptr(s), ctypes.byref(R), ctypes.byref(L)) == sodlib.SOD_ERR_INVALID_ARG
+    assert lib.sod_context_synchronize(None) == sodlib.SOD_ERR_INVALID_ARG
+
+
+def test_no_device_fails_loudly(sodlib):
+    """Without a GPU the compute path refuses to start (there is no CPU fallback)."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    rc = sodlib.load().sod_context_create(0, ctypes.byref(h))
+    assert rc == sodlib.SOD_ERR_NO_DEVICE
+    from surfaceonlydeformables_gb300.api import Context
+
+    with pytest.raises(sodlib.SodError):
+        Context(0)
