@@ -55,6 +55,19 @@ def make_workload(seed: int = 2024, n_objects: int = 24):
     return objs
 
 
+def make_single(level: int = 3):
+    """One object: icosphere radius 0.1 m, E 1e5, nu 0.3, rho 1000, dt 0.01, BDF2, N 32, 7-point rule
+    (the reference's CPU-runnable collocation case at level 3: 642 vertices / 1280 triangles)."""
+    from surfaceonlydeformables_gb300.meshes import Material, make_icosphere_mesh
+
+    return [dict(mesh=make_icosphere_mesh(level, 0.1), mat=Material(1e5, 0.3, 1000.0), N=32, dt=0.01, bdf=2,
+                 order=5, subdiv=1)]
+
+
+CASES = {"mixed24": make_workload, "coll642": lambda: make_single(3), "coll2562": lambda: make_single(4),
+         "coll162": lambda: make_single(2)}
+
+
 def entries(nV: int, nfreq: int) -> int:
     return nfreq * (2 * (3 * nV) ** 2 + 12 * 3 * nV)
 
@@ -145,7 +158,7 @@ def cpu_sample(objs, threads: int, nfreq: int = 2):
 
 
 def run_reference(args):
-    objs = make_workload()
+    objs = CASES[args.case]()
     threads = os.cpu_count() or 1
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -188,7 +201,7 @@ def run_gpu(args):
     from surfaceonlydeformables_gb300 import build as B
 
     B.build()
-    objs = make_workload()
+    objs = CASES[args.case]()
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
     ctx = api.Context(local, stream=stream)
@@ -211,9 +224,7 @@ def run_gpu(args):
 
     def step():
         for o, m, per in zip(objs, meshes, outs):
-            for kind in KINDS:
-                api.assemble_frequencies(ctx, m, kind, o["mat"], o["s"], order=o["order"], subdiv=o["subdiv"],
-                                         out=per[kind], dtype=L.C64)
+            api.assemble_all(ctx, m, o["mat"], o["s"], order=o["order"], subdiv=o["subdiv"], outs=per, dtype=L.C64)
 
     for _ in range(args.warmup):
         step()
@@ -338,6 +349,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    ap.add_argument("--case", default="mixed24", choices=sorted(CASES),
+                    help="workload: the 24-object set (default) or one object for profiling captures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

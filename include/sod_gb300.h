@@ -121,6 +121,14 @@ int sod_cqbem_assemble_frequencies(sod_context *ctx, const sod_mesh *mesh, int k
                                    double c2, double rho, const double *s, int nfreq, int order, int subdiv,
                                    int sorder, int ssub, int parts, void *out, int out_dtype);
 
+/* Every kind whose output pointer is non-NULL, for nfreq frequencies, in one call: the kinds share
+ * the FP64 radial terms of the polar-rule singular pass (G, B_trans, B_angular) and the regular
+ * B_trans/B_angular pass.  The per-object unit of compute_H_matrices + compute_G_matrices +
+ * compute_B_trans_matrices + compute_B_angular_tensors (src/elastodynamics_cqbem_matrix_collection.cpp:90-93,165-166). */
+int sod_cqbem_assemble_all(sod_context *ctx, const sod_mesh *mesh, int method, double c1, double c2, double rho,
+                           const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, int parts,
+                           void *out_G, void *out_H, void *out_B_trans, void *out_B_angular, int out_dtype);
+
 /* ---- inverse transform to CQ time weights (FP64-accurate) --------------------------------- */
 /* X_n = R^-n / L * sum_{l=0}^{L/2} c_l Re(Xhat_l zeta^-nl),  c_0 = 1, c_l = 2 otherwise except
  * c_{L/2} = 1 for even L;  n = 0..L-1 (src/elastodynamics_cqbem_G.cu:324-337).

@@ -123,6 +123,26 @@ def assemble_frequencies(ctx: Context, mesh: Mesh, kind, mat: Material, s, order
     return out
 
 
+def assemble_all(ctx: Context, mesh: Mesh, mat: Material, s, order: int = 5, subdiv: int = 1,
+                 sorder: int | None = None, ssub: int | None = None, method: int = L.COLLOCATION,
+                 parts: int = L.PART_ALL, outs: dict | None = None, dtype: int = L.C128, kinds=("G", "H", "B_trans", "B_angular")):
+    """Several kinds for all listed frequencies in one call (shared FP64 radial terms).  Returns a dict
+    kind -> array of shape (len(s),) + out_shape(kind)."""
+    s = np.ascontiguousarray(np.asarray(s, dtype=np.complex128).ravel())
+    outs = dict(outs or {})
+    cd = np.complex128 if dtype == L.C128 else np.complex64
+    for k in kinds:
+        if k not in outs:
+            outs[k] = np.empty((len(s),) + out_shape(L.KINDS[k], mesh.nV), dtype=cd)
+    sorder = sorder or min(order, 5)
+    ssub = ssub or subdiv
+    ptrs = [L.ptr(outs[k]) if k in outs else None for k in ("G", "H", "B_trans", "B_angular")]
+    L.check(L.load().sod_cqbem_assemble_all(ctx.handle, mesh.handle, method, mat.c1, mat.c2, mat.rho,
+                                            L.ptr(s.view(np.float64)), len(s), order, subdiv, sorder, ssub, parts,
+                                            *ptrs, dtype))
+    return outs
+
+
 def inverse_transform(ctx: Context, Xhat, L_: int, R: float, out=None, out_dtype: int = L.F64):
     """Time-domain CQ weights from Laplace-domain blocks: Xhat (L/2+1, ...) complex -> (L, ...) real."""
     in_dtype = L.C128 if str(Xhat.dtype).endswith("complex128") else L.C64

@@ -472,57 +472,96 @@ int sod_mesh_destroy(sod_mesh *mesh) {
     return SOD_OK;
 }
 
-int sod_cqbem_assemble_frequencies(sod_context *ctx, const sod_mesh *mesh, int kind, int method, double c1, double c2,
-                                   double rho, const double *s, int nfreq, int order, int subdiv, int sorder, int ssub,
-                                   int parts, void *out, int out_dtype) {
+static size_t kind_elems(int kind, int nV) {
+    const size_t ncol = kind <= SOD_H ? 3 * (size_t)nV : (kind == SOD_B_TRANS ? 3 : 9);
+    return 3 * (size_t)nV * ncol;
+}
+
+// Shared driver: validates, stages host outputs through device memory, launches, copies back.
+static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int method, double c1, double c2,
+                          double rho, const double *s, int nfreq, int order, int subdiv, int sorder, int ssub,
+                          int parts, void *const outs[4], int out_dtype) {
     SOD_TRY(check_context(ctx));
     SOD_REQUIRE(mesh && mesh->ctx == ctx, "mesh does not belong to this context");
-    SOD_REQUIRE(kind >= SOD_G && kind <= SOD_B_ANGULAR, "kind must be G, H, B_trans or B_angular");
     SOD_REQUIRE(out_dtype == SOD_C128 || out_dtype == SOD_C64, "output dtype must be complex128 or complex64");
     SOD_REQUIRE(parts >= 1 && parts <= 3, "parts must be regular (1), singular (2) or both (3)");
-    SOD_REQUIRE(out != nullptr && s != nullptr, "null buffer");
+    SOD_REQUIRE(s != nullptr, "null frequency array");
     SOD_REQUIRE(nfreq >= 1 && nfreq <= 65535, "nfreq must be in [1, 65535]");
     SOD_REQUIRE(c1 > 0 && c2 > 0 && rho > 0 && std::isfinite(c1) && std::isfinite(c2) && std::isfinite(rho),
                 "wave speeds and density must be positive and finite");
     for (int l = 0; l < nfreq; l++)
         SOD_REQUIRE(std::isfinite(s[2 * l]) && std::isfinite(s[2 * l + 1]) && (s[2 * l] != 0.0 || s[2 * l + 1] != 0.0),
                     "Laplace frequencies must be finite and non-zero");
+    for (int kd = 0; kd < 4; kd++)
+        if (mask & (1 << kd)) SOD_REQUIRE(outs[kd] != nullptr, "null output buffer");
     if (method != SOD_COLLOCATION) {
         set_error("Galerkin assembly is not available in this build");
         return SOD_ERR_UNSUPPORTED;
     }
     SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
-    const size_t ncol = kind <= SOD_H ? 3 * (size_t)mesh->nV : (kind == SOD_B_TRANS ? 3 : 9);
-    const size_t nelem = 3 * (size_t)mesh->nV * ncol;
     const size_t esz = out_dtype == SOD_C128 ? 16 : 8;
-    const bool dev_out = is_device_ptr(out);
-    void *dout = out;
-    if (!dev_out) {
-        SOD_TRY(ctx->staging.ensure(nelem * esz * nfreq));
-        dout = ctx->staging.p;
+    CollLaunch L{};
+    L.mesh = mesh;
+    L.kind_mask = mask;
+    L.nfreq = nfreq;
+    // host outputs are staged in one device buffer, kinds back to back
+    bool host_out[4] = {false, false, false, false};
+    size_t staged = 0, off[4] = {0, 0, 0, 0};
+    for (int kd = 0; kd < 4; kd++) {
+        if (!(mask & (1 << kd))) continue;
+        host_out[kd] = !is_device_ptr(outs[kd]);
+        if (host_out[kd]) {
+            off[kd] = staged;
+            staged += kind_elems(kd, mesh->nV) * nfreq * esz;
+        }
+    }
+    if (staged) SOD_TRY(ctx->staging.ensure(staged));
+    for (int kd = 0; kd < 4; kd++) {
+        L.freq_stride[kd] = (long long)kind_elems(kd, mesh->nV);
+        if (!(mask & (1 << kd))) continue;
+        L.out[kd] = host_out[kd] ? ctx->staging.as<char>() + off[kd] : outs[kd];
     }
     std::vector<KConst<double>> kd(nfreq);
     for (int l = 0; l < nfreq; l++) kd[l] = make_kconst(c1, c2, rho, s[2 * l], s[2 * l + 1]);
-    CollLaunch L;
-    L.mesh = mesh;
-    L.kind = kind;
-    L.nfreq = nfreq;
     L.kc_host = kd.data();
     L.order = order;
     L.subdiv = subdiv;
     L.sorder = sorder;
     L.ssub = ssub;
     L.parts = parts;
-    L.out = dout;
     L.out_dtype = out_dtype;
-    L.freq_stride = (long long)nelem;
     L.stream = ctx->stream;
     SOD_TRY(launch_collocation(ctx, L));
-    if (!dev_out) {
-        SOD_CHECK_CUDA(cudaMemcpyAsync(out, dout, nelem * esz * nfreq, cudaMemcpyDeviceToHost, ctx->stream));
+    if (staged) {
+        for (int kd2 = 0; kd2 < 4; kd2++)
+            if (host_out[kd2])
+                SOD_CHECK_CUDA(cudaMemcpyAsync(outs[kd2], L.out[kd2], kind_elems(kd2, mesh->nV) * nfreq * esz,
+                                               cudaMemcpyDeviceToHost, ctx->stream));
         SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
     }
     return SOD_OK;
+}
+
+int sod_cqbem_assemble_frequencies(sod_context *ctx, const sod_mesh *mesh, int kind, int method, double c1, double c2,
+                                   double rho, const double *s, int nfreq, int order, int subdiv, int sorder, int ssub,
+                                   int parts, void *out, int out_dtype) {
+    SOD_REQUIRE(kind >= SOD_G && kind <= SOD_B_ANGULAR, "kind must be G, H, B_trans or B_angular");
+    void *outs[4] = {nullptr, nullptr, nullptr, nullptr};
+    outs[kind] = out;
+    return assemble_kinds(ctx, mesh, 1 << kind, method, c1, c2, rho, s, nfreq, order, subdiv, sorder, ssub, parts,
+                          outs, out_dtype);
+}
+
+int sod_cqbem_assemble_all(sod_context *ctx, const sod_mesh *mesh, int method, double c1, double c2, double rho,
+                           const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, int parts,
+                           void *out_G, void *out_H, void *out_B_trans, void *out_B_angular, int out_dtype) {
+    void *outs[4] = {out_G, out_H, out_B_trans, out_B_angular};
+    int mask = 0;
+    for (int kd = 0; kd < 4; kd++)
+        if (outs[kd]) mask |= 1 << kd;
+    SOD_REQUIRE(mask != 0, "no output requested");
+    return assemble_kinds(ctx, mesh, mask, method, c1, c2, rho, s, nfreq, order, subdiv, sorder, ssub, parts, outs,
+                          out_dtype);
 }
 
 int sod_cqbem_assemble(sod_context *ctx, const sod_mesh *mesh, int kind, int method, double c1, double c2, double rho,

@@ -1,22 +1,24 @@
 // sod_collocation.cu -- collocation assembly of the Laplace-domain CQBEM matrices on sm_103a.
 //
-// Replaces, for all field vertices at once, the reference's per-row kernels
-//   compute_elastodynamic_{G,H,B_trans,B_angular}_kernel_collocation
-//   (src/elastodynamics_cqbem_{G,H,B_trans,B_angular}_collocation.cu).
+// Replaces, for all field vertices and any set of Laplace frequencies at once, the reference's
+// per-row kernels compute_elastodynamic_{G,H,B_trans,B_angular}_kernel_collocation
+// (src/elastodynamics_cqbem_{G,H,B_trans,B_angular}_collocation.cu).
 //
-// Work split
+// Work split (one CTA per (field vertex i, frequency) in every kernel):
 //   * regular (non-singular) face integrals, FP32:
-//       G, H   : one CTA per (field vertex i, frequency).  The CTA keeps the whole row block
-//                U[3i:3i+3, :] in shared memory and walks the faces in colour order: faces of
-//                one colour share no vertex, so every thread adds its face's three corner blocks
-//                without conflicts, and the summation order is fixed -> bitwise reproducible
-//                results with no atomics.  One __syncthreads() separates colours.
-//       B_t,B_a: one CTA per (i, frequency), per-thread partial sums over faces, fixed-order
+//       G, H   : the CTA keeps the row block U[3i:3i+3, :] in shared memory and walks the faces in
+//                colour order; faces of one colour share no vertex, so every thread adds its face's
+//                three corner blocks without conflicts and the summation order is fixed ->
+//                bitwise reproducible results with no atomics.  One barrier separates colours.
+//       B_t,B_a: fused; per-face moments in registers, per-thread sums over faces, fixed-order
 //                warp/CTA reduction in FP64.
-//   * singular (x_i on the face) integrals, FP64: polar rule (G, B_trans, B_angular,
-//     include/integrator_collocation.hpp:19-63) or Guiggiani's CPV rule (H, :68-124), one warp
-//     per (i, star face), deterministic warp reduction, summed per neighbour slot into a small
-//     FP64 side buffer that the regular kernel's epilogue adds before the single store.
+//   * singular (x_i on the face) integrals, FP64, one warp per star face:
+//       G, B_t, B_a: fused polar rule (include/integrator_collocation.hpp:19-63) -- the FP64
+//                radial terms (two complex exponentials, two psi) are evaluated once for all three;
+//       H       : Guiggiani-Gigante CPV rule (include/integrator_collocation.hpp:68-124).
+//     Deterministic warp reductions; per-neighbour-slot sums land in small FP64 side buffers
+//     that the regular kernels' epilogues add before the single store of each entry.
+#include <algorithm>
 #include <cstdio>
 
 #include "sod_internal.h"
@@ -26,6 +28,8 @@ namespace sod {
 // 1-D Gauss-Legendre rules on [-1,1], orders 1..5 (include/integrator.hpp:117-133 of the reference)
 __constant__ double c_glx[5][5];
 __constant__ double c_glw[5][5];
+
+constexpr int KM_G = 1 << SOD_G, KM_H = 1 << SOD_H, KM_BT = 1 << SOD_B_TRANS, KM_BA = 1 << SOD_B_ANGULAR;
 
 struct FaceRec {
     float3 y1, y2, y3, n;
@@ -49,21 +53,20 @@ __device__ __forceinline__ FaceRec load_face(const float4 *__restrict__ faces, i
 
 struct CollArgs {
     int nV, nF;
-    const float4 *faces;       // coloured (scatter kernels) or natural (reduce kernels) order
-    const int4 *canonF;        // canonical corner ids per face record, or null
-    const int *color_off;      // ncolors+1 (scatter kernels)
+    const float4 *faces;   // coloured (scatter kernels) or natural (reduce kernels) order
+    const int4 *canonF;    // canonical corner ids per face record, or null
+    const int *color_off;  // ncolors+1 (scatter kernels)
     int ncolors;
-    const float *Vf;           // nV x 3
-    const int *canonV;         // canonical id per vertex, or null
-    void *out;
-    int out_c64;               // 1: complex64 output, 0: complex128
-    long long ld;              // row stride of out (elements)
-    long long fstride;         // frequency stride of out (elements)
+    const float *Vf;       // nV x 3
+    const int *canonV;     // canonical id per vertex, or null
+    void *out[4];          // per kind (G, H, B_trans, B_angular)
+    long long fstride[4];  // elements between frequencies of out[kind]
+    int out_c64;           // 1: complex64 output, 0: complex128
     int do_regular;
-    const cd *S;               // singular corrections (null if none)
-    const int *nbr_off;        // G/H: per vertex slot ranges
+    const cd *S[4];        // singular corrections per kind (null if none)
+    long long S_fstride[4];
+    const int *nbr_off;    // G/H: per vertex slot ranges
     const int *nbr_vert;
-    long long S_fstride;       // elements (cd) between frequencies in S
 };
 
 __device__ __forceinline__ bool is_singular(const CollArgs &a, int i, int ci, int f, const FaceRec &fr) {
@@ -97,86 +100,86 @@ __global__ void __launch_bounds__(512, 1) coll_scatter_kernel(CollArgs a, PointT
     __syncthreads();
     if (a.do_regular) {
         for (int c = 0; c < a.ncolors; c++) {
-            const int f = a.color_off[c] + threadIdx.x;
-            if (f < a.color_off[c + 1]) {
+            const int fend = a.color_off[c + 1];
+            for (int f = a.color_off[c] + threadIdx.x; f < fend; f += blockDim.x) {
                 const FaceRec fr = load_face(a.faces, f);
-                if (!is_singular(a, i, ci, f, fr)) {
-                    cf part[3][NC];
+                if (is_singular(a, i, ci, f, fr)) continue;
+                cf part[3][NC];
 #pragma unroll
-                    for (int kk = 0; kk < 3; kk++)
+                for (int kk = 0; kk < 3; kk++)
 #pragma unroll
-                        for (int cc = 0; cc < NC; cc++) part[kk][cc] = mk(0.f, 0.f);
-                    for (int q = 0; q < pt.n; q++) {
-                        const float4 P = pt.p[q];
-                        const float yx = P.x * fr.y1.x + P.y * fr.y2.x + P.z * fr.y3.x;
-                        const float yy = P.x * fr.y1.y + P.y * fr.y2.y + P.z * fr.y3.y;
-                        const float yz = P.x * fr.y1.z + P.y * fr.y2.z + P.z * fr.y3.z;
-                        const float dx = yx - x.x, dy = yy - x.y, dz = yz - x.z;
-                        const float r2 = dx * dx + dy * dy + dz * dz;
-                        const float rinv = rsqrtf(r2);
-                        const float r = r2 * rinv;
-                        const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                        const RadialTerms<float, cf> t = radial<float, cf>(r, k);
-                        cf u[NC];
-                        if (KIND == SOD_G) {
-                            cf al, be;
-                            g_coeffs(t, k, rinv, al, be);
+                    for (int cc = 0; cc < NC; cc++) part[kk][cc] = mk(0.f, 0.f);
+                for (int q = 0; q < pt.n; q++) {
+                    const float4 P = pt.p[q];
+                    const float yx = P.x * fr.y1.x + P.y * fr.y2.x + P.z * fr.y3.x;
+                    const float yy = P.x * fr.y1.y + P.y * fr.y2.y + P.z * fr.y3.y;
+                    const float yz = P.x * fr.y1.z + P.y * fr.y2.z + P.z * fr.y3.z;
+                    const float dx = yx - x.x, dy = yy - x.y, dz = yz - x.z;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    const float rinv = rsqrtf(r2);
+                    const float r = r2 * rinv;
+                    const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
+                    const RadialTerms<float, cf> t = radial<float, cf>(r, k);
+                    cf u[NC];
+                    if (KIND == SOD_G) {
+                        cf al, be;
+                        g_coeffs(t, k, rinv, al, be);
 #pragma unroll
-                            for (int p = 0; p < 3; p++)
+                        for (int p = 0; p < 3; p++)
 #pragma unroll
-                                for (int qq = p; qq < 3; qq++) {
-                                    cf v = al * (rh[p] * rh[qq]);
-                                    if (p == qq) v = v + be;
-                                    u[sym_index(p, qq)] = v;
-                                }
-                        } else {
-                            cf ha, hb, hd;
-                            h_coeffs(t, k, rinv * rinv, ha, hb, hd);
-                            const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
-                            const float rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
-                            const cf hdr = hd * rn, hbr = hb * rn;
+                            for (int qq = p; qq < 3; qq++) {
+                                cf v = al * (rh[p] * rh[qq]);
+                                if (p == qq) v = v + be;
+                                u[sym_index(p, qq)] = v;
+                            }
+                    } else {
+                        cf ha, hb, hd;
+                        h_coeffs(t, k, rinv * rinv, ha, hb, hd);
+                        const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
+                        const float rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
+                        const cf hdr = hd * rn, hbr = hb * rn;
 #pragma unroll
-                            for (int p = 0; p < 3; p++)
+                        for (int p = 0; p < 3; p++)
 #pragma unroll
-                                for (int qq = 0; qq < 3; qq++) {
-                                    cf v = ha * (rh[p] * nn[qq]) + hb * (nn[p] * rh[qq]) + hdr * (rh[p] * rh[qq]);
-                                    if (p == qq) v = v + hbr;
-                                    u[3 * p + qq] = v;
-                                }
-                        }
-                        const float w = P.w * fr.area;
-                        const float wl[3] = {w * P.x, w * P.y, w * P.z};
-#pragma unroll
-                        for (int kk = 0; kk < 3; kk++)
-#pragma unroll
-                            for (int cc = 0; cc < NC; cc++) cfma(part[kk][cc], u[cc], wl[kk]);
+                            for (int qq = 0; qq < 3; qq++) {
+                                cf v = ha * (rh[p] * nn[qq]) + hb * (nn[p] * rh[qq]) + hdr * (rh[p] * rh[qq]);
+                                if (p == qq) v = v + hbr;
+                                u[3 * p + qq] = v;
+                            }
                     }
-                    const int jj[3] = {fr.j0, fr.j1, fr.j2};
+                    const float w = P.w * fr.area;
+                    const float wl[3] = {w * P.x, w * P.y, w * P.z};
 #pragma unroll
                     for (int kk = 0; kk < 3; kk++)
 #pragma unroll
-                        for (int cc = 0; cc < NC; cc++) {
-                            float2 &s = acc[cc * nV + jj[kk]];
-                            s.x += part[kk][cc].x;
-                            s.y += part[kk][cc].y;
-                        }
+                        for (int cc = 0; cc < NC; cc++) cfma(part[kk][cc], u[cc], wl[kk]);
                 }
+                const int jj[3] = {fr.j0, fr.j1, fr.j2};
+#pragma unroll
+                for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+                    for (int cc = 0; cc < NC; cc++) {
+                        float2 &s = acc[cc * nV + jj[kk]];
+                        s.x += part[kk][cc].x;
+                        s.y += part[kk][cc].y;
+                    }
             }
             __syncthreads();
         }
     }
     // epilogue: row block 3 x 3nV
-    const long long base = (long long)fq * a.fstride + (long long)(3 * i) * a.ld;
+    const long long ld = 3LL * nV;
+    const long long base = (long long)fq * a.fstride[KIND] + (long long)(3 * i) * ld;
     const int ncol = 3 * nV;
     for (int p = 0; p < 3; p++) {
         for (int col = threadIdx.x; col < ncol; col += blockDim.x) {
             const int j = col / 3, qq = col - 3 * j;
             const int comp = KIND == SOD_G ? sym_index(p, qq) : 3 * p + qq;
             const float2 v = acc[comp * nV + j];
-            store_out(a.out, a.out_c64, base + p * a.ld + col, v.x, v.y);
+            store_out(a.out[KIND], a.out_c64, base + p * ld + col, v.x, v.y);
         }
     }
-    if (a.S) {
+    if (a.S[KIND]) {
         __syncthreads();
         const int s0 = a.nbr_off[i], ns = a.nbr_off[i + 1] - s0;
         for (int e = threadIdx.x; e < ns * 9; e += blockDim.x) {
@@ -184,18 +187,22 @@ __global__ void __launch_bounds__(512, 1) coll_scatter_kernel(CollArgs a, PointT
             const int j = a.nbr_vert[sl];
             const int comp = KIND == SOD_G ? sym_index(p, qq) : pq;
             const float2 v = acc[comp * nV + j];
-            const cd sv = a.S[(long long)fq * a.S_fstride + (long long)sl * 9 + pq];
-            store_out(a.out, a.out_c64, base + p * a.ld + 3 * j + qq, (double)v.x + sv.x, (double)v.y + sv.y);
+            const cd sv = a.S[KIND][(long long)fq * a.S_fstride[KIND] + (long long)sl * 9 + pq];
+            store_out(a.out[KIND], a.out_c64, base + p * ld + 3 * j + qq, (double)v.x + sv.x, (double)v.y + sv.y);
         }
     }
 }
 
 // -------------------------------------------------------------------------------------------
-// B_trans / B_angular regular reduction kernel
-template <int KIND>
+// B_trans / B_angular regular reduction kernel (MASK subset of KM_BT | KM_BA)
+//   per-face moments (the tensor structure depends only on the face normal):
+//     B_trans   b_pq  = Ms_p n_q + Ms_q n_p + d_pq Md
+//     B_angular b_pqk = M1_pk n_q + M1_qk n_p + (M0 + SB)(d_qk n_p + d_pk n_q) + SC d_pq n_k
+template <int MASK>
 __global__ void __launch_bounds__(256) coll_reduce_kernel(CollArgs a, PointTable pt,
                                                           const __grid_constant__ FreqTable ft) {
-    constexpr int NC = KIND == SOD_B_TRANS ? 6 : 18;  // Ba: (pq sym) x k
+    constexpr bool BT = (MASK & KM_BT) != 0, BA = (MASK & KM_BA) != 0;
+    constexpr int NT = BT ? 6 : 0, NA = BA ? 18 : 0, NC = NT + NA;
     const int i = blockIdx.x, fq = blockIdx.y;
     const KConst<float> k = ft.kf[fq];
     const float3 x = make_float3(a.Vf[3 * i], a.Vf[3 * i + 1], a.Vf[3 * i + 2]);
@@ -208,9 +215,11 @@ __global__ void __launch_bounds__(256) coll_reduce_kernel(CollArgs a, PointTable
             const FaceRec fr = load_face(a.faces, f);
             if (is_singular(a, i, ci, f, fr)) continue;
             const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
-            cf part[NC];
+            cf Ms[3], Md = mk(0.f, 0.f), M1[6], M0 = mk(0.f, 0.f), SB = mk(0.f, 0.f), SC = mk(0.f, 0.f);
 #pragma unroll
-            for (int c = 0; c < NC; c++) part[c] = mk(0.f, 0.f);
+            for (int c = 0; c < 3; c++) Ms[c] = mk(0.f, 0.f);
+#pragma unroll
+            for (int c = 0; c < 6; c++) M1[c] = mk(0.f, 0.f);
             for (int q = 0; q < pt.n; q++) {
                 const float4 P = pt.p[q];
                 const float dx = P.x * fr.y1.x + P.y * fr.y2.x + P.z * fr.y3.x - x.x;
@@ -220,40 +229,55 @@ __global__ void __launch_bounds__(256) coll_reduce_kernel(CollArgs a, PointTable
                 const float rinv = rsqrtf(r2);
                 const float r = r2 * rinv;
                 const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                const float rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
                 const RadialTerms<float, cf> t = radial<float, cf>(r, k);
                 const float w = P.w;
-                if (KIND == SOD_B_TRANS) {
+                if (BT) {
                     cf sy, di;
                     bt_coeffs(t, k, 1.0f, sy, di);
+                    const cf ws = sy * w;
 #pragma unroll
-                    for (int p = 0; p < 3; p++)
-#pragma unroll
-                        for (int qq = p; qq < 3; qq++) {
-                            cf v = sy * (rh[p] * nn[qq] + rh[qq] * nn[p]);
-                            if (p == qq) v = v + di * rn;
-                            cfma(part[sym_index(p, qq)], v, w);
-                        }
-                } else {
+                    for (int p = 0; p < 3; p++) cfma(Ms[p], ws, rh[p]);
+                    cfma(Md, di, w * (rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2]));
+                }
+                if (BA) {
                     cf A, Bq, Cq;
                     ba_coeffs(t, k, r, 1.0f, A, Bq, Cq);
+                    const cf wA = A * w;
 #pragma unroll
                     for (int p = 0; p < 3; p++)
 #pragma unroll
-                        for (int qq = p; qq < 3; qq++)
-#pragma unroll
-                            for (int kk = 0; kk < 3; kk++) {
-                                const float T1 = rh[p] * rh[kk] * nn[qq] + rh[qq] * rh[kk] * nn[p] +
-                                                 (qq == kk ? nn[p] : 0.f) + (p == kk ? nn[qq] : 0.f);
-                                const float T2 = (qq == kk ? nn[p] : 0.f) + (p == kk ? nn[qq] : 0.f);
-                                const float T3 = p == qq ? nn[kk] : 0.f;
-                                cf v = A * T1 + Bq * T2 + Cq * T3;
-                                cfma(part[3 * sym_index(p, qq) + kk], v, w);
-                            }
+                        for (int kk = p; kk < 3; kk++) cfma(M1[sym_index(p, kk)], wA, rh[p] * rh[kk]);
+                    M0 = M0 + wA;
+                    cfma(SB, Bq, w);
+                    cfma(SC, Cq, w);
                 }
             }
+            const float ar = fr.area;
+            if (BT) {
 #pragma unroll
-            for (int c = 0; c < NC; c++) cfma(accl[c], part[c], fr.area);
+                for (int p = 0; p < 3; p++)
+#pragma unroll
+                    for (int qq = p; qq < 3; qq++) {
+                        cf v = Ms[p] * nn[qq] + Ms[qq] * nn[p];
+                        if (p == qq) v = v + Md;
+                        cfma(accl[sym_index(p, qq)], v, ar);
+                    }
+            }
+            if (BA) {
+                const cf M0B = M0 + SB;
+#pragma unroll
+                for (int p = 0; p < 3; p++)
+#pragma unroll
+                    for (int qq = p; qq < 3; qq++)
+#pragma unroll
+                        for (int kk = 0; kk < 3; kk++) {
+                            cf v = M1[sym_index(p, kk)] * nn[qq] + M1[sym_index(qq, kk)] * nn[p];
+                            const float t2 = (qq == kk ? nn[p] : 0.f) + (p == kk ? nn[qq] : 0.f);
+                            v = v + M0B * t2;
+                            if (p == qq) v = v + SC * nn[kk];
+                            cfma(accl[NT + 3 * sym_index(p, qq) + kk], v, ar);
+                        }
+            }
         }
     }
     // deterministic reduction in FP64: warp butterfly then fixed-order over warps
@@ -271,22 +295,26 @@ __global__ void __launch_bounds__(256) coll_reduce_kernel(CollArgs a, PointTable
     }
     __syncthreads();
     const int nw = blockDim.x >> 5;
-    const long long base = (long long)fq * a.fstride + (long long)(3 * i) * a.ld;
-    if (KIND == SOD_B_TRANS) {
+    if (BT) {
+        const long long base = (long long)fq * a.fstride[SOD_B_TRANS] + (long long)(3 * i) * 3;
         for (int e = threadIdx.x; e < 9; e += blockDim.x) {
             const int p = e / 3, qq = e % 3;
             cd s = mk(0.0, 0.0);
             for (int w = 0; w < nw; w++) s = s + wsum[w][sym_index(p, qq)];
-            if (a.S) s = s + a.S[(long long)fq * a.S_fstride + (long long)i * 9 + e];
-            store_out(a.out, a.out_c64, base + p * a.ld + qq, s.x, s.y);
+            if (a.S[SOD_B_TRANS])
+                s = s + a.S[SOD_B_TRANS][(long long)fq * a.S_fstride[SOD_B_TRANS] + (long long)i * 9 + e];
+            store_out(a.out[SOD_B_TRANS], a.out_c64, base + e, s.x, s.y);
         }
-    } else {
+    }
+    if (BA) {
+        const long long base = (long long)fq * a.fstride[SOD_B_ANGULAR] + (long long)(3 * i) * 9;
         for (int e = threadIdx.x; e < 27; e += blockDim.x) {
             const int p = e / 9, qq = (e / 3) % 3, kk = e % 3;
             cd s = mk(0.0, 0.0);
-            for (int w = 0; w < nw; w++) s = s + wsum[w][3 * sym_index(p, qq) + kk];
-            if (a.S) s = s + a.S[(long long)fq * a.S_fstride + (long long)i * 27 + e];
-            store_out(a.out, a.out_c64, base + p * a.ld + 3 * qq + kk, s.x, s.y);
+            for (int w = 0; w < nw; w++) s = s + wsum[w][NT + 3 * sym_index(p, qq) + kk];
+            if (a.S[SOD_B_ANGULAR])
+                s = s + a.S[SOD_B_ANGULAR][(long long)fq * a.S_fstride[SOD_B_ANGULAR] + (long long)i * 27 + e];
+            store_out(a.out[SOD_B_ANGULAR], a.out_c64, base + e, s.x, s.y);
         }
     }
 }
@@ -301,8 +329,8 @@ struct SingArgs {
     const int *star_off, *star_face, *star_corner, *star_slot;
     const int *nbr_off;
     int sorder, ssub;
-    cd *S;
-    long long S_fstride;
+    cd *S[4];
+    long long S_fstride[4];
 };
 
 constexpr int MAX_STAR = 32;
@@ -320,7 +348,6 @@ __device__ __forceinline__ double3 nrmz(double3 a) {
     const double n = norm3(a);
     return n > 0.0 ? a * (1.0 / n) : a;
 }
-__device__ __forceinline__ double comp3(double3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
 
 // barycentrics of P in (A,B,C), clamped (include/barycentric_coordinates.cuh:14-38)
 __device__ __forceinline__ void bary_clamped(double3 P, double3 A, double3 B, double3 C, double L[3]) {
@@ -333,8 +360,7 @@ __device__ __forceinline__ void bary_clamped(double3 P, double3 A, double3 B, do
     for (int c = 0; c < 3; c++) L[c] = fmin(1.0, fmax(0.0, L[c]));
 }
 
-template <int NVAL>
-__device__ __forceinline__ void warp_sum(cd (&v)[NVAL]) {
+template <int NVAL> __device__ __forceinline__ void warp_sum(cd (&v)[NVAL]) {
 #pragma unroll
     for (int c = 0; c < NVAL; c++) {
 #pragma unroll
@@ -381,11 +407,141 @@ __device__ __forceinline__ void polar_point(const Polar &g, int pidx, int sorder
     w = c_glw[sorder - 1][tq] * (tb - ta) / 2. * c_glw[sorder - 1][rq] * (rb - ra) / 2.;
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(256) coll_singular_kernel(SingArgs a, const __grid_constant__ FreqTable ft) {
-    constexpr int NC = KIND == SOD_G ? 6 : (KIND == SOD_H ? 9 : (KIND == SOD_B_TRANS ? 6 : 18));
-    constexpr int NCORN = (KIND == SOD_G || KIND == SOD_H) ? 3 : 1;
-    __shared__ cd fres[MAX_STAR][NCORN * NC];
+// Sum the per-face results of the star of i into the neighbour slots of G/H (9 comps per slot)
+template <int NC, int STRIDE>
+__device__ __forceinline__ void scatter_slots(const SingArgs &a, int kind, int i, int fq, int s0, int ns,
+                                              const cd (*fres)[STRIDE], int off, bool sym) {
+    const int n0 = a.nbr_off[i], nsl = a.nbr_off[i + 1] - n0;
+    cd *S = a.S[kind] + (long long)fq * a.S_fstride[kind];
+    for (int e = threadIdx.x; e < nsl * 9; e += blockDim.x) {
+        const int sl = n0 + e / 9, pq = e % 9, p = pq / 3, qq = pq % 3;
+        const int comp = sym ? sym_index(p, qq) : pq;
+        cd s = mk(0.0, 0.0);
+        for (int si = 0; si < ns; si++)
+            for (int c = 0; c < 3; c++)
+                if (a.star_slot[3 * (s0 + si) + c] == sl) s = s + fres[si][off + c * NC + comp];
+        S[(long long)sl * 9 + pq] = s;
+    }
+}
+
+// Fused polar-rule kernel for G (MASK & KM_G), B_trans, B_angular: the FP64 radial terms are
+// evaluated once per point for every requested kind.
+template <int MASK>
+__global__ void __launch_bounds__(256) coll_polar_kernel(SingArgs a, const __grid_constant__ FreqTable ft) {
+    constexpr bool DG = (MASK & KM_G) != 0, DT = (MASK & KM_BT) != 0, DA = (MASK & KM_BA) != 0;
+    constexpr int NG = DG ? 18 : 0, NT = DT ? 6 : 0, NA = DA ? 18 : 0;  // per-face result sizes
+    constexpr int OG = 0, OT = NG, OA = NG + NT, STRIDE = NG + NT + NA;
+    __shared__ cd fres[MAX_STAR][STRIDE];
+    const int i = blockIdx.x, fq = blockIdx.y;
+    const KConst<double> k = ft.kd[fq];
+    const int s0 = a.star_off[i], ns = min(a.star_off[i + 1] - a.star_off[i], MAX_STAR);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nq = a.sorder * a.ssub;
+    // accumulators: G corners x 6 sym comps, B_trans moments (Ms[3], Md), B_angular moments
+    // (M1[6], M0, SB, SC)
+    constexpr int NACC = (DG ? 18 : 0) + (DT ? 4 : 0) + (DA ? 9 : 0);
+    constexpr int AG = 0, AT = DG ? 18 : 0, AA = AT + (DT ? 4 : 0);
+    for (int si = warp; si < ns; si += nw) {
+        const int f = a.star_face[s0 + si], sc = a.star_corner[s0 + si];
+        const int jj[3] = {a.F[3 * f + sc], a.F[3 * f + (sc + 1) % 3], a.F[3 * f + (sc + 2) % 3]};
+        const double3 y1 = ld3(a.V, jj[0]), y2 = ld3(a.V, jj[1]), y3 = ld3(a.V, jj[2]);
+        const double3 n = ld3(a.N, f);
+        const double nn[3] = {n.x, n.y, n.z};
+        cd acc[NACC];
+#pragma unroll
+        for (int c = 0; c < NACC; c++) acc[c] = mk(0.0, 0.0);
+        const Polar g = polar_setup(y1, y2, y3);
+        for (int pidx = lane; pidx < nq * nq; pidx += 32) {
+            double r, w;
+            double3 rh;
+            polar_point(g, pidx, a.sorder, a.ssub, r, rh, w);
+            const double rr[3] = {rh.x, rh.y, rh.z};
+            const RadialTerms<double, cd> t = radial<double, cd>(r, k);
+            if (DG) {
+                double L[3];
+                bary_clamped(y1 + rh * r, y1, y2, y3, L);
+                cd al, be;
+                g_coeffs(t, k, 1.0, al, be);  // r * u
+#pragma unroll
+                for (int p = 0; p < 3; p++)
+#pragma unroll
+                    for (int qq = p; qq < 3; qq++) {
+                        cd v = al * (rr[p] * rr[qq]);
+                        if (p == qq) v = v + be;
+#pragma unroll
+                        for (int c = 0; c < 3; c++) cfma(acc[AG + c * 6 + sym_index(p, qq)], v, w * L[c]);
+                    }
+            }
+            if (DT) {
+                cd sy, di;
+                bt_coeffs(t, k, r, sy, di);  // r * b
+                const cd ws = sy * w;
+#pragma unroll
+                for (int p = 0; p < 3; p++) cfma(acc[AT + p], ws, rr[p]);
+                cfma(acc[AT + 3], di, w * dot3(rh, n));
+            }
+            if (DA) {
+                cd A, Bq, Cq;
+                ba_coeffs(t, k, r, r, A, Bq, Cq);  // r * b
+                const cd wA = A * w;
+#pragma unroll
+                for (int p = 0; p < 3; p++)
+#pragma unroll
+                    for (int kk = p; kk < 3; kk++) cfma(acc[AA + sym_index(p, kk)], wA, rr[p] * rr[kk]);
+                acc[AA + 6] = acc[AA + 6] + wA;
+                cfma(acc[AA + 7], Bq, w);
+                cfma(acc[AA + 8], Cq, w);
+            }
+        }
+        warp_sum<NACC>(acc);
+        if (lane == 0) {
+            if (DG)
+                for (int c = 0; c < 18; c++) fres[si][OG + c] = acc[AG + c];
+            if (DT)
+                for (int p = 0; p < 3; p++)
+                    for (int qq = p; qq < 3; qq++) {
+                        cd v = acc[AT + p] * nn[qq] + acc[AT + qq] * nn[p];
+                        if (p == qq) v = v + acc[AT + 3];
+                        fres[si][OT + sym_index(p, qq)] = v;
+                    }
+            if (DA) {
+                const cd M0B = acc[AA + 6] + acc[AA + 7];
+                for (int p = 0; p < 3; p++)
+                    for (int qq = p; qq < 3; qq++)
+                        for (int kk = 0; kk < 3; kk++) {
+                            cd v = acc[AA + sym_index(p, kk)] * nn[qq] + acc[AA + sym_index(qq, kk)] * nn[p];
+                            v = v + M0B * ((qq == kk ? nn[p] : 0.0) + (p == kk ? nn[qq] : 0.0));
+                            if (p == qq) v = v + acc[AA + 8] * nn[kk];
+                            fres[si][OA + 3 * sym_index(p, qq) + kk] = v;
+                        }
+            }
+        }
+    }
+    __syncthreads();
+    if (DG) scatter_slots<6, STRIDE>(a, SOD_G, i, fq, s0, ns, fres, OG, true);
+    if (DT) {
+        cd *S = a.S[SOD_B_TRANS] + (long long)fq * a.S_fstride[SOD_B_TRANS] + (long long)i * 9;
+        for (int e = threadIdx.x; e < 9; e += blockDim.x) {
+            cd s = mk(0.0, 0.0);
+            for (int si = 0; si < ns; si++) s = s + fres[si][OT + sym_index(e / 3, e % 3)];
+            S[e] = s;
+        }
+    }
+    if (DA) {
+        cd *S = a.S[SOD_B_ANGULAR] + (long long)fq * a.S_fstride[SOD_B_ANGULAR] + (long long)i * 27;
+        for (int e = threadIdx.x; e < 27; e += blockDim.x) {
+            const int p = e / 9, qq = (e / 3) % 3, kk = e % 3;
+            cd s = mk(0.0, 0.0);
+            for (int si = 0; si < ns; si++) s = s + fres[si][OA + 3 * sym_index(p, qq) + kk];
+            S[e] = s;
+        }
+    }
+}
+
+// Guiggiani-Gigante rule for the strongly singular H faces (include/integrator_collocation.hpp:68-124)
+__global__ void __launch_bounds__(256) coll_guiggiani_kernel(SingArgs a, const __grid_constant__ FreqTable ft) {
+    constexpr int NC = 9;
+    __shared__ cd fres[MAX_STAR][3 * NC];
     const int i = blockIdx.x, fq = blockIdx.y;
     const KConst<double> k = ft.kd[fq];
     const int s0 = a.star_off[i], ns = min(a.star_off[i + 1] - a.star_off[i], MAX_STAR);
@@ -397,143 +553,63 @@ __global__ void __launch_bounds__(256) coll_singular_kernel(SingArgs a, const __
         const double3 y1 = ld3(a.V, jj[0]), y2 = ld3(a.V, jj[1]), y3 = ld3(a.V, jj[2]);
         const double3 n = ld3(a.N, f);
         const double nn[3] = {n.x, n.y, n.z};
-        cd acc[NCORN * NC];
+        cd acc[3 * NC];
 #pragma unroll
-        for (int c = 0; c < NCORN * NC; c++) acc[c] = mk(0.0, 0.0);
-        if (KIND != SOD_H) {
-            const Polar g = polar_setup(y1, y2, y3);
-            for (int pidx = lane; pidx < nq * nq; pidx += 32) {
-                double r, w;
-                double3 rh;
-                polar_point(g, pidx, a.sorder, a.ssub, r, rh, w);
-                const double rr[3] = {rh.x, rh.y, rh.z};
-                const RadialTerms<double, cd> t = radial<double, cd>(r, k);
-                if (KIND == SOD_G) {
-                    double L[3];
-                    bary_clamped(y1 + rh * r, y1, y2, y3, L);
-                    cd al, be;
-                    g_coeffs(t, k, 1.0, al, be);  // r * u
+        for (int c = 0; c < 3 * NC; c++) acc[c] = mk(0.0, 0.0);
+        const double3 v1 = y2 - y1, v2 = y3 - y1;
+        const double J = norm3(cross3(v1, v2));
+        const double kc = k.inv4pi * k.kappa;
+        const double tmax = CUDART_PI / 2.;
+        for (int pidx = lane; pidx < nq * nq; pidx += 32) {
+            const int ti = pidx / nq, ri = pidx % nq;
+            const int ts = ti / a.sorder, tq = ti % a.sorder, rs = ri / a.sorder, rq = ri % a.sorder;
+            const double ta = tmax * ts / a.ssub, tb = tmax * (ts + 1) / a.ssub;
+            const double th = (tb - ta) * c_glx[a.sorder - 1][tq] / 2. + (ta + tb) / 2.;
+            const double wt = c_glw[a.sorder - 1][tq] * (tb - ta) / 2.;
+            double st, ct;
+            sincos(th, &st, &ct);
+            const double3 Av = v1 * ct + v2 * st;
+            const double A = norm3(Av);
+            const double3 Ah = nrmz(Av);
+            const double ah[3] = {Ah.x, Ah.y, Ah.z};
+            const double rho_bar = 1. / (cos(th - CUDART_PI / 4.) * sqrt(2.));
+            const double ra = rho_bar * rs / a.ssub, rb = rho_bar * (rs + 1) / a.ssub;
+            const double rho = (rb - ra) * c_glx[a.sorder - 1][rq] / 2. + (ra + rb) / 2.;
+            const double w = wt * c_glw[a.sorder - 1][rq] * (rb - ra) / 2.;
+            const double L[3] = {1. - rho * (ct + st), rho * ct, rho * st};
+            const double3 rv = Av * rho;
+            const double r = norm3(rv);
+            const double3 rh = nrmz(rv);
+            const double rr[3] = {rh.x, rh.y, rh.z};
+            const double rn = dot3(rh, n);
+            const RadialTerms<double, cd> t = radial<double, cd>(r, k);
+            cd ha, hb, hd;
+            h_coeffs(t, k, 1.0 / (r * r), ha, hb, hd);
+            const double logt = (ri == 0) ? log(rho_bar * A) : 0.0;
 #pragma unroll
-                    for (int p = 0; p < 3; p++)
+            for (int p = 0; p < 3; p++)
 #pragma unroll
-                        for (int qq = p; qq < 3; qq++) {
-                            cd v = al * (rr[p] * rr[qq]);
-                            if (p == qq) v = v + be;
+                for (int qq = 0; qq < 3; qq++) {
+                    cd v = ha * (rr[p] * nn[qq]) + hb * (nn[p] * rr[qq]) + hd * (rn * rr[p] * rr[qq]);
+                    if (p == qq) v = v + hb * rn;
+                    const double f0 = kc * (ah[p] * nn[qq] - ah[qq] * nn[p]) / (A * A) * J;
 #pragma unroll
-                            for (int c = 0; c < 3; c++) cfma(acc[c * NC + sym_index(p, qq)], v, w * L[c]);
-                        }
-                } else if (KIND == SOD_B_TRANS) {
-                    const double rn = dot3(rh, n);
-                    cd sy, di;
-                    bt_coeffs(t, k, r, sy, di);  // r * b
-#pragma unroll
-                    for (int p = 0; p < 3; p++)
-#pragma unroll
-                        for (int qq = p; qq < 3; qq++) {
-                            cd v = sy * (rr[p] * nn[qq] + rr[qq] * nn[p]);
-                            if (p == qq) v = v + di * rn;
-                            cfma(acc[sym_index(p, qq)], v, w);
-                        }
-                } else {
-                    cd A, Bq, Cq;
-                    ba_coeffs(t, k, r, r, A, Bq, Cq);  // r * b
-#pragma unroll
-                    for (int p = 0; p < 3; p++)
-#pragma unroll
-                        for (int qq = p; qq < 3; qq++)
-#pragma unroll
-                            for (int kk = 0; kk < 3; kk++) {
-                                const double T1 = rr[p] * rr[kk] * nn[qq] + rr[qq] * rr[kk] * nn[p] +
-                                                  (qq == kk ? nn[p] : 0.0) + (p == kk ? nn[qq] : 0.0);
-                                const double T2 = (qq == kk ? nn[p] : 0.0) + (p == kk ? nn[qq] : 0.0);
-                                const double T3 = p == qq ? nn[kk] : 0.0;
-                                cd v = A * T1 + Bq * T2 + Cq * T3;
-                                cfma(acc[3 * sym_index(p, qq) + kk], v, w);
-                            }
+                    for (int c = 0; c < 3; c++) cfma(acc[c * NC + 3 * p + qq], v, w * L[c] * J * rho);
+                    acc[3 * p + qq].x += -w * f0 / rho + wt * f0 * logt;
                 }
-            }
-        } else {
-            // Guiggiani-Gigante rule (include/integrator_collocation.hpp:68-124)
-            const double3 v1 = y2 - y1, v2 = y3 - y1;
-            const double J = norm3(cross3(v1, v2));
-            const double kc = k.inv4pi * k.kappa;
-            const double tmax = CUDART_PI / 2.;
-            for (int pidx = lane; pidx < nq * nq; pidx += 32) {
-                const int ti = pidx / nq, ri = pidx % nq;
-                const int ts = ti / a.sorder, tq = ti % a.sorder, rs = ri / a.sorder, rq = ri % a.sorder;
-                const double ta = tmax * ts / a.ssub, tb = tmax * (ts + 1) / a.ssub;
-                const double th = (tb - ta) * c_glx[a.sorder - 1][tq] / 2. + (ta + tb) / 2.;
-                const double wt = c_glw[a.sorder - 1][tq] * (tb - ta) / 2.;
-                double st, ct;
-                sincos(th, &st, &ct);
-                const double3 Av = v1 * ct + v2 * st;
-                const double A = norm3(Av);
-                const double3 Ah = nrmz(Av);
-                const double ah[3] = {Ah.x, Ah.y, Ah.z};
-                const double rho_bar = 1. / (cos(th - CUDART_PI / 4.) * sqrt(2.));
-                const double ra = rho_bar * rs / a.ssub, rb = rho_bar * (rs + 1) / a.ssub;
-                const double rho = (rb - ra) * c_glx[a.sorder - 1][rq] / 2. + (ra + rb) / 2.;
-                const double w = wt * c_glw[a.sorder - 1][rq] * (rb - ra) / 2.;
-                const double L[3] = {1. - rho * (ct + st), rho * ct, rho * st};
-                const double3 rv = Av * rho;
-                const double r = norm3(rv);
-                const double3 rh = nrmz(rv);
-                const double rr[3] = {rh.x, rh.y, rh.z};
-                const double rn = dot3(rh, n);
-                const RadialTerms<double, cd> t = radial<double, cd>(r, k);
-                cd ha, hb, hd;
-                h_coeffs(t, k, 1.0 / (r * r), ha, hb, hd);
-                const double logt = (ri == 0) ? log(rho_bar * A) : 0.0;
-#pragma unroll
-                for (int p = 0; p < 3; p++)
-#pragma unroll
-                    for (int qq = 0; qq < 3; qq++) {
-                        cd v = ha * (rr[p] * nn[qq]) + hb * (nn[p] * rr[qq]) + hd * (rn * rr[p] * rr[qq]);
-                        if (p == qq) v = v + hb * rn;
-                        const double f0 = kc * (ah[p] * nn[qq] - ah[qq] * nn[p]) / (A * A) * J;
-#pragma unroll
-                        for (int c = 0; c < 3; c++) cfma(acc[c * NC + 3 * p + qq], v, w * L[c] * J * rho);
-                        acc[3 * p + qq].x += -w * f0 / rho + wt * f0 * logt;
-                    }
-            }
         }
-        warp_sum<NCORN * NC>(acc);
-        if (lane == 0 && si < MAX_STAR) {
+        warp_sum<3 * NC>(acc);
+        if (lane == 0) {
 #pragma unroll
-            for (int c = 0; c < NCORN * NC; c++) fres[si][c] = acc[c];
+            for (int c = 0; c < 3 * NC; c++) fres[si][c] = acc[c];
         }
     }
     __syncthreads();
-    const long long sb = (long long)fq * a.S_fstride;
-    if (KIND == SOD_G || KIND == SOD_H) {
-        const int n0 = a.nbr_off[i], nsl = a.nbr_off[i + 1] - n0;
-        for (int e = threadIdx.x; e < nsl * 9; e += blockDim.x) {
-            const int sl = n0 + e / 9, pq = e % 9, p = pq / 3, qq = pq % 3;
-            const int comp = KIND == SOD_G ? sym_index(p, qq) : pq;
-            cd s = mk(0.0, 0.0);
-            for (int si = 0; si < ns; si++)
-                for (int c = 0; c < 3; c++)
-                    if (a.star_slot[3 * (s0 + si) + c] == sl) s = s + fres[si][c * NC + comp];
-            a.S[sb + (long long)sl * 9 + pq] = s;
-        }
-    } else if (KIND == SOD_B_TRANS) {
-        for (int e = threadIdx.x; e < 9; e += blockDim.x) {
-            cd s = mk(0.0, 0.0);
-            for (int si = 0; si < ns; si++) s = s + fres[si][sym_index(e / 3, e % 3)];
-            a.S[sb + (long long)i * 9 + e] = s;
-        }
-    } else {
-        for (int e = threadIdx.x; e < 27; e += blockDim.x) {
-            const int p = e / 9, qq = (e / 3) % 3, kk = e % 3;
-            cd s = mk(0.0, 0.0);
-            for (int si = 0; si < ns; si++) s = s + fres[si][3 * sym_index(p, qq) + kk];
-            a.S[sb + (long long)i * 27 + e] = s;
-        }
-    }
+    scatter_slots<9, 3 * NC>(a, SOD_H, i, fq, s0, ns, fres, 0, false);
 }
 
 // -------------------------------------------------------------------------------------------
-// host launcher
+// host side
 static bool g_const_ready[64] = {};
 
 static int ensure_gl_constants(int device) {
@@ -550,41 +626,91 @@ static int ensure_gl_constants(int device) {
     return SOD_OK;
 }
 
+// Autotuner for the scatter kernels.  A CTA walks the faces colour by colour with one barrier per
+// colour, so a colour with fewer faces than threads leaves lanes idle and a CTA with few warps
+// cannot hide the barrier.  For every candidate CTA size T (multiples of 32 up to 512) the mesh is
+// coloured with capacity T and the cost is modelled as
+//     slots(T) / occupancy(T),   slots = ncolours * T,
+//     occupancy = min(1, resident warps per SM / 24)  (shared memory and register limits).
+// The choice depends only on the mesh and the device limits, so results stay bitwise reproducible.
+int autotune_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int *threads) {
+    const int slot = kind == SOD_G ? 0 : 1;
+    if (m->tuned_threads[slot] > 0) {
+        *threads = m->tuned_threads[slot];
+        return SOD_OK;
+    }
+    const size_t smem = sizeof(float2) * (kind == SOD_G ? 6 : 9) * (size_t)m->nV + 1024;
+    const int regs = kind == SOD_G ? 112 : 128;
+    const size_t smem_sm = 228 * 1024;
+    double best = 1e300;
+    int bestT = 128;
+    for (int T = 32; T <= 512; T += 32) {
+        const sod_mesh::Coloured *col = nullptr;
+        SOD_TRY(m->coloured_for(T, &col));
+        const int by_smem = (int)std::max<size_t>(1, smem_sm / smem);
+        const int by_regs = std::max(1, 65536 / (regs * T));
+        const int by_warps = std::max(1, 64 / (T / 32));
+        const int ctas = std::min(std::min(by_smem, by_regs), by_warps);
+        const double warps = (double)ctas * T / 32.0;
+        const double occ = std::min(1.0, warps / 24.0);
+        const double cost = (double)col->ncolors * T / occ;
+        if (cost < best * 0.999) {
+            best = cost;
+            bestT = T;
+        }
+    }
+    m->tuned_threads[slot] = bestT;
+    *threads = bestT;
+    (void)ctx;
+    return SOD_OK;
+}
+
 int launch_collocation(sod_context *ctx, const CollLaunch &L) {
     const sod_mesh *m = L.mesh;
+    const int mask = L.kind_mask;
+    SOD_REQUIRE(mask > 0 && mask < 16, "empty kind set");
     SOD_TRY(ensure_gl_constants(ctx->device));
     PointTable pt;
     SOD_TRY(make_point_table(L.order, L.subdiv, pt));
     SOD_REQUIRE(L.sorder >= 1 && L.sorder <= 5 && L.ssub >= 1 && L.ssub <= 8,
                 "singular quadrature order must be 1..5, subdivision 1..8");
     const bool sing = (L.parts & SOD_PART_SINGULAR) != 0;
-    const bool gh = L.kind == SOD_G || L.kind == SOD_H;
-    const int ncomp_s = L.kind == SOD_B_ANGULAR ? 27 : 9;
-    const long long s_fstride = gh ? (long long)m->nbr_off.back() * 9 : (long long)m->nV * ncomp_s;
     const int chunk = std::min(L.nfreq, MAX_FREQ_PER_LAUNCH);
-    cd *S = nullptr;
+    // singular side buffers (per kind, one chunk of frequencies)
+    const long long nslots = m->nbr_off.back();
+    const long long sfs[4] = {nslots * 9, nslots * 9, (long long)m->nV * 9, (long long)m->nV * 27};
+    long long soff[4] = {0, 0, 0, 0}, stot = 0;
+    for (int kd = 0; kd < 4; kd++)
+        if (mask & (1 << kd)) {
+            soff[kd] = stot;
+            stot += sfs[kd] * chunk;
+        }
+    cd *Sb = nullptr;
     if (sing) {
-        SOD_TRY(ctx->sing.ensure(sizeof(cd) * (size_t)s_fstride * chunk));
-        S = ctx->sing.as<cd>();
+        SOD_TRY(ctx->sing.ensure(sizeof(cd) * (size_t)stot));
+        Sb = ctx->sing.as<cd>();
     }
-    int threads = 256;
-    const sod_mesh::Coloured *col = nullptr;
-    size_t smem = 0;
-    if (gh) {
-        threads = ctx->coll_threads;
-        if (threads <= 0) threads = m->nF >= 4096 ? 512 : (m->nF >= 1024 ? 256 : 128);
-        threads = std::max(32, std::min(512, (threads / 32) * 32));
-        SOD_TRY(const_cast<sod_mesh *>(m)->coloured_for(threads, &col));
-        smem = sizeof(float2) * (L.kind == SOD_G ? 6 : 9) * (size_t)m->nV;
-        if (smem > ctx->smem_optin) {
+    // scatter kernel configuration
+    int threads[2] = {0, 0};
+    const sod_mesh::Coloured *col[2] = {nullptr, nullptr};
+    size_t smem[2] = {0, 0};
+    for (int kd = 0; kd < 2; kd++) {
+        if (!(mask & (1 << kd))) continue;
+        int T = ctx->coll_threads;
+        if (T <= 0) SOD_TRY(autotune_scatter_threads(ctx, const_cast<sod_mesh *>(m), kd, &T));
+        T = std::max(32, std::min(512, (T / 32) * 32));
+        threads[kd] = T;
+        SOD_TRY(const_cast<sod_mesh *>(m)->coloured_for(T, &col[kd]));
+        smem[kd] = sizeof(float2) * (kd == SOD_G ? 6 : 9) * (size_t)m->nV;
+        if (smem[kd] > ctx->smem_optin) {
             set_error("mesh too large for the shared-memory row accumulator (" + std::to_string(m->nV) + " vertices)");
             return SOD_ERR_UNSUPPORTED;
         }
-        if (L.kind == SOD_G)
-            SOD_CHECK_CUDA(cudaFuncSetAttribute(coll_scatter_kernel<SOD_G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        else
-            SOD_CHECK_CUDA(cudaFuncSetAttribute(coll_scatter_kernel<SOD_H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const void *fn = kd == SOD_G ? (const void *)coll_scatter_kernel<SOD_G> : (const void *)coll_scatter_kernel<SOD_H>;
+        SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[kd]));
+        SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     }
+    const size_t esz = L.out_dtype == SOD_C64 ? 8 : 16;
     for (int f0 = 0; f0 < L.nfreq; f0 += chunk) {
         const int nf = std::min(chunk, L.nfreq - f0);
         FreqTable ft;
@@ -594,65 +720,85 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
             ft.kf[l] = to_float(ft.kd[l]);
         }
         const dim3 grid(m->nV, nf);
+        SingArgs sa{};
+        sa.nV = m->nV;
+        sa.V = m->dV.as<double>();
+        sa.F = m->dF.as<int>();
+        sa.N = m->dN.as<double>();
+        sa.star_off = m->dStarOff.as<int>();
+        sa.star_face = m->dStarFace.as<int>();
+        sa.star_corner = m->dStarCorner.as<int>();
+        sa.star_slot = m->dStarSlot.as<int>();
+        sa.nbr_off = m->dNbrOff.as<int>();
+        sa.sorder = L.sorder;
+        sa.ssub = L.ssub;
+        for (int kd = 0; kd < 4; kd++) {
+            sa.S[kd] = (sing && (mask & (1 << kd))) ? Sb + soff[kd] : nullptr;
+            sa.S_fstride[kd] = sfs[kd];
+        }
         if (sing) {
-            SingArgs sa;
-            sa.nV = m->nV;
-            sa.V = m->dV.as<double>();
-            sa.F = m->dF.as<int>();
-            sa.N = m->dN.as<double>();
-            sa.star_off = m->dStarOff.as<int>();
-            sa.star_face = m->dStarFace.as<int>();
-            sa.star_corner = m->dStarCorner.as<int>();
-            sa.star_slot = m->dStarSlot.as<int>();
-            sa.nbr_off = m->dNbrOff.as<int>();
-            sa.sorder = L.sorder;
-            sa.ssub = L.ssub;
-            sa.S = S;
-            sa.S_fstride = s_fstride;
-            switch (L.kind) {
-            case SOD_G: coll_singular_kernel<SOD_G><<<grid, 256, 0, L.stream>>>(sa, ft); break;
-            case SOD_H: coll_singular_kernel<SOD_H><<<grid, 256, 0, L.stream>>>(sa, ft); break;
-            case SOD_B_TRANS: coll_singular_kernel<SOD_B_TRANS><<<grid, 256, 0, L.stream>>>(sa, ft); break;
-            default: coll_singular_kernel<SOD_B_ANGULAR><<<grid, 256, 0, L.stream>>>(sa, ft); break;
+            const int pm = mask & (KM_G | KM_BT | KM_BA);
+            switch (pm) {
+            case 0: break;
+            case KM_G: coll_polar_kernel<KM_G><<<grid, 256, 0, L.stream>>>(sa, ft); break;
+            case KM_BT: coll_polar_kernel<KM_BT><<<grid, 256, 0, L.stream>>>(sa, ft); break;
+            case KM_BA: coll_polar_kernel<KM_BA><<<grid, 256, 0, L.stream>>>(sa, ft); break;
+            case KM_BT | KM_BA: coll_polar_kernel<KM_BT | KM_BA><<<grid, 256, 0, L.stream>>>(sa, ft); break;
+            case KM_G | KM_BT: coll_polar_kernel<KM_G | KM_BT><<<grid, 256, 0, L.stream>>>(sa, ft); break;
+            case KM_G | KM_BA: coll_polar_kernel<KM_G | KM_BA><<<grid, 256, 0, L.stream>>>(sa, ft); break;
+            default: coll_polar_kernel<KM_G | KM_BT | KM_BA><<<grid, 256, 0, L.stream>>>(sa, ft); break;
             }
-            SOD_CHECK_CUDA(cudaGetLastError());
-            ctx->count();
+            if (pm) {
+                SOD_CHECK_CUDA(cudaGetLastError());
+                ctx->count();
+            }
+            if (mask & KM_H) {
+                coll_guiggiani_kernel<<<grid, 256, 0, L.stream>>>(sa, ft);
+                SOD_CHECK_CUDA(cudaGetLastError());
+                ctx->count();
+            }
         }
         CollArgs a{};
         a.nV = m->nV;
         a.nF = m->nF;
         a.Vf = m->dVf.as<float>();
         a.canonV = m->has_vmap ? m->dCanon.as<int>() : nullptr;
-        const size_t esz = L.out_dtype == SOD_C64 ? 8 : 16;
-        a.out = static_cast<char *>(L.out) + (size_t)f0 * (size_t)L.freq_stride * esz;
         a.out_c64 = L.out_dtype == SOD_C64;
-        a.fstride = L.freq_stride;
         a.do_regular = (L.parts & SOD_PART_REGULAR) != 0;
-        a.S = S;
         a.nbr_off = m->dNbrOff.as<int>();
         a.nbr_vert = m->dNbrVert.as<int>();
-        a.S_fstride = s_fstride;
-        if (gh) {
-            a.faces = col->dFaces.as<float4>();
-            a.canonF = m->has_vmap ? col->dCanonF.as<int4>() : nullptr;
-            a.color_off = col->dOff.as<int>();
-            a.ncolors = col->ncolors;
-            a.ld = 3LL * m->nV;
-            if (L.kind == SOD_G)
-                coll_scatter_kernel<SOD_G><<<grid, threads, smem, L.stream>>>(a, pt, ft);
+        for (int kd = 0; kd < 4; kd++) {
+            a.out[kd] = L.out[kd] ? static_cast<char *>(L.out[kd]) + (size_t)f0 * (size_t)L.freq_stride[kd] * esz : nullptr;
+            a.fstride[kd] = L.freq_stride[kd];
+            a.S[kd] = sa.S[kd];
+            a.S_fstride[kd] = sfs[kd];
+        }
+        for (int kd = 0; kd < 2; kd++) {
+            if (!(mask & (1 << kd))) continue;
+            a.faces = col[kd]->dFaces.as<float4>();
+            a.canonF = m->has_vmap ? col[kd]->dCanonF.as<int4>() : nullptr;
+            a.color_off = col[kd]->dOff.as<int>();
+            a.ncolors = col[kd]->ncolors;
+            if (kd == SOD_G)
+                coll_scatter_kernel<SOD_G><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
             else
-                coll_scatter_kernel<SOD_H><<<grid, threads, smem, L.stream>>>(a, pt, ft);
-        } else {
+                coll_scatter_kernel<SOD_H><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
+            SOD_CHECK_CUDA(cudaGetLastError());
+            ctx->count();
+        }
+        const int rm = mask & (KM_BT | KM_BA);
+        if (rm) {
             a.faces = m->dFacesNat.as<float4>();
             a.canonF = m->has_vmap ? m->dCanonNat.as<int4>() : nullptr;
-            a.ld = L.kind == SOD_B_TRANS ? 3 : 9;
-            if (L.kind == SOD_B_TRANS)
-                coll_reduce_kernel<SOD_B_TRANS><<<grid, 256, 0, L.stream>>>(a, pt, ft);
+            if (rm == KM_BT)
+                coll_reduce_kernel<KM_BT><<<grid, 256, 0, L.stream>>>(a, pt, ft);
+            else if (rm == KM_BA)
+                coll_reduce_kernel<KM_BA><<<grid, 256, 0, L.stream>>>(a, pt, ft);
             else
-                coll_reduce_kernel<SOD_B_ANGULAR><<<grid, 256, 0, L.stream>>>(a, pt, ft);
+                coll_reduce_kernel<KM_BT | KM_BA><<<grid, 256, 0, L.stream>>>(a, pt, ft);
+            SOD_CHECK_CUDA(cudaGetLastError());
+            ctx->count();
         }
-        SOD_CHECK_CUDA(cudaGetLastError());
-        ctx->count();
     }
     return SOD_OK;
 }

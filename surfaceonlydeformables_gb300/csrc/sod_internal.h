@@ -135,6 +135,7 @@ struct sod_mesh {
         sod::DevBuf dOff;
     };
     std::map<int, std::unique_ptr<Coloured>> coloured;
+    int tuned_threads[2] = {0, 0};  // scatter CTA size chosen by the autotuner for G, H (0 = not yet)
     // all faces in natural order (for the reduction kernels and Galerkin)
     sod::DevBuf dFacesNat, dCanonNat;
     int coloured_for(int threads, const Coloured **out);
@@ -151,16 +152,18 @@ struct FreqTable {
 };
 struct CollLaunch {
     const sod_mesh *mesh;
-    int kind;
+    int kind_mask;  // bit k set: assemble kind k (SOD_G .. SOD_B_ANGULAR)
     int nfreq;
     const KConst<double> *kc_host;  // host array, nfreq entries
     int order, subdiv, sorder, ssub, parts;
-    void *out;  // device
+    void *out[4];  // device, per kind (null where the bit is clear)
     int out_dtype;
-    long long freq_stride;  // elements between consecutive frequencies of out
+    long long freq_stride[4];  // elements between consecutive frequencies of out[kind]
     cudaStream_t stream;
 };
 int launch_collocation(sod_context *ctx, const CollLaunch &L);
+// Deterministic autotuner of the scatter kernels' CTA size (see sod_collocation.cu).
+int autotune_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int *threads);
 int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, int64_t M, int nfreq, int L,
                              double R, void *out, int out_dtype, cudaStream_t stream);
 KConst<double> make_kconst(double c1, double c2, double rho, double sr, double si);

@@ -190,3 +190,19 @@ def test_torch_stream_ordering(dev_meshes, sodlib, freqs):
     st.synchronize()
     ref = api.assemble(ctx, m, "H", MAT, freqs[0], dtype=L.C64)
     assert abs(float(total) - np.abs(ref).sum()) < 1e-3 * np.abs(ref).sum()
+
+
+def test_assemble_all_matches_per_kind(gpu_ctx, dev_meshes, meshes, oracle, sodlib):
+    """The fused all-kinds call (shared FP64 radial terms) equals the per-kind calls to FP32 rounding
+    (different kernel instantiations may contract FP32 operations differently) and matches the oracle."""
+    from surfaceonlydeformables_gb300 import api
+
+    s, R, Lq = sodlib.cq_frequencies(2, 0.01, 8)
+    allk = api.assemble_all(gpu_ctx, dev_meshes[2], MAT, s)
+    for kind in KINDS:
+        one = api.assemble_frequencies(gpu_ctx, dev_meshes[2], kind, MAT, s)
+        assert rel_fro(allk[kind], one) < 1e-6, kind
+        ref = oracle.collocation(kind, meshes[2], MAT, s[2])
+        assert rel_fro(allk[kind][2], ref) <= 1e-5, kind
+    part = api.assemble_all(gpu_ctx, dev_meshes[2], MAT, s, kinds=("G", "B_angular"))
+    assert set(part) == {"G", "B_angular"} and rel_fro(part["G"], allk["G"]) < 1e-6
