@@ -129,6 +129,27 @@ int sod_cqbem_assemble_all(sod_context *ctx, const sod_mesh *mesh, int method, d
                            const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, int parts,
                            void *out_G, void *out_H, void *out_B_trans, void *out_B_angular, int out_dtype);
 
+/* Allocation-free variant of sod_cqbem_assemble_frequencies (collocation, one kind).  It has no
+ * counterpart in the reference.  It is for callers that cannot allocate device memory while they
+ * run -- a host program that reserves its whole device memory budget at start-up and forbids
+ * libraries from calling the CUDA allocator, or a real-time step loop in which cudaMalloc (which
+ * may synchronise the device) would break the frame budget.  The call makes no cudaMalloc /
+ * cudaFree or other allocation: its only scratch, the FP64 singular side buffer, is a fixed 4 MiB
+ * device array inside the library (held on every GPU that loads the library until exit).
+ * Requirements and limits:
+ *   - `out` must be device memory; `mesh` must have been assembled once through
+ *     sod_cqbem_assemble* during set-up (that builds the scatter schedule, with allocation);
+ *   - one frequency's side buffer (9 complex doubles per neighbour slot for G/H, 9 or 27 per vertex
+ *     for B_trans/B_angular) must fit in 4 MiB, else SOD_ERR_CAPACITY (G/H: up to about 3600
+ *     vertices); frequencies are processed in chunks that fit;
+ *   - the first call on a device looks up the array's device address (cudaGetSymbolAddress); make
+ *     that first call before any stream capture;
+ *   - all calls share the array: calls whose kernels overlap on the GPU (other streams, other host
+ *     threads) race on it and must be serialised by the caller. */
+int sod_cqbem_assemble_noalloc(sod_context *ctx, const sod_mesh *mesh, int kind, double c1, double c2, double rho,
+                               const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, void *out,
+                               int out_dtype);
+
 /* ---- inverse transform to CQ time weights (FP64-accurate) --------------------------------- */
 /* X_n = R^-n / L * sum_{l=0}^{L/2} c_l Re(Xhat_l zeta^-nl),  c_0 = 1, c_l = 2 otherwise except
  * c_{L/2} = 1 for even L;  n = 0..L-1 (src/elastodynamics_cqbem_G.cu:324-337).

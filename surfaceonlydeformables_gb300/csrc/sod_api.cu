@@ -175,6 +175,8 @@ static bool is_device_ptr(const void *p) {
     return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
+bool is_device_pointer(const void *p) { return is_device_ptr(p); }
+
 template <class T> static int upload(DevBuf &b, const std::vector<T> &v) {
     SOD_TRY(b.ensure(sizeof(T) * std::max<size_t>(v.size(), 1)));
     if (!v.empty()) SOD_CHECK_CUDA(cudaMemcpy(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));

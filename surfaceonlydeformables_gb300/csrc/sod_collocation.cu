@@ -803,4 +803,147 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
     return SOD_OK;
 }
 
+// -------------------------------------------------------------------------------------------
+// Launcher that allocates nothing (for sod_cqbem_assemble_noalloc): the singular side buffer is
+// caller-provided device memory of `scratch_elems` complex doubles, the scatter schedule must
+// already exist on the mesh, the point table is built on the stack, and frequencies are chunked so
+// that one chunk's side buffer fits the scratch.
+static int point_table_on_stack(int order, int subdiv, PointTable &pt) {
+    int nq = 0;
+    const double(*rule)[4] = tri_rule_table(order, nq);
+    SOD_REQUIRE(rule != nullptr, "triangle quadrature order must be 1..5 or 7 (13-point rule)");
+    SOD_REQUIRE(subdiv >= 1 && subdiv <= 4, "quadrature subdivision must be 1..4");
+    double tri[16][9];
+    int nt = 0;
+    const double h = 1.0 / subdiv;
+    auto push = [&](double a0, double b0, double a1, double b1, double a2, double b2) {
+        const double c[9] = {1 - a0 - b0, a0, b0, 1 - a1 - b1, a1, b1, 1 - a2 - b2, a2, b2};
+        for (int t = 0; t < 9; t++) tri[nt][t] = c[t];
+        nt++;
+    };
+    push(0, 0, h, 0, 0, h);
+    for (int i = 0; i < subdiv; i++)
+        for (int j = 0; j < subdiv; j++) {
+            if (!(i == 0 && j == 0) && i + j < subdiv) push(i * h, j * h, (i + 1) * h, j * h, i * h, (j + 1) * h);
+            if (i + j < subdiv - 1) push((i + 1) * h, (j + 1) * h, (i + 1) * h, j * h, i * h, (j + 1) * h);
+        }
+    SOD_REQUIRE(nt * nq <= MAX_TRI_PTS, "too many quadrature points");
+    pt.n = 0;
+    const double ws = 1.0 / ((double)subdiv * subdiv);
+    for (int t = 0; t < nt; t++)
+        for (int q = 0; q < nq; q++) {
+            double l[3];
+            for (int c = 0; c < 3; c++) l[c] = rule[q][0] * tri[t][c] + rule[q][1] * tri[t][3 + c] + rule[q][2] * tri[t][6 + c];
+            pt.p[pt.n++] = make_float4((float)l[0], (float)l[1], (float)l[2], (float)(rule[q][3] * ws));
+        }
+    return SOD_OK;
+}
+
+int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, double c1, double c2, double rho,
+                                const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, void *out,
+                                int out_dtype, cd *scratch, long long scratch_elems, cudaStream_t stream) {
+    SOD_REQUIRE(kind >= SOD_G && kind <= SOD_B_ANGULAR, "kind must be G, H, B_trans or B_angular");
+    SOD_REQUIRE(sorder >= 1 && sorder <= 5 && ssub >= 1 && ssub <= 8, "singular quadrature order must be 1..5, subdivision 1..8");
+    SOD_TRY(ensure_gl_constants(ctx->device));
+    PointTable pt;
+    SOD_TRY(point_table_on_stack(order, subdiv, pt));
+    const long long nslots = m->nbr_off.back();
+    const long long sfs = kind <= SOD_H ? nslots * 9 : (long long)m->nV * (kind == SOD_B_TRANS ? 9 : 27);
+    const long long fit = scratch_elems / sfs;
+    if (fit < 1) {
+        set_error("mesh too large for the fixed scratch of the allocation-free entry point (needs " +
+                  std::to_string(sfs * (long long)sizeof(cd)) + " bytes per frequency, has " +
+                  std::to_string(scratch_elems * (long long)sizeof(cd)) + ")");
+        return SOD_ERR_CAPACITY;
+    }
+    const int chunk = (int)std::min<long long>(std::min<long long>(fit, MAX_FREQ_PER_LAUNCH), nfreq);
+    int threads = 256;
+    const sod_mesh::Coloured *col = nullptr;
+    size_t smem = 0;
+    if (kind <= SOD_H) {
+        threads = ctx->coll_threads > 0 ? ctx->coll_threads : m->tuned_threads[kind];
+        auto it = threads > 0 ? m->coloured.find(threads) : m->coloured.end();
+        if (it == m->coloured.end()) {
+            set_error("the mesh has no scatter schedule yet: assemble it once with sod_cqbem_assemble* during set-up");
+            return SOD_ERR_INVALID_ARG;
+        }
+        col = it->second.get();
+        smem = sizeof(float2) * (kind == SOD_G ? 6 : 9) * (size_t)m->nV;
+        if (smem > ctx->smem_optin) {
+            set_error("mesh too large for the shared-memory row accumulator");
+            return SOD_ERR_UNSUPPORTED;
+        }
+        const void *fn = kind == SOD_G ? (const void *)coll_scatter_kernel<SOD_G> : (const void *)coll_scatter_kernel<SOD_H>;
+        SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    }
+    const long long per = kind <= SOD_H ? 9LL * m->nV * m->nV : (kind == SOD_B_TRANS ? 9LL : 27LL) * m->nV;
+    const size_t esz = out_dtype == SOD_C64 ? 8 : 16;
+    for (int f0 = 0; f0 < nfreq; f0 += chunk) {
+        const int nf = std::min(chunk, nfreq - f0);
+        FreqTable ft;
+        ft.n = nf;
+        for (int l = 0; l < nf; l++) {
+            ft.kd[l] = make_kconst(c1, c2, rho, s[2 * (f0 + l)], s[2 * (f0 + l) + 1]);
+            ft.kf[l] = to_float(ft.kd[l]);
+        }
+        const dim3 grid(m->nV, nf);
+        SingArgs sa{};
+        sa.nV = m->nV;
+        sa.V = m->dV.as<double>();
+        sa.F = m->dF.as<int>();
+        sa.N = m->dN.as<double>();
+        sa.star_off = m->dStarOff.as<int>();
+        sa.star_face = m->dStarFace.as<int>();
+        sa.star_corner = m->dStarCorner.as<int>();
+        sa.star_slot = m->dStarSlot.as<int>();
+        sa.nbr_off = m->dNbrOff.as<int>();
+        sa.sorder = sorder;
+        sa.ssub = ssub;
+        sa.S[kind] = scratch;  // every slot is written by the singular pass before it is read
+        sa.S_fstride[kind] = sfs;
+        switch (kind) {
+        case SOD_G: coll_polar_kernel<KM_G><<<grid, 256, 0, stream>>>(sa, ft); break;
+        case SOD_B_TRANS: coll_polar_kernel<KM_BT><<<grid, 256, 0, stream>>>(sa, ft); break;
+        case SOD_B_ANGULAR: coll_polar_kernel<KM_BA><<<grid, 256, 0, stream>>>(sa, ft); break;
+        default: coll_guiggiani_kernel<<<grid, 256, 0, stream>>>(sa, ft); break;
+        }
+        SOD_CHECK_CUDA(cudaGetLastError());
+        ctx->count();
+        CollArgs a{};
+        a.nV = m->nV;
+        a.nF = m->nF;
+        a.Vf = m->dVf.as<float>();
+        a.canonV = m->has_vmap ? m->dCanon.as<int>() : nullptr;
+        a.out_c64 = out_dtype == SOD_C64;
+        a.do_regular = 1;
+        a.nbr_off = m->dNbrOff.as<int>();
+        a.nbr_vert = m->dNbrVert.as<int>();
+        a.out[kind] = static_cast<char *>(out) + (size_t)f0 * (size_t)per * esz;
+        a.fstride[kind] = per;
+        a.S[kind] = scratch;
+        a.S_fstride[kind] = sfs;
+        if (kind <= SOD_H) {
+            a.faces = col->dFaces.as<float4>();
+            a.canonF = m->has_vmap ? col->dCanonF.as<int4>() : nullptr;
+            a.color_off = col->dOff.as<int>();
+            a.ncolors = col->ncolors;
+            if (kind == SOD_G)
+                coll_scatter_kernel<SOD_G><<<grid, threads, smem, stream>>>(a, pt, ft);
+            else
+                coll_scatter_kernel<SOD_H><<<grid, threads, smem, stream>>>(a, pt, ft);
+        } else {
+            a.faces = m->dFacesNat.as<float4>();
+            a.canonF = m->has_vmap ? m->dCanonNat.as<int4>() : nullptr;
+            if (kind == SOD_B_TRANS)
+                coll_reduce_kernel<KM_BT><<<grid, 256, 0, stream>>>(a, pt, ft);
+            else
+                coll_reduce_kernel<KM_BA><<<grid, 256, 0, stream>>>(a, pt, ft);
+        }
+        SOD_CHECK_CUDA(cudaGetLastError());
+        ctx->count();
+    }
+    return SOD_OK;
+}
+
 }  // namespace sod

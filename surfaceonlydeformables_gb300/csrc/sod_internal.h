@@ -162,6 +162,11 @@ struct CollLaunch {
     cudaStream_t stream;
 };
 int launch_collocation(sod_context *ctx, const CollLaunch &L);
+// Allocation-free launcher over caller-provided scratch (see sod_collocation.cu).
+int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, double c1, double c2, double rho,
+                                const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, void *out,
+                                int out_dtype, cd *scratch, long long scratch_elems, cudaStream_t stream);
+bool is_device_pointer(const void *p);
 // Deterministic autotuner of the scatter kernels' CTA size (see sod_collocation.cu).
 int autotune_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int *threads);
 int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, int64_t M, int nfreq, int L,
