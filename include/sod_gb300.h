@@ -150,6 +150,21 @@ int sod_cqbem_assemble_noalloc(sod_context *ctx, const sod_mesh *mesh, int kind,
                                const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, void *out,
                                int out_dtype);
 
+/* ---- time-domain precomputation of one object ------------------------------------------------ */
+/* Replaces compute_H_matrices, compute_G_matrices, compute_B_trans_matrices,
+ * compute_B_angular_tensors and compute_B_euler_matrices of ElastodynamicsCQBEMMatrixCollection
+ * (src/elastodynamics_cqbem_{G,H,B_trans,B_angular}.cu, src/elastodynamics_cqbem_matrix_collection.cpp:90-93,
+ * 165-167, 280-305).  CQ frequencies from (bdf, dt, N), L = N+1 time weights per kind:
+ *   G_out  [L][3nV][3nV], H_out [L][3nV][3nV] (H_0 includes the free term C; not negated),
+ *   B_trans_out [L][3nV][3], B_angular_out [L][3nV][3][3] (with the B_trans (x - cm) shift),
+ *   B_euler_out [L][3nV][3].
+ * Any output may be NULL; all non-NULL outputs must be device memory; dtype SOD_F64 or SOD_F32.
+ * nu is the Poisson ratio (collocation free term); cm the centre of mass (3 doubles). */
+int sod_cqbem_precompute(sod_context *ctx, const sod_mesh *mesh, int method, double c1, double c2, double rho,
+                         double nu, int bdf, double dt, int N, int order, int subdiv, int sorder, int ssub,
+                         const double *cm, void *G_out, void *H_out, void *B_trans_out, void *B_angular_out,
+                         void *B_euler_out, int out_dtype);
+
 /* ---- inverse transform to CQ time weights (FP64-accurate) --------------------------------- */
 /* X_n = R^-n / L * sum_{l=0}^{L/2} c_l Re(Xhat_l zeta^-nl),  c_0 = 1, c_l = 2 otherwise except
  * c_{L/2} = 1 for even L;  n = 0..L-1 (src/elastodynamics_cqbem_G.cu:324-337).

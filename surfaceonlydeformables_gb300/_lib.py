@@ -47,6 +47,9 @@ _SIGS = {
                                 _c.c_int, _c.c_int, _c.c_int, _c.c_int, _P, _P, _P, _P, _c.c_int], _c.c_int),
     "sod_cqbem_assemble_noalloc": ([_P, _P, _c.c_int, _c.c_double, _c.c_double, _c.c_double, _P, _c.c_int,
                                     _c.c_int, _c.c_int, _c.c_int, _c.c_int, _P, _c.c_int], _c.c_int),
+    "sod_cqbem_precompute": ([_P, _P, _c.c_int, _c.c_double, _c.c_double, _c.c_double, _c.c_double, _c.c_int,
+                              _c.c_double, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _P, _P, _P, _P, _P, _P,
+                              _c.c_int], _c.c_int),
     "sod_cq_inverse_transform": ([_P, _P, _c.c_int, _c.c_int64, _c.c_int, _c.c_int, _c.c_double, _P, _c.c_int],
                                  _c.c_int),
 }

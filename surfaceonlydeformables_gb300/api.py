@@ -143,6 +143,25 @@ def assemble_all(ctx: Context, mesh: Mesh, mat: Material, s, order: int = 5, sub
     return outs
 
 
+def precompute(ctx: Context, mesh: Mesh, mat: Material, bdf: int, dt: float, N: int, order: int = 5,
+               subdiv: int = 1, sorder: int | None = None, ssub: int | None = None, method: int = L.COLLOCATION,
+               cm=(0.0, 0.0, 0.0), out_dtype: int = L.F64, kinds=("G", "H", "B_trans", "B_angular", "B_euler")):
+    """Time-domain CQ weights of one object (torch CUDA tensors): dict kind -> (L, ...) array."""
+    torch = _torch()
+    nV = mesh.nV
+    Lq = N + 1
+    shapes = {"G": (Lq, 3 * nV, 3 * nV), "H": (Lq, 3 * nV, 3 * nV), "B_trans": (Lq, 3 * nV, 3),
+              "B_angular": (Lq, 3 * nV, 3, 3), "B_euler": (Lq, 3 * nV, 3)}
+    dt_ = torch.float64 if out_dtype == L.F64 else torch.float32
+    outs = {k: torch.empty(shapes[k], dtype=dt_, device=f"cuda:{ctx.device}") for k in kinds}
+    cmv = np.ascontiguousarray(np.asarray(cm, dtype=np.float64))
+    ptrs = [L.ptr(outs[k]) if k in outs else None for k in ("G", "H", "B_trans", "B_angular", "B_euler")]
+    L.check(L.load().sod_cqbem_precompute(ctx.handle, mesh.handle, method, mat.c1, mat.c2, mat.rho, mat.nu, bdf, dt,
+                                          N, order, subdiv, sorder or min(order, 5), ssub or subdiv, L.ptr(cmv),
+                                          *ptrs, out_dtype))
+    return outs
+
+
 def inverse_transform(ctx: Context, Xhat, L_: int, R: float, out=None, out_dtype: int = L.F64):
     """Time-domain CQ weights from Laplace-domain blocks: Xhat (L/2+1, ...) complex -> (L, ...) real."""
     in_dtype = L.C128 if str(Xhat.dtype).endswith("complex128") else L.C64

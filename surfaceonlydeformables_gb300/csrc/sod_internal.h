@@ -109,6 +109,8 @@ struct sod_context {
     sod::DevBuf staging;   // device staging for host outputs
     sod::DevBuf staging2;  // device staging for host inputs
     sod::DevBuf twiddle;   // inverse-transform twiddles
+    sod::DevBuf freqbuf;   // Laplace-domain intermediates of the precompute
+    sod::DevBuf small;     // small per-call tables (free terms, adjacency)
     void count(int n = 1) { launches += n; }
 };
 
