@@ -60,6 +60,7 @@ enum sod_parts { SOD_PART_REGULAR = 1, SOD_PART_SINGULAR = 2, SOD_PART_ALL = 3 }
 
 typedef struct sod_context sod_context;
 typedef struct sod_mesh sod_mesh;
+typedef struct sod_batch sod_batch;
 
 /* ---- library / diagnostics -------------------------------------------------------------- */
 int sod_version(void);
@@ -149,6 +150,26 @@ int sod_cqbem_assemble_all(sod_context *ctx, const sod_mesh *mesh, int method, d
 int sod_cqbem_assemble_noalloc(sod_context *ctx, const sod_mesh *mesh, int kind, double c1, double c2, double rho,
                                const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, void *out,
                                int out_dtype);
+
+/* ---- batched assembly of many objects (persistent kernels under a CUDA graph) ------------------- */
+/* The reference assembles one object at a time, one launch per frequency
+ * (ElastodynamicsCQBEMMatrixCollection::init per object group, src/simulator.cpp:102,118).  A batch
+ * takes every frequency of every object into persistent launches fed from an (object, field
+ * vertex, frequency) work queue, largest objects first, and replays them as one CUDA graph.
+ * kind_mask: bit k selects kind k for every object of the batch.  Outputs: device memory, one
+ * buffer per (object, kind) holding nfreq consecutive matrices in the reference layout.  An
+ * object's results are identical whether it is run alone or in a batch. */
+int sod_batch_create(sod_context *ctx, int kind_mask, int out_dtype, sod_batch **batch);
+int sod_batch_add(sod_batch *batch, const sod_mesh *mesh, double c1, double c2, double rho, const double *s,
+                  int nfreq, int order, int subdiv, int sorder, int ssub, void *out_G, void *out_H,
+                  void *out_B_trans, void *out_B_angular);
+/* Builds descriptors, colourings, work lists and captures the graph (allocates; call at set-up). */
+int sod_batch_finalize(sod_batch *batch);
+/* Replays the graph on the context's stream (finalizes first if needed). */
+int sod_batch_run(sod_batch *batch);
+/* Number of persistent launches in one replay. */
+int sod_batch_launch_count(const sod_batch *batch);
+int sod_batch_destroy(sod_batch *batch);
 
 /* ---- time-domain precomputation of one object ------------------------------------------------ */
 /* Replaces compute_H_matrices, compute_G_matrices, compute_B_trans_matrices,

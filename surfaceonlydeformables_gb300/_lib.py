@@ -50,6 +50,13 @@ _SIGS = {
     "sod_cqbem_precompute": ([_P, _P, _c.c_int, _c.c_double, _c.c_double, _c.c_double, _c.c_double, _c.c_int,
                               _c.c_double, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _P, _P, _P, _P, _P, _P,
                               _c.c_int], _c.c_int),
+    "sod_batch_create": ([_P, _c.c_int, _c.c_int, _P], _c.c_int),
+    "sod_batch_add": ([_P, _P, _c.c_double, _c.c_double, _c.c_double, _P, _c.c_int, _c.c_int, _c.c_int, _c.c_int,
+                       _c.c_int, _P, _P, _P, _P], _c.c_int),
+    "sod_batch_finalize": ([_P], _c.c_int),
+    "sod_batch_run": ([_P], _c.c_int),
+    "sod_batch_launch_count": ([_P], _c.c_int),
+    "sod_batch_destroy": ([_P], _c.c_int),
     "sod_cq_inverse_transform": ([_P, _P, _c.c_int, _c.c_int64, _c.c_int, _c.c_int, _c.c_double, _P, _c.c_int],
                                  _c.c_int),
 }

@@ -143,6 +143,59 @@ def assemble_all(ctx: Context, mesh: Mesh, mat: Material, s, order: int = 5, sub
     return outs
 
 
+class Batch:
+    """Many objects assembled by persistent kernels under one CUDA graph (sod_batch).
+
+    add() takes device output tensors (torch CUDA) per kind; run() replays the captured step."""
+
+    def __init__(self, ctx: Context, kinds=("G", "H", "B_trans", "B_angular"), dtype: int = L.C64):
+        self.ctx = ctx
+        self.kinds = tuple(kinds)
+        self.dtype = dtype
+        mask = 0
+        for k in self.kinds:
+            mask |= 1 << L.KINDS[k]
+        self._h = ctypes.c_void_p()
+        L.check(L.load().sod_batch_create(ctx.handle, mask, dtype, ctypes.byref(self._h)))
+        self._keep = []
+
+    def add(self, mesh: Mesh, mat: Material, s, outs: dict, order: int = 5, subdiv: int = 1,
+            sorder: int | None = None, ssub: int | None = None) -> None:
+        sv = np.ascontiguousarray(np.asarray(s, dtype=np.complex128).ravel())
+        self._keep.append((mesh, outs))
+        ptrs = [L.ptr(outs[k]) if k in self.kinds else None for k in ("G", "H", "B_trans", "B_angular")]
+        L.check(L.load().sod_batch_add(self._h, mesh.handle, mat.c1, mat.c2, mat.rho, L.ptr(sv.view(np.float64)),
+                                       len(sv), order, subdiv, sorder or min(order, 5), ssub or subdiv, *ptrs))
+
+    def finalize(self) -> None:
+        L.check(L.load().sod_batch_finalize(self._h))
+
+    def run(self) -> None:
+        L.check(L.load().sod_batch_run(self._h))
+
+    @property
+    def launches_per_step(self) -> int:
+        return int(L.load().sod_batch_launch_count(self._h))
+
+    def close(self) -> None:
+        if self._h:
+            L.load().sod_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def alloc_outputs(mesh: Mesh, nfreq: int, kinds=("G", "H", "B_trans", "B_angular"), dtype: int = L.C64, device=0):
+    """torch CUDA output buffers for one object: kind -> (nfreq,) + out_shape(kind)."""
+    torch = _torch()
+    td = torch.complex64 if dtype == L.C64 else torch.complex128
+    return {k: torch.empty((nfreq,) + out_shape(L.KINDS[k], mesh.nV), dtype=td, device=f"cuda:{device}") for k in kinds}
+
+
 def precompute(ctx: Context, mesh: Mesh, mat: Material, bdf: int, dt: float, N: int, order: int = 5,
                subdiv: int = 1, sorder: int | None = None, ssub: int | None = None, method: int = L.COLLOCATION,
                cm=(0.0, 0.0, 0.0), out_dtype: int = L.F64, kinds=("G", "H", "B_trans", "B_angular", "B_euler")):

@@ -1,0 +1,262 @@
+// sod_batch.cu -- batched assembly of many objects of uneven size in persistent launches under a
+// CUDA graph.
+//
+// A batch collects objects (mesh, material, Laplace frequencies, device outputs).  finalize():
+//   * picks every object's scatter CTA size with the mesh autotuner and builds its colourings;
+//   * lays out one FP64 singular side buffer for all (object, frequency) pairs;
+//   * writes one device descriptor per object (kernel arguments of every pass);
+//   * builds the work lists -- (object, field vertex, frequency) items, largest objects first --
+//     for the singular passes, one scatter list per (kind, CTA size) class and the B reduction;
+//   * captures the whole step (counter resets + persistent launches) into a CUDA graph.
+// run() replays the graph on the context's stream: one host call per step, no per-object launches.
+#include <algorithm>
+#include <array>
+#include <map>
+#include <numeric>
+#include <vector>
+
+#include "sod_internal.h"
+
+namespace sod {
+constexpr int KMASK_ALL = 15;
+}
+using namespace sod;
+
+struct sod_batch {
+    sod_context *ctx = nullptr;
+    int mask = 0;
+    int out_dtype = SOD_C64;
+    struct Obj {
+        const sod_mesh *mesh;
+        double c1, c2, rho;
+        std::vector<double> s;
+        int order, subdiv, sorder, ssub;
+        void *out[4];
+        int T[2];
+    };
+    std::vector<Obj> objs;
+    bool ready = false;
+    DevBuf dObjs, dKcf, dKcd, dPts, dItems, dCounters, dS;
+    struct Launch {
+        int which, items_off, nitems, threads, counter;
+        size_t smem;
+    };
+    std::vector<Launch> launches;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~sod_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (cap) cudaStreamDestroy(cap);
+    }
+};
+
+static int finalize_batch(sod_batch *b) {
+    sod_context *ctx = b->ctx;
+    SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
+    const int nobj = (int)b->objs.size();
+    // quadrature tables (deduplicated) and per-frequency constants
+    std::vector<PointTable> pts;
+    std::map<std::pair<int, int>, int> pt_index;
+    std::vector<KConst<float>> kcf;
+    std::vector<KConst<double>> kcd;
+    std::vector<int> kc_off(nobj), pt_idx(nobj);
+    size_t smem[2] = {0, 0};
+    for (int o = 0; o < nobj; o++) {
+        auto &ob = b->objs[o];
+        auto key = std::make_pair(ob.order, ob.subdiv);
+        auto it = pt_index.find(key);
+        if (it == pt_index.end()) {
+            PointTable pt;
+            SOD_TRY(make_point_table(ob.order, ob.subdiv, pt));
+            pt_index[key] = (int)pts.size();
+            pts.push_back(pt);
+            it = pt_index.find(key);
+        }
+        pt_idx[o] = it->second;
+        kc_off[o] = (int)kcd.size();
+        for (size_t l = 0; l < ob.s.size() / 2; l++) {
+            const KConst<double> k = make_kconst(ob.c1, ob.c2, ob.rho, ob.s[2 * l], ob.s[2 * l + 1]);
+            kcd.push_back(k);
+            kcf.push_back(to_float(k));
+        }
+        for (int kd = 0; kd < 2; kd++) {
+            ob.T[kd] = 0;
+            if (!(b->mask & (1 << kd))) continue;
+            int T = ctx->coll_threads;
+            if (T <= 0) SOD_TRY(autotune_scatter_threads(ctx, const_cast<sod_mesh *>(ob.mesh), kd, &T));
+            ob.T[kd] = T;
+            const sod_mesh::Coloured *c = nullptr;
+            SOD_TRY(const_cast<sod_mesh *>(ob.mesh)->coloured_for(T, &c));
+            const size_t sm = sizeof(float2) * (kd == SOD_G ? 6 : 9) * (size_t)ob.mesh->nV;
+            if (sm > ctx->smem_optin) {
+                set_error("mesh too large for the shared-memory row accumulator");
+                return SOD_ERR_UNSUPPORTED;
+            }
+            smem[kd] = std::max(smem[kd], sm);
+        }
+    }
+    // singular side buffer layout
+    std::vector<std::array<long long, 4>> soff(nobj);
+    long long stot = 0;
+    for (int o = 0; o < nobj; o++) {
+        const sod_mesh *m = b->objs[o].mesh;
+        const long long nf = (long long)b->objs[o].s.size() / 2, nslots = m->nbr_off.back();
+        const long long sfs[4] = {nslots * 9, nslots * 9, (long long)m->nV * 9, (long long)m->nV * 27};
+        for (int kd = 0; kd < 4; kd++) {
+            soff[o][kd] = stot;
+            if (b->mask & (1 << kd)) stot += sfs[kd] * nf;
+        }
+    }
+    SOD_TRY(b->dS.ensure(sizeof(cd) * (size_t)std::max<long long>(stot, 1)));
+    // device descriptors
+    const size_t osz = batch_obj_size();
+    std::vector<char> host(osz * nobj);
+    for (int o = 0; o < nobj; o++) {
+        auto &ob = b->objs[o];
+        cd *S[4];
+        for (int kd = 0; kd < 4; kd++) S[kd] = b->dS.as<cd>() + soff[o][kd];
+        const sod_mesh::Coloured *cg = nullptr, *ch = nullptr;
+        if (ob.T[0]) SOD_TRY(const_cast<sod_mesh *>(ob.mesh)->coloured_for(ob.T[0], &cg));
+        if (ob.T[1]) SOD_TRY(const_cast<sod_mesh *>(ob.mesh)->coloured_for(ob.T[1], &ch));
+        batch_fill_args_host(ob.mesh, b->mask, b->out_dtype, ob.out, S, cg, ch, ob.sorder, ob.ssub, kc_off[o], pt_idx[o],
+                             host.data() + osz * o);
+    }
+    SOD_TRY(b->dObjs.ensure(host.size()));
+    SOD_CHECK_CUDA(cudaMemcpy(b->dObjs.p, host.data(), host.size(), cudaMemcpyHostToDevice));
+    SOD_TRY(b->dKcf.ensure(sizeof(KConst<float>) * kcf.size()));
+    SOD_TRY(b->dKcd.ensure(sizeof(KConst<double>) * kcd.size()));
+    SOD_TRY(b->dPts.ensure(sizeof(PointTable) * pts.size()));
+    SOD_CHECK_CUDA(cudaMemcpy(b->dKcf.p, kcf.data(), sizeof(KConst<float>) * kcf.size(), cudaMemcpyHostToDevice));
+    SOD_CHECK_CUDA(cudaMemcpy(b->dKcd.p, kcd.data(), sizeof(KConst<double>) * kcd.size(), cudaMemcpyHostToDevice));
+    SOD_CHECK_CUDA(cudaMemcpy(b->dPts.p, pts.data(), sizeof(PointTable) * pts.size(), cudaMemcpyHostToDevice));
+    // work lists, objects ordered by decreasing face count (largest items first)
+    std::vector<int> order(nobj);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return b->objs[x].mesh->nF > b->objs[y].mesh->nF; });
+    std::vector<int4> items;
+    b->launches.clear();
+    auto add_list = [&](int which, int threads, size_t sm, const std::vector<int> &objs_in) {
+        const int off = (int)items.size();
+        for (int o : objs_in) {
+            const int nV = b->objs[o].mesh->nV, nf = (int)b->objs[o].s.size() / 2;
+            for (int fq = 0; fq < nf; fq++)
+                for (int i = 0; i < nV; i++) items.push_back(make_int4(o, i, fq, 0));
+        }
+        const int n = (int)items.size() - off;
+        if (n > 0) b->launches.push_back({which, off, n, threads, (int)b->launches.size(), sm});
+    };
+    if (b->mask & (KMASK_ALL & ~(1 << SOD_H))) add_list(0, 256, 0, order);
+    if (b->mask & (1 << SOD_H)) add_list(1, 256, 0, order);
+    for (int kd = 0; kd < 2; kd++) {
+        if (!(b->mask & (1 << kd))) continue;
+        std::map<int, std::vector<int>> classes;  // CTA size -> objects
+        for (int o : order) classes[b->objs[o].T[kd]].push_back(o);
+        for (auto &c : classes) {
+            size_t sm = 0;
+            for (int o : c.second) sm = std::max(sm, sizeof(float2) * (kd == SOD_G ? 6 : 9) * (size_t)b->objs[o].mesh->nV);
+            add_list(2 + kd, c.first, sm, c.second);
+        }
+    }
+    if (b->mask & ((1 << SOD_B_TRANS) | (1 << SOD_B_ANGULAR))) add_list(4, 256, 0, order);
+    SOD_TRY(b->dItems.ensure(sizeof(int4) * std::max<size_t>(items.size(), 1)));
+    SOD_CHECK_CUDA(cudaMemcpy(b->dItems.p, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+    SOD_TRY(b->dCounters.ensure(sizeof(int) * std::max<size_t>(b->launches.size(), 1)));
+    SOD_TRY(batch_prepare_kernels(ctx, smem[0], smem[1]));
+    // capture the step into a CUDA graph
+    if (!b->cap) SOD_CHECK_CUDA(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (b->graph) {
+        cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    SOD_CHECK_CUDA(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
+    int rc = SOD_OK;
+    for (const auto &L : b->launches) {
+        rc = batch_launch(ctx, L.which, b->mask, b->dObjs.p, b->dItems.as<int4>() + L.items_off, L.nitems,
+                          b->dCounters.as<int>() + L.counter, b->dKcf.as<KConst<float>>(),
+                          b->dKcd.as<KConst<double>>(), b->dPts.as<PointTable>(), L.threads, L.smem, b->cap);
+        if (rc != SOD_OK) break;
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(b->cap, &g);
+    if (rc != SOD_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    SOD_CHECK_CUDA(ce);
+    b->graph = g;
+    SOD_CHECK_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    b->ready = true;
+    return SOD_OK;
+}
+
+extern "C" {
+
+int sod_batch_create(sod_context *ctx, int kind_mask, int out_dtype, sod_batch **out) {
+    SOD_REQUIRE(ctx && out, "null argument");
+    SOD_REQUIRE(kind_mask > 0 && kind_mask <= KMASK_ALL, "kind mask must select at least one of G, H, B_trans, B_angular");
+    SOD_REQUIRE(out_dtype == SOD_C128 || out_dtype == SOD_C64, "output dtype must be complex128 or complex64");
+    auto *b = new sod_batch();
+    b->ctx = ctx;
+    b->mask = kind_mask;
+    b->out_dtype = out_dtype;
+    *out = b;
+    return SOD_OK;
+}
+
+int sod_batch_add(sod_batch *b, const sod_mesh *mesh, double c1, double c2, double rho, const double *s, int nfreq,
+                  int order, int subdiv, int sorder, int ssub, void *out_G, void *out_H, void *out_B_trans,
+                  void *out_B_angular) {
+    SOD_REQUIRE(b && mesh && mesh->ctx == b->ctx, "bad batch or mesh");
+    SOD_REQUIRE(s && nfreq >= 1, "need at least one Laplace frequency");
+    SOD_REQUIRE(c1 > 0 && c2 > 0 && rho > 0 && std::isfinite(c1) && std::isfinite(c2) && std::isfinite(rho),
+                "wave speeds and density must be positive and finite");
+    SOD_REQUIRE(sorder >= 1 && sorder <= 5 && ssub >= 1 && ssub <= 8, "singular quadrature order must be 1..5, subdivision 1..8");
+    PointTable pt;
+    SOD_TRY(make_point_table(order, subdiv, pt));
+    void *outs[4] = {out_G, out_H, out_B_trans, out_B_angular};
+    for (int kd = 0; kd < 4; kd++) {
+        if (!(b->mask & (1 << kd))) continue;
+        SOD_REQUIRE(outs[kd] != nullptr && is_device_pointer(outs[kd]), "batch outputs must be device memory");
+    }
+    for (int l = 0; l < nfreq; l++)
+        SOD_REQUIRE(std::isfinite(s[2 * l]) && std::isfinite(s[2 * l + 1]) && (s[2 * l] != 0.0 || s[2 * l + 1] != 0.0),
+                    "Laplace frequencies must be finite and non-zero");
+    sod_batch::Obj o{mesh, c1, c2, rho, std::vector<double>(s, s + 2 * (size_t)nfreq), order, subdiv, sorder, ssub,
+                     {out_G, out_H, out_B_trans, out_B_angular}, {0, 0}};
+    b->objs.push_back(std::move(o));
+    b->ready = false;
+    return SOD_OK;
+}
+
+int sod_batch_finalize(sod_batch *b) {
+    SOD_REQUIRE(b && !b->objs.empty(), "empty batch");
+    return finalize_batch(b);
+}
+
+int sod_batch_run(sod_batch *b) {
+    SOD_REQUIRE(b, "null batch");
+    if (!b->ready) SOD_TRY(finalize_batch(b));
+    SOD_CHECK_CUDA(cudaSetDevice(b->ctx->device));
+    SOD_CHECK_CUDA(cudaGraphLaunch(b->exec, b->ctx->stream));
+    b->ctx->count((int)b->launches.size());
+    return SOD_OK;
+}
+
+int sod_batch_launch_count(const sod_batch *b) { return b ? (int)b->launches.size() : -1; }
+
+int sod_batch_destroy(sod_batch *b) {
+    if (b) {
+        cudaSetDevice(b->ctx->device);
+        delete b;
+    }
+    return SOD_OK;
+}
+
+}  // extern "C"

@@ -87,14 +87,11 @@ __device__ __forceinline__ void store_out(void *out, int c64, long long idx, dou
 // -------------------------------------------------------------------------------------------
 // G / H regular scatter kernel
 template <int KIND>
-__global__ void __launch_bounds__(512, 1) coll_scatter_kernel(CollArgs a, PointTable pt,
-                                                               const __grid_constant__ FreqTable ft) {
-    constexpr int NC = KIND == SOD_G ? 6 : 9;
-    extern __shared__ float2 acc[];  // [NC][nV]
-    const int i = blockIdx.x, fq = blockIdx.y;
+__device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable &pt, const KConst<float> k, int i,
+                                             int fq, float2 *acc) {
+    constexpr int NC = KIND == SOD_G ? 6 : 9;  // acc: [NC][nV]
     const int nV = a.nV;
     for (int t = threadIdx.x; t < NC * nV; t += blockDim.x) acc[t] = make_float2(0.f, 0.f);
-    const KConst<float> k = ft.kf[fq];
     const float3 x = make_float3(a.Vf[3 * i], a.Vf[3 * i + 1], a.Vf[3 * i + 2]);
     const int ci = a.canonV ? a.canonV[i] : i;
     __syncthreads();
@@ -193,18 +190,23 @@ __global__ void __launch_bounds__(512, 1) coll_scatter_kernel(CollArgs a, PointT
     }
 }
 
+template <int KIND>
+__global__ void __launch_bounds__(512, 1) coll_scatter_kernel(CollArgs a, PointTable pt,
+                                                               const __grid_constant__ FreqTable ft) {
+    extern __shared__ float2 acc[];
+    scatter_body<KIND>(a, pt, ft.kf[blockIdx.y], blockIdx.x, blockIdx.y, acc);
+}
+
 // -------------------------------------------------------------------------------------------
 // B_trans / B_angular regular reduction kernel (MASK subset of KM_BT | KM_BA)
 //   per-face moments (the tensor structure depends only on the face normal):
 //     B_trans   b_pq  = Ms_p n_q + Ms_q n_p + d_pq Md
 //     B_angular b_pqk = M1_pk n_q + M1_qk n_p + (M0 + SB)(d_qk n_p + d_pk n_q) + SC d_pq n_k
 template <int MASK>
-__global__ void __launch_bounds__(256) coll_reduce_kernel(CollArgs a, PointTable pt,
-                                                          const __grid_constant__ FreqTable ft) {
+__device__ __forceinline__ void reduce_body(const CollArgs &a, const PointTable &pt, const KConst<float> k, int i,
+                                            int fq) {
     constexpr bool BT = (MASK & KM_BT) != 0, BA = (MASK & KM_BA) != 0;
     constexpr int NT = BT ? 6 : 0, NA = BA ? 18 : 0, NC = NT + NA;
-    const int i = blockIdx.x, fq = blockIdx.y;
-    const KConst<float> k = ft.kf[fq];
     const float3 x = make_float3(a.Vf[3 * i], a.Vf[3 * i + 1], a.Vf[3 * i + 2]);
     const int ci = a.canonV ? a.canonV[i] : i;
     cf accl[NC];
@@ -319,6 +321,12 @@ __global__ void __launch_bounds__(256) coll_reduce_kernel(CollArgs a, PointTable
     }
 }
 
+template <int MASK>
+__global__ void __launch_bounds__(256) coll_reduce_kernel(CollArgs a, PointTable pt,
+                                                          const __grid_constant__ FreqTable ft) {
+    reduce_body<MASK>(a, pt, ft.kf[blockIdx.y], blockIdx.x, blockIdx.y);
+}
+
 // -------------------------------------------------------------------------------------------
 // FP64 singular kernels
 struct SingArgs {
@@ -334,6 +342,16 @@ struct SingArgs {
 };
 
 constexpr int MAX_STAR = 32;
+
+// Device-side descriptor of one object in a batch (sod_batch): the kernel arguments of its scatter
+// (coloured for the G and H CTA sizes), reduction and singular passes.
+struct BatchObjDev {
+    CollArgs aG, aH, aR;
+    SingArgs sa;
+    int kc_off;  // first entry of this object in the batch's per-frequency constant arrays
+    int pt_idx;  // its quadrature point table
+    int pad[2];
+};
 
 __device__ __forceinline__ double3 ld3(const double *p, int i) { return make_double3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
 __device__ __forceinline__ double3 operator-(double3 a, double3 b) { return make_double3(a.x - b.x, a.y - b.y, a.z - b.z); }
@@ -427,13 +445,11 @@ __device__ __forceinline__ void scatter_slots(const SingArgs &a, int kind, int i
 // Fused polar-rule kernel for G (MASK & KM_G), B_trans, B_angular: the FP64 radial terms are
 // evaluated once per point for every requested kind.
 template <int MASK>
-__global__ void __launch_bounds__(256) coll_polar_kernel(SingArgs a, const __grid_constant__ FreqTable ft) {
+__device__ __forceinline__ void polar_body(const SingArgs &a, const KConst<double> k, int i, int fq) {
     constexpr bool DG = (MASK & KM_G) != 0, DT = (MASK & KM_BT) != 0, DA = (MASK & KM_BA) != 0;
     constexpr int NG = DG ? 18 : 0, NT = DT ? 6 : 0, NA = DA ? 18 : 0;  // per-face result sizes
     constexpr int OG = 0, OT = NG, OA = NG + NT, STRIDE = NG + NT + NA;
     __shared__ cd fres[MAX_STAR][STRIDE];
-    const int i = blockIdx.x, fq = blockIdx.y;
-    const KConst<double> k = ft.kd[fq];
     const int s0 = a.star_off[i], ns = min(a.star_off[i + 1] - a.star_off[i], MAX_STAR);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int nq = a.sorder * a.ssub;
@@ -538,12 +554,15 @@ __global__ void __launch_bounds__(256) coll_polar_kernel(SingArgs a, const __gri
     }
 }
 
+template <int MASK>
+__global__ void __launch_bounds__(256) coll_polar_kernel(SingArgs a, const __grid_constant__ FreqTable ft) {
+    polar_body<MASK>(a, ft.kd[blockIdx.y], blockIdx.x, blockIdx.y);
+}
+
 // Guiggiani-Gigante rule for the strongly singular H faces (include/integrator_collocation.hpp:68-124)
-__global__ void __launch_bounds__(256) coll_guiggiani_kernel(SingArgs a, const __grid_constant__ FreqTable ft) {
+__device__ __forceinline__ void guiggiani_body(const SingArgs &a, const KConst<double> k, int i, int fq) {
     constexpr int NC = 9;
     __shared__ cd fres[MAX_STAR][3 * NC];
-    const int i = blockIdx.x, fq = blockIdx.y;
-    const KConst<double> k = ft.kd[fq];
     const int s0 = a.star_off[i], ns = min(a.star_off[i + 1] - a.star_off[i], MAX_STAR);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int nq = a.sorder * a.ssub;
@@ -606,6 +625,82 @@ __global__ void __launch_bounds__(256) coll_guiggiani_kernel(SingArgs a, const _
     }
     __syncthreads();
     scatter_slots<9, 3 * NC>(a, SOD_H, i, fq, s0, ns, fres, 0, false);
+}
+
+__global__ void __launch_bounds__(256) coll_guiggiani_kernel(SingArgs a, const __grid_constant__ FreqTable ft) {
+    guiggiani_body(a, ft.kd[blockIdx.y], blockIdx.x, blockIdx.y);
+}
+
+// -------------------------------------------------------------------------------------------
+// Persistent batched kernels: one launch per kernel type covers many objects of uneven size.  Each
+// CTA pulls (object, field vertex, frequency) items from a global counter until the list is empty;
+// the lists are ordered largest object first so the tail is made of cheap items.  The per-item
+// work is the same device function as in the per-object kernels, so an object's matrices are the
+// same whether it is assembled alone or in a batch.
+__device__ __forceinline__ int next_item(int *counter, int *s_item) {
+    if (threadIdx.x == 0) *s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = *s_item;
+    __syncthreads();
+    return it;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(512, 1) batch_scatter_kernel(const BatchObjDev *__restrict__ objs,
+                                                               const int4 *__restrict__ items, int nitems,
+                                                               int *counter, const KConst<float> *__restrict__ kcf,
+                                                               const PointTable *__restrict__ pts) {
+    extern __shared__ float2 acc[];
+    __shared__ int s_item;
+    for (;;) {
+        const int it = next_item(counter, &s_item);
+        if (it >= nitems) break;
+        const int4 w = items[it];
+        const BatchObjDev &o = objs[w.x];
+        scatter_body<KIND>(KIND == SOD_G ? o.aG : o.aH, pts[o.pt_idx], kcf[o.kc_off + w.z], w.y, w.z, acc);
+    }
+}
+
+template <int MASK>
+__global__ void __launch_bounds__(256) batch_reduce_kernel(const BatchObjDev *__restrict__ objs,
+                                                           const int4 *__restrict__ items, int nitems, int *counter,
+                                                           const KConst<float> *__restrict__ kcf,
+                                                           const PointTable *__restrict__ pts) {
+    __shared__ int s_item;
+    for (;;) {
+        const int it = next_item(counter, &s_item);
+        if (it >= nitems) break;
+        const int4 w = items[it];
+        const BatchObjDev &o = objs[w.x];
+        reduce_body<MASK>(o.aR, pts[o.pt_idx], kcf[o.kc_off + w.z], w.y, w.z);
+    }
+}
+
+template <int MASK>
+__global__ void __launch_bounds__(256) batch_polar_kernel(const BatchObjDev *__restrict__ objs,
+                                                          const int4 *__restrict__ items, int nitems, int *counter,
+                                                          const KConst<double> *__restrict__ kcd) {
+    __shared__ int s_item;
+    for (;;) {
+        const int it = next_item(counter, &s_item);
+        if (it >= nitems) break;
+        const int4 w = items[it];
+        const BatchObjDev &o = objs[w.x];
+        polar_body<MASK>(o.sa, kcd[o.kc_off + w.z], w.y, w.z);
+    }
+}
+
+__global__ void __launch_bounds__(256) batch_guiggiani_kernel(const BatchObjDev *__restrict__ objs,
+                                                              const int4 *__restrict__ items, int nitems,
+                                                              int *counter, const KConst<double> *__restrict__ kcd) {
+    __shared__ int s_item;
+    for (;;) {
+        const int it = next_item(counter, &s_item);
+        if (it >= nitems) break;
+        const int4 w = items[it];
+        const BatchObjDev &o = objs[w.x];
+        guiggiani_body(o.sa, kcd[o.kc_off + w.z], w.y, w.z);
+    }
 }
 
 // -------------------------------------------------------------------------------------------
@@ -943,6 +1038,153 @@ int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, d
         SOD_CHECK_CUDA(cudaGetLastError());
         ctx->count();
     }
+    return SOD_OK;
+}
+
+// -------------------------------------------------------------------------------------------
+// Batched launcher (host): fills the per-object device descriptors' kernel arguments and issues
+// the persistent launches on `stream` (which may be capturing into a CUDA graph).
+size_t batch_obj_size() { return sizeof(BatchObjDev); }
+
+static void batch_fill_args(const sod_mesh *m, int kind_mask, int out_dtype, void *const out[4], cd *const S[4],
+                            const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, int sorder, int ssub,
+                            BatchObjDev &o) {
+    const long long nslots = m->nbr_off.back();
+    const long long sfs[4] = {nslots * 9, nslots * 9, (long long)m->nV * 9, (long long)m->nV * 27};
+    const long long per[4] = {9LL * m->nV * m->nV, 9LL * m->nV * m->nV, 9LL * m->nV, 27LL * m->nV};
+    CollArgs a{};
+    a.nV = m->nV;
+    a.nF = m->nF;
+    a.Vf = m->dVf.as<float>();
+    a.canonV = m->has_vmap ? m->dCanon.as<int>() : nullptr;
+    a.out_c64 = out_dtype == SOD_C64;
+    a.do_regular = 1;
+    a.nbr_off = m->dNbrOff.as<int>();
+    a.nbr_vert = m->dNbrVert.as<int>();
+    for (int kd = 0; kd < 4; kd++) {
+        a.out[kd] = (kind_mask & (1 << kd)) ? out[kd] : nullptr;
+        a.fstride[kd] = per[kd];
+        a.S[kd] = (kind_mask & (1 << kd)) ? S[kd] : nullptr;
+        a.S_fstride[kd] = sfs[kd];
+    }
+    o.aG = a;
+    o.aH = a;
+    o.aR = a;
+    if (colG) {
+        o.aG.faces = colG->dFaces.as<float4>();
+        o.aG.canonF = m->has_vmap ? colG->dCanonF.as<int4>() : nullptr;
+        o.aG.color_off = colG->dOff.as<int>();
+        o.aG.ncolors = colG->ncolors;
+    }
+    if (colH) {
+        o.aH.faces = colH->dFaces.as<float4>();
+        o.aH.canonF = m->has_vmap ? colH->dCanonF.as<int4>() : nullptr;
+        o.aH.color_off = colH->dOff.as<int>();
+        o.aH.ncolors = colH->ncolors;
+    }
+    o.aR.faces = m->dFacesNat.as<float4>();
+    o.aR.canonF = m->has_vmap ? m->dCanonNat.as<int4>() : nullptr;
+    SingArgs &sa = o.sa;
+    sa = SingArgs{};
+    sa.nV = m->nV;
+    sa.V = m->dV.as<double>();
+    sa.F = m->dF.as<int>();
+    sa.N = m->dN.as<double>();
+    sa.star_off = m->dStarOff.as<int>();
+    sa.star_face = m->dStarFace.as<int>();
+    sa.star_corner = m->dStarCorner.as<int>();
+    sa.star_slot = m->dStarSlot.as<int>();
+    sa.nbr_off = m->dNbrOff.as<int>();
+    sa.sorder = sorder;
+    sa.ssub = ssub;
+    for (int kd = 0; kd < 4; kd++) {
+        sa.S[kd] = (kind_mask & (1 << kd)) ? S[kd] : nullptr;
+        sa.S_fstride[kd] = sfs[kd];
+    }
+}
+
+void batch_fill_args_host(const sod_mesh *m, int kind_mask, int out_dtype, void *const out[4], cd *const S[4],
+                          const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, int sorder, int ssub,
+                          int kc_off, int pt_idx, void *dst) {
+    BatchObjDev o{};
+    batch_fill_args(m, kind_mask, out_dtype, out, S, colG, colH, sorder, ssub, o);
+    o.kc_off = kc_off;
+    o.pt_idx = pt_idx;
+    *static_cast<BatchObjDev *>(dst) = o;
+}
+
+int batch_prepare_kernels(sod_context *ctx, size_t smem_G, size_t smem_H) {
+    SOD_TRY(ensure_gl_constants(ctx->device));
+    if (smem_G) {
+        SOD_CHECK_CUDA(cudaFuncSetAttribute(batch_scatter_kernel<SOD_G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_G));
+        SOD_CHECK_CUDA(cudaFuncSetAttribute(batch_scatter_kernel<SOD_G>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    }
+    if (smem_H) {
+        SOD_CHECK_CUDA(cudaFuncSetAttribute(batch_scatter_kernel<SOD_H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_H));
+        SOD_CHECK_CUDA(cudaFuncSetAttribute(batch_scatter_kernel<SOD_H>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    }
+    return SOD_OK;
+}
+
+// One persistent launch; grid = resident CTAs per SM x SMs.  `which`: 0 polar, 1 Guiggiani,
+// 2 scatter G, 3 scatter H, 4 reduce.
+int batch_launch(sod_context *ctx, int which, int mask, const void *objs_v, const int4 *items, int nitems,
+                 int *counter, const KConst<float> *kcf, const KConst<double> *kcd, const PointTable *pts, int threads,
+                 size_t smem, cudaStream_t stream) {
+    if (nitems <= 0) return SOD_OK;
+    const BatchObjDev *objs = static_cast<const BatchObjDev *>(objs_v);
+    int per_sm = 1;
+    const void *fn = nullptr;
+    const int pm = mask & (KM_G | KM_BT | KM_BA), rm = mask & (KM_BT | KM_BA);
+    switch (which) {
+    case 0:
+        fn = pm == (KM_G | KM_BT | KM_BA) ? (const void *)batch_polar_kernel<KM_G | KM_BT | KM_BA>
+           : pm == KM_G                   ? (const void *)batch_polar_kernel<KM_G>
+           : pm == (KM_BT | KM_BA)        ? (const void *)batch_polar_kernel<KM_BT | KM_BA>
+           : pm == (KM_G | KM_BT)         ? (const void *)batch_polar_kernel<KM_G | KM_BT>
+           : pm == (KM_G | KM_BA)         ? (const void *)batch_polar_kernel<KM_G | KM_BA>
+           : pm == KM_BT                  ? (const void *)batch_polar_kernel<KM_BT>
+                                          : (const void *)batch_polar_kernel<KM_BA>;
+        break;
+    case 1: fn = (const void *)batch_guiggiani_kernel; break;
+    case 2: fn = (const void *)batch_scatter_kernel<SOD_G>; break;
+    case 3: fn = (const void *)batch_scatter_kernel<SOD_H>; break;
+    default:
+        fn = rm == (KM_BT | KM_BA) ? (const void *)batch_reduce_kernel<KM_BT | KM_BA>
+           : rm == KM_BT           ? (const void *)batch_reduce_kernel<KM_BT>
+                                   : (const void *)batch_reduce_kernel<KM_BA>;
+        break;
+    }
+    SOD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+    per_sm = std::max(1, per_sm);
+    const int grid = std::min(nitems, per_sm * ctx->num_sms);
+    SOD_CHECK_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), stream));
+    switch (which) {
+    case 0:
+        switch (pm) {
+        case KM_G | KM_BT | KM_BA: batch_polar_kernel<KM_G | KM_BT | KM_BA><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
+        case KM_G: batch_polar_kernel<KM_G><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
+        case KM_BT | KM_BA: batch_polar_kernel<KM_BT | KM_BA><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
+        case KM_G | KM_BT: batch_polar_kernel<KM_G | KM_BT><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
+        case KM_G | KM_BA: batch_polar_kernel<KM_G | KM_BA><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
+        case KM_BT: batch_polar_kernel<KM_BT><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
+        default: batch_polar_kernel<KM_BA><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
+        }
+        break;
+    case 1: batch_guiggiani_kernel<<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
+    case 2: batch_scatter_kernel<SOD_G><<<grid, threads, smem, stream>>>(objs, items, nitems, counter, kcf, pts); break;
+    case 3: batch_scatter_kernel<SOD_H><<<grid, threads, smem, stream>>>(objs, items, nitems, counter, kcf, pts); break;
+    default:
+        if (rm == (KM_BT | KM_BA))
+            batch_reduce_kernel<KM_BT | KM_BA><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcf, pts);
+        else if (rm == KM_BT)
+            batch_reduce_kernel<KM_BT><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcf, pts);
+        else
+            batch_reduce_kernel<KM_BA><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcf, pts);
+        break;
+    }
+    SOD_CHECK_CUDA(cudaGetLastError());
+    ctx->count();
     return SOD_OK;
 }
 

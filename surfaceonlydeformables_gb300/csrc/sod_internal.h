@@ -169,6 +169,16 @@ int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, d
                                 const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, void *out,
                                 int out_dtype, cd *scratch, long long scratch_elems, cudaStream_t stream);
 bool is_device_pointer(const void *p);
+// Batched persistent path (sod_collocation.cu); BatchObjDev is defined there.
+struct BatchObjDev;
+size_t batch_obj_size();
+void batch_fill_args_host(const sod_mesh *m, int kind_mask, int out_dtype, void *const out[4], cd *const S[4],
+                          const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, int sorder, int ssub,
+                          int kc_off, int pt_idx, void *dst);
+int batch_prepare_kernels(sod_context *ctx, size_t smem_G, size_t smem_H);
+int batch_launch(sod_context *ctx, int which, int mask, const void *objs, const int4 *items, int nitems, int *counter,
+                 const KConst<float> *kcf, const KConst<double> *kcd, const PointTable *pts, int threads, size_t smem,
+                 cudaStream_t stream);
 // Deterministic autotuner of the scatter kernels' CTA size (see sod_collocation.cu).
 int autotune_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int *threads);
 int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, int64_t M, int nfreq, int L,

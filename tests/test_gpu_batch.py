@@ -1,0 +1,91 @@
+"""Batched persistent assembly under a CUDA graph (sod_batch): every object matches its per-object
+assembly and the FP64 oracle, an object's result is bitwise the same alone and in the mix, and
+replays are bitwise reproducible."""
+import numpy as np
+import pytest
+
+from surfaceonlydeformables_gb300.meshes import Material, make_icosphere_mesh
+
+from .conftest import rel_fro
+
+pytestmark = pytest.mark.gpu
+KINDS = ("G", "H", "B_trans", "B_angular")
+
+
+@pytest.fixture(scope="module")
+def objects(gpu_ctx, sodlib):
+    from surfaceonlydeformables_gb300 import api
+
+    specs = [(3, (1.0, 1.0, 1.0), Material(1e5, 0.3, 1000.0), 16),
+             (2, (1.6, 0.7, 1.1), Material(3e4, 0.42, 1000.0), 8),
+             (2, (0.6, 1.3, 0.9), Material(5e5, 0.25, 1000.0), 16)]
+    objs = []
+    for k, (lev, axes, mat, N) in enumerate(specs):
+        m = make_icosphere_mesh(lev, 0.1, axes=axes, seed=k)
+        s, R, L = sodlib.cq_frequencies(2, 1 / 200, N)
+        objs.append(dict(host=m, dev=api.Mesh(gpu_ctx, m), mat=mat, s=s))
+    return objs
+
+
+def run_batch(ctx, objs):
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    b = api.Batch(ctx, KINDS, L.C64)
+    outs = []
+    for o in objs:
+        out = api.alloc_outputs(o["dev"], len(o["s"]), KINDS, L.C64)
+        b.add(o["dev"], o["mat"], o["s"], out)
+        outs.append(out)
+    b.finalize()
+    b.run()
+    ctx.synchronize()
+    return b, [{k: v.cpu().numpy() for k, v in out.items()} for out in outs]
+
+
+def test_batch_matches_per_object_and_oracle(gpu_ctx, objects, oracle):
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    b, res = run_batch(gpu_ctx, objects)
+    assert b.launches_per_step >= 5
+    for o, r in zip(objects, res):
+        single = api.assemble_all(gpu_ctx, o["dev"], o["mat"], o["s"], dtype=L.C64)
+        for k in KINDS:
+            assert rel_fro(r[k], single[k]) <= 1e-6, k
+        l = len(o["s"]) // 2
+        for k in KINDS:
+            ref = oracle.collocation(k, o["host"], o["mat"], o["s"][l])
+            assert rel_fro(r[k][l], ref) <= 1e-5, k
+
+
+def test_same_result_alone_and_in_the_mix(gpu_ctx, objects):
+    _, mix = run_batch(gpu_ctx, objects)
+    for j in range(len(objects)):
+        _, alone = run_batch(gpu_ctx, [objects[j]])
+        for k in KINDS:
+            assert np.array_equal(alone[0][k].view(np.uint8), mix[j][k].view(np.uint8)), (j, k)
+
+
+def test_batch_replay_reproducible(gpu_ctx, objects):
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    b = api.Batch(gpu_ctx, KINDS, L.C64)
+    outs = []
+    for o in objects:
+        out = api.alloc_outputs(o["dev"], len(o["s"]), KINDS, L.C64)
+        b.add(o["dev"], o["mat"], o["s"], out)
+        outs.append(out)
+    b.finalize()
+    b.run()
+    gpu_ctx.synchronize()
+    first = [{k: v.clone() for k, v in out.items()} for out in outs]
+    for out in outs:
+        for v in out.values():
+            v.zero_()
+    b.run()
+    gpu_ctx.synchronize()
+    for a, c in zip(first, outs):
+        for k in KINDS:
+            assert bool((a[k] == c[k]).all()), k
