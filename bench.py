@@ -36,6 +36,11 @@ sys.path.insert(0, ROOT)
 # algorithmic FP32 flops per kernel evaluation (field point x quadrature point x frequency),
 # regular collocation pass: geometry + two complex exponentials + kernel combination
 FLOPS_PER_EVAL = {"G": 130, "H": 240, "B_trans": 60, "B_angular": 150}
+# per batched pass: the B reduction evaluates B_trans and B_angular from one set of radial terms
+PASS_FLOPS = {"scatter_G": 130, "scatter_H": 240, "reduce_B": 210}
+# DRAM bytes per evaluation of each pass from an ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum over the launch's evaluations); filled from the committed profile summaries
+TRAFFIC_BYTES_PER_EVAL: dict = {}
 KINDS = ("G", "H", "B_trans", "B_angular")
 
 
@@ -70,6 +75,11 @@ CASES = {"mixed24": make_workload, "coll642": lambda: make_single(3), "coll2562"
 
 def entries(nV: int, nfreq: int) -> int:
     return nfreq * (2 * (3 * nV) ** 2 + 12 * 3 * nV)
+
+
+def kind_entries(kind: str, nV: int) -> int:
+    """complex entries of one frequency of one kind: 3V x 3V (G, H), 3V x 3, 3V x 9"""
+    return {"G": (3 * nV) ** 2, "H": (3 * nV) ** 2, "B_trans": 9 * nV, "B_angular": 27 * nV}[kind]
 
 
 class ClockSampler:
@@ -139,22 +149,33 @@ def measure_fp32_peak(torch, dev) -> float:
     return best
 
 
-def cpu_sample(objs, threads: int, nfreq: int = 2):
-    """Reference CPU path (oracle, reference-mixed precision) on one 642-vertex object."""
+def cpu_sample(objs, threads: int, budget_s: float = 12.0):
+    """Reference CPU path (oracle, reference-mixed precision, OpenMP over field vertices) on a bounded
+    sample of the workload: (object, kind, frequency) calls in workload order until `budget_s` has
+    elapsed; returns entries/s over the calls that ran."""
     from oracle import oracle as O
 
     O.build()
     cores = O.set_threads(threads)
-    obj = next((o for o in objs if o["mesh"].nV == 642), objs[0])
-    m, mat = obj["mesh"], obj["mat"]
-    s, R, L = O.cq_frequencies(obj["bdf"], obj["dt"], obj["N"])
     t0 = time.perf_counter()
-    for kind in KINDS:
-        for sl in s[:nfreq]:
-            O.collocation(kind, m, mat, sl, order=obj["order"], subdiv=obj["subdiv"], mode=O.MIXED)
+    done, calls, seen = 0, 0, set()
+    for k, obj in enumerate(objs):
+        m, mat = obj["mesh"], obj["mat"]
+        s, R, L = O.cq_frequencies(obj["bdf"], obj["dt"], obj["N"])
+        for sl in s:
+            for kind in KINDS:
+                O.collocation(kind, m, mat, sl, order=obj["order"], subdiv=obj["subdiv"], mode=O.MIXED)
+                calls += 1
+                done += kind_entries(kind, m.nV)
+                seen.add(k)
+            if time.perf_counter() - t0 > budget_s:
+                break
+        if time.perf_counter() - t0 > budget_s:
+            break
     dt = time.perf_counter() - t0
-    ent = entries(m.nV, nfreq)
-    return ent / dt, dt, cores, f"1 object (nV={m.nV}), 4 kinds, {nfreq} of {len(s)} frequencies, all rows"
+    sample = (f"{calls} (object, kind, frequency) calls over the first {len(seen)} objects of the workload "
+              f"in order, {dt:.1f} s")
+    return done / dt, dt, cores, sample
 
 
 def run_reference(args):
@@ -165,7 +186,7 @@ def run_reference(args):
         return 0
     rates = []
     for it in range(args.warmup + args.steps):
-        r, dt, cores, sample = cpu_sample(objs, threads, nfreq=1)
+        r, dt, cores, sample = cpu_sample(objs, threads, budget_s=10.0)
         if it >= args.warmup:
             rates.append((r, dt))
     value = float(np.mean([r for r, _ in rates]))
@@ -283,11 +304,13 @@ def run_gpu(args):
     value = world * total_entries * args.steps / t_max
 
     # ---- the same workload through the per-object and the plain per-(kind, frequency) drop-in ----
-    step_per_object()
-    step_plain()
-    torch.cuda.synchronize()
-    t_per_object = timed(step_per_object, max(1, args.steps // 2))
-    t_plain = timed(step_plain, max(1, args.steps // 2))
+    t_per_object = t_plain = None
+    if not args.value_only:
+        step_per_object()
+        step_plain()
+        torch.cuda.synchronize()
+        t_per_object = timed(step_per_object, max(1, args.steps // 2))
+        t_plain = timed(step_plain, max(1, args.steps // 2))
 
     # ---- end to end: plain per-frequency drop-in with pinned host buffers (reference layout) ----
     big = max(m.nV for m in meshes)
@@ -307,7 +330,7 @@ def run_gpu(args):
         return d2h
 
     e2e_value, d2h_bytes = None, 0
-    if not args.no_e2e:
+    if not (args.no_e2e or args.value_only):
         e2e_step()  # warm the staging buffers
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -318,42 +341,42 @@ def run_gpu(args):
         e2e_value = world * total_entries * e2e_steps / e2e_t
     h2d_bytes = sum(16 * len(o["s"]) + 64 for o in objs) * 4  # per-call frequency constants
 
-    # ---- roofline of the dominant kernel: regular (FP32) H scatter on the largest object ----
+    # ---- roofline of the dominant kernel of the batched step: per-launch CUDA-event times ----
     peak_fp32 = measure_fp32_peak(torch, dev)
-    iL = int(np.argmax([m.nV for m in meshes]))
-    o, m = objs[iL], meshes[iL]
-    rows = {}
-    for kind in KINDS:
-        for part, pname in ((L.PART_REGULAR, "regular"), (L.PART_SINGULAR, "singular")):
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            reps = 3
-            e0.record(stream)
-            for _ in range(reps):
-                api.assemble_frequencies(ctx, m, kind, o["mat"], o["s"], order=o["order"], subdiv=o["subdiv"],
-                                         parts=part, out=outs[iL][kind], dtype=L.C64)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            rows[(kind, pname)] = e0.elapsed_time(e1) * 1e-3 / reps
-    dom = max(rows, key=rows.get)
-    nq = 7
-    evals = (m.nV * m.nF - 3 * m.nF) * nq * len(o["s"])
-    kind_dom = "H"
-    flops = evals * FLOPS_PER_EVAL[kind_dom]
-    achieved = flops / rows[(kind_dom, "regular")] / 1e12
-    roofline = {"bound": "fp32", "kernel": f"coll_scatter_kernel<H> (nV={m.nV}, {len(o['s'])} frequencies)",
+    prof = batch.profile()
+    for _ in range(2):
+        p2 = batch.profile()
+        for a_, b_ in zip(prof, p2):
+            a_["ms"] = min(a_["ms"], b_["ms"])
+    step_ms = sum(p["ms"] for p in prof)
+    fp32 = [p for p in prof if p["pass"] in PASS_FLOPS]
+    dom = max(fp32, key=lambda p: p["ms"])
+    achieved = dom["evals"] * PASS_FLOPS[dom["pass"]] / (dom["ms"] * 1e-3) / 1e12
+    traffic = TRAFFIC_BYTES_PER_EVAL.get(dom["pass"])
+    roofline = {"bound": "fp32", "kernel": f"batch_scatter_kernel<{dom['pass'][-1]}>" if "scatter" in dom["pass"]
+                else "batch_reduce_kernel<B_trans|B_angular>",
                 "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s", "frac": achieved / peak_fp32,
-                "peak_source": "measured live: cuBLAS SGEMM 8192^3, TF32 off", "traffic": None,
-                "flops_per_eval": FLOPS_PER_EVAL[kind_dom], "evals_per_launch": evals,
-                "launch_ms": rows[(kind_dom, "regular")] * 1e3,
-                "dominant": f"{dom[0]}/{dom[1]}", "pass_ms": {f"{k}/{p}": v * 1e3 for (k, p), v in rows.items()}}
+                "peak_source": "measured live: cuBLAS SGEMM 8192^3, TF32 off (no FP32 figure in the measured "
+                               "peaks file)",
+                "traffic": traffic * dom["evals"] if traffic else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per evaluation, scaled by "
+                                  "the launch's evaluations" if traffic else None,
+                "flops_per_eval": PASS_FLOPS[dom["pass"]], "evals_per_launch": dom["evals"],
+                "launch_ms": dom["ms"], "launch_share": dom["ms"] / step_ms,
+                "launches": [{"pass": p["pass"], "ms": round(p["ms"], 3), "share": round(p["ms"] / step_ms, 4),
+                              "evals": p["evals"]} for p in prof]}
 
     # ---- CPU baseline (rank 0, N = 1 only) ----
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if rank == 0 and world == 1 and not (args.no_cpu or args.value_only):
         r, dtc, cores, sample = cpu_sample(objs, os.cpu_count() or 1)
         cpu = {"value": r, "unit": "entries/s", "cores": cores, "kind": "port", "sample": sample,
                "seconds": dtc}
+    paths = {"batched_graph": {"entries_per_s": value, "launches_per_step": batch.launches_per_step}}
+    if t_plain:
+        paths["per_object_fused"] = {"entries_per_s": total_entries / t_per_object, "ms_per_step": t_per_object * 1e3}
+        paths["plain_per_kind_frequency"] = {"entries_per_s": total_entries / t_plain, "ms_per_step": t_plain * 1e3}
+        paths["batched_over_plain"] = t_plain / (t_max / args.steps)
     if rank == 0:
         line = {"metric": "CQBEM Laplace-domain entries/s (mixed-size 24-object set)", "value": value,
                 "unit": "entries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -368,12 +391,7 @@ def run_gpu(args):
                                  f"{total_entries * 8 / 1e9:.0f} GB complex64) exceed L2",
                            "parallelism": f"replicas x{world}"},
                 "roofline": roofline, "cpu_baseline": cpu,
-                "paths": {"batched_graph": {"entries_per_s": value, "launches_per_step": batch.launches_per_step},
-                          "per_object_fused": {"entries_per_s": total_entries / t_per_object,
-                                               "ms_per_step": t_per_object * 1e3},
-                          "plain_per_kind_frequency": {"entries_per_s": total_entries / t_plain,
-                                                       "ms_per_step": t_plain * 1e3},
-                          "batched_over_plain": (total_entries / (t_max / args.steps)) / (total_entries / t_plain)},
+                "paths": paths,
                 "e2e": {"value": e2e_value, "unit": "entries/s", "h2d_bytes_per_step": h2d_bytes,
                         "d2h_bytes_per_step": d2h_bytes, "path": "sod_cqbem_assemble per (object, kind, "
                         "frequency) into pinned host memory, complex128 reference layout", "steps": e2e_steps},
@@ -392,6 +410,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    ap.add_argument("--value-only", action="store_true",
+                    help="profiling runs: time the batched step only (no comparison paths, e2e or CPU leg)")
     ap.add_argument("--case", default="mixed24", choices=sorted(CASES),
                     help="workload: the 24-object set (default) or one object for profiling captures")
     args = ap.parse_args()

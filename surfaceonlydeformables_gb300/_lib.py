@@ -56,6 +56,7 @@ _SIGS = {
     "sod_batch_finalize": ([_P], _c.c_int),
     "sod_batch_run": ([_P], _c.c_int),
     "sod_batch_launch_count": ([_P], _c.c_int),
+    "sod_batch_profile": ([_P, _c.c_int, _P, _P, _P], _c.c_int),
     "sod_batch_destroy": ([_P], _c.c_int),
     "sod_cq_inverse_transform": ([_P, _P, _c.c_int, _c.c_int64, _c.c_int, _c.c_int, _c.c_double, _P, _c.c_int],
                                  _c.c_int),

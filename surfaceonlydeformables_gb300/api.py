@@ -177,6 +177,17 @@ class Batch:
     def launches_per_step(self) -> int:
         return int(L.load().sod_batch_launch_count(self._h))
 
+    PASS_NAMES = ("singular_polar", "singular_guiggiani", "scatter_G", "scatter_H", "reduce_B")
+
+    def profile(self) -> list[dict]:
+        """Per-launch device times of one eager (non-graph) step: [{pass, evals, ms}]."""
+        n = self.launches_per_step
+        which = np.zeros(n, dtype=np.int32)
+        evals = np.zeros(n, dtype=np.float64)
+        ms = np.zeros(n, dtype=np.float32)
+        L.check(L.load().sod_batch_profile(self._h, n, L.ptr(which), L.ptr(evals), L.ptr(ms)))
+        return [{"pass": self.PASS_NAMES[w], "evals": float(e), "ms": float(t)} for w, e, t in zip(which, evals, ms)]
+
     def close(self) -> None:
         if self._h:
             L.load().sod_batch_destroy(self._h)

@@ -38,19 +38,30 @@ struct sod_batch {
     bool ready = false;
     DevBuf dObjs, dKcf, dKcd, dPts, dItems, dCounters, dS;
     struct Launch {
-        int which, items_off, nitems, threads, counter;
+        int which, items_off, nitems, threads, counter, chain;
         size_t smem;
+        double evals;  // kernel evaluations (regular) or singular quadrature points in the launch
     };
     std::vector<Launch> launches;
-    cudaStream_t cap = nullptr;
+    cudaStream_t cap = nullptr, cap2 = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     ~sod_batch() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
         if (cap) cudaStreamDestroy(cap);
+        if (cap2) cudaStreamDestroy(cap2);
     }
 };
+
+static int issue_launch(sod_batch *b, const sod_batch::Launch &L, cudaStream_t st) {
+    return batch_launch(b->ctx, L.which, b->mask, b->dObjs.p, b->dItems.as<int4>() + L.items_off, L.nitems,
+                        b->dCounters.as<int>() + L.counter, b->dKcf.as<KConst<float>>(), b->dKcd.as<KConst<double>>(),
+                        b->dPts.as<PointTable>(), L.threads, L.smem, st);
+}
 
 static int finalize_batch(sod_batch *b) {
     sod_context *ctx = b->ctx;
@@ -136,37 +147,55 @@ static int finalize_batch(sod_batch *b) {
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
                      [&](int x, int y) { return b->objs[x].mesh->nF > b->objs[y].mesh->nF; });
+    SOD_TRY(batch_prepare_kernels(ctx, smem[0], smem[1]));
     std::vector<int4> items;
     b->launches.clear();
-    auto add_list = [&](int which, int threads, size_t sm, const std::vector<int> &objs_in) {
+    // chain 0: weakly singular pass -> G scatter classes -> B reduction; chain 1: Guiggiani -> H
+    // scatter classes.  The two chains run concurrently inside the graph.
+    auto add_list = [&](int which, int threads, size_t sm, const std::vector<int> &objs_in, int chain) {
         const int off = (int)items.size();
+        double evals = 0;
         for (int o : objs_in) {
-            const int nV = b->objs[o].mesh->nV, nf = (int)b->objs[o].s.size() / 2;
+            const auto &ob = b->objs[o];
+            const int nV = ob.mesh->nV, nF = ob.mesh->nF, nf = (int)ob.s.size() / 2;
             for (int fq = 0; fq < nf; fq++)
                 for (int i = 0; i < nV; i++) items.push_back(make_int4(o, i, fq, 0));
+            if (which <= 1)
+                evals += (double)nf * 3.0 * nF * (double)(ob.sorder * ob.ssub) * (ob.sorder * ob.ssub);
+            else
+                evals += (double)nf * ((double)nV * nF - 3.0 * nF) * pts[pt_idx[o]].n;
         }
         const int n = (int)items.size() - off;
-        if (n > 0) b->launches.push_back({which, off, n, threads, (int)b->launches.size(), sm});
+        if (n > 0) b->launches.push_back({which, off, n, threads, (int)b->launches.size(), chain, sm, evals});
     };
-    if (b->mask & (KMASK_ALL & ~(1 << SOD_H))) add_list(0, 256, 0, order);
-    if (b->mask & (1 << SOD_H)) add_list(1, 256, 0, order);
+    if (b->mask & (KMASK_ALL & ~(1 << SOD_H))) add_list(0, 256, 0, order, 0);
+    if (b->mask & (1 << SOD_H)) add_list(1, 256, 0, order, 1);
     for (int kd = 0; kd < 2; kd++) {
         if (!(b->mask & (1 << kd))) continue;
-        std::map<int, std::vector<int>> classes;  // CTA size -> objects
-        for (int o : order) classes[b->objs[o].T[kd]].push_back(o);
+        // one launch per (CTA size, occupancy) class: a launch has one dynamic smem size, so small
+        // objects are not grouped with large ones that would lower their resident CTAs per SM
+        std::map<std::pair<int, int>, std::vector<int>> classes;
+        for (int o : order) {
+            const size_t sm = sizeof(float2) * (kd == SOD_G ? 6 : 9) * (size_t)b->objs[o].mesh->nV;
+            int per_sm = 0;
+            SOD_TRY(batch_scatter_occupancy(kd, b->objs[o].T[kd], sm, &per_sm));
+            classes[{-per_sm, b->objs[o].T[kd]}].push_back(o);
+        }
         for (auto &c : classes) {
             size_t sm = 0;
             for (int o : c.second) sm = std::max(sm, sizeof(float2) * (kd == SOD_G ? 6 : 9) * (size_t)b->objs[o].mesh->nV);
-            add_list(2 + kd, c.first, sm, c.second);
+            add_list(2 + kd, c.first.second, sm, c.second, kd == SOD_G ? 0 : 1);
         }
     }
-    if (b->mask & ((1 << SOD_B_TRANS) | (1 << SOD_B_ANGULAR))) add_list(4, 256, 0, order);
+    if (b->mask & ((1 << SOD_B_TRANS) | (1 << SOD_B_ANGULAR))) add_list(4, 256, 0, order, 0);
     SOD_TRY(b->dItems.ensure(sizeof(int4) * std::max<size_t>(items.size(), 1)));
     SOD_CHECK_CUDA(cudaMemcpy(b->dItems.p, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
     SOD_TRY(b->dCounters.ensure(sizeof(int) * std::max<size_t>(b->launches.size(), 1)));
-    SOD_TRY(batch_prepare_kernels(ctx, smem[0], smem[1]));
-    // capture the step into a CUDA graph
+    // capture the step into a CUDA graph: fork chain 1 onto a second stream, join at the end
     if (!b->cap) SOD_CHECK_CUDA(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
+    if (!b->cap2) SOD_CHECK_CUDA(cudaStreamCreateWithFlags(&b->cap2, cudaStreamNonBlocking));
+    if (!b->fork) SOD_CHECK_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    if (!b->join) SOD_CHECK_CUDA(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
     if (b->exec) {
         cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
@@ -177,19 +206,26 @@ static int finalize_batch(sod_batch *b) {
     }
     SOD_CHECK_CUDA(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
     int rc = SOD_OK;
+    cudaError_t ce = cudaEventRecord(b->fork, b->cap);
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->cap2, b->fork, 0);
+    if (ce != cudaSuccess) rc = SOD_ERR_CUDA;
     for (const auto &L : b->launches) {
-        rc = batch_launch(ctx, L.which, b->mask, b->dObjs.p, b->dItems.as<int4>() + L.items_off, L.nitems,
-                          b->dCounters.as<int>() + L.counter, b->dKcf.as<KConst<float>>(),
-                          b->dKcd.as<KConst<double>>(), b->dPts.as<PointTable>(), L.threads, L.smem, b->cap);
         if (rc != SOD_OK) break;
+        rc = issue_launch(b, L, L.chain ? b->cap2 : b->cap);
+    }
+    if (rc == SOD_OK) {
+        ce = cudaEventRecord(b->join, b->cap2);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->cap, b->join, 0);
+        if (ce != cudaSuccess) rc = SOD_ERR_CUDA;
     }
     cudaGraph_t g = nullptr;
-    const cudaError_t ce = cudaStreamEndCapture(b->cap, &g);
+    const cudaError_t ce_end = cudaStreamEndCapture(b->cap, &g);
     if (rc != SOD_OK) {
         if (g) cudaGraphDestroy(g);
+        if (rc == SOD_ERR_CUDA && ce != cudaSuccess) set_error(cudaGetErrorString(ce));
         return rc;
     }
-    SOD_CHECK_CUDA(ce);
+    SOD_CHECK_CUDA(ce_end);
     b->graph = g;
     SOD_CHECK_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
     b->ready = true;
@@ -250,6 +286,33 @@ int sod_batch_run(sod_batch *b) {
 }
 
 int sod_batch_launch_count(const sod_batch *b) { return b ? (int)b->launches.size() : -1; }
+
+int sod_batch_profile(sod_batch *b, int cap, int *which, double *evals, float *ms) {
+    SOD_REQUIRE(b && cap >= 0, "null batch or negative capacity");
+    if (!b->ready) SOD_TRY(finalize_batch(b));
+    const int n = (int)b->launches.size();
+    SOD_REQUIRE(cap >= n && which && evals && ms, "output arrays must hold sod_batch_launch_count() entries");
+    SOD_CHECK_CUDA(cudaSetDevice(b->ctx->device));
+    std::vector<cudaEvent_t> ev(n + 1, nullptr);
+    int rc = SOD_OK;
+    for (auto &e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) rc = SOD_ERR_CUDA;
+    if (rc == SOD_OK && cudaEventRecord(ev[0], b->ctx->stream) != cudaSuccess) rc = SOD_ERR_CUDA;
+    for (int k = 0; k < n && rc == SOD_OK; k++) {
+        rc = issue_launch(b, b->launches[k], b->ctx->stream);
+        if (rc == SOD_OK && cudaEventRecord(ev[k + 1], b->ctx->stream) != cudaSuccess) rc = SOD_ERR_CUDA;
+    }
+    if (rc == SOD_OK && cudaEventSynchronize(ev[n]) != cudaSuccess) rc = SOD_ERR_CUDA;
+    for (int k = 0; k < n && rc == SOD_OK; k++) {
+        which[k] = b->launches[k].which;
+        evals[k] = b->launches[k].evals;
+        if (cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]) != cudaSuccess) rc = SOD_ERR_CUDA;
+    }
+    for (auto &e : ev)
+        if (e) cudaEventDestroy(e);
+    if (rc != SOD_OK) set_error("batch profiling: a CUDA event call failed");
+    return rc;
+}
 
 int sod_batch_destroy(sod_batch *b) {
     if (b) {

@@ -1126,6 +1126,14 @@ int batch_prepare_kernels(sod_context *ctx, size_t smem_G, size_t smem_H) {
     return SOD_OK;
 }
 
+// Resident CTAs per SM of the persistent G (kind 0) or H (kind 1) scatter at a CTA size and
+// dynamic shared-memory size (batch_prepare_kernels must have raised the kernel's smem limit).
+int batch_scatter_occupancy(int kind, int threads, size_t smem, int *per_sm) {
+    const void *fn = kind == SOD_G ? (const void *)batch_scatter_kernel<SOD_G> : (const void *)batch_scatter_kernel<SOD_H>;
+    SOD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, fn, threads, smem));
+    return SOD_OK;
+}
+
 // One persistent launch; grid = resident CTAs per SM x SMs.  `which`: 0 polar, 1 Guiggiani,
 // 2 scatter G, 3 scatter H, 4 reduce.
 int batch_launch(sod_context *ctx, int which, int mask, const void *objs_v, const int4 *items, int nitems,

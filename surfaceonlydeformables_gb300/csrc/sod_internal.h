@@ -176,6 +176,7 @@ void batch_fill_args_host(const sod_mesh *m, int kind_mask, int out_dtype, void 
                           const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, int sorder, int ssub,
                           int kc_off, int pt_idx, void *dst);
 int batch_prepare_kernels(sod_context *ctx, size_t smem_G, size_t smem_H);
+int batch_scatter_occupancy(int kind, int threads, size_t smem, int *per_sm);
 int batch_launch(sod_context *ctx, int which, int mask, const void *objs, const int4 *items, int nitems, int *counter,
                  const KConst<float> *kcf, const KConst<double> *kcd, const PointTable *pts, int threads, size_t smem,
                  cudaStream_t stream);

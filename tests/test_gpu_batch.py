@@ -89,3 +89,21 @@ def test_batch_replay_reproducible(gpu_ctx, objects):
     for a, c in zip(first, outs):
         for k in KINDS:
             assert bool((a[k] == c[k]).all()), k
+
+
+def test_batch_profile_reports_every_launch(gpu_ctx, objects):
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    b = api.Batch(gpu_ctx, KINDS, L.C64)
+    for o in objects:
+        b.add(o["dev"], o["mat"], o["s"], api.alloc_outputs(o["dev"], len(o["s"]), KINDS, L.C64))
+    b.finalize()
+    prof = b.profile()
+    assert len(prof) == b.launches_per_step
+    passes = {p["pass"] for p in prof}
+    assert {"singular_polar", "singular_guiggiani", "scatter_G", "scatter_H", "reduce_B"} <= passes
+    assert all(p["ms"] > 0 and p["evals"] > 0 for p in prof)
+    # regular evaluations of the G scatter: nfreq * (nV nF - 3 nF) * 7 points, summed over objects
+    want = sum(len(o["s"]) * (o["host"].nV * o["host"].nF - 3 * o["host"].nF) * 7 for o in objects)
+    assert sum(p["evals"] for p in prof if p["pass"] == "scatter_G") == want
