@@ -171,8 +171,9 @@ int sod_batch_run(sod_batch *batch);
 int sod_batch_launch_count(const sod_batch *batch);
 /* Runs the step's launches one by one on the context's stream with CUDA events between them and
  * returns, per launch: which pass (0 weakly singular, 1 Guiggiani, 2 G scatter, 3 H scatter,
- * 4 B reduction), its kernel evaluations (singular quadrature points for 0/1) and its device time
- * in ms.  Arrays hold `cap` >= sod_batch_launch_count() entries.  Synchronises the stream. */
+ * 4 B reduction, 5 singular combine of G/B_trans/B_angular, 6 singular combine of H), its work
+ * (kernel evaluations; singular quadrature points for 0/1; vertex-frequencies for 5/6) and its
+ * device time in ms.  Arrays hold `cap` >= sod_batch_launch_count() entries.  Synchronises the stream. */
 int sod_batch_profile(sod_batch *batch, int cap, int *which, double *evals, float *ms);
 int sod_batch_destroy(sod_batch *batch);
 

@@ -177,7 +177,8 @@ class Batch:
     def launches_per_step(self) -> int:
         return int(L.load().sod_batch_launch_count(self._h))
 
-    PASS_NAMES = ("singular_polar", "singular_guiggiani", "scatter_G", "scatter_H", "reduce_B")
+    PASS_NAMES = ("singular_polar", "singular_guiggiani", "scatter_G", "scatter_H", "reduce_B", "combine_GB",
+                  "combine_H")
 
     def profile(self) -> list[dict]:
         """Per-launch device times of one eager (non-graph) step: [{pass, evals, ms}]."""

@@ -11,7 +11,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libsod_gb300.so")
-SOURCES = ["sod_api.cu", "sod_collocation.cu", "sod_transform.cu", "sod_noalloc.cu", "sod_precompute.cu", "sod_batch.cu"]
+SOURCES = ["sod_api.cu", "sod_collocation.cu", "sod_singular.cu", "sod_transform.cu", "sod_noalloc.cu", "sod_precompute.cu",
+           "sod_batch.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
          "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

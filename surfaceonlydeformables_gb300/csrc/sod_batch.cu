@@ -36,7 +36,7 @@ struct sod_batch {
     };
     std::vector<Obj> objs;
     bool ready = false;
-    DevBuf dObjs, dKcf, dKcd, dPts, dItems, dCounters, dS;
+    DevBuf dObjs, dSing, dKcf, dKcd, dPts, dItems, dCounters, dS, dRes;
     struct Launch {
         int which, items_off, nitems, threads, counter, chain;
         size_t smem;
@@ -57,10 +57,17 @@ struct sod_batch {
     }
 };
 
+// `which`: 0 polar (double-float), 1 Guiggiani (double-float), 2 G scatter, 3 H scatter, 4 B reduction,
+// 5 combine of G/B_trans/B_angular, 6 combine of H
 static int issue_launch(sod_batch *b, const sod_batch::Launch &L, cudaStream_t st) {
-    return batch_launch(b->ctx, L.which, b->mask, b->dObjs.p, b->dItems.as<int4>() + L.items_off, L.nitems,
-                        b->dCounters.as<int>() + L.counter, b->dKcf.as<KConst<float>>(), b->dKcd.as<KConst<double>>(),
-                        b->dPts.as<PointTable>(), L.threads, L.smem, st);
+    const int4 *items = b->dItems.as<int4>() + L.items_off;
+    if (L.which >= 2 && L.which <= 4)
+        return batch_launch(b->ctx, L.which, b->mask, b->dObjs.p, items, L.nitems, b->dCounters.as<int>() + L.counter,
+                            b->dKcf.as<KConst<float>>(), b->dPts.as<PointTable>(), L.threads, L.smem, st);
+    const int which = L.which == 5 ? 2 : L.which == 6 ? 2 : L.which;
+    const int mask = L.which == 6 ? (1 << SOD_H) : L.which == 5 ? (b->mask & ~(1 << SOD_H)) : b->mask;
+    return sing_batch_launch(b->ctx, which, mask, b->dSing.as<SingBatchObj>(), items, L.nitems, b->dKcd.as<KConst<double>>(),
+                             st);
 }
 
 static int finalize_batch(sod_batch *b) {
@@ -131,11 +138,56 @@ static int finalize_batch(sod_batch *b) {
         const sod_mesh::Coloured *cg = nullptr, *ch = nullptr;
         if (ob.T[0]) SOD_TRY(const_cast<sod_mesh *>(ob.mesh)->coloured_for(ob.T[0], &cg));
         if (ob.T[1]) SOD_TRY(const_cast<sod_mesh *>(ob.mesh)->coloured_for(ob.T[1], &ch));
-        batch_fill_args_host(ob.mesh, b->mask, b->out_dtype, ob.out, S, cg, ch, ob.sorder, ob.ssub, kc_off[o], pt_idx[o],
+        batch_fill_args_host(ob.mesh, b->mask, b->out_dtype, ob.out, S, cg, ch, kc_off[o], pt_idx[o],
                              host.data() + osz * o);
     }
     SOD_TRY(b->dObjs.ensure(host.size()));
     SOD_CHECK_CUDA(cudaMemcpy(b->dObjs.p, host.data(), host.size(), cudaMemcpyHostToDevice));
+    // singular passes: geometry tables (built once per mesh and rule), per-star-entry result buffers
+    std::vector<SingBatchObj> sing(nobj);
+    std::vector<size_t> roff(nobj), goff(nobj);
+    size_t rtot = 0;
+    for (int o = 0; o < nobj; o++) {
+        const sod_mesh *m = b->objs[o].mesh;
+        const int nstar = m->star_off.back(), nf = (int)b->objs[o].s.size() / 2;
+        roff[o] = rtot;
+        rtot += sing_result_elems(b->mask, nstar, nf, false);
+        goff[o] = rtot;
+        rtot += sing_result_elems(b->mask, nstar, nf, true);
+    }
+    SOD_TRY(b->dRes.ensure(sizeof(double2) * std::max<size_t>(rtot, 1)));
+    for (int o = 0; o < nobj; o++) {
+        auto &ob = b->objs[o];
+        const sod_mesh *m = ob.mesh;
+        const sod_mesh::SingGeom *g = nullptr;
+        SOD_TRY(const_cast<sod_mesh *>(m)->sing_geom_for(ob.sorder, ob.ssub, ctx->stream, &g));
+        SingBatchObj &d = sing[o];
+        d = SingBatchObj{};
+        d.nV = m->nV;
+        d.nstar = m->star_off.back();
+        d.nq2 = g->nq2;
+        d.polar = g->polar.as<float2>();
+        d.guig = g->guig.as<float2>();
+        d.guig_sub = g->guig_sub.as<double>();
+        d.star_off = m->dStarOff.as<int>();
+        d.star_face = m->dStarFace.as<int>();
+        d.star_slot = m->dStarSlot.as<int>();
+        d.nbr_off = m->dNbrOff.as<int>();
+        d.N = m->dN.as<double>();
+        d.Rp = b->dRes.as<double2>() + roff[o];
+        d.Rg = b->dRes.as<double2>() + goff[o];
+        const long long nslots = m->nbr_off.back();
+        const long long sfs[4] = {nslots * 9, nslots * 9, (long long)m->nV * 9, (long long)m->nV * 27};
+        for (int kd = 0; kd < 4; kd++) {
+            d.S[kd] = (b->mask & (1 << kd)) ? b->dS.as<cd>() + soff[o][kd] : nullptr;
+            d.S_fstride[kd] = sfs[kd];
+        }
+        d.kc_off = kc_off[o];
+        d.nf = (int)ob.s.size() / 2;
+    }
+    SOD_TRY(b->dSing.ensure(sizeof(SingBatchObj) * nobj));
+    SOD_CHECK_CUDA(cudaMemcpy(b->dSing.p, sing.data(), sizeof(SingBatchObj) * nobj, cudaMemcpyHostToDevice));
+    SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));  // geometry tables are complete before capture
     SOD_TRY(b->dKcf.ensure(sizeof(KConst<float>) * kcf.size()));
     SOD_TRY(b->dKcd.ensure(sizeof(KConst<double>) * kcd.size()));
     SOD_TRY(b->dPts.ensure(sizeof(PointTable) * pts.size()));
@@ -168,8 +220,32 @@ static int finalize_batch(sod_batch *b) {
         const int n = (int)items.size() - off;
         if (n > 0) b->launches.push_back({which, off, n, threads, (int)b->launches.size(), chain, sm, evals});
     };
-    if (b->mask & (KMASK_ALL & ~(1 << SOD_H))) add_list(0, 256, 0, order, 0);
-    if (b->mask & (1 << SOD_H)) add_list(1, 256, 0, order, 1);
+    // singular items: (object, frequency, first star entry) blocks of 128 entries, or (object,
+    // frequency, first vertex) blocks of 4 vertices for the combine
+    auto add_sing = [&](int which, int chain) {
+        const int off = (int)items.size();
+        const bool comb = which >= 5;
+        double evals = 0;
+        for (int o : order) {
+            const auto &ob = b->objs[o];
+            const int nstar = ob.mesh->star_off.back(), nV = ob.mesh->nV, nf = (int)ob.s.size() / 2;
+            const int nq = ob.sorder * ob.ssub;
+            const int n = comb ? nV : nstar, step = comb ? 4 : 128;
+            for (int fq = 0; fq < nf; fq++)
+                for (int x = 0; x < n; x += step) items.push_back(make_int4(o, fq, x, 0));
+            evals += comb ? (double)nf * nV : (double)nf * nstar * nq * nq;
+        }
+        const int n = (int)items.size() - off;
+        if (n > 0) b->launches.push_back({which, off, n, 128, (int)b->launches.size(), chain, 0, evals});
+    };
+    if (b->mask & (KMASK_ALL & ~(1 << SOD_H))) {
+        add_sing(0, 0);
+        add_sing(5, 0);
+    }
+    if (b->mask & (1 << SOD_H)) {
+        add_sing(1, 1);
+        add_sing(6, 1);
+    }
     for (int kd = 0; kd < 2; kd++) {
         if (!(b->mask & (1 << kd))) continue;
         // one launch per (CTA size, occupancy) class: a launch has one dynamic smem size, so small

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cstdio>
 
+#include "sod_geom.cuh"
 #include "sod_internal.h"
 
 namespace sod {
@@ -29,7 +30,7 @@ namespace sod {
 __constant__ double c_glx[5][5];
 __constant__ double c_glw[5][5];
 
-constexpr int KM_G = 1 << SOD_G, KM_H = 1 << SOD_H, KM_BT = 1 << SOD_B_TRANS, KM_BA = 1 << SOD_B_ANGULAR;
+constexpr int KM_G = 1 << SOD_G, KM_BT = 1 << SOD_B_TRANS, KM_BA = 1 << SOD_B_ANGULAR;
 
 struct FaceRec {
     float3 y1, y2, y3, n;
@@ -347,36 +348,10 @@ constexpr int MAX_STAR = 32;
 // (coloured for the G and H CTA sizes), reduction and singular passes.
 struct BatchObjDev {
     CollArgs aG, aH, aR;
-    SingArgs sa;
     int kc_off;  // first entry of this object in the batch's per-frequency constant arrays
     int pt_idx;  // its quadrature point table
     int pad[2];
 };
-
-__device__ __forceinline__ double3 ld3(const double *p, int i) { return make_double3(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
-__device__ __forceinline__ double3 operator-(double3 a, double3 b) { return make_double3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ double3 operator+(double3 a, double3 b) { return make_double3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ double3 operator*(double3 a, double s) { return make_double3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ double dot3(double3 a, double3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ double3 cross3(double3 a, double3 b) {
-    return make_double3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-}
-__device__ __forceinline__ double norm3(double3 a) { return sqrt(dot3(a, a)); }
-__device__ __forceinline__ double3 nrmz(double3 a) {
-    const double n = norm3(a);
-    return n > 0.0 ? a * (1.0 / n) : a;
-}
-
-// barycentrics of P in (A,B,C), clamped (include/barycentric_coordinates.cuh:14-38)
-__device__ __forceinline__ void bary_clamped(double3 P, double3 A, double3 B, double3 C, double L[3]) {
-    const double3 v0 = B - A, v1 = C - A, v2 = P - A;
-    const double d00 = dot3(v0, v0), d01 = dot3(v0, v1), d11 = dot3(v1, v1), d20 = dot3(v2, v0), d21 = dot3(v2, v1);
-    const double den = d00 * d11 - d01 * d01;
-    L[1] = (d11 * d20 - d01 * d21) / den;
-    L[2] = (d00 * d21 - d01 * d20) / den;
-    L[0] = 1.0 - (L[1] + L[2]);
-    for (int c = 0; c < 3; c++) L[c] = fmin(1.0, fmax(0.0, L[c]));
-}
 
 template <int NVAL> __device__ __forceinline__ void warp_sum(cd (&v)[NVAL]) {
 #pragma unroll
@@ -387,25 +362,6 @@ template <int NVAL> __device__ __forceinline__ void warp_sum(cd (&v)[NVAL]) {
             v[c].y += __shfl_xor_sync(0xffffffffu, v[c].y, o);
         }
     }
-}
-
-// Polar-rule geometry about the singular vertex (include/integrator_collocation.hpp:28-36)
-struct Polar {
-    double3 y1, y2, y3, xh, yh;
-    double a, alpha, beta;
-};
-__device__ __forceinline__ Polar polar_setup(double3 y1, double3 y2, double3 y3) {
-    Polar g;
-    g.y1 = y1, g.y2 = y2, g.y3 = y3;
-    const double3 v1 = y2 - y1, v2 = y3 - y1;
-    const double3 v1n = nrmz(v1), v2n = nrmz(v2);
-    g.xh = v1n;
-    g.yh = nrmz(cross3(cross3(g.xh, v2n), g.xh));
-    const double3 v12 = v1 + nrmz(v2 - v1) * dot3(v1, nrmz(v1 - v2));
-    g.a = norm3(v12);
-    g.alpha = acos(dot3(v1n, v2n));
-    g.beta = acos(fmin(1.0, fmax(-1.0, dot3(nrmz(v12), v1n))));
-    return g;
 }
 
 // (theta, r, weight) of flattened polar point pidx
@@ -676,33 +632,6 @@ __global__ void __launch_bounds__(256) batch_reduce_kernel(const BatchObjDev *__
     }
 }
 
-template <int MASK>
-__global__ void __launch_bounds__(256) batch_polar_kernel(const BatchObjDev *__restrict__ objs,
-                                                          const int4 *__restrict__ items, int nitems, int *counter,
-                                                          const KConst<double> *__restrict__ kcd) {
-    __shared__ int s_item;
-    for (;;) {
-        const int it = next_item(counter, &s_item);
-        if (it >= nitems) break;
-        const int4 w = items[it];
-        const BatchObjDev &o = objs[w.x];
-        polar_body<MASK>(o.sa, kcd[o.kc_off + w.z], w.y, w.z);
-    }
-}
-
-__global__ void __launch_bounds__(256) batch_guiggiani_kernel(const BatchObjDev *__restrict__ objs,
-                                                              const int4 *__restrict__ items, int nitems,
-                                                              int *counter, const KConst<double> *__restrict__ kcd) {
-    __shared__ int s_item;
-    for (;;) {
-        const int it = next_item(counter, &s_item);
-        if (it >= nitems) break;
-        const int4 w = items[it];
-        const BatchObjDev &o = objs[w.x];
-        guiggiani_body(o.sa, kcd[o.kc_off + w.z], w.y, w.z);
-    }
-}
-
 // -------------------------------------------------------------------------------------------
 // host side
 static bool g_const_ready[64] = {};
@@ -831,28 +760,7 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
             sa.S[kd] = (sing && (mask & (1 << kd))) ? Sb + soff[kd] : nullptr;
             sa.S_fstride[kd] = sfs[kd];
         }
-        if (sing) {
-            const int pm = mask & (KM_G | KM_BT | KM_BA);
-            switch (pm) {
-            case 0: break;
-            case KM_G: coll_polar_kernel<KM_G><<<grid, 256, 0, L.stream>>>(sa, ft); break;
-            case KM_BT: coll_polar_kernel<KM_BT><<<grid, 256, 0, L.stream>>>(sa, ft); break;
-            case KM_BA: coll_polar_kernel<KM_BA><<<grid, 256, 0, L.stream>>>(sa, ft); break;
-            case KM_BT | KM_BA: coll_polar_kernel<KM_BT | KM_BA><<<grid, 256, 0, L.stream>>>(sa, ft); break;
-            case KM_G | KM_BT: coll_polar_kernel<KM_G | KM_BT><<<grid, 256, 0, L.stream>>>(sa, ft); break;
-            case KM_G | KM_BA: coll_polar_kernel<KM_G | KM_BA><<<grid, 256, 0, L.stream>>>(sa, ft); break;
-            default: coll_polar_kernel<KM_G | KM_BT | KM_BA><<<grid, 256, 0, L.stream>>>(sa, ft); break;
-            }
-            if (pm) {
-                SOD_CHECK_CUDA(cudaGetLastError());
-                ctx->count();
-            }
-            if (mask & KM_H) {
-                coll_guiggiani_kernel<<<grid, 256, 0, L.stream>>>(sa, ft);
-                SOD_CHECK_CUDA(cudaGetLastError());
-                ctx->count();
-            }
-        }
+        if (sing) SOD_TRY(launch_singular(ctx, m, mask, L.sorder, L.ssub, ft.kd, nf, sa.S, sa.S_fstride, L.stream));
         CollArgs a{};
         a.nV = m->nV;
         a.nF = m->nF;
@@ -1047,8 +955,7 @@ int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, d
 size_t batch_obj_size() { return sizeof(BatchObjDev); }
 
 static void batch_fill_args(const sod_mesh *m, int kind_mask, int out_dtype, void *const out[4], cd *const S[4],
-                            const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, int sorder, int ssub,
-                            BatchObjDev &o) {
+                            const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, BatchObjDev &o) {
     const long long nslots = m->nbr_off.back();
     const long long sfs[4] = {nslots * 9, nslots * 9, (long long)m->nV * 9, (long long)m->nV * 27};
     const long long per[4] = {9LL * m->nV * m->nV, 9LL * m->nV * m->nV, 9LL * m->nV, 27LL * m->nV};
@@ -1084,30 +991,13 @@ static void batch_fill_args(const sod_mesh *m, int kind_mask, int out_dtype, voi
     }
     o.aR.faces = m->dFacesNat.as<float4>();
     o.aR.canonF = m->has_vmap ? m->dCanonNat.as<int4>() : nullptr;
-    SingArgs &sa = o.sa;
-    sa = SingArgs{};
-    sa.nV = m->nV;
-    sa.V = m->dV.as<double>();
-    sa.F = m->dF.as<int>();
-    sa.N = m->dN.as<double>();
-    sa.star_off = m->dStarOff.as<int>();
-    sa.star_face = m->dStarFace.as<int>();
-    sa.star_corner = m->dStarCorner.as<int>();
-    sa.star_slot = m->dStarSlot.as<int>();
-    sa.nbr_off = m->dNbrOff.as<int>();
-    sa.sorder = sorder;
-    sa.ssub = ssub;
-    for (int kd = 0; kd < 4; kd++) {
-        sa.S[kd] = (kind_mask & (1 << kd)) ? S[kd] : nullptr;
-        sa.S_fstride[kd] = sfs[kd];
-    }
 }
 
 void batch_fill_args_host(const sod_mesh *m, int kind_mask, int out_dtype, void *const out[4], cd *const S[4],
-                          const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, int sorder, int ssub,
-                          int kc_off, int pt_idx, void *dst) {
+                          const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, int kc_off, int pt_idx,
+                          void *dst) {
     BatchObjDev o{};
-    batch_fill_args(m, kind_mask, out_dtype, out, S, colG, colH, sorder, ssub, o);
+    batch_fill_args(m, kind_mask, out_dtype, out, S, colG, colH, o);
     o.kc_off = kc_off;
     o.pt_idx = pt_idx;
     *static_cast<BatchObjDev *>(dst) = o;
@@ -1137,49 +1027,23 @@ int batch_scatter_occupancy(int kind, int threads, size_t smem, int *per_sm) {
 // One persistent launch; grid = resident CTAs per SM x SMs.  `which`: 0 polar, 1 Guiggiani,
 // 2 scatter G, 3 scatter H, 4 reduce.
 int batch_launch(sod_context *ctx, int which, int mask, const void *objs_v, const int4 *items, int nitems,
-                 int *counter, const KConst<float> *kcf, const KConst<double> *kcd, const PointTable *pts, int threads,
-                 size_t smem, cudaStream_t stream) {
+                 int *counter, const KConst<float> *kcf, const PointTable *pts, int threads, size_t smem,
+                 cudaStream_t stream) {
     if (nitems <= 0) return SOD_OK;
+    SOD_REQUIRE(which >= 2 && which <= 4, "batch_launch: not a regular pass");
     const BatchObjDev *objs = static_cast<const BatchObjDev *>(objs_v);
     int per_sm = 1;
-    const void *fn = nullptr;
-    const int pm = mask & (KM_G | KM_BT | KM_BA), rm = mask & (KM_BT | KM_BA);
-    switch (which) {
-    case 0:
-        fn = pm == (KM_G | KM_BT | KM_BA) ? (const void *)batch_polar_kernel<KM_G | KM_BT | KM_BA>
-           : pm == KM_G                   ? (const void *)batch_polar_kernel<KM_G>
-           : pm == (KM_BT | KM_BA)        ? (const void *)batch_polar_kernel<KM_BT | KM_BA>
-           : pm == (KM_G | KM_BT)         ? (const void *)batch_polar_kernel<KM_G | KM_BT>
-           : pm == (KM_G | KM_BA)         ? (const void *)batch_polar_kernel<KM_G | KM_BA>
-           : pm == KM_BT                  ? (const void *)batch_polar_kernel<KM_BT>
-                                          : (const void *)batch_polar_kernel<KM_BA>;
-        break;
-    case 1: fn = (const void *)batch_guiggiani_kernel; break;
-    case 2: fn = (const void *)batch_scatter_kernel<SOD_G>; break;
-    case 3: fn = (const void *)batch_scatter_kernel<SOD_H>; break;
-    default:
-        fn = rm == (KM_BT | KM_BA) ? (const void *)batch_reduce_kernel<KM_BT | KM_BA>
-           : rm == KM_BT           ? (const void *)batch_reduce_kernel<KM_BT>
-                                   : (const void *)batch_reduce_kernel<KM_BA>;
-        break;
-    }
+    const int rm = mask & (KM_BT | KM_BA);
+    const void *fn = which == 2 ? (const void *)batch_scatter_kernel<SOD_G>
+                   : which == 3 ? (const void *)batch_scatter_kernel<SOD_H>
+                   : rm == (KM_BT | KM_BA) ? (const void *)batch_reduce_kernel<KM_BT | KM_BA>
+                   : rm == KM_BT ? (const void *)batch_reduce_kernel<KM_BT>
+                                 : (const void *)batch_reduce_kernel<KM_BA>;
     SOD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
     per_sm = std::max(1, per_sm);
     const int grid = std::min(nitems, per_sm * ctx->num_sms);
     SOD_CHECK_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), stream));
     switch (which) {
-    case 0:
-        switch (pm) {
-        case KM_G | KM_BT | KM_BA: batch_polar_kernel<KM_G | KM_BT | KM_BA><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
-        case KM_G: batch_polar_kernel<KM_G><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
-        case KM_BT | KM_BA: batch_polar_kernel<KM_BT | KM_BA><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
-        case KM_G | KM_BT: batch_polar_kernel<KM_G | KM_BT><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
-        case KM_G | KM_BA: batch_polar_kernel<KM_G | KM_BA><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
-        case KM_BT: batch_polar_kernel<KM_BT><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
-        default: batch_polar_kernel<KM_BA><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
-        }
-        break;
-    case 1: batch_guiggiani_kernel<<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcd); break;
     case 2: batch_scatter_kernel<SOD_G><<<grid, threads, smem, stream>>>(objs, items, nitems, counter, kcf, pts); break;
     case 3: batch_scatter_kernel<SOD_H><<<grid, threads, smem, stream>>>(objs, items, nitems, counter, kcf, pts); break;
     default:

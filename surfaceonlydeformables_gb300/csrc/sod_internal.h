@@ -105,6 +105,7 @@ struct sod_context {
     size_t smem_optin = 0;
     // scratch
     sod::DevBuf sing;      // singular corrections
+    sod::DevBuf sing_res;  // per-star-entry results of the double-float singular passes
     sod::DevBuf kconst;    // per-frequency constants
     sod::DevBuf staging;   // device staging for host outputs
     sod::DevBuf staging2;  // device staging for host inputs
@@ -138,6 +139,15 @@ struct sod_mesh {
     };
     std::map<int, std::unique_ptr<Coloured>> coloured;
     int tuned_threads[2] = {0, 0};  // scatter CTA size chosen by the autotuner for G, H (0 = not yet)
+    // frequency-independent singular-quadrature geometry per (order, subdivision), double-float
+    struct SingGeom {
+        int nq2 = 0;          // points per star entry
+        sod::DevBuf polar;    // [nq2][9][nstar] float2: r, rh.x, rh.y, rh.z, rh.n, w, w L0, w L1, w L2
+        sod::DevBuf guig;     // [nq2][8][nstar] float2: r, rh.x, rh.y, rh.z, rh.n, w L_c J rho / r^2 (c = 0..2)
+        sod::DevBuf guig_sub; // [9][nstar] double: Cauchy principal value subtraction (times kappa / 4 pi)
+    };
+    std::map<std::pair<int, int>, std::unique_ptr<SingGeom>> sing_geom;
+    int sing_geom_for(int sorder, int ssub, cudaStream_t stream, const SingGeom **out);
     // all faces in natural order (for the reduction kernels and Galerkin)
     sod::DevBuf dFacesNat, dCanonNat;
     int coloured_for(int threads, const Coloured **out);
@@ -164,6 +174,27 @@ struct CollLaunch {
     cudaStream_t stream;
 };
 int launch_collocation(sod_context *ctx, const CollLaunch &L);
+// Singular passes in double-float (sod_singular.cu): fills the side buffers S[kind] (per kind in
+// `mask`, layout of the regular kernels' epilogue) for nf frequencies; kc is a host array.
+int launch_singular(sod_context *ctx, const sod_mesh *m, int mask, int sorder, int ssub, const KConst<double> *kc,
+                    int nf, cd *const S[4], const long long S_fstride[4], cudaStream_t stream);
+// Batched singular passes: one descriptor per object, flat work lists, launched by sod_batch.
+struct SingBatchObj {
+    int nV, nstar, nq2, pad0;
+    const float2 *polar, *guig;
+    const double *guig_sub;
+    const int *star_off, *star_face, *star_slot, *nbr_off;
+    const double *N;
+    double2 *Rp, *Rg;  // per (frequency, component, star entry) results of the two passes
+    cd *S[4];
+    long long S_fstride[4];
+    int kc_off, nf;
+};
+size_t sing_result_elems(int mask, int nstar, int nf, bool guiggiani);
+// singular passes of a batch: `which` 0 polar (G, B_trans, B_angular), 1 Guiggiani (H), 2 combine
+// of the kinds in `mask`; one CTA per item
+int sing_batch_launch(sod_context *ctx, int which, int mask, const SingBatchObj *objs, const int4 *items, int nitems,
+                      const KConst<double> *kcd, cudaStream_t stream);
 // Allocation-free launcher over caller-provided scratch (see sod_collocation.cu).
 int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, double c1, double c2, double rho,
                                 const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, void *out,
@@ -173,13 +204,13 @@ bool is_device_pointer(const void *p);
 struct BatchObjDev;
 size_t batch_obj_size();
 void batch_fill_args_host(const sod_mesh *m, int kind_mask, int out_dtype, void *const out[4], cd *const S[4],
-                          const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, int sorder, int ssub,
-                          int kc_off, int pt_idx, void *dst);
+                          const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, int kc_off, int pt_idx,
+                          void *dst);
 int batch_prepare_kernels(sod_context *ctx, size_t smem_G, size_t smem_H);
 int batch_scatter_occupancy(int kind, int threads, size_t smem, int *per_sm);
+// regular passes of a batch: `which` 2 G scatter, 3 H scatter, 4 B reduction (persistent launches)
 int batch_launch(sod_context *ctx, int which, int mask, const void *objs, const int4 *items, int nitems, int *counter,
-                 const KConst<float> *kcf, const KConst<double> *kcd, const PointTable *pts, int threads, size_t smem,
-                 cudaStream_t stream);
+                 const KConst<float> *kcf, const PointTable *pts, int threads, size_t smem, cudaStream_t stream);
 // Deterministic autotuner of the scatter kernels' CTA size (see sod_collocation.cu).
 int autotune_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int *threads);
 int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, int64_t M, int nfreq, int L,
