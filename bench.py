@@ -36,8 +36,9 @@ sys.path.insert(0, ROOT)
 # algorithmic FP32 flops per kernel evaluation (field point x quadrature point x frequency),
 # regular collocation pass: geometry + two complex exponentials + kernel combination
 FLOPS_PER_EVAL = {"G": 130, "H": 240, "B_trans": 60, "B_angular": 150}
-# per batched pass: the B reduction evaluates B_trans and B_angular from one set of radial terms
-PASS_FLOPS = {"scatter_G": 130, "scatter_H": 240, "reduce_B": 210}
+# per batched pass: the G scatter also integrates B_trans and B_angular from the same radial terms
+# (130 + 60 + 150); the stand-alone B reduction (batches without G) does 60 + 150
+PASS_FLOPS = {"scatter_G": 340, "scatter_H": 240, "reduce_B": 210}
 # DRAM bytes per evaluation of each pass from an ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum over the launch's evaluations); filled from the committed profile summaries
 TRAFFIC_BYTES_PER_EVAL: dict = {}
@@ -353,8 +354,9 @@ def run_gpu(args):
     dom = max(fp32, key=lambda p: p["ms"])
     achieved = dom["evals"] * PASS_FLOPS[dom["pass"]] / (dom["ms"] * 1e-3) / 1e12
     traffic = TRAFFIC_BYTES_PER_EVAL.get(dom["pass"])
-    roofline = {"bound": "fp32", "kernel": f"batch_scatter_kernel<{dom['pass'][-1]}>" if "scatter" in dom["pass"]
-                else "batch_reduce_kernel<B_trans|B_angular>",
+    names = {"scatter_G": "batch_scatter_kernel<G, B_trans|B_angular>", "scatter_H": "batch_scatter_kernel<H>",
+             "reduce_B": "batch_reduce_kernel<B_trans|B_angular>"}
+    roofline = {"bound": "fp32", "kernel": names[dom["pass"]],
                 "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s", "frac": achieved / peak_fp32,
                 "peak_source": "measured live: cuBLAS SGEMM 8192^3, TF32 off (no FP32 figure in the measured "
                                "peaks file)",

@@ -3,23 +3,32 @@
 //
 // A batch collects objects (mesh, material, Laplace frequencies, device outputs).  finalize():
 //   * picks every object's scatter CTA size with the mesh autotuner and builds its colourings;
-//   * lays out one FP64 singular side buffer for all (object, frequency) pairs;
-//   * writes one device descriptor per object (kernel arguments of every pass);
-//   * builds the work lists -- (object, field vertex, frequency) items, largest objects first --
-//     for the singular passes, one scatter list per (kind, CTA size) class and the B reduction;
-//   * captures the whole step (counter resets + persistent launches) into a CUDA graph.
+//   * lays out one FP64 singular side buffer for all (object, frequency) pairs and the per-star-
+//     entry result buffers of the double-float singular passes;
+//   * builds the work lists, largest objects first: (object, frequency, star-entry block) items for
+//     the singular passes, (object, field vertex, frequency) items for one persistent launch per
+//     (pass, CTA size, occupancy, point table) class of the regular passes, whose kernel arguments
+//     travel in kernel-parameter space (up to BATCH_OBJS objects per launch);
+//   * captures the whole step into a CUDA graph with two concurrent chains:
+//       0: polar (G, B) -> combine -> G scatter (B_trans / B_angular fused in),
+//       1: Guiggiani (H) -> combine -> H scatter.
 // run() replays the graph on the context's stream: one host call per step, no per-object launches.
 #include <algorithm>
 #include <array>
 #include <map>
+#include <memory>
 #include <numeric>
+#include <tuple>
 #include <vector>
 
 #include "sod_internal.h"
 
 namespace sod {
 constexpr int KMASK_ALL = 15;
-}
+struct RegularDeleter {
+    void operator()(BatchRegular *r) const { batch_regular_free(r); }
+};
+}  // namespace sod
 using namespace sod;
 
 struct sod_batch {
@@ -36,11 +45,11 @@ struct sod_batch {
     };
     std::vector<Obj> objs;
     bool ready = false;
-    DevBuf dObjs, dSing, dKcf, dKcd, dPts, dItems, dCounters, dS, dRes;
+    DevBuf dSing, dKcf, dKcd, dItems, dCounters, dS, dRes;
     struct Launch {
         int which, items_off, nitems, threads, counter, chain;
-        size_t smem;
-        double evals;  // kernel evaluations (regular) or singular quadrature points in the launch
+        double evals;  // kernel evaluations (regular), singular quadrature points, or vertex-frequencies
+        std::shared_ptr<BatchRegular> reg;  // regular passes: kernel arguments
     };
     std::vector<Launch> launches;
     cudaStream_t cap = nullptr, cap2 = nullptr;
@@ -57,30 +66,31 @@ struct sod_batch {
     }
 };
 
-// `which`: 0 polar (double-float), 1 Guiggiani (double-float), 2 G scatter, 3 H scatter, 4 B reduction,
-// 5 combine of G/B_trans/B_angular, 6 combine of H
+// `which`: 0 polar (double-float), 1 Guiggiani (double-float), 2 G scatter (+B), 3 H scatter,
+// 4 B reduction, 5 combine of G/B_trans/B_angular, 6 combine of H
 static int issue_launch(sod_batch *b, const sod_batch::Launch &L, cudaStream_t st) {
     const int4 *items = b->dItems.as<int4>() + L.items_off;
     if (L.which >= 2 && L.which <= 4)
-        return batch_launch(b->ctx, L.which, b->mask, b->dObjs.p, items, L.nitems, b->dCounters.as<int>() + L.counter,
-                            b->dKcf.as<KConst<float>>(), b->dPts.as<PointTable>(), L.threads, L.smem, st);
-    const int which = L.which == 5 ? 2 : L.which == 6 ? 2 : L.which;
+        return batch_regular_issue(b->ctx, L.reg.get(), items, L.nitems, b->dCounters.as<int>() + L.counter,
+                                   b->dKcf.as<KConst<float>>(), st);
+    const int which = L.which >= 5 ? 2 : L.which;
     const int mask = L.which == 6 ? (1 << SOD_H) : L.which == 5 ? (b->mask & ~(1 << SOD_H)) : b->mask;
-    return sing_batch_launch(b->ctx, which, mask, b->dSing.as<SingBatchObj>(), items, L.nitems, b->dKcd.as<KConst<double>>(),
-                             st);
+    return sing_batch_launch(b->ctx, which, mask, b->dSing.as<SingBatchObj>(), items, L.nitems,
+                             b->dKcd.as<KConst<double>>(), st);
 }
 
 static int finalize_batch(sod_batch *b) {
     sod_context *ctx = b->ctx;
     SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
     const int nobj = (int)b->objs.size();
+    const bool hasG = (b->mask & (1 << SOD_G)) != 0;
+    const int bmask = b->mask & ((1 << SOD_B_TRANS) | (1 << SOD_B_ANGULAR));
     // quadrature tables (deduplicated) and per-frequency constants
     std::vector<PointTable> pts;
     std::map<std::pair<int, int>, int> pt_index;
     std::vector<KConst<float>> kcf;
     std::vector<KConst<double>> kcd;
     std::vector<int> kc_off(nobj), pt_idx(nobj);
-    size_t smem[2] = {0, 0};
     for (int o = 0; o < nobj; o++) {
         auto &ob = b->objs[o];
         auto key = std::make_pair(ob.order, ob.subdiv);
@@ -102,17 +112,10 @@ static int finalize_batch(sod_batch *b) {
         for (int kd = 0; kd < 2; kd++) {
             ob.T[kd] = 0;
             if (!(b->mask & (1 << kd))) continue;
+            const int bm = kd == SOD_G ? bmask : 0;
             int T = ctx->coll_threads;
-            if (T <= 0) SOD_TRY(autotune_scatter_threads(ctx, const_cast<sod_mesh *>(ob.mesh), kd, &T));
+            if (T <= 0) SOD_TRY(autotune_scatter_threads(ctx, const_cast<sod_mesh *>(ob.mesh), kd, bm, &T));
             ob.T[kd] = T;
-            const sod_mesh::Coloured *c = nullptr;
-            SOD_TRY(const_cast<sod_mesh *>(ob.mesh)->coloured_for(T, &c));
-            const size_t sm = sizeof(float2) * (kd == SOD_G ? 6 : 9) * (size_t)ob.mesh->nV;
-            if (sm > ctx->smem_optin) {
-                set_error("mesh too large for the shared-memory row accumulator");
-                return SOD_ERR_UNSUPPORTED;
-            }
-            smem[kd] = std::max(smem[kd], sm);
         }
     }
     // singular side buffer layout
@@ -128,21 +131,6 @@ static int finalize_batch(sod_batch *b) {
         }
     }
     SOD_TRY(b->dS.ensure(sizeof(cd) * (size_t)std::max<long long>(stot, 1)));
-    // device descriptors
-    const size_t osz = batch_obj_size();
-    std::vector<char> host(osz * nobj);
-    for (int o = 0; o < nobj; o++) {
-        auto &ob = b->objs[o];
-        cd *S[4];
-        for (int kd = 0; kd < 4; kd++) S[kd] = b->dS.as<cd>() + soff[o][kd];
-        const sod_mesh::Coloured *cg = nullptr, *ch = nullptr;
-        if (ob.T[0]) SOD_TRY(const_cast<sod_mesh *>(ob.mesh)->coloured_for(ob.T[0], &cg));
-        if (ob.T[1]) SOD_TRY(const_cast<sod_mesh *>(ob.mesh)->coloured_for(ob.T[1], &ch));
-        batch_fill_args_host(ob.mesh, b->mask, b->out_dtype, ob.out, S, cg, ch, kc_off[o], pt_idx[o],
-                             host.data() + osz * o);
-    }
-    SOD_TRY(b->dObjs.ensure(host.size()));
-    SOD_CHECK_CUDA(cudaMemcpy(b->dObjs.p, host.data(), host.size(), cudaMemcpyHostToDevice));
     // singular passes: geometry tables (built once per mesh and rule), per-star-entry result buffers
     std::vector<SingBatchObj> sing(nobj);
     std::vector<size_t> roff(nobj), goff(nobj);
@@ -190,36 +178,15 @@ static int finalize_batch(sod_batch *b) {
     SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));  // geometry tables are complete before capture
     SOD_TRY(b->dKcf.ensure(sizeof(KConst<float>) * kcf.size()));
     SOD_TRY(b->dKcd.ensure(sizeof(KConst<double>) * kcd.size()));
-    SOD_TRY(b->dPts.ensure(sizeof(PointTable) * pts.size()));
     SOD_CHECK_CUDA(cudaMemcpy(b->dKcf.p, kcf.data(), sizeof(KConst<float>) * kcf.size(), cudaMemcpyHostToDevice));
     SOD_CHECK_CUDA(cudaMemcpy(b->dKcd.p, kcd.data(), sizeof(KConst<double>) * kcd.size(), cudaMemcpyHostToDevice));
-    SOD_CHECK_CUDA(cudaMemcpy(b->dPts.p, pts.data(), sizeof(PointTable) * pts.size(), cudaMemcpyHostToDevice));
     // work lists, objects ordered by decreasing face count (largest items first)
     std::vector<int> order(nobj);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
                      [&](int x, int y) { return b->objs[x].mesh->nF > b->objs[y].mesh->nF; });
-    SOD_TRY(batch_prepare_kernels(ctx, smem[0], smem[1]));
     std::vector<int4> items;
     b->launches.clear();
-    // chain 0: weakly singular pass -> G scatter classes -> B reduction; chain 1: Guiggiani -> H
-    // scatter classes.  The two chains run concurrently inside the graph.
-    auto add_list = [&](int which, int threads, size_t sm, const std::vector<int> &objs_in, int chain) {
-        const int off = (int)items.size();
-        double evals = 0;
-        for (int o : objs_in) {
-            const auto &ob = b->objs[o];
-            const int nV = ob.mesh->nV, nF = ob.mesh->nF, nf = (int)ob.s.size() / 2;
-            for (int fq = 0; fq < nf; fq++)
-                for (int i = 0; i < nV; i++) items.push_back(make_int4(o, i, fq, 0));
-            if (which <= 1)
-                evals += (double)nf * 3.0 * nF * (double)(ob.sorder * ob.ssub) * (ob.sorder * ob.ssub);
-            else
-                evals += (double)nf * ((double)nV * nF - 3.0 * nF) * pts[pt_idx[o]].n;
-        }
-        const int n = (int)items.size() - off;
-        if (n > 0) b->launches.push_back({which, off, n, threads, (int)b->launches.size(), chain, sm, evals});
-    };
     // singular items: (object, frequency, first star entry) blocks of 128 entries, or (object,
     // frequency, first vertex) blocks of 4 vertices for the combine
     auto add_sing = [&](int which, int chain) {
@@ -236,7 +203,7 @@ static int finalize_batch(sod_batch *b) {
             evals += comb ? (double)nf * nV : (double)nf * nstar * nq * nq;
         }
         const int n = (int)items.size() - off;
-        if (n > 0) b->launches.push_back({which, off, n, 128, (int)b->launches.size(), chain, 0, evals});
+        if (n > 0) b->launches.push_back({which, off, n, 128, (int)b->launches.size(), chain, evals, nullptr});
     };
     if (b->mask & (KMASK_ALL & ~(1 << SOD_H))) {
         add_sing(0, 0);
@@ -246,24 +213,61 @@ static int finalize_batch(sod_batch *b) {
         add_sing(1, 1);
         add_sing(6, 1);
     }
-    for (int kd = 0; kd < 2; kd++) {
-        if (!(b->mask & (1 << kd))) continue;
-        // one launch per (CTA size, occupancy) class: a launch has one dynamic smem size, so small
-        // objects are not grouped with large ones that would lower their resident CTAs per SM
-        std::map<std::pair<int, int>, std::vector<int>> classes;
+    // regular passes: one persistent launch per (pass, CTA size, occupancy, point table) class and
+    // per BATCH_OBJS objects; a launch shares one dynamic smem size, so small objects are not
+    // grouped with large ones that would lower their resident CTAs per SM
+    auto add_regular = [&](int which, int chain) -> int {
+        const int kind = which == 3 ? SOD_H : SOD_G;
+        const int bm = which == 3 ? 0 : bmask;
+        std::map<std::tuple<int, int, int>, std::vector<int>> classes;
         for (int o : order) {
-            const size_t sm = sizeof(float2) * (kd == SOD_G ? 6 : 9) * (size_t)b->objs[o].mesh->nV;
-            int per_sm = 0;
-            SOD_TRY(batch_scatter_occupancy(kd, b->objs[o].T[kd], sm, &per_sm));
-            classes[{-per_sm, b->objs[o].T[kd]}].push_back(o);
+            const auto &ob = b->objs[o];
+            int T = 256, per_sm = 0;
+            if (which != 4) {
+                T = ob.T[kind];
+                SOD_TRY(scatter_occupancy(ctx, kind, bm, true, T, scatter_smem_bytes(kind, bm, ob.mesh->nV, T), &per_sm));
+                if (per_sm <= 0) {
+                    set_error("mesh too large for the shared-memory row accumulator");
+                    return SOD_ERR_UNSUPPORTED;
+                }
+            }
+            classes[std::make_tuple(-per_sm, T, pt_idx[o])].push_back(o);
         }
         for (auto &c : classes) {
-            size_t sm = 0;
-            for (int o : c.second) sm = std::max(sm, sizeof(float2) * (kd == SOD_G ? 6 : 9) * (size_t)b->objs[o].mesh->nV);
-            add_list(2 + kd, c.first.second, sm, c.second, kd == SOD_G ? 0 : 1);
+            const int T = std::get<1>(c.first), pi = std::get<2>(c.first);
+            const auto &members = c.second;
+            for (size_t g0 = 0; g0 < members.size(); g0 += BATCH_OBJS) {
+                const size_t g1 = std::min(members.size(), g0 + (size_t)BATCH_OBJS);
+                size_t sm = 0;
+                for (size_t g = g0; g < g1; g++)
+                    if (which != 4) sm = std::max(sm, scatter_smem_bytes(kind, bm, b->objs[members[g]].mesh->nV, T));
+                std::shared_ptr<BatchRegular> reg(batch_regular_new(which, b->mask, T, sm, pts[pi]), RegularDeleter());
+                const int off = (int)items.size();
+                double evals = 0;
+                for (size_t g = g0; g < g1; g++) {
+                    const int o = members[g];
+                    const auto &ob = b->objs[o];
+                    const sod_mesh *m = ob.mesh;
+                    cd *S[4];
+                    for (int kd = 0; kd < 4; kd++) S[kd] = b->dS.as<cd>() + soff[o][kd];
+                    const sod_mesh::Coloured *col = nullptr;
+                    if (which != 4) SOD_TRY(const_cast<sod_mesh *>(m)->coloured_for(T, &col));
+                    int slot = 0;
+                    SOD_TRY(batch_regular_add(reg.get(), m, b->out_dtype, ob.out, S, col, kc_off[o], &slot));
+                    const int nf = (int)ob.s.size() / 2;
+                    for (int fq = 0; fq < nf; fq++)
+                        for (int i = 0; i < m->nV; i++) items.push_back(make_int4(slot, i, fq, 0));
+                    evals += (double)nf * ((double)m->nV * m->nF - 3.0 * m->nF) * pts[pi].n;
+                }
+                const int n = (int)items.size() - off;
+                if (n > 0) b->launches.push_back({which, off, n, T, (int)b->launches.size(), chain, evals, reg});
+            }
         }
-    }
-    if (b->mask & ((1 << SOD_B_TRANS) | (1 << SOD_B_ANGULAR))) add_list(4, 256, 0, order, 0);
+        return SOD_OK;
+    };
+    if (hasG) SOD_TRY(add_regular(2, 0));
+    if (b->mask & (1 << SOD_H)) SOD_TRY(add_regular(3, 1));
+    if (!hasG && bmask) SOD_TRY(add_regular(4, 0));
     SOD_TRY(b->dItems.ensure(sizeof(int4) * std::max<size_t>(items.size(), 1)));
     SOD_CHECK_CUDA(cudaMemcpy(b->dItems.p, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
     SOD_TRY(b->dCounters.ensure(sizeof(int) * std::max<size_t>(b->launches.size(), 1)));

@@ -86,13 +86,119 @@ __device__ __forceinline__ void store_out(void *out, int c64, long long idx, dou
 }
 
 // -------------------------------------------------------------------------------------------
-// G / H regular scatter kernel
-template <int KIND>
+// B_trans / B_angular moments of one face (BM subset of KM_BT | KM_BA).  The tensor structure
+// depends only on the face normal, so the quadrature accumulates scalar moments and the face
+// tensor is formed once per face:
+//     B_trans   b_pq  = Ms_p n_q + Ms_q n_p + d_pq Md
+//     B_angular b_pqk = M1_pk n_q + M1_qk n_p + (M0 + SB)(d_qk n_p + d_pk n_q) + SC d_pq n_k
+// Component order of the face tensor: B_trans sym(p,q) (6), then B_angular 3 sym(p,q) + k (18).
+template <int BM> struct BMom {
+    static constexpr bool BT = (BM & KM_BT) != 0, BA = (BM & KM_BA) != 0;
+    static constexpr int NT = BT ? 6 : 0, NA = BA ? 18 : 0, NC = NT + NA;
+    cf Ms[3], Md, M1[6], M0, SB, SC;
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int c = 0; c < 3; c++) Ms[c] = mk(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < 6; c++) M1[c] = mk(0.f, 0.f);
+        Md = M0 = SB = SC = mk(0.f, 0.f);
+    }
+    __device__ __forceinline__ void add(const RadialTerms<float, cf> &t, const KConst<float> &k, float r,
+                                        const float rh[3], const float nn[3], float w) {
+        if (BT) {
+            cf sy, di;
+            bt_coeffs(t, k, 1.0f, sy, di);
+            const cf ws = sy * w;
+#pragma unroll
+            for (int p = 0; p < 3; p++) cfma(Ms[p], ws, rh[p]);
+            cfma(Md, di, w * (rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2]));
+        }
+        if (BA) {
+            cf A, Bq, Cq;
+            ba_coeffs(t, k, r, 1.0f, A, Bq, Cq);
+            const cf wA = A * w;
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int kk = p; kk < 3; kk++) cfma(M1[sym_index(p, kk)], wA, rh[p] * rh[kk]);
+            M0 = M0 + wA;
+            cfma(SB, Bq, w);
+            cfma(SC, Cq, w);
+        }
+    }
+    // face tensor times `ar`, component by component: sink(c, value)
+    template <class Sink> __device__ __forceinline__ void emit(const float nn[3], float ar, Sink &&sink) const {
+        if (BT) {
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int qq = p; qq < 3; qq++) {
+                    cf v = Ms[p] * nn[qq] + Ms[qq] * nn[p];
+                    if (p == qq) v = v + Md;
+                    sink(sym_index(p, qq), v * ar);
+                }
+        }
+        if (BA) {
+            const cf M0B = M0 + SB;
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int qq = p; qq < 3; qq++)
+#pragma unroll
+                    for (int kk = 0; kk < 3; kk++) {
+                        cf v = M1[sym_index(p, kk)] * nn[qq] + M1[sym_index(qq, kk)] * nn[p];
+                        const float t2 = (qq == kk ? nn[p] : 0.f) + (p == kk ? nn[qq] : 0.f);
+                        v = v + M0B * t2;
+                        if (p == qq) v = v + SC * nn[kk];
+                        sink(NT + 3 * sym_index(p, qq) + kk, v * ar);
+                    }
+        }
+    }
+};
+
+// Final B_trans / B_angular store of field vertex i from the CTA's component sums `bsum` (FP64),
+// plus the singular side buffers.
+template <int BM>
+__device__ __forceinline__ void store_b(const CollArgs &a, const cd *bsum, int i, int fq) {
+    using M = BMom<BM>;
+    if (M::BT) {
+        const long long base = (long long)fq * a.fstride[SOD_B_TRANS] + (long long)(3 * i) * 3;
+        for (int e = threadIdx.x; e < 9; e += blockDim.x) {
+            const int p = e / 3, qq = e % 3;
+            cd s = bsum[sym_index(p, qq)];
+            if (a.S[SOD_B_TRANS])
+                s = s + a.S[SOD_B_TRANS][(long long)fq * a.S_fstride[SOD_B_TRANS] + (long long)i * 9 + e];
+            store_out(a.out[SOD_B_TRANS], a.out_c64, base + e, s.x, s.y);
+        }
+    }
+    if (M::BA) {
+        const long long base = (long long)fq * a.fstride[SOD_B_ANGULAR] + (long long)(3 * i) * 9;
+        for (int e = threadIdx.x; e < 27; e += blockDim.x) {
+            const int p = e / 9, qq = (e / 3) % 3, kk = e % 3;
+            cd s = bsum[M::NT + 3 * sym_index(p, qq) + kk];
+            if (a.S[SOD_B_ANGULAR])
+                s = s + a.S[SOD_B_ANGULAR][(long long)fq * a.S_fstride[SOD_B_ANGULAR] + (long long)i * 27 + e];
+            store_out(a.out[SOD_B_ANGULAR], a.out_c64, base + e, s.x, s.y);
+        }
+    }
+}
+
+// -------------------------------------------------------------------------------------------
+// G / H regular scatter kernel.  With BM != 0 (G only) the same pass also integrates B_trans /
+// B_angular: the radial terms are shared, each thread adds its faces' B tensors into its own column
+// of a shared [NC_B][blockDim] accumulator, and the CTA sums the columns in FP64 in fixed order.
+// Dynamic shared memory: NC * nV float2 (row accumulator) + NC_B * blockDim float2.
+template <int KIND, int BM>
 __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable &pt, const KConst<float> k, int i,
                                              int fq, float2 *acc) {
     constexpr int NC = KIND == SOD_G ? 6 : 9;  // acc: [NC][nV]
+    using BMo = BMom<KIND == SOD_G ? BM : 0>;
+    constexpr int NCB = BMo::NC;
     const int nV = a.nV;
+    float2 *accB = acc + NC * nV;  // [NCB][blockDim.x]
     for (int t = threadIdx.x; t < NC * nV; t += blockDim.x) acc[t] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int c = 0; c < NCB; c++) accB[c * blockDim.x + threadIdx.x] = make_float2(0.f, 0.f);
     const float3 x = make_float3(a.Vf[3 * i], a.Vf[3 * i + 1], a.Vf[3 * i + 2]);
     const int ci = a.canonV ? a.canonV[i] : i;
     __syncthreads();
@@ -102,11 +208,14 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
             for (int f = a.color_off[c] + threadIdx.x; f < fend; f += blockDim.x) {
                 const FaceRec fr = load_face(a.faces, f);
                 if (is_singular(a, i, ci, f, fr)) continue;
+                const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
                 cf part[3][NC];
 #pragma unroll
                 for (int kk = 0; kk < 3; kk++)
 #pragma unroll
                     for (int cc = 0; cc < NC; cc++) part[kk][cc] = mk(0.f, 0.f);
+                BMo bm;
+                if (NCB) bm.zero();
                 for (int q = 0; q < pt.n; q++) {
                     const float4 P = pt.p[q];
                     const float yx = P.x * fr.y1.x + P.y * fr.y2.x + P.z * fr.y3.x;
@@ -133,7 +242,6 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
                     } else {
                         cf ha, hb, hd;
                         h_coeffs(t, k, rinv * rinv, ha, hb, hd);
-                        const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
                         const float rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
                         const cf hdr = hd * rn, hbr = hb * rn;
 #pragma unroll
@@ -151,6 +259,7 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
                     for (int kk = 0; kk < 3; kk++)
 #pragma unroll
                         for (int cc = 0; cc < NC; cc++) cfma(part[kk][cc], u[cc], wl[kk]);
+                    if (NCB) bm.add(t, k, r, rh, nn, P.w);
                 }
                 const int jj[3] = {fr.j0, fr.j1, fr.j2};
 #pragma unroll
@@ -161,6 +270,14 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
                         s.x += part[kk][cc].x;
                         s.y += part[kk][cc].y;
                     }
+                if (NCB) {
+                    float2 *col = accB + threadIdx.x;
+                    bm.emit(nn, fr.area, [&](int cc, cf v) {
+                        float2 &s = col[cc * blockDim.x];
+                        s.x += v.x;
+                        s.y += v.y;
+                    });
+                }
             }
             __syncthreads();
         }
@@ -189,25 +306,50 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
             store_out(a.out[KIND], a.out_c64, base + p * ld + 3 * j + qq, (double)v.x + sv.x, (double)v.y + sv.y);
         }
     }
+    if (NCB) {
+        // column sums in FP64: 32 lanes per component, strided partial sums, fixed xor-tree
+        __shared__ cd bsum[24];
+        __syncthreads();
+        const int T = blockDim.x;
+        for (int p = threadIdx.x; p < NCB * 32; p += T) {
+            const int cc = p >> 5, l = p & 31;
+            double sx = 0.0, sy = 0.0;
+            for (int j = l; j < T; j += 32) {
+                const float2 v = accB[cc * T + j];
+                sx += v.x;
+                sy += v.y;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sx += __shfl_xor_sync(0xffffffffu, sx, o);
+                sy += __shfl_xor_sync(0xffffffffu, sy, o);
+            }
+            if (l == 0) bsum[cc] = mk(sx, sy);
+        }
+        __syncthreads();
+        store_b<BM>(a, bsum, i, fq);
+    }
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(512, 1) coll_scatter_kernel(CollArgs a, PointTable pt,
+// Fused G + B variants are limited to 384 threads so that they may use up to 170 registers.
+template <int KIND, int BM> constexpr int scatter_max_threads() { return (KIND == SOD_G && BM) ? 384 : 512; }
+
+template <int KIND, int BM>
+__global__ void __launch_bounds__(scatter_max_threads<KIND, BM>(), 1) coll_scatter_kernel(CollArgs a, PointTable pt,
                                                                const __grid_constant__ FreqTable ft) {
     extern __shared__ float2 acc[];
-    scatter_body<KIND>(a, pt, ft.kf[blockIdx.y], blockIdx.x, blockIdx.y, acc);
+    scatter_body<KIND, BM>(a, pt, ft.kf[blockIdx.y], blockIdx.x, blockIdx.y, acc);
 }
 
 // -------------------------------------------------------------------------------------------
-// B_trans / B_angular regular reduction kernel (MASK subset of KM_BT | KM_BA)
-//   per-face moments (the tensor structure depends only on the face normal):
-//     B_trans   b_pq  = Ms_p n_q + Ms_q n_p + d_pq Md
-//     B_angular b_pqk = M1_pk n_q + M1_qk n_p + (M0 + SB)(d_qk n_p + d_pk n_q) + SC d_pq n_k
+// B_trans / B_angular regular reduction kernel (MASK subset of KM_BT | KM_BA), used when G is not
+// assembled in the same call: per-thread sums over faces in FP32, fixed-order warp/CTA reduction in
+// FP64.
 template <int MASK>
 __device__ __forceinline__ void reduce_body(const CollArgs &a, const PointTable &pt, const KConst<float> k, int i,
                                             int fq) {
-    constexpr bool BT = (MASK & KM_BT) != 0, BA = (MASK & KM_BA) != 0;
-    constexpr int NT = BT ? 6 : 0, NA = BA ? 18 : 0, NC = NT + NA;
+    using BMo = BMom<MASK>;
+    constexpr int NC = BMo::NC;
     const float3 x = make_float3(a.Vf[3 * i], a.Vf[3 * i + 1], a.Vf[3 * i + 2]);
     const int ci = a.canonV ? a.canonV[i] : i;
     cf accl[NC];
@@ -218,11 +360,8 @@ __device__ __forceinline__ void reduce_body(const CollArgs &a, const PointTable 
             const FaceRec fr = load_face(a.faces, f);
             if (is_singular(a, i, ci, f, fr)) continue;
             const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
-            cf Ms[3], Md = mk(0.f, 0.f), M1[6], M0 = mk(0.f, 0.f), SB = mk(0.f, 0.f), SC = mk(0.f, 0.f);
-#pragma unroll
-            for (int c = 0; c < 3; c++) Ms[c] = mk(0.f, 0.f);
-#pragma unroll
-            for (int c = 0; c < 6; c++) M1[c] = mk(0.f, 0.f);
+            BMo bm;
+            bm.zero();
             for (int q = 0; q < pt.n; q++) {
                 const float4 P = pt.p[q];
                 const float dx = P.x * fr.y1.x + P.y * fr.y2.x + P.z * fr.y3.x - x.x;
@@ -233,58 +372,14 @@ __device__ __forceinline__ void reduce_body(const CollArgs &a, const PointTable 
                 const float r = r2 * rinv;
                 const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
                 const RadialTerms<float, cf> t = radial<float, cf>(r, k);
-                const float w = P.w;
-                if (BT) {
-                    cf sy, di;
-                    bt_coeffs(t, k, 1.0f, sy, di);
-                    const cf ws = sy * w;
-#pragma unroll
-                    for (int p = 0; p < 3; p++) cfma(Ms[p], ws, rh[p]);
-                    cfma(Md, di, w * (rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2]));
-                }
-                if (BA) {
-                    cf A, Bq, Cq;
-                    ba_coeffs(t, k, r, 1.0f, A, Bq, Cq);
-                    const cf wA = A * w;
-#pragma unroll
-                    for (int p = 0; p < 3; p++)
-#pragma unroll
-                        for (int kk = p; kk < 3; kk++) cfma(M1[sym_index(p, kk)], wA, rh[p] * rh[kk]);
-                    M0 = M0 + wA;
-                    cfma(SB, Bq, w);
-                    cfma(SC, Cq, w);
-                }
+                bm.add(t, k, r, rh, nn, P.w);
             }
-            const float ar = fr.area;
-            if (BT) {
-#pragma unroll
-                for (int p = 0; p < 3; p++)
-#pragma unroll
-                    for (int qq = p; qq < 3; qq++) {
-                        cf v = Ms[p] * nn[qq] + Ms[qq] * nn[p];
-                        if (p == qq) v = v + Md;
-                        cfma(accl[sym_index(p, qq)], v, ar);
-                    }
-            }
-            if (BA) {
-                const cf M0B = M0 + SB;
-#pragma unroll
-                for (int p = 0; p < 3; p++)
-#pragma unroll
-                    for (int qq = p; qq < 3; qq++)
-#pragma unroll
-                        for (int kk = 0; kk < 3; kk++) {
-                            cf v = M1[sym_index(p, kk)] * nn[qq] + M1[sym_index(qq, kk)] * nn[p];
-                            const float t2 = (qq == kk ? nn[p] : 0.f) + (p == kk ? nn[qq] : 0.f);
-                            v = v + M0B * t2;
-                            if (p == qq) v = v + SC * nn[kk];
-                            cfma(accl[NT + 3 * sym_index(p, qq) + kk], v, ar);
-                        }
-            }
+            bm.emit(nn, fr.area, [&](int c, cf v) { accl[c] = accl[c] + v; });
         }
     }
     // deterministic reduction in FP64: warp butterfly then fixed-order over warps
     __shared__ cd wsum[8][NC];
+    __shared__ cd bsum[NC];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int c = 0; c < NC; c++) {
@@ -298,28 +393,13 @@ __device__ __forceinline__ void reduce_body(const CollArgs &a, const PointTable 
     }
     __syncthreads();
     const int nw = blockDim.x >> 5;
-    if (BT) {
-        const long long base = (long long)fq * a.fstride[SOD_B_TRANS] + (long long)(3 * i) * 3;
-        for (int e = threadIdx.x; e < 9; e += blockDim.x) {
-            const int p = e / 3, qq = e % 3;
-            cd s = mk(0.0, 0.0);
-            for (int w = 0; w < nw; w++) s = s + wsum[w][sym_index(p, qq)];
-            if (a.S[SOD_B_TRANS])
-                s = s + a.S[SOD_B_TRANS][(long long)fq * a.S_fstride[SOD_B_TRANS] + (long long)i * 9 + e];
-            store_out(a.out[SOD_B_TRANS], a.out_c64, base + e, s.x, s.y);
-        }
+    for (int c = threadIdx.x; c < NC; c += blockDim.x) {
+        cd s = mk(0.0, 0.0);
+        for (int w = 0; w < nw; w++) s = s + wsum[w][c];
+        bsum[c] = s;
     }
-    if (BA) {
-        const long long base = (long long)fq * a.fstride[SOD_B_ANGULAR] + (long long)(3 * i) * 9;
-        for (int e = threadIdx.x; e < 27; e += blockDim.x) {
-            const int p = e / 9, qq = (e / 3) % 3, kk = e % 3;
-            cd s = mk(0.0, 0.0);
-            for (int w = 0; w < nw; w++) s = s + wsum[w][NT + 3 * sym_index(p, qq) + kk];
-            if (a.S[SOD_B_ANGULAR])
-                s = s + a.S[SOD_B_ANGULAR][(long long)fq * a.S_fstride[SOD_B_ANGULAR] + (long long)i * 27 + e];
-            store_out(a.out[SOD_B_ANGULAR], a.out_c64, base + e, s.x, s.y);
-        }
-    }
+    __syncthreads();
+    store_b<MASK>(a, bsum, i, fq);
 }
 
 template <int MASK>
@@ -343,15 +423,6 @@ struct SingArgs {
 };
 
 constexpr int MAX_STAR = 32;
-
-// Device-side descriptor of one object in a batch (sod_batch): the kernel arguments of its scatter
-// (coloured for the G and H CTA sizes), reduction and singular passes.
-struct BatchObjDev {
-    CollArgs aG, aH, aR;
-    int kc_off;  // first entry of this object in the batch's per-frequency constant arrays
-    int pt_idx;  // its quadrature point table
-    int pad[2];
-};
 
 template <int NVAL> __device__ __forceinline__ void warp_sum(cd (&v)[NVAL]) {
 #pragma unroll
@@ -601,34 +672,40 @@ __device__ __forceinline__ int next_item(int *counter, int *s_item) {
     return it;
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(512, 1) batch_scatter_kernel(const BatchObjDev *__restrict__ objs,
+// Kernel arguments of one batched launch, in kernel-parameter (constant bank) space: the point
+// table and up to BATCH_OBJS objects' arguments, indexed by the item's object slot.
+struct BatchLaunchArgs {
+    PointTable pt;
+    int nobj;
+    int kc_off[BATCH_OBJS];  // first entry of the object in the batch's per-frequency constants
+    CollArgs a[BATCH_OBJS];
+};
+static_assert(sizeof(BatchLaunchArgs) <= 32000, "batched launch arguments exceed the kernel parameter space");
+
+template <int KIND, int BM>
+__global__ void __launch_bounds__(scatter_max_threads<KIND, BM>(), 1) batch_scatter_kernel(const __grid_constant__ BatchLaunchArgs p,
                                                                const int4 *__restrict__ items, int nitems,
-                                                               int *counter, const KConst<float> *__restrict__ kcf,
-                                                               const PointTable *__restrict__ pts) {
+                                                               int *counter, const KConst<float> *__restrict__ kcf) {
     extern __shared__ float2 acc[];
     __shared__ int s_item;
     for (;;) {
         const int it = next_item(counter, &s_item);
         if (it >= nitems) break;
         const int4 w = items[it];
-        const BatchObjDev &o = objs[w.x];
-        scatter_body<KIND>(KIND == SOD_G ? o.aG : o.aH, pts[o.pt_idx], kcf[o.kc_off + w.z], w.y, w.z, acc);
+        scatter_body<KIND, BM>(p.a[w.x], p.pt, kcf[p.kc_off[w.x] + w.z], w.y, w.z, acc);
     }
 }
 
 template <int MASK>
-__global__ void __launch_bounds__(256) batch_reduce_kernel(const BatchObjDev *__restrict__ objs,
+__global__ void __launch_bounds__(256) batch_reduce_kernel(const __grid_constant__ BatchLaunchArgs p,
                                                            const int4 *__restrict__ items, int nitems, int *counter,
-                                                           const KConst<float> *__restrict__ kcf,
-                                                           const PointTable *__restrict__ pts) {
+                                                           const KConst<float> *__restrict__ kcf) {
     __shared__ int s_item;
     for (;;) {
         const int it = next_item(counter, &s_item);
         if (it >= nitems) break;
         const int4 w = items[it];
-        const BatchObjDev &o = objs[w.x];
-        reduce_body<MASK>(o.aR, pts[o.pt_idx], kcf[o.kc_off + w.z], w.y, w.z);
+        reduce_body<MASK>(p.a[w.x], p.pt, kcf[p.kc_off[w.x] + w.z], w.y, w.z);
     }
 }
 
@@ -650,32 +727,83 @@ static int ensure_gl_constants(int device) {
     return SOD_OK;
 }
 
+// Scatter kernel variants: G or H, and for G the B kinds fused into the same pass.
+static const void *scatter_fn(int kind, int bm, bool batch) {
+    if (kind == SOD_H) return batch ? (const void *)batch_scatter_kernel<SOD_H, 0> : (const void *)coll_scatter_kernel<SOD_H, 0>;
+    switch (bm) {
+    case KM_BT: return batch ? (const void *)batch_scatter_kernel<SOD_G, KM_BT> : (const void *)coll_scatter_kernel<SOD_G, KM_BT>;
+    case KM_BA: return batch ? (const void *)batch_scatter_kernel<SOD_G, KM_BA> : (const void *)coll_scatter_kernel<SOD_G, KM_BA>;
+    case KM_BT | KM_BA:
+        return batch ? (const void *)batch_scatter_kernel<SOD_G, KM_BT | KM_BA>
+                     : (const void *)coll_scatter_kernel<SOD_G, KM_BT | KM_BA>;
+    default: return batch ? (const void *)batch_scatter_kernel<SOD_G, 0> : (const void *)coll_scatter_kernel<SOD_G, 0>;
+    }
+}
+
+size_t scatter_smem_bytes(int kind, int bm, int nV, int threads) {
+    const int nc = kind == SOD_G ? 6 : 9;
+    const int ncb = kind == SOD_G ? ((bm & KM_BT) ? 6 : 0) + ((bm & KM_BA) ? 18 : 0) : 0;
+    return sizeof(float2) * ((size_t)nc * nV + (size_t)ncb * threads);
+}
+
+// Raise every scatter variant's dynamic shared-memory limit to the device maximum (once per device).
+static bool g_scatter_ready[64] = {};
+static int prepare_scatter(sod_context *ctx) {
+    if (ctx->device >= 0 && ctx->device < 64 && g_scatter_ready[ctx->device]) return SOD_OK;
+    const int bms[4] = {0, KM_BT, KM_BA, KM_BT | KM_BA};
+    for (int batch = 0; batch < 2; batch++)
+        for (int kind = 0; kind < 2; kind++)
+            for (int v = 0; v < (kind == SOD_G ? 4 : 1); v++) {
+                const void *fn = scatter_fn(kind, bms[v], batch != 0);
+                cudaFuncAttributes attr;
+                SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
+                SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)(ctx->smem_optin - attr.sharedSizeBytes)));
+                SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+            }
+    if (ctx->device >= 0 && ctx->device < 64) g_scatter_ready[ctx->device] = true;
+    return SOD_OK;
+}
+
+int scatter_occupancy(sod_context *ctx, int kind, int bm, bool batch, int threads, size_t smem, int *per_sm) {
+    SOD_TRY(prepare_scatter(ctx));
+    *per_sm = 0;
+    const void *fn = scatter_fn(kind, bm, batch);
+    cudaFuncAttributes attr;
+    SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
+    if (smem + attr.sharedSizeBytes > ctx->smem_optin || threads > attr.maxThreadsPerBlock) return SOD_OK;
+    SOD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, fn, threads, smem));
+    return SOD_OK;
+}
+
 // Autotuner for the scatter kernels.  A CTA walks the faces colour by colour with one barrier per
 // colour, so a colour with fewer faces than threads leaves lanes idle and a CTA with few warps
-// cannot hide the barrier.  For every candidate CTA size T (multiples of 32 up to 512) the mesh is
-// coloured with capacity T and the cost is modelled as
+// cannot hide the barrier.  For every feasible CTA size T (multiples of 32 up to the variant's
+// limit) the mesh is coloured with capacity T and the cost is modelled as
 //     slots(T) / occupancy(T),   slots = ncolours * T,
-//     occupancy = min(1, resident warps per SM / 24)  (shared memory and register limits).
-// The choice depends only on the mesh and the device limits, so results stay bitwise reproducible.
-int autotune_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int *threads) {
-    const int slot = kind == SOD_G ? 0 : 1;
-    if (m->tuned_threads[slot] > 0) {
-        *threads = m->tuned_threads[slot];
+//     occupancy = min(1, resident warps per SM / 24)  (from the CUDA occupancy calculator with the
+//     variant's registers and shared memory).
+// The choice depends only on the mesh and the device, so results stay bitwise reproducible.
+int autotune_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int bm, int *threads) {
+    const int key = kind * 16 + bm;
+    auto it = m->tuned.find(key);
+    if (it != m->tuned.end()) {
+        *threads = it->second;
         return SOD_OK;
     }
-    const size_t smem = sizeof(float2) * (kind == SOD_G ? 6 : 9) * (size_t)m->nV + 1024;
-    const int regs = kind == SOD_G ? 112 : 128;
-    const size_t smem_sm = 228 * 1024;
+    SOD_TRY(prepare_scatter(ctx));
+    cudaFuncAttributes attr;
+    SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, scatter_fn(kind, bm, false)));
     double best = 1e300;
-    int bestT = 128;
-    for (int T = 32; T <= 512; T += 32) {
+    int bestT = 0;
+    for (int T = 32; T <= std::min(512, attr.maxThreadsPerBlock); T += 32) {
+        const size_t smem = scatter_smem_bytes(kind, bm, m->nV, T);
+        int per_sm = 0;
+        SOD_TRY(scatter_occupancy(ctx, kind, bm, false, T, smem, &per_sm));
+        if (per_sm <= 0) continue;
         const sod_mesh::Coloured *col = nullptr;
         SOD_TRY(m->coloured_for(T, &col));
-        const int by_smem = (int)std::max<size_t>(1, smem_sm / smem);
-        const int by_regs = std::max(1, 65536 / (regs * T));
-        const int by_warps = std::max(1, 64 / (T / 32));
-        const int ctas = std::min(std::min(by_smem, by_regs), by_warps);
-        const double warps = (double)ctas * T / 32.0;
+        const double warps = (double)per_sm * T / 32.0;
         const double occ = std::min(1.0, warps / 24.0);
         const double cost = (double)col->ncolors * T / occ;
         if (cost < best * 0.999) {
@@ -683,9 +811,12 @@ int autotune_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int *threa
             bestT = T;
         }
     }
-    m->tuned_threads[slot] = bestT;
+    if (bestT == 0) {
+        set_error("mesh too large for the shared-memory row accumulator (" + std::to_string(m->nV) + " vertices)");
+        return SOD_ERR_UNSUPPORTED;
+    }
+    m->tuned[key] = bestT;
     *threads = bestT;
-    (void)ctx;
     return SOD_OK;
 }
 
@@ -714,25 +845,28 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
         SOD_TRY(ctx->sing.ensure(sizeof(cd) * (size_t)stot));
         Sb = ctx->sing.as<cd>();
     }
-    // scatter kernel configuration
+    // scatter kernel configuration; with G requested the B kinds ride along in the G pass
+    const int bmG = (mask & KM_G) ? (mask & (KM_BT | KM_BA)) : 0;
     int threads[2] = {0, 0};
     const sod_mesh::Coloured *col[2] = {nullptr, nullptr};
     size_t smem[2] = {0, 0};
     for (int kd = 0; kd < 2; kd++) {
         if (!(mask & (1 << kd))) continue;
+        const int bm = kd == SOD_G ? bmG : 0;
         int T = ctx->coll_threads;
-        if (T <= 0) SOD_TRY(autotune_scatter_threads(ctx, const_cast<sod_mesh *>(m), kd, &T));
-        T = std::max(32, std::min(512, (T / 32) * 32));
+        if (T <= 0) SOD_TRY(autotune_scatter_threads(ctx, const_cast<sod_mesh *>(m), kd, bm, &T));
+        cudaFuncAttributes attr;
+        SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, scatter_fn(kd, bm, false)));
+        T = std::max(32, std::min(std::min(512, attr.maxThreadsPerBlock), (T / 32) * 32));
         threads[kd] = T;
         SOD_TRY(const_cast<sod_mesh *>(m)->coloured_for(T, &col[kd]));
-        smem[kd] = sizeof(float2) * (kd == SOD_G ? 6 : 9) * (size_t)m->nV;
-        if (smem[kd] > ctx->smem_optin) {
+        smem[kd] = scatter_smem_bytes(kd, bm, m->nV, T);
+        int per_sm = 0;
+        SOD_TRY(scatter_occupancy(ctx, kd, bm, false, T, smem[kd], &per_sm));
+        if (per_sm <= 0) {
             set_error("mesh too large for the shared-memory row accumulator (" + std::to_string(m->nV) + " vertices)");
             return SOD_ERR_UNSUPPORTED;
         }
-        const void *fn = kd == SOD_G ? (const void *)coll_scatter_kernel<SOD_G> : (const void *)coll_scatter_kernel<SOD_H>;
-        SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[kd]));
-        SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     }
     const size_t esz = L.out_dtype == SOD_C64 ? 8 : 16;
     for (int f0 = 0; f0 < L.nfreq; f0 += chunk) {
@@ -782,14 +916,20 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
             a.canonF = m->has_vmap ? col[kd]->dCanonF.as<int4>() : nullptr;
             a.color_off = col[kd]->dOff.as<int>();
             a.ncolors = col[kd]->ncolors;
-            if (kd == SOD_G)
-                coll_scatter_kernel<SOD_G><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
+            if (kd == SOD_H)
+                coll_scatter_kernel<SOD_H, 0><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
+            else if (bmG == KM_BT)
+                coll_scatter_kernel<SOD_G, KM_BT><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
+            else if (bmG == KM_BA)
+                coll_scatter_kernel<SOD_G, KM_BA><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
+            else if (bmG)
+                coll_scatter_kernel<SOD_G, KM_BT | KM_BA><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
             else
-                coll_scatter_kernel<SOD_H><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
+                coll_scatter_kernel<SOD_G, 0><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
             SOD_CHECK_CUDA(cudaGetLastError());
             ctx->count();
         }
-        const int rm = mask & (KM_BT | KM_BA);
+        const int rm = (mask & KM_G) ? 0 : (mask & (KM_BT | KM_BA));
         if (rm) {
             a.faces = m->dFacesNat.as<float4>();
             a.canonF = m->has_vmap ? m->dCanonNat.as<int4>() : nullptr;
@@ -864,21 +1004,30 @@ int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, d
     const sod_mesh::Coloured *col = nullptr;
     size_t smem = 0;
     if (kind <= SOD_H) {
-        threads = ctx->coll_threads > 0 ? ctx->coll_threads : m->tuned_threads[kind];
+        threads = ctx->coll_threads;
+        if (threads <= 0) {  // the CTA size the autotuner chose for this kind (any fused variant)
+            auto tt = m->tuned.find(kind * 16);
+            if (tt == m->tuned.end())
+                for (auto &kv : m->tuned)
+                    if (kv.first / 16 == kind) {
+                        tt = m->tuned.find(kv.first);
+                        break;
+                    }
+            threads = tt != m->tuned.end() ? tt->second : 0;
+        }
         auto it = threads > 0 ? m->coloured.find(threads) : m->coloured.end();
         if (it == m->coloured.end()) {
             set_error("the mesh has no scatter schedule yet: assemble it once with sod_cqbem_assemble* during set-up");
             return SOD_ERR_INVALID_ARG;
         }
         col = it->second.get();
-        smem = sizeof(float2) * (kind == SOD_G ? 6 : 9) * (size_t)m->nV;
-        if (smem > ctx->smem_optin) {
+        smem = scatter_smem_bytes(kind, 0, m->nV, threads);
+        int per_sm = 0;
+        SOD_TRY(scatter_occupancy(ctx, kind, 0, false, threads, smem, &per_sm));
+        if (per_sm <= 0) {
             set_error("mesh too large for the shared-memory row accumulator");
             return SOD_ERR_UNSUPPORTED;
         }
-        const void *fn = kind == SOD_G ? (const void *)coll_scatter_kernel<SOD_G> : (const void *)coll_scatter_kernel<SOD_H>;
-        SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     }
     const long long per = kind <= SOD_H ? 9LL * m->nV * m->nV : (kind == SOD_B_TRANS ? 9LL : 27LL) * m->nV;
     const size_t esz = out_dtype == SOD_C64 ? 8 : 16;
@@ -932,9 +1081,9 @@ int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, d
             a.color_off = col->dOff.as<int>();
             a.ncolors = col->ncolors;
             if (kind == SOD_G)
-                coll_scatter_kernel<SOD_G><<<grid, threads, smem, stream>>>(a, pt, ft);
+                coll_scatter_kernel<SOD_G, 0><<<grid, threads, smem, stream>>>(a, pt, ft);
             else
-                coll_scatter_kernel<SOD_H><<<grid, threads, smem, stream>>>(a, pt, ft);
+                coll_scatter_kernel<SOD_H, 0><<<grid, threads, smem, stream>>>(a, pt, ft);
         } else {
             a.faces = m->dFacesNat.as<float4>();
             a.canonF = m->has_vmap ? m->dCanonNat.as<int4>() : nullptr;
@@ -950,12 +1099,30 @@ int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, d
 }
 
 // -------------------------------------------------------------------------------------------
-// Batched launcher (host): fills the per-object device descriptors' kernel arguments and issues
-// the persistent launches on `stream` (which may be capturing into a CUDA graph).
-size_t batch_obj_size() { return sizeof(BatchObjDev); }
+// Batched launches (host): one BatchRegular per persistent launch holds the kernel arguments of up
+// to BATCH_OBJS objects (same CTA size, point table and pass) and issues the launch on a stream,
+// which may be capturing into a CUDA graph.
+struct BatchRegular {
+    int which, mask, threads;
+    size_t smem;
+    BatchLaunchArgs args;
+};
 
-static void batch_fill_args(const sod_mesh *m, int kind_mask, int out_dtype, void *const out[4], cd *const S[4],
-                            const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, BatchObjDev &o) {
+BatchRegular *batch_regular_new(int which, int mask, int threads, size_t smem, const PointTable &pt) {
+    auto *r = new BatchRegular();
+    r->which = which;
+    r->mask = mask;
+    r->threads = threads;
+    r->smem = smem;
+    r->args.pt = pt;
+    r->args.nobj = 0;
+    return r;
+}
+void batch_regular_free(BatchRegular *r) { delete r; }
+
+int batch_regular_add(BatchRegular *r, const sod_mesh *m, int out_dtype, void *const out[4], cd *const S[4],
+                      const sod_mesh::Coloured *col, int kc_off, int *slot) {
+    SOD_REQUIRE(r->args.nobj < BATCH_OBJS, "batched launch is full");
     const long long nslots = m->nbr_off.back();
     const long long sfs[4] = {nslots * 9, nslots * 9, (long long)m->nV * 9, (long long)m->nV * 27};
     const long long per[4] = {9LL * m->nV * m->nV, 9LL * m->nV * m->nV, 9LL * m->nV, 27LL * m->nV};
@@ -969,90 +1136,66 @@ static void batch_fill_args(const sod_mesh *m, int kind_mask, int out_dtype, voi
     a.nbr_off = m->dNbrOff.as<int>();
     a.nbr_vert = m->dNbrVert.as<int>();
     for (int kd = 0; kd < 4; kd++) {
-        a.out[kd] = (kind_mask & (1 << kd)) ? out[kd] : nullptr;
+        a.out[kd] = (r->mask & (1 << kd)) ? out[kd] : nullptr;
         a.fstride[kd] = per[kd];
-        a.S[kd] = (kind_mask & (1 << kd)) ? S[kd] : nullptr;
+        a.S[kd] = (r->mask & (1 << kd)) ? S[kd] : nullptr;
         a.S_fstride[kd] = sfs[kd];
     }
-    o.aG = a;
-    o.aH = a;
-    o.aR = a;
-    if (colG) {
-        o.aG.faces = colG->dFaces.as<float4>();
-        o.aG.canonF = m->has_vmap ? colG->dCanonF.as<int4>() : nullptr;
-        o.aG.color_off = colG->dOff.as<int>();
-        o.aG.ncolors = colG->ncolors;
+    if (r->which == 4) {
+        a.faces = m->dFacesNat.as<float4>();
+        a.canonF = m->has_vmap ? m->dCanonNat.as<int4>() : nullptr;
+    } else {
+        SOD_REQUIRE(col != nullptr, "scatter launch needs a colouring");
+        a.faces = col->dFaces.as<float4>();
+        a.canonF = m->has_vmap ? col->dCanonF.as<int4>() : nullptr;
+        a.color_off = col->dOff.as<int>();
+        a.ncolors = col->ncolors;
     }
-    if (colH) {
-        o.aH.faces = colH->dFaces.as<float4>();
-        o.aH.canonF = m->has_vmap ? colH->dCanonF.as<int4>() : nullptr;
-        o.aH.color_off = colH->dOff.as<int>();
-        o.aH.ncolors = colH->ncolors;
-    }
-    o.aR.faces = m->dFacesNat.as<float4>();
-    o.aR.canonF = m->has_vmap ? m->dCanonNat.as<int4>() : nullptr;
-}
-
-void batch_fill_args_host(const sod_mesh *m, int kind_mask, int out_dtype, void *const out[4], cd *const S[4],
-                          const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, int kc_off, int pt_idx,
-                          void *dst) {
-    BatchObjDev o{};
-    batch_fill_args(m, kind_mask, out_dtype, out, S, colG, colH, o);
-    o.kc_off = kc_off;
-    o.pt_idx = pt_idx;
-    *static_cast<BatchObjDev *>(dst) = o;
-}
-
-int batch_prepare_kernels(sod_context *ctx, size_t smem_G, size_t smem_H) {
-    SOD_TRY(ensure_gl_constants(ctx->device));
-    if (smem_G) {
-        SOD_CHECK_CUDA(cudaFuncSetAttribute(batch_scatter_kernel<SOD_G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_G));
-        SOD_CHECK_CUDA(cudaFuncSetAttribute(batch_scatter_kernel<SOD_G>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    }
-    if (smem_H) {
-        SOD_CHECK_CUDA(cudaFuncSetAttribute(batch_scatter_kernel<SOD_H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_H));
-        SOD_CHECK_CUDA(cudaFuncSetAttribute(batch_scatter_kernel<SOD_H>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    }
+    const int k = r->args.nobj++;
+    r->args.a[k] = a;
+    r->args.kc_off[k] = kc_off;
+    *slot = k;
     return SOD_OK;
 }
 
-// Resident CTAs per SM of the persistent G (kind 0) or H (kind 1) scatter at a CTA size and
-// dynamic shared-memory size (batch_prepare_kernels must have raised the kernel's smem limit).
-int batch_scatter_occupancy(int kind, int threads, size_t smem, int *per_sm) {
-    const void *fn = kind == SOD_G ? (const void *)batch_scatter_kernel<SOD_G> : (const void *)batch_scatter_kernel<SOD_H>;
-    SOD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, fn, threads, smem));
-    return SOD_OK;
-}
-
-// One persistent launch; grid = resident CTAs per SM x SMs.  `which`: 0 polar, 1 Guiggiani,
-// 2 scatter G, 3 scatter H, 4 reduce.
-int batch_launch(sod_context *ctx, int which, int mask, const void *objs_v, const int4 *items, int nitems,
-                 int *counter, const KConst<float> *kcf, const PointTable *pts, int threads, size_t smem,
-                 cudaStream_t stream) {
+// One persistent launch; grid = resident CTAs per SM x SMs.  `which`: 2 G scatter (with the B kinds
+// of the mask fused in), 3 H scatter, 4 B reduction (when G is not assembled).
+int batch_regular_issue(sod_context *ctx, const BatchRegular *r, const int4 *items, int nitems, int *counter,
+                        const KConst<float> *kcf, cudaStream_t stream) {
     if (nitems <= 0) return SOD_OK;
-    SOD_REQUIRE(which >= 2 && which <= 4, "batch_launch: not a regular pass");
-    const BatchObjDev *objs = static_cast<const BatchObjDev *>(objs_v);
+    const int bm = r->mask & (KM_BT | KM_BA);
+    const int T = r->threads;
+    const void *fn = r->which == 2   ? scatter_fn(SOD_G, bm, true)
+                     : r->which == 3 ? scatter_fn(SOD_H, 0, true)
+                     : bm == (KM_BT | KM_BA) ? (const void *)batch_reduce_kernel<KM_BT | KM_BA>
+                     : bm == KM_BT           ? (const void *)batch_reduce_kernel<KM_BT>
+                                             : (const void *)batch_reduce_kernel<KM_BA>;
+    SOD_TRY(prepare_scatter(ctx));
     int per_sm = 1;
-    const int rm = mask & (KM_BT | KM_BA);
-    const void *fn = which == 2 ? (const void *)batch_scatter_kernel<SOD_G>
-                   : which == 3 ? (const void *)batch_scatter_kernel<SOD_H>
-                   : rm == (KM_BT | KM_BA) ? (const void *)batch_reduce_kernel<KM_BT | KM_BA>
-                   : rm == KM_BT ? (const void *)batch_reduce_kernel<KM_BT>
-                                 : (const void *)batch_reduce_kernel<KM_BA>;
-    SOD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
-    per_sm = std::max(1, per_sm);
+    SOD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, T, r->smem));
+    SOD_REQUIRE(per_sm > 0, "batched launch does not fit on an SM");
     const int grid = std::min(nitems, per_sm * ctx->num_sms);
     SOD_CHECK_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), stream));
-    switch (which) {
-    case 2: batch_scatter_kernel<SOD_G><<<grid, threads, smem, stream>>>(objs, items, nitems, counter, kcf, pts); break;
-    case 3: batch_scatter_kernel<SOD_H><<<grid, threads, smem, stream>>>(objs, items, nitems, counter, kcf, pts); break;
-    default:
-        if (rm == (KM_BT | KM_BA))
-            batch_reduce_kernel<KM_BT | KM_BA><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcf, pts);
-        else if (rm == KM_BT)
-            batch_reduce_kernel<KM_BT><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcf, pts);
+    const BatchLaunchArgs &p = r->args;
+    switch (r->which) {
+    case 2:
+        if (bm == (KM_BT | KM_BA))
+            batch_scatter_kernel<SOD_G, KM_BT | KM_BA><<<grid, T, r->smem, stream>>>(p, items, nitems, counter, kcf);
+        else if (bm == KM_BT)
+            batch_scatter_kernel<SOD_G, KM_BT><<<grid, T, r->smem, stream>>>(p, items, nitems, counter, kcf);
+        else if (bm == KM_BA)
+            batch_scatter_kernel<SOD_G, KM_BA><<<grid, T, r->smem, stream>>>(p, items, nitems, counter, kcf);
         else
-            batch_reduce_kernel<KM_BA><<<grid, threads, 0, stream>>>(objs, items, nitems, counter, kcf, pts);
+            batch_scatter_kernel<SOD_G, 0><<<grid, T, r->smem, stream>>>(p, items, nitems, counter, kcf);
+        break;
+    case 3: batch_scatter_kernel<SOD_H, 0><<<grid, T, r->smem, stream>>>(p, items, nitems, counter, kcf); break;
+    default:
+        if (bm == (KM_BT | KM_BA))
+            batch_reduce_kernel<KM_BT | KM_BA><<<grid, T, 0, stream>>>(p, items, nitems, counter, kcf);
+        else if (bm == KM_BT)
+            batch_reduce_kernel<KM_BT><<<grid, T, 0, stream>>>(p, items, nitems, counter, kcf);
+        else
+            batch_reduce_kernel<KM_BA><<<grid, T, 0, stream>>>(p, items, nitems, counter, kcf);
         break;
     }
     SOD_CHECK_CUDA(cudaGetLastError());

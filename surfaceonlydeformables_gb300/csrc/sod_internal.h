@@ -138,7 +138,7 @@ struct sod_mesh {
         sod::DevBuf dOff;
     };
     std::map<int, std::unique_ptr<Coloured>> coloured;
-    int tuned_threads[2] = {0, 0};  // scatter CTA size chosen by the autotuner for G, H (0 = not yet)
+    std::map<int, int> tuned;  // scatter CTA size chosen by the autotuner, key kind * 16 + fused B kinds
     // frequency-independent singular-quadrature geometry per (order, subdivision), double-float
     struct SingGeom {
         int nq2 = 0;          // points per star entry
@@ -200,19 +200,22 @@ int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, d
                                 const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, void *out,
                                 int out_dtype, cd *scratch, long long scratch_elems, cudaStream_t stream);
 bool is_device_pointer(const void *p);
-// Batched persistent path (sod_collocation.cu); BatchObjDev is defined there.
-struct BatchObjDev;
-size_t batch_obj_size();
-void batch_fill_args_host(const sod_mesh *m, int kind_mask, int out_dtype, void *const out[4], cd *const S[4],
-                          const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, int kc_off, int pt_idx,
-                          void *dst);
-int batch_prepare_kernels(sod_context *ctx, size_t smem_G, size_t smem_H);
-int batch_scatter_occupancy(int kind, int threads, size_t smem, int *per_sm);
-// regular passes of a batch: `which` 2 G scatter, 3 H scatter, 4 B reduction (persistent launches)
-int batch_launch(sod_context *ctx, int which, int mask, const void *objs, const int4 *items, int nitems, int *counter,
-                 const KConst<float> *kcf, const PointTable *pts, int threads, size_t smem, cudaStream_t stream);
+// Batched persistent launches of the regular passes (sod_collocation.cu).  One BatchRegular holds
+// the arguments of up to BATCH_OBJS objects in kernel-parameter space; `which` 2 G scatter (B kinds
+// of the mask fused in), 3 H scatter, 4 B reduction.
+constexpr int BATCH_OBJS = 112;
+struct BatchRegular;
+BatchRegular *batch_regular_new(int which, int mask, int threads, size_t smem, const PointTable &pt);
+void batch_regular_free(BatchRegular *r);
+int batch_regular_add(BatchRegular *r, const sod_mesh *m, int out_dtype, void *const out[4], cd *const S[4],
+                      const sod_mesh::Coloured *col, int kc_off, int *slot);
+int batch_regular_issue(sod_context *ctx, const BatchRegular *r, const int4 *items, int nitems, int *counter,
+                        const KConst<float> *kcf, cudaStream_t stream);
+// Dynamic shared memory and occupancy of the scatter variants (bm: B kinds fused into G).
+size_t scatter_smem_bytes(int kind, int bm, int nV, int threads);
+int scatter_occupancy(sod_context *ctx, int kind, int bm, bool batch, int threads, size_t smem, int *per_sm);
 // Deterministic autotuner of the scatter kernels' CTA size (see sod_collocation.cu).
-int autotune_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int *threads);
+int autotune_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int bm, int *threads);
 int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, int64_t M, int nfreq, int L,
                              double R, void *out, int out_dtype, cudaStream_t stream);
 KConst<double> make_kconst(double c1, double c2, double rho, double sr, double si);

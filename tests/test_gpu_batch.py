@@ -102,8 +102,34 @@ def test_batch_profile_reports_every_launch(gpu_ctx, objects):
     prof = b.profile()
     assert len(prof) == b.launches_per_step
     passes = {p["pass"] for p in prof}
-    assert {"singular_polar", "singular_guiggiani", "scatter_G", "scatter_H", "reduce_B"} <= passes
+    # with G in the batch the B kinds ride along in the G scatter: no separate reduction launch
+    assert {"singular_polar", "singular_guiggiani", "combine_GB", "combine_H", "scatter_G", "scatter_H"} == passes
     assert all(p["ms"] > 0 and p["evals"] > 0 for p in prof)
     # regular evaluations of the G scatter: nfreq * (nV nF - 3 nF) * 7 points, summed over objects
     want = sum(len(o["s"]) * (o["host"].nV * o["host"].nF - 3 * o["host"].nF) * 7 for o in objects)
     assert sum(p["evals"] for p in prof if p["pass"] == "scatter_G") == want
+
+
+@pytest.mark.parametrize("kinds", [("B_trans", "B_angular"), ("H", "B_angular"), ("G", "B_trans")])
+def test_batch_kind_subsets(gpu_ctx, objects, oracle, kinds):
+    """Batches of a subset of the kinds (B without G runs the separate reduction pass)."""
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    b = api.Batch(gpu_ctx, kinds, L.C64)
+    outs = []
+    for o in objects[1:]:
+        out = api.alloc_outputs(o["dev"], len(o["s"]), kinds, L.C64)
+        b.add(o["dev"], o["mat"], o["s"], out)
+        outs.append(out)
+    b.run()
+    gpu_ctx.synchronize()
+    if "G" not in kinds:
+        assert "reduce_B" in {p["pass"] for p in b.profile()} or not set(kinds) & {"B_trans", "B_angular"}
+    for o, out in zip(objects[1:], outs):
+        single = api.assemble_all(gpu_ctx, o["dev"], o["mat"], o["s"], dtype=L.C64)
+        l = len(o["s"]) - 1
+        for k in kinds:
+            r = out[k].cpu().numpy()
+            assert rel_fro(r, single[k]) <= 1e-6, k
+            assert rel_fro(r[l], oracle.collocation(k, o["host"], o["mat"], o["s"][l])) <= 1e-5, k
