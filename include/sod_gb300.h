@@ -177,6 +177,28 @@ int sod_batch_launch_count(const sod_batch *batch);
 int sod_batch_profile(sod_batch *batch, int cap, int *which, double *evals, float *ms);
 int sod_batch_destroy(sod_batch *batch);
 
+/* ---- per-step history convolution ----------------------------------------------------------- */
+/* Replaces the dense history loop of ElastodynamicsCQBEMObject::estimate_next_state
+ * (src/elastodynamics_cqbem_object.cpp:44-48):
+ *   b = sum_{i=0}^{min(n,K)-1} G_{i+1} p_{n-1-i} - H_{i+1} u_{n-1-i} + B_{i+1} a_{n-1-i}
+ * (H as computed by the CQ precompute, i.e. before the reference's negation at load,
+ * src/elastodynamics_cqbem_matrix_collection.cpp:140).  A bank keeps G_k, -H_k (nrow x ncol each,
+ * k = 1..K) device-resident as FP32 or as BF16 with one FP32 scale per (k, matrix, row), B_k
+ * (nrow x 6, FP64) and a ring of the last K steps' vectors.  R right-hand sides per step (1 or 16);
+ * vectors are [ncol][R] row-major doubles, a is [6][R], b is [nrow][R].  Host or device pointers. */
+typedef struct sod_history sod_history;
+int sod_history_create(sod_context *ctx, int nrow, int ncol, int K, int R, int weight_dtype, sod_history **bank);
+/* G_k, H_k: nrow x ncol row-major, dtype SOD_F64 or SOD_F32; k in 1..K. */
+int sod_history_set_weights(sod_history *bank, int k, const void *G_k, const void *H_k, int in_dtype);
+int sod_history_set_b(sod_history *bank, int k, const double *B_k);
+/* Appends step n's p, u (and a, may be NULL) to the ring. */
+int sod_history_push(sod_history *bank, const double *p, const double *u, const double *a);
+/* b for the next step from the pushed history (the min(n, K) most recent steps). */
+int sod_history_convolve(sod_history *bank, double *b);
+int sod_history_reset(sod_history *bank);
+int sod_history_bytes(const sod_history *bank, int64_t *weight_bytes);
+int sod_history_destroy(sod_history *bank);
+
 /* ---- time-domain precomputation of one object ------------------------------------------------ */
 /* Replaces compute_H_matrices, compute_G_matrices, compute_B_trans_matrices,
  * compute_B_angular_tensors and compute_B_euler_matrices of ElastodynamicsCQBEMMatrixCollection

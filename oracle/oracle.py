@@ -160,7 +160,7 @@ def history_convolution(G, H, p_hist, u_hist, B=None, a_hist=None):
     H is negated at load, src/elastodynamics_cqbem_matrix_collection.cpp:140).
     G, H: (N+1, 3V, 3V); p_hist/u_hist: (K, 3V[, R]) with index 0 the most recent step (n-1)."""
     K = p_hist.shape[0]
-    b = np.zeros(p_hist.shape[1:], dtype=np.float64)
+    b = np.zeros((G.shape[1],) + p_hist.shape[2:], dtype=np.float64)
     for k in range(1, K + 1):
         b += G[k].astype(np.float64) @ p_hist[k - 1] - H[k].astype(np.float64) @ u_hist[k - 1]
         if B is not None:

@@ -58,6 +58,14 @@ _SIGS = {
     "sod_batch_launch_count": ([_P], _c.c_int),
     "sod_batch_profile": ([_P, _c.c_int, _P, _P, _P], _c.c_int),
     "sod_batch_destroy": ([_P], _c.c_int),
+    "sod_history_create": ([_P, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _P], _c.c_int),
+    "sod_history_set_weights": ([_P, _c.c_int, _P, _P, _c.c_int], _c.c_int),
+    "sod_history_set_b": ([_P, _c.c_int, _P], _c.c_int),
+    "sod_history_push": ([_P, _P, _P, _P], _c.c_int),
+    "sod_history_convolve": ([_P, _P], _c.c_int),
+    "sod_history_reset": ([_P], _c.c_int),
+    "sod_history_bytes": ([_P, _P], _c.c_int),
+    "sod_history_destroy": ([_P], _c.c_int),
     "sod_cq_inverse_transform": ([_P, _P, _c.c_int, _c.c_int64, _c.c_int, _c.c_int, _c.c_double, _P, _c.c_int],
                                  _c.c_int),
 }

@@ -237,3 +237,61 @@ def inverse_transform(ctx: Context, Xhat, L_: int, R: float, out=None, out_dtype
     L.check(L.load().sod_cq_inverse_transform(ctx.handle, L.ptr(Xhat), in_dtype, M, nfreq, L_, R, L.ptr(out),
                                               out_dtype))
     return out
+
+
+class HistoryBank:
+    """Device-resident history convolution of one object (sod_history): G_k, -H_k (k = 1..K) as FP32
+    or BF16 + per-row scales, a ring of the last K steps' vectors, b = sum G p - H u + B a."""
+
+    def __init__(self, ctx: Context, nrow: int, ncol: int, K: int, R: int = 1, weight_dtype: int = L.F32):
+        self.ctx, self.nrow, self.ncol, self.K, self.R = ctx, nrow, ncol, K, R
+        self._h = ctypes.c_void_p()
+        L.check(L.load().sod_history_create(ctx.handle, nrow, ncol, K, R, weight_dtype, ctypes.byref(self._h)))
+
+    @staticmethod
+    def _arr(x, dtype=np.float64):
+        if hasattr(x, "data_ptr"):
+            return x
+        return np.ascontiguousarray(np.asarray(x, dtype=dtype))
+
+    def set_weights(self, k: int, G, H) -> None:
+        G, H = self._arr(G), self._arr(H)
+        dt = L.F32 if (getattr(G, "dtype", None) in (np.float32,) or str(getattr(G, "dtype", "")) == "torch.float32") \
+            else L.F64
+        L.check(L.load().sod_history_set_weights(self._h, k, L.ptr(G), L.ptr(H), dt))
+        self._keep = (G, H)
+
+    def set_b(self, k: int, B) -> None:
+        B = self._arr(B)
+        L.check(L.load().sod_history_set_b(self._h, k, L.ptr(B)))
+
+    def push(self, p, u, a=None) -> None:
+        p, u = self._arr(p), self._arr(u)
+        a = None if a is None else self._arr(a)
+        L.check(L.load().sod_history_push(self._h, L.ptr(p), L.ptr(u), L.ptr(a) if a is not None else None))
+
+    def convolve(self, out=None):
+        if out is None:
+            out = np.empty((self.nrow, self.R) if self.R > 1 else (self.nrow,), dtype=np.float64)
+        L.check(L.load().sod_history_convolve(self._h, L.ptr(out)))
+        return out
+
+    def reset(self) -> None:
+        L.check(L.load().sod_history_reset(self._h))
+
+    @property
+    def weight_bytes(self) -> int:
+        v = ctypes.c_int64()
+        L.check(L.load().sod_history_bytes(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    def close(self) -> None:
+        if self._h:
+            L.load().sod_history_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,392 @@
+// sod_history.cu -- the per-step history convolution of a CQBEM object on sm_103a.
+//
+// Replaces the dense loop of ElastodynamicsCQBEMObject::estimate_next_state
+// (src/elastodynamics_cqbem_object.cpp:44-48):
+//     b = sum_{i=0}^{min(n, K)-1} ( G_{i+1} p_{n-1-i} - H_{i+1} u_{n-1-i} + B_{i+1} a_{n-1-i} )
+// (the reference negates H at load, src/elastodynamics_cqbem_matrix_collection.cpp:140).
+//
+// A history bank keeps everything device-resident:
+//   * weights [K][2][nrow][ldw] -- G_k and -H_k, FP32 or BF16 with one FP32 scale per (k, G/H, row)
+//     (rows are normalised to max |w| = 1 before rounding), ldw = ncol rounded up to 8 so that
+//     every row starts on a 16-byte boundary;
+//   * B weights [K][nrow][6] (FP64, small);
+//   * a ring of the last K steps' vectors x [K][2][ldw][R] (p, u; zero-padded) and a [K][6][R].
+// push() writes the newest step into the ring (one small kernel), convolve() streams the whole
+// bank once: HBM-bound at R = 1 (and for FP32 weights at R = 16); 2 * 2K * nrow * ncol * R flops.
+//
+// convolve: CTA = 8 warps, each warp owns RW rows and splits a column chunk over its 32 lanes
+// (4 FP32 or 8 BF16 consecutive columns per lane and step: one 16-byte weight load per row), accumulates in
+// FP32 registers over all matrices, and the lanes' partial sums are combined in FP64 with a fixed
+// xor tree; a second kernel sums the column chunks in fixed order and adds the B term in FP64.
+// Results are bitwise reproducible.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <memory>
+#include <vector>
+
+#include "sod_internal.h"
+
+using namespace sod;
+
+struct sod_history {
+    sod_context *ctx = nullptr;
+    int nrow = 0, ncol = 0, K = 0, R = 0, wdtype = SOD_F32, ldw = 0;
+    int head = 0;   // ring slot of the next push
+    int count = 0;  // steps pushed (saturates at K)
+    DevBuf W, scale, Bw, X, A, partial, tmp;
+    bool has_b = false;
+    int nchunk = 0, cchunk = 0;
+};
+
+namespace {
+
+constexpr int HIST_THREADS = 256;
+
+// VEC consecutive weights of one row with a single 16-byte load (4 FP32 or 8 BF16)
+template <class WT> struct WVec {
+    static constexpr int VEC = 16 / sizeof(WT);
+};
+__device__ __forceinline__ void load_w(const float *w, float v[4]) {
+    const float4 q = __ldg(reinterpret_cast<const float4 *>(w));
+    v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+}
+__device__ __forceinline__ void load_w(const __nv_bfloat16 *w, float v[8]) {
+    const uint4 q = __ldg(reinterpret_cast<const uint4 *>(w));
+    const unsigned int u[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u[k]));
+        v[2 * k] = f.x, v[2 * k + 1] = f.y;
+    }
+}
+
+// partial[chunk][row][j] = sum over the used history of this column chunk (FP64 after the lane tree)
+template <int R, int RW, class WT>
+__global__ void __launch_bounds__(HIST_THREADS) hist_conv_kernel(const WT *__restrict__ W,
+                                                                 const float *__restrict__ scale,
+                                                                 const float *__restrict__ X, int used, int head,
+                                                                 int K, int nrow, int ldw, int cchunk,
+                                                                 double *__restrict__ partial) {
+    constexpr int VEC = WVec<WT>::VEC;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row0 = (blockIdx.y * (HIST_THREADS / 32) + warp) * RW;
+    if (row0 >= nrow) return;
+    const int c0 = blockIdx.x * cchunk, c1 = min(ldw, c0 + cchunk);
+    float acc[RW][R];
+#pragma unroll
+    for (int r = 0; r < RW; r++)
+#pragma unroll
+        for (int j = 0; j < R; j++) acc[r][j] = 0.f;
+    int rows[RW];
+#pragma unroll
+    for (int r = 0; r < RW; r++) rows[r] = min(row0 + r, nrow - 1);  // duplicated tail rows are not stored
+    for (int i = 0; i < used; i++) {
+        const int slot = (head - 1 - i + 2 * K) % K;
+        for (int t = 0; t < 2; t++) {
+            const size_t mat = (size_t)i * 2 + t;
+            const WT *Wm = W + mat * nrow * (size_t)ldw;
+            const float *Xm = X + ((size_t)slot * 2 + t) * ldw * (size_t)R;
+            float sc[RW];
+#pragma unroll
+            for (int r = 0; r < RW; r++) sc[r] = scale ? __ldg(scale + mat * nrow + rows[r]) : 1.0f;
+            for (int c = c0 + VEC * lane; c < c1; c += 32 * VEC) {
+                float w[RW][VEC];
+#pragma unroll
+                for (int r = 0; r < RW; r++) load_w(Wm + (size_t)rows[r] * ldw + c, w[r]);
+                if (scale) {
+#pragma unroll
+                    for (int r = 0; r < RW; r++)
+#pragma unroll
+                        for (int q = 0; q < VEC; q++) w[r][q] *= sc[r];
+                }
+#pragma unroll
+                for (int q = 0; q < VEC; q++) {
+                    float x[R];
+                    if (R % 4 == 0) {
+#pragma unroll
+                        for (int j = 0; j < R; j += 4) {
+                            const float4 v = __ldg(reinterpret_cast<const float4 *>(Xm + (size_t)(c + q) * R + j));
+                            x[j] = v.x, x[j + 1] = v.y, x[j + 2] = v.z, x[j + 3] = v.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < R; j++) x[j] = __ldg(Xm + (size_t)(c + q) * R + j);
+                    }
+#pragma unroll
+                    for (int r = 0; r < RW; r++)
+#pragma unroll
+                        for (int j = 0; j < R; j++) acc[r][j] = fmaf(w[r][q], x[j], acc[r][j]);
+                }
+            }
+        }
+    }
+    // lanes -> one value per (row, j) in FP64, fixed xor tree
+#pragma unroll
+    for (int r = 0; r < RW; r++)
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            double v = acc[r][j];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0 && row0 + r < nrow) partial[((size_t)blockIdx.x * nrow + row0 + r) * R + j] = v;
+        }
+}
+
+// b[row][j] = sum_chunks partial + sum_i B_{i+1}[row][:] a_slot[:][j]   (FP64, fixed order)
+__global__ void hist_finish_kernel(const double *__restrict__ partial, int nchunk, const double *__restrict__ Bw,
+                                   const double *__restrict__ A, int used, int head, int K, int nrow, int R,
+                                   double *__restrict__ out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nrow * R) return;
+    const int row = e / R, j = e % R;
+    double s = 0.0;
+    for (int c = 0; c < nchunk; c++) s += partial[(size_t)c * nrow * R + e];
+    if (Bw) {
+        for (int i = 0; i < used; i++) {
+            const int slot = (head - 1 - i + 2 * K) % K;
+            const double *b = Bw + ((size_t)i * nrow + row) * 6;
+            const double *a = A + (size_t)slot * 6 * R;
+            for (int c = 0; c < 6; c++) s += b[c] * a[c * R + j];
+        }
+    }
+    out[e] = s;
+}
+
+// One matrix (nrow x ncol, FP64 or FP32, row-major) -> bank layout, with `sign` and per-row scale.
+template <class WT>
+__global__ void hist_pack_kernel(const void *__restrict__ src, int src_f64, int nrow, int ncol, int ldw, double sign,
+                                 WT *__restrict__ dst, float *__restrict__ scale) {
+    const int row = blockIdx.x;
+    if (row >= nrow) return;
+    const double *s64 = static_cast<const double *>(src) + (size_t)row * ncol;
+    const float *s32 = static_cast<const float *>(src) + (size_t)row * ncol;
+    float sc = 1.0f;
+    if (scale) {  // power-of-two scale that maps max |w| of the row into [0.5, 1)
+        __shared__ double red[HIST_THREADS];
+        double m = 0.0;
+        for (int c = threadIdx.x; c < ncol; c += blockDim.x) m = fmax(m, fabs(src_f64 ? s64[c] : (double)s32[c]));
+        red[threadIdx.x] = m;
+        __syncthreads();
+        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+            __syncthreads();
+        }
+        int ex = 0;
+        frexp(red[0], &ex);
+        sc = red[0] > 0.0 ? ldexpf(1.0f, max(-126, min(127, ex))) : 1.0f;
+        if (threadIdx.x == 0) scale[row] = sc;
+    }
+    const double inv = 1.0 / sc;
+    for (int c = threadIdx.x; c < ldw; c += blockDim.x) {
+        const double v = c < ncol ? sign * (src_f64 ? s64[c] : (double)s32[c]) * inv : 0.0;
+        if constexpr (sizeof(WT) == 4)
+            dst[(size_t)row * ldw + c] = (float)v;
+        else
+            dst[(size_t)row * ldw + c] = __double2bfloat16(v);
+    }
+}
+
+// newest step -> ring slot: x[slot][0] = p, x[slot][1] = u (FP32, zero padded), a[slot] = a
+__global__ void hist_push_kernel(const double *__restrict__ p, const double *__restrict__ u,
+                                 const double *__restrict__ a, int ncol, int ldw, int R, int slot,
+                                 float *__restrict__ X, double *__restrict__ A) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < ldw * R) {
+        const int c = e / R;
+        float *x = X + (size_t)slot * 2 * ldw * R;
+        x[e] = c < ncol ? (float)p[e] : 0.0f;
+        x[(size_t)ldw * R + e] = c < ncol ? (float)u[e] : 0.0f;
+    }
+    if (e < 6 * R) A[(size_t)slot * 6 * R + e] = a ? a[e] : 0.0;
+}
+
+template <int R, int RW, class WT>
+void launch_conv(const sod_history *h, cudaStream_t st, int used) {
+    const int rows_per_cta = (HIST_THREADS / 32) * RW;
+    const dim3 grid(h->nchunk, (h->nrow + rows_per_cta - 1) / rows_per_cta);
+    hist_conv_kernel<R, RW, WT><<<grid, HIST_THREADS, 0, st>>>(
+        h->W.as<WT>(), h->wdtype == SOD_BF16 ? h->scale.as<float>() : nullptr, h->X.as<float>(), used, h->head, h->K,
+        h->nrow, h->ldw, h->cchunk, h->partial.as<double>());
+}
+
+}  // namespace
+
+extern "C" {
+
+int sod_history_create(sod_context *ctx, int nrow, int ncol, int K, int R, int weight_dtype, sod_history **out) {
+    SOD_REQUIRE(ctx && out, "null argument");
+    SOD_REQUIRE(nrow >= 1 && ncol >= 1 && K >= 1, "history bank needs nrow, ncol, K >= 1");
+    SOD_REQUIRE(R == 1 || R == 16, "right-hand sides per step must be 1 or 16");
+    SOD_REQUIRE(weight_dtype == SOD_F32 || weight_dtype == SOD_BF16, "weights are SOD_F32 or SOD_BF16");
+    SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
+    auto h = std::make_unique<sod_history>();
+    h->ctx = ctx;
+    h->nrow = nrow, h->ncol = ncol, h->K = K, h->R = R, h->wdtype = weight_dtype;
+    h->ldw = (ncol + 7) / 8 * 8;
+    const size_t esz = weight_dtype == SOD_F32 ? 4 : 2;
+    SOD_TRY(h->W.ensure(esz * (size_t)K * 2 * nrow * h->ldw));
+    SOD_CHECK_CUDA(cudaMemsetAsync(h->W.p, 0, h->W.bytes, ctx->stream));
+    if (weight_dtype == SOD_BF16) {
+        SOD_TRY(h->scale.ensure(sizeof(float) * (size_t)K * 2 * nrow));
+        SOD_CHECK_CUDA(cudaMemsetAsync(h->scale.p, 0, h->scale.bytes, ctx->stream));
+    }
+    SOD_TRY(h->X.ensure(sizeof(float) * (size_t)K * 2 * h->ldw * R));
+    SOD_CHECK_CUDA(cudaMemsetAsync(h->X.p, 0, h->X.bytes, ctx->stream));
+    SOD_TRY(h->A.ensure(sizeof(double) * (size_t)K * 6 * R));
+    SOD_CHECK_CUDA(cudaMemsetAsync(h->A.p, 0, h->A.bytes, ctx->stream));
+    // column chunks: enough CTAs to cover the SMs several times over
+    const int RW = R == 1 ? 8 : 4;
+    const int row_ctas = (nrow + 8 * RW - 1) / (8 * RW);
+    const int want = std::max(1, (ctx->num_sms * 8 + row_ctas - 1) / row_ctas);
+    const int step = weight_dtype == SOD_F32 ? 128 : 256;  // columns a warp covers per step
+    const int steps = (h->ldw + step - 1) / step;
+    h->nchunk = std::max(1, std::min(want, steps));
+    h->cchunk = ((steps + h->nchunk - 1) / h->nchunk) * step;
+    h->nchunk = (h->ldw + h->cchunk - 1) / h->cchunk;
+    SOD_TRY(h->partial.ensure(sizeof(double) * (size_t)h->nchunk * nrow * R));
+    *out = h.release();
+    return SOD_OK;
+}
+
+int sod_history_set_weights(sod_history *h, int k, const void *G_k, const void *H_k, int in_dtype) {
+    SOD_REQUIRE(h, "null history bank");
+    SOD_REQUIRE(k >= 1 && k <= h->K, "weight index k must be in 1..K");
+    SOD_REQUIRE(G_k && H_k, "null weight matrix");
+    SOD_REQUIRE(in_dtype == SOD_F64 || in_dtype == SOD_F32, "input matrices are SOD_F64 or SOD_F32");
+    sod_context *ctx = h->ctx;
+    SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
+    const size_t isz = in_dtype == SOD_F64 ? 8 : 4, bytes = isz * (size_t)h->nrow * h->ncol;
+    const void *src[2] = {G_k, H_k};
+    for (int t = 0; t < 2; t++) {
+        const void *d = src[t];
+        if (!is_device_pointer(d)) {
+            SOD_TRY(h->tmp.ensure(bytes));
+            SOD_CHECK_CUDA(cudaMemcpyAsync(h->tmp.p, d, bytes, cudaMemcpyHostToDevice, ctx->stream));
+            d = h->tmp.p;
+        }
+        const size_t mat = (size_t)(k - 1) * 2 + t;
+        const double sign = t == 0 ? 1.0 : -1.0;
+        if (h->wdtype == SOD_F32)
+            hist_pack_kernel<float><<<h->nrow, HIST_THREADS, 0, ctx->stream>>>(
+                d, in_dtype == SOD_F64, h->nrow, h->ncol, h->ldw, sign, h->W.as<float>() + mat * h->nrow * h->ldw,
+                nullptr);
+        else
+            hist_pack_kernel<__nv_bfloat16><<<h->nrow, HIST_THREADS, 0, ctx->stream>>>(
+                d, in_dtype == SOD_F64, h->nrow, h->ncol, h->ldw, sign,
+                h->W.as<__nv_bfloat16>() + mat * h->nrow * h->ldw, h->scale.as<float>() + mat * h->nrow);
+        SOD_CHECK_CUDA(cudaGetLastError());
+        ctx->count();
+        if (d == h->tmp.p) SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));  // tmp is reused
+    }
+    return SOD_OK;
+}
+
+int sod_history_set_b(sod_history *h, int k, const double *B_k) {
+    SOD_REQUIRE(h && B_k, "null argument");
+    SOD_REQUIRE(k >= 1 && k <= h->K, "weight index k must be in 1..K");
+    sod_context *ctx = h->ctx;
+    SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
+    if (!h->has_b) {
+        SOD_TRY(h->Bw.ensure(sizeof(double) * (size_t)h->K * h->nrow * 6));
+        SOD_CHECK_CUDA(cudaMemsetAsync(h->Bw.p, 0, h->Bw.bytes, ctx->stream));
+        h->has_b = true;
+    }
+    SOD_CHECK_CUDA(cudaMemcpyAsync(h->Bw.as<double>() + (size_t)(k - 1) * h->nrow * 6, B_k,
+                                   sizeof(double) * (size_t)h->nrow * 6, cudaMemcpyDefault, ctx->stream));
+    return SOD_OK;
+}
+
+int sod_history_push(sod_history *h, const double *p, const double *u, const double *a) {
+    SOD_REQUIRE(h && p && u, "null argument");
+    sod_context *ctx = h->ctx;
+    SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
+    const size_t vb = sizeof(double) * (size_t)h->ncol * h->R, ab = sizeof(double) * 6 * (size_t)h->R;
+    const double *dp = p, *du = u, *da = a;
+    const bool hp = !is_device_pointer(p), hu = !is_device_pointer(u), ha = a && !is_device_pointer(a);
+    if (hp || hu || ha) {
+        SOD_TRY(h->tmp.ensure(2 * vb + ab));
+        char *t = h->tmp.as<char>();
+        if (hp) {
+            SOD_CHECK_CUDA(cudaMemcpyAsync(t, p, vb, cudaMemcpyHostToDevice, ctx->stream));
+            dp = reinterpret_cast<const double *>(t);
+        }
+        if (hu) {
+            SOD_CHECK_CUDA(cudaMemcpyAsync(t + vb, u, vb, cudaMemcpyHostToDevice, ctx->stream));
+            du = reinterpret_cast<const double *>(t + vb);
+        }
+        if (ha) {
+            SOD_CHECK_CUDA(cudaMemcpyAsync(t + 2 * vb, a, ab, cudaMemcpyHostToDevice, ctx->stream));
+            da = reinterpret_cast<const double *>(t + 2 * vb);
+        }
+    }
+    const int n = h->ldw * h->R;
+    hist_push_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(dp, du, da, h->ncol, h->ldw, h->R, h->head,
+                                                              h->X.as<float>(), h->A.as<double>());
+    SOD_CHECK_CUDA(cudaGetLastError());
+    ctx->count();
+    h->head = (h->head + 1) % h->K;
+    h->count = std::min(h->count + 1, h->K);
+    if (hp || hu || ha) SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));  // staging is reused
+    return SOD_OK;
+}
+
+int sod_history_convolve(sod_history *h, double *b_out) {
+    SOD_REQUIRE(h && b_out, "null argument");
+    sod_context *ctx = h->ctx;
+    SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
+    const bool host = !is_device_pointer(b_out);
+    const size_t ob = sizeof(double) * (size_t)h->nrow * h->R;
+    double *dst = b_out;
+    if (host) {
+        SOD_TRY(ctx->staging.ensure(ob));
+        dst = ctx->staging.as<double>();
+    }
+    const int used = h->count;
+    if (used > 0) {
+        const bool bf = h->wdtype == SOD_BF16;
+        if (h->R == 1)
+            bf ? launch_conv<1, 8, __nv_bfloat16>(h, ctx->stream, used) : launch_conv<1, 8, float>(h, ctx->stream, used);
+        else
+            bf ? launch_conv<16, 4, __nv_bfloat16>(h, ctx->stream, used) : launch_conv<16, 4, float>(h, ctx->stream, used);
+        SOD_CHECK_CUDA(cudaGetLastError());
+        ctx->count();
+    } else {
+        SOD_CHECK_CUDA(cudaMemsetAsync(h->partial.p, 0, h->partial.bytes, ctx->stream));
+    }
+    const int n = h->nrow * h->R;
+    hist_finish_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(h->partial.as<double>(), h->nchunk,
+                                                                h->has_b ? h->Bw.as<double>() : nullptr,
+                                                                h->A.as<double>(), used, h->head, h->K, h->nrow,
+                                                                h->R, dst);
+    SOD_CHECK_CUDA(cudaGetLastError());
+    ctx->count();
+    if (host) {
+        SOD_CHECK_CUDA(cudaMemcpyAsync(b_out, dst, ob, cudaMemcpyDeviceToHost, ctx->stream));
+        SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    return SOD_OK;
+}
+
+int sod_history_reset(sod_history *h) {
+    SOD_REQUIRE(h, "null history bank");
+    h->head = 0;
+    h->count = 0;
+    return SOD_OK;
+}
+
+int sod_history_bytes(const sod_history *h, int64_t *weight_bytes) {
+    SOD_REQUIRE(h && weight_bytes, "null argument");
+    *weight_bytes = (int64_t)(h->W.bytes + h->scale.bytes);
+    return SOD_OK;
+}
+
+int sod_history_destroy(sod_history *h) {
+    if (h) {
+        cudaSetDevice(h->ctx->device);
+        delete h;
+    }
+    return SOD_OK;
+}
+
+}  // extern "C"

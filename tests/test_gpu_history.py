@@ -1,0 +1,92 @@
+"""History convolution (sod_history) against the FP64 oracle restatement of
+src/elastodynamics_cqbem_object.cpp:44-48.
+
+Tolerances (relative Frobenius norm of b):
+  FP32 weights : <= 2e-6 (FP32 rounding of weights and history vectors);
+  BF16 weights : <= 4e-3 (8-bit significand of the weights; per-row power-of-two scales)."""
+import numpy as np
+import pytest
+
+from .conftest import rel_fro
+
+pytestmark = pytest.mark.gpu
+
+
+def decaying_bank(rng, K, n, m):
+    """G_k, H_k with the magnitude decay of CQ weights (index 0 unused, as in the oracle)."""
+    G = np.zeros((K + 1, n, m))
+    H = np.zeros((K + 1, n, m))
+    for k in range(1, K + 1):
+        G[k] = rng.normal(size=(n, m)) * 1e-6 * 0.8 ** k
+        H[k] = rng.normal(size=(n, m)) * 0.8 ** k
+    return G, H
+
+
+def run(gpu_ctx, oracle, n, m, K, R, wdt, nsteps, with_b, seed=0):
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    rng = np.random.default_rng(seed)
+    G, H = decaying_bank(rng, K, n, m)
+    B = rng.normal(size=(K + 1, n, 6)) * 1e-3 if with_b else None
+    bank = api.HistoryBank(gpu_ctx, n, m, K, R, wdt)
+    for k in range(1, K + 1):
+        bank.set_weights(k, G[k], H[k])
+        if with_b:
+            bank.set_b(k, B[k])
+    shape = (m, R) if R > 1 else (m,)
+    ps, us, as_ = [], [], []
+    for step in range(nsteps):
+        p = rng.normal(size=shape) * 10.0
+        u = rng.normal(size=shape) * 1e-4
+        a = rng.normal(size=(6, R) if R > 1 else (6,))
+        bank.push(p, u, a if with_b else None)
+        ps.append(p), us.append(u), as_.append(a)
+    got = bank.convolve()
+    used = min(nsteps, K)
+    ph = np.stack(ps[::-1][:used])
+    uh = np.stack(us[::-1][:used])
+    ref = oracle.history_convolution(G, H, ph, uh, B if with_b else None, np.stack(as_[::-1][:used]) if with_b else None)
+    return got, ref, bank
+
+
+@pytest.mark.parametrize("R", [1, 16])
+@pytest.mark.parametrize("nsteps", [3, 11])  # fewer steps than K, and a wrapped ring
+def test_history_fp32(gpu_ctx, oracle, R, nsteps):
+    from surfaceonlydeformables_gb300 import _lib as L
+
+    got, ref, bank = run(gpu_ctx, oracle, 126, 126, 8, R, L.F32, nsteps, with_b=True)
+    assert got.shape == ref.shape
+    assert rel_fro(got, ref) <= 2e-6
+    again = bank.convolve()
+    assert np.array_equal(got.view(np.uint8), again.view(np.uint8))  # bitwise reproducible
+
+
+@pytest.mark.parametrize("R", [1, 16])
+def test_history_bf16(gpu_ctx, oracle, R):
+    from surfaceonlydeformables_gb300 import _lib as L
+
+    got, ref, bank = run(gpu_ctx, oracle, 126, 130, 8, R, L.BF16, 9, with_b=False, seed=3)
+    assert rel_fro(got, ref) <= 4e-3
+    assert bank.weight_bytes == 8 * 2 * 126 * 136 * 2 + 8 * 2 * 126 * 4
+
+
+def test_history_larger_object(gpu_ctx, oracle):
+    """3V = 1926 (642 vertices), K = 24, 16 right-hand sides, ring wrapped, with the B term."""
+    from surfaceonlydeformables_gb300 import _lib as L
+
+    got, ref, _ = run(gpu_ctx, oracle, 1926, 1926, 24, 16, L.F32, 30, with_b=True, seed=5)
+    assert rel_fro(got, ref) <= 2e-6
+
+
+def test_history_empty_and_reset(gpu_ctx):
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    bank = api.HistoryBank(gpu_ctx, 10, 10, 4, 1, L.F32)
+    assert np.all(bank.convolve() == 0.0)
+    bank.set_weights(1, np.eye(10), np.zeros((10, 10)))
+    bank.push(np.arange(10.0), np.zeros(10))
+    assert np.allclose(bank.convolve(), np.arange(10.0))
+    bank.reset()
+    assert np.all(bank.convolve() == 0.0)
