@@ -177,6 +177,15 @@ int sod_batch_launch_count(const sod_batch *batch);
 int sod_batch_profile(sod_batch *batch, int cap, int *which, double *evals, float *ms);
 int sod_batch_destroy(sod_batch *batch);
 
+/* ---- elastostatic BEM matrices ----------------------------------------------------------------- */
+/* Replaces ElasticsBEMMatrixCollection::compute_elastostatic_{G,H}_matrix_collocation
+ * (src/elastics_bem_matrix_collection.cpp:43-243): the Kelvin single- and double-layer matrices,
+ * 3nV x 3nV row-major, H with the rigid-mode diagonal correction H_ii = -sum_{j != i} H_ij.
+ * Regular faces in FP32, singular faces and the correction in FP64.  out: SOD_F64 or SOD_F32, host
+ * or device.  method: SOD_COLLOCATION. */
+int sod_elastostatic_assemble(sod_context *ctx, const sod_mesh *mesh, int kind, int method, double nu, double mu,
+                              int order, int subdiv, int sorder, int ssub, void *out, int out_dtype);
+
 /* ---- per-step history convolution ----------------------------------------------------------- */
 /* Replaces the dense history loop of ElastodynamicsCQBEMObject::estimate_next_state
  * (src/elastodynamics_cqbem_object.cpp:44-48):

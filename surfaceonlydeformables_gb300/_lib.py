@@ -58,6 +58,8 @@ _SIGS = {
     "sod_batch_launch_count": ([_P], _c.c_int),
     "sod_batch_profile": ([_P, _c.c_int, _P, _P, _P], _c.c_int),
     "sod_batch_destroy": ([_P], _c.c_int),
+    "sod_elastostatic_assemble": ([_P, _P, _c.c_int, _c.c_int, _c.c_double, _c.c_double, _c.c_int, _c.c_int,
+                                   _c.c_int, _c.c_int, _P, _c.c_int], _c.c_int),
     "sod_history_create": ([_P, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _P], _c.c_int),
     "sod_history_set_weights": ([_P, _c.c_int, _P, _P, _c.c_int], _c.c_int),
     "sod_history_set_b": ([_P, _c.c_int, _P], _c.c_int),

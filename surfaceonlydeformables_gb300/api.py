@@ -239,6 +239,17 @@ def inverse_transform(ctx: Context, Xhat, L_: int, R: float, out=None, out_dtype
     return out
 
 
+def elastostatic(ctx: Context, mesh: Mesh, kind: str, mat: Material, order: int = 5, subdiv: int = 1,
+                 sorder: int | None = None, ssub: int | None = None, method: int = L.COLLOCATION, out=None,
+                 dtype: int = L.F64):
+    """Elastostatic Kelvin G or H (3nV x 3nV; H with the rigid-mode diagonal correction)."""
+    if out is None:
+        out = np.empty((3 * mesh.nV, 3 * mesh.nV), dtype=np.float64 if dtype == L.F64 else np.float32)
+    L.check(L.load().sod_elastostatic_assemble(ctx.handle, mesh.handle, L.KINDS[kind], method, mat.nu, mat.mu, order,
+                                               subdiv, sorder or min(order, 5), ssub or subdiv, L.ptr(out), dtype))
+    return out
+
+
 class HistoryBank:
     """Device-resident history convolution of one object (sod_history): G_k, -H_k (k = 1..K) as FP32
     or BF16 + per-row scales, a ring of the last K steps' vectors, b = sum G p - H u + B a."""

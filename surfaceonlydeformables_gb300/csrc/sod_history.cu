@@ -90,6 +90,28 @@ __global__ void __launch_bounds__(HIST_THREADS) hist_conv_kernel(const WT *__res
             float sc[RW];
 #pragma unroll
             for (int r = 0; r < RW; r++) sc[r] = scale ? __ldg(scale + mat * nrow + rows[r]) : 1.0f;
+            if (R == 1) {
+                // one right-hand side: accumulate the matrix's chunk unscaled, scale once per row
+                float part[RW];
+#pragma unroll
+                for (int r = 0; r < RW; r++) part[r] = 0.f;
+                for (int c = c0 + VEC * lane; c < c1; c += 32 * VEC) {
+                    float w[RW][VEC], x[VEC];
+#pragma unroll
+                    for (int r = 0; r < RW; r++) load_w(Wm + (size_t)rows[r] * ldw + c, w[r]);
+#pragma unroll
+                    for (int q = 0; q < VEC; q += 4) {
+                        const float4 v = __ldg(reinterpret_cast<const float4 *>(Xm + c + q));
+                        x[q] = v.x, x[q + 1] = v.y, x[q + 2] = v.z, x[q + 3] = v.w;
+                    }
+#pragma unroll
+                    for (int r = 0; r < RW; r++)
+#pragma unroll
+                        for (int q = 0; q < VEC; q++) part[r] = fmaf(w[r][q], x[q], part[r]);
+                }
+#pragma unroll
+                for (int r = 0; r < RW; r++) acc[r][0] = fmaf(part[r], sc[r], acc[r][0]);
+            } else {
             for (int c = c0 + VEC * lane; c < c1; c += 32 * VEC) {
                 float w[RW][VEC];
 #pragma unroll
@@ -103,21 +125,17 @@ __global__ void __launch_bounds__(HIST_THREADS) hist_conv_kernel(const WT *__res
 #pragma unroll
                 for (int q = 0; q < VEC; q++) {
                     float x[R];
-                    if (R % 4 == 0) {
 #pragma unroll
-                        for (int j = 0; j < R; j += 4) {
-                            const float4 v = __ldg(reinterpret_cast<const float4 *>(Xm + (size_t)(c + q) * R + j));
-                            x[j] = v.x, x[j + 1] = v.y, x[j + 2] = v.z, x[j + 3] = v.w;
-                        }
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < R; j++) x[j] = __ldg(Xm + (size_t)(c + q) * R + j);
+                    for (int j = 0; j < R; j += 4) {
+                        const float4 v = __ldg(reinterpret_cast<const float4 *>(Xm + (size_t)(c + q) * R + j));
+                        x[j] = v.x, x[j + 1] = v.y, x[j + 2] = v.z, x[j + 3] = v.w;
                     }
 #pragma unroll
                     for (int r = 0; r < RW; r++)
 #pragma unroll
                         for (int j = 0; j < R; j++) acc[r][j] = fmaf(w[r][q], x[j], acc[r][j]);
                 }
+            }
             }
         }
     }

@@ -178,6 +178,9 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L);
 // `mask`, layout of the regular kernels' epilogue) for nf frequencies; kc is a host array.
 int launch_singular(sod_context *ctx, const sod_mesh *m, int mask, int sorder, int ssub, const KConst<double> *kc,
                     int nf, cd *const S[4], const long long S_fstride[4], cudaStream_t stream);
+// Elastostatic (Kelvin) singular blocks of G / H into S (sod_singular.cu), FP64.
+int launch_static_singular(sod_context *ctx, const sod_mesh *m, int mask, int sorder, int ssub, double nu, double mu,
+                           cd *const S[4], cudaStream_t stream);
 // Batched singular passes: one descriptor per object, flat work lists, launched by sod_batch.
 struct SingBatchObj {
     int nV, nstar, nq2, pad0;

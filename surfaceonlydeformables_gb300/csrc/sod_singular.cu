@@ -431,6 +431,60 @@ __global__ void __launch_bounds__(128) batch_combine_kernel(const SingBatchObj *
                        i, lane);
 }
 
+// ---- elastostatic (Kelvin) singular integrals, FP64 from the same geometry tables ---------------
+//   G: r u* = a_g ((3 - 4 nu) d_pq + rh_p rh_q) / a_g'..., i.e. alpha rh_p rh_q + beta d_pq (polar rule);
+//   H: p* in the traction-kernel structure with constant coefficients (Guiggiani rule), the 1/(4 pi)
+//      and the CPV subtraction (times kappa / 4 pi = (1 - 2 nu) / (8 pi (1 - nu))) added by the combine.
+struct StaticSing {
+    double g_alpha, g_beta;  // G (r u form)
+    double ha, hb, hd;       // H (times 1 / (4 pi r^2) from the weights and the combine)
+};
+__device__ __forceinline__ double dlo(const float2 *p) {
+    const float2 v = __ldg(p);
+    return (double)v.x + (double)v.y;
+}
+__global__ void __launch_bounds__(128) static_sing_kernel(const float2 *__restrict__ polar,
+                                                          const float2 *__restrict__ guig, int nstar, int nq2,
+                                                          const int *__restrict__ star_face,
+                                                          const double *__restrict__ N, int do_g, int do_h,
+                                                          StaticSing c, double2 *__restrict__ Rp,
+                                                          double2 *__restrict__ Rg) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nstar) return;
+    if (do_g) {
+        double acc[18] = {};
+        for (int p = 0; p < nq2; p++) {
+            const float2 *t = polar + (size_t)p * POLAR_FIELDS * nstar + e;
+            const double rh[3] = {dlo(t + nstar), dlo(t + 2 * (size_t)nstar), dlo(t + 3 * (size_t)nstar)};
+            const double wl[3] = {dlo(t + 6 * (size_t)nstar), dlo(t + 7 * (size_t)nstar), dlo(t + 8 * (size_t)nstar)};
+            for (int p2 = 0; p2 < 3; p2++)
+                for (int q2 = p2; q2 < 3; q2++) {
+                    const double v = c.g_alpha * rh[p2] * rh[q2] + (p2 == q2 ? c.g_beta : 0.0);
+                    for (int k = 0; k < 3; k++) acc[k * 6 + sym_index(p2, q2)] += v * wl[k];
+                }
+        }
+        for (int k = 0; k < 18; k++) Rp[(size_t)k * nstar + e] = make_double2(acc[k], 0.0);
+    }
+    if (do_h) {
+        const int f = star_face[e];
+        const double nn[3] = {N[3 * f], N[3 * f + 1], N[3 * f + 2]};
+        double acc[27] = {};
+        for (int p = 0; p < nq2; p++) {
+            const float2 *t = guig + (size_t)p * GUIG_FIELDS * nstar + e;
+            const double rh[3] = {dlo(t + nstar), dlo(t + 2 * (size_t)nstar), dlo(t + 3 * (size_t)nstar)};
+            const double rn = dlo(t + 4 * (size_t)nstar);
+            const double wc[3] = {dlo(t + 5 * (size_t)nstar), dlo(t + 6 * (size_t)nstar), dlo(t + 7 * (size_t)nstar)};
+            for (int p2 = 0; p2 < 3; p2++)
+                for (int q2 = 0; q2 < 3; q2++) {
+                    double v = c.ha * rh[p2] * nn[q2] + c.hb * nn[p2] * rh[q2] + c.hd * rn * rh[p2] * rh[q2];
+                    if (p2 == q2) v += c.hb * rn;
+                    for (int k = 0; k < 3; k++) acc[k * 9 + 3 * p2 + q2] += v * wc[k];
+                }
+        }
+        for (int k = 0; k < 27; k++) Rg[(size_t)k * nstar + e] = make_double2(acc[k], 0.0);
+    }
+}
+
 }  // namespace
 
 // ---- mesh cache of the geometry tables -------------------------------------------------------
@@ -605,6 +659,63 @@ int sing_batch_launch(sod_context *ctx, int which, int mask, const SingBatchObj 
 #undef SOD_BC
         break;
     }
+    SOD_CHECK_CUDA(cudaGetLastError());
+    ctx->count();
+    return SOD_OK;
+}
+
+// Singular blocks of the elastostatic Kelvin kernels into S[SOD_G] / S[SOD_H] (per-slot 3x3 blocks,
+// complex layout with zero imaginary parts), FP64.
+int launch_static_singular(sod_context *ctx, const sod_mesh *m, int mask, int sorder, int ssub, double nu, double mu,
+                           cd *const S[4], cudaStream_t stream) {
+    const sod_mesh::SingGeom *g = nullptr;
+    SOD_TRY(const_cast<sod_mesh *>(m)->sing_geom_for(sorder, ssub, stream, &g));
+    const int nstar = m->star_off.back();
+    if (nstar == 0) return SOD_OK;
+    const bool dg = (mask & KM_G) != 0, dh = (mask & KM_H) != 0;
+    const size_t np = dg ? (size_t)18 * nstar : 0, ng = dh ? (size_t)GUIG_COMPS * nstar : 0;
+    SOD_TRY(ctx->sing_res.ensure(sizeof(double2) * std::max<size_t>(np + ng, 1)));
+    double2 *Rp = dg ? ctx->sing_res.as<double2>() : nullptr;
+    double2 *Rg = dh ? ctx->sing_res.as<double2>() + np : nullptr;
+    StaticSing c;
+    c.g_alpha = 1.0 / (16.0 * CUDART_PI * (1.0 - nu) * mu);
+    c.g_beta = (3.0 - 4.0 * nu) * c.g_alpha;
+    const double C = (1.0 - 2.0 * nu) / (8.0 * CUDART_PI * (1.0 - nu));
+    c.ha = 4.0 * CUDART_PI * C;
+    c.hb = -4.0 * CUDART_PI * C;
+    c.hd = -12.0 * CUDART_PI * C / (1.0 - 2.0 * nu);
+    static_sing_kernel<<<(nstar + 127) / 128, 128, 0, stream>>>(g->polar.as<float2>(), g->guig.as<float2>(), nstar,
+                                                               g->nq2, m->dStarFace.as<int>(), m->dN.as<double>(),
+                                                               dg, dh, c, Rp, Rg);
+    SOD_CHECK_CUDA(cudaGetLastError());
+    ctx->count();
+    CombineObj a{};
+    a.nV = m->nV;
+    a.nstar = nstar;
+    a.star_off = m->dStarOff.as<int>();
+    a.star_face = m->dStarFace.as<int>();
+    a.star_slot = m->dStarSlot.as<int>();
+    a.nbr_off = m->dNbrOff.as<int>();
+    a.N = m->dN.as<double>();
+    a.Rp = Rp;
+    a.Rg = Rg;
+    a.guig_sub = g->guig_sub.as<double>();
+    for (int kd = 0; kd < 4; kd++) a.S[kd] = (mask & (1 << kd)) ? S[kd] : nullptr;
+    FreqD fd;
+    fd.n = 1;
+    fd.k[0] = KConst<double>{};
+    fd.k[0].inv4pi = 1.0 / (4.0 * CUDART_PI);
+    fd.k[0].kappa = (1.0 - 2.0 * nu) / (2.0 * (1.0 - nu));  // kappa / (4 pi) = C
+    CombineStrides st{};
+    st.rp = (long long)np;
+    st.rg = (long long)ng;
+    const int sm = mask & (KM_G | KM_H);
+    if (sm == KM_G)
+        launch_combine<KM_G>(a, st, 1, fd, stream);
+    else if (sm == KM_H)
+        launch_combine<KM_H>(a, st, 1, fd, stream);
+    else
+        launch_combine<KM_G | KM_H>(a, st, 1, fd, stream);
     SOD_CHECK_CUDA(cudaGetLastError());
     ctx->count();
     return SOD_OK;
