@@ -208,6 +208,31 @@ int sod_history_reset(sod_history *bank);
 int sod_history_bytes(const sod_history *bank, int64_t *weight_bytes);
 int sod_history_destroy(sod_history *bank);
 
+/* ---- request loop (continuous batching) ------------------------------------------------------ */
+/* A server owns `slots` assembly contexts and one step context on `device`.  Assembly requests
+ * build a resident object (CQ precompute of G_k, H_k, k = 1..N, into an FP32 history bank, BDF
+ * order bdf, collocation with the 2D rule `order` and subdivision `subdiv`); the request id is the
+ * object id.  Step requests push p, u (3nV doubles each) of that object and produce
+ * b = sum_k G_k p_{n-k} - H_k u_{n-k} (3nV doubles, read with sod_server_result).  Requests are
+ * admitted while slots are free and the bytes of resident banks plus in-flight assembly buffers
+ * stay below hbm_cap_bytes (least recently used idle objects are evicted; later steps for them
+ * complete with SOD_ERR_INVALID_ARG).  All calls are thread-safe. */
+typedef struct sod_server sod_server;
+int sod_server_create(int device, int64_t hbm_cap_bytes, int slots, int max_vertices, sod_server **server);
+int sod_server_submit_assembly(sod_server *server, const double *V, int nV, const int *F, int nF, double E,
+                               double nu, double rho, int bdf, double dt, int N, int order, int subdiv,
+                               int64_t *request_id);
+int sod_server_submit_step(sod_server *server, int64_t object_id, const double *p, const double *u, int n,
+                           int64_t *request_id);
+/* Up to `cap` completions since the last call: request ids, status codes, latency (ns, submission to
+ * completion). */
+int sod_server_poll(sod_server *server, int64_t *ids, int *status, int64_t *latency_ns, int cap, int *n);
+int sod_server_result(sod_server *server, int64_t request_id, double *b, int n);
+/* Waits until every submitted request has completed (SOD_ERR_TIMEOUT after timeout_s seconds). */
+int sod_server_drain(sod_server *server, double timeout_s);
+int sod_server_stats(sod_server *server, int64_t *committed_bytes, int *resident_objects);
+int sod_server_destroy(sod_server *server);
+
 /* ---- time-domain precomputation of one object ------------------------------------------------ */
 /* Replaces compute_H_matrices, compute_G_matrices, compute_B_trans_matrices,
  * compute_B_angular_tensors and compute_B_euler_matrices of ElastodynamicsCQBEMMatrixCollection

@@ -60,6 +60,15 @@ _SIGS = {
     "sod_batch_destroy": ([_P], _c.c_int),
     "sod_elastostatic_assemble": ([_P, _P, _c.c_int, _c.c_int, _c.c_double, _c.c_double, _c.c_int, _c.c_int,
                                    _c.c_int, _c.c_int, _P, _c.c_int], _c.c_int),
+    "sod_server_create": ([_c.c_int, _c.c_int64, _c.c_int, _c.c_int, _P], _c.c_int),
+    "sod_server_submit_assembly": ([_P, _P, _c.c_int, _P, _c.c_int, _c.c_double, _c.c_double, _c.c_double, _c.c_int,
+                                    _c.c_double, _c.c_int, _c.c_int, _c.c_int, _P], _c.c_int),
+    "sod_server_submit_step": ([_P, _c.c_int64, _P, _P, _c.c_int, _P], _c.c_int),
+    "sod_server_poll": ([_P, _P, _P, _P, _c.c_int, _P], _c.c_int),
+    "sod_server_result": ([_P, _c.c_int64, _P, _c.c_int], _c.c_int),
+    "sod_server_drain": ([_P, _c.c_double], _c.c_int),
+    "sod_server_stats": ([_P, _P, _P], _c.c_int),
+    "sod_server_destroy": ([_P], _c.c_int),
     "sod_history_create": ([_P, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _P], _c.c_int),
     "sod_history_set_weights": ([_P, _c.c_int, _P, _P, _c.c_int], _c.c_int),
     "sod_history_set_b": ([_P, _c.c_int, _P], _c.c_int),

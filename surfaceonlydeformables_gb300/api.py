@@ -306,3 +306,59 @@ class HistoryBank:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Request loop with continuous batching (sod_server): assembly requests create device-resident
+    objects, step requests run their history convolution; completions carry per-request latency."""
+
+    def __init__(self, device: int = 0, hbm_cap_bytes: int = 150 << 30, slots: int = 2, max_vertices: int = 2562):
+        self._h = ctypes.c_void_p()
+        L.check(L.load().sod_server_create(device, int(hbm_cap_bytes), slots, max_vertices, ctypes.byref(self._h)))
+        self.n_of = {}
+
+    def submit_assembly(self, mesh: SurfaceMesh, mat: Material, bdf: int, dt: float, N: int, order: int = 5,
+                        subdiv: int = 1) -> int:
+        V = np.ascontiguousarray(mesh.V, dtype=np.float64)
+        F = np.ascontiguousarray(mesh.F, dtype=np.int32)
+        rid = ctypes.c_int64()
+        L.check(L.load().sod_server_submit_assembly(self._h, L.ptr(V), mesh.nV, L.ptr(F), mesh.nF, mat.E, mat.nu,
+                                                    mat.rho, bdf, dt, N, order, subdiv, ctypes.byref(rid)))
+        self.n_of[rid.value] = 3 * mesh.nV
+        return rid.value
+
+    def submit_step(self, obj: int, p, u) -> int:
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        rid = ctypes.c_int64()
+        L.check(L.load().sod_server_submit_step(self._h, obj, L.ptr(p), L.ptr(u), p.size, ctypes.byref(rid)))
+        self.n_of[rid.value] = p.size
+        return rid.value
+
+    def poll(self, cap: int = 4096):
+        ids = np.zeros(cap, dtype=np.int64)
+        st = np.zeros(cap, dtype=np.int32)
+        lat = np.zeros(cap, dtype=np.int64)
+        n = ctypes.c_int()
+        L.check(L.load().sod_server_poll(self._h, L.ptr(ids), L.ptr(st), L.ptr(lat), cap, ctypes.byref(n)))
+        k = n.value
+        return list(zip(ids[:k].tolist(), st[:k].tolist(), lat[:k].tolist()))
+
+    def result(self, rid: int) -> np.ndarray:
+        b = np.empty(self.n_of[rid], dtype=np.float64)
+        L.check(L.load().sod_server_result(self._h, rid, L.ptr(b), b.size))
+        return b
+
+    def drain(self, timeout_s: float = 600.0) -> None:
+        L.check(L.load().sod_server_drain(self._h, timeout_s))
+
+    def close(self) -> None:
+        if self._h:
+            L.load().sod_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
