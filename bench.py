@@ -179,6 +179,189 @@ def cpu_sample(objs, threads: int, budget_s: float = 12.0):
     return done / dt, dt, cores, sample
 
 
+def measured_hbm_gbs() -> float:
+    """HBM copy bandwidth measured on the GB300s (MEASURED_PEAKS.json), else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
+
+
+def history_leg(torch, ctx, stream, n: int = 7686, K: int = 64, reps: int = 10):
+    """Per-step history convolution of one 2562-vertex object (3V = 7686), N = 64 weights of G and H:
+    FP32 and BF16 (+ per-row scales) banks, 1 and 16 right-hand sides.  Inputs resident in HBM;
+    weights far larger than L2.  Algorithmic bytes = the bank's weight bytes per step."""
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    hbm = measured_hbm_gbs()
+    rows = []
+    for wdt, name in ((L.F32, "f32"), (L.BF16, "bf16")):
+        for R in (1, 16):
+            bank = api.HistoryBank(ctx, n, n, K, R, wdt)
+            g = torch.empty((n, n), dtype=torch.float32, device="cuda")
+            gen = torch.Generator(device="cuda")
+            gen.manual_seed(7)
+            for k in range(1, K + 1):
+                g.normal_(0.0, 0.8 ** k, generator=gen)
+                bank.set_weights(k, g, g)
+            shape = (n, R) if R > 1 else (n,)
+            for _ in range(K):
+                t = torch.randn(shape, dtype=torch.float64, device="cuda", generator=gen) * 10.0
+                d = torch.randn(shape, dtype=torch.float64, device="cuda", generator=gen) * 1e-4
+                bank.push(t, d)
+            out = torch.empty(shape, dtype=torch.float64, device="cuda")
+            for _ in range(3):
+                bank.convolve(out)
+            torch.cuda.synchronize()
+            ts = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                bank.convolve(out)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ms = float(np.median(ts))
+            wb = bank.weight_bytes
+            rows.append({"weights": name, "rhs": R, "ms": round(ms, 4), "gb_per_s": round(wb / ms / 1e6, 1),
+                         "hbm_frac": round(wb / ms / 1e6 / hbm, 4), "bytes": wb,
+                         "tflops": round(4.0 * K * n * n * R / ms / 1e9, 2)})
+            bank.close()
+            del g, out
+            torch.cuda.empty_cache()
+    return {"object": "3V = 7686 (2562 vertices), N = 64", "peak_gbs": hbm,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth, measured)", "cases": rows}
+
+
+def elastostatic_leg(torch, ctx, stream):
+    """Elastostatic Kelvin G and H (H with the rigid-mode diagonal correction) of the 2562-vertex
+    object, device-resident FP64 output."""
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+    from surfaceonlydeformables_gb300.meshes import Material, make_icosphere_mesh
+
+    m = make_icosphere_mesh(4, 0.1, jitter=0.2, seed=11)
+    dm = api.Mesh(ctx, m)
+    mat = Material(1e5, 0.45, 1000.0)
+    out = torch.empty((3 * m.nV, 3 * m.nV), dtype=torch.float64, device="cuda")
+    res = {}
+    for kind in ("G", "H"):
+        api.elastostatic(ctx, dm, kind, mat, out=out)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        api.elastostatic(ctx, dm, kind, mat, out=out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res[kind] = {"ms": round(e0.elapsed_time(e1), 3), "entries_per_s": (3 * m.nV) ** 2 / (e0.elapsed_time(e1) * 1e-3)}
+    return {"mesh": f"icosphere level 4, {m.nV} vertices, jittered", **res}
+
+
+def serving_requests(seed: int, n_requests: int, rate_hz: float):
+    """Poisson arrivals; 30% assembly requests (objects from the mixed-size distribution), 70% time
+    steps of already-submitted objects with seeded Gaussian tractions (10 Pa) and displacements."""
+    from surfaceonlydeformables_gb300.meshes import Material, make_icosphere_mesh
+
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    reqs = []
+    objs = []
+    for k in range(n_requests):
+        t += rng.exponential(1.0 / rate_hz)
+        if not objs or rng.random() < 0.3:
+            level = int(rng.choice([2, 3, 4], p=[0.5, 0.35, 0.15]))
+            axes = rng.uniform(0.5, 2.0, size=3)
+            E = float(np.exp(rng.uniform(np.log(1e4), np.log(1e6))))
+            nu = float(rng.uniform(0.2, 0.45))
+            N = int(rng.choice([16, 32]))
+            mesh = make_icosphere_mesh(level, 0.1, axes=axes, seed=seed + k)
+            objs.append(len(reqs))
+            reqs.append(dict(t=t, type="assembly", mesh=mesh, mat=Material(E, nu, 1000.0), N=N))
+        else:
+            j = objs[int(rng.integers(len(objs)))]
+            n = 3 * reqs[j]["mesh"].nV
+            reqs.append(dict(t=t, type="step", target=j, p=rng.normal(size=n) * 10.0, u=rng.normal(size=n) * 1e-4))
+    return reqs
+
+
+def serving_leg(torch, ctx, n_requests: int = 240, rate_hz: float = 150.0, cap_gb: float = 150.0, seed: int = 99):
+    """Request loop (continuous batching, HBM-cap admission) against the plain drop-in on the same
+    request stream (one request at a time, in arrival order)."""
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    reqs = serving_requests(seed, n_requests, rate_hz)
+
+    def summary(lat, t_total):
+        out = {}
+        for ty in ("assembly", "step"):
+            v = np.array([l for r, l in zip(reqs, lat) if r["type"] == ty and l is not None]) * 1e3
+            if len(v):
+                out[ty] = {"n": int(len(v)), "p50_ms": round(float(np.percentile(v, 50)), 3),
+                           "p99_ms": round(float(np.percentile(v, 99)), 3)}
+        out["requests_per_s"] = round(len(reqs) / t_total, 2)
+        return out
+
+    # served: submit at the arrival times, collect completions
+    srv = api.Server(0, int(cap_gb * (1 << 30)), 2, 2562)
+    rid = [None] * len(reqs)
+    t0 = time.perf_counter()
+    for k, r in enumerate(reqs):
+        while time.perf_counter() - t0 < r["t"]:
+            time.sleep(0.0002)
+        if r["type"] == "assembly":
+            rid[k] = srv.submit_assembly(r["mesh"], r["mat"], 2, 1 / 200, r["N"])
+        else:
+            rid[k] = srv.submit_step(rid[r["target"]], r["p"], r["u"])
+    srv.drain(600)
+    t_served = time.perf_counter() - t0
+    done = {i: (st, lat) for i, st, lat in srv.poll(1 << 20)}
+    lat_served = [done[i][1] * 1e-9 if done[i][0] == 0 else None for i in rid]
+    n_failed = sum(1 for i in rid if done[i][0] != 0)
+    srv.close()
+    # plain drop-in: the same stream through the per-object API, one request at a time
+    banks = {}  # insertion / use order = LRU order; evicted beyond the same HBM cap
+    lat_plain = [None] * len(reqs)
+    cap = cap_gb * (1 << 30)
+    t0 = time.perf_counter()
+    for k, r in enumerate(reqs):
+        now = time.perf_counter() - t0
+        if now < r["t"]:
+            time.sleep(r["t"] - now)
+        if r["type"] == "assembly":
+            n = 3 * r["mesh"].nV
+            need = 8 * (r["N"] + 1) * n * n + 8 * r["N"] * n * ((n + 7) // 8 * 8)
+            while banks and sum(b.weight_bytes for b in banks.values()) + need > cap:
+                banks.pop(next(iter(banks))).close()
+            m = api.Mesh(ctx, r["mesh"])
+            pre = api.precompute(ctx, m, r["mat"], 2, 1 / 200, r["N"], kinds=("G", "H"), out_dtype=L.F32)
+            bank = api.HistoryBank(ctx, n, n, r["N"], 1, L.F32)
+            for i in range(1, r["N"] + 1):
+                bank.set_weights(i, pre["G"][i], pre["H"][i])
+            torch.cuda.synchronize()
+            del pre, m
+            torch.cuda.empty_cache()
+            banks[k] = bank
+        elif r["target"] in banks:
+            bank = banks.pop(r["target"])
+            banks[r["target"]] = bank  # most recently used
+            bank.push(r["p"], r["u"])
+            bank.convolve()
+        else:
+            continue  # evicted: the served loop reports these as failed requests too
+        lat_plain[k] = time.perf_counter() - t0 - r["t"]
+    t_plain = time.perf_counter() - t0
+    for b in banks.values():
+        b.close()
+    torch.cuda.empty_cache()
+    return {"requests": len(reqs), "arrivals": f"Poisson, {rate_hz} req/s, seed {seed}",
+            "mix": "30% assembly (mixed-size set distribution, N in {16, 32}), 70% steps of submitted objects",
+            "hbm_cap_gb": cap_gb, "assembly_slots": 2, "failed": n_failed,
+            "served": summary(lat_served, t_served), "plain_drop_in": summary(lat_plain, t_plain)}
+
+
 def run_reference(args):
     objs = CASES[args.case]()
     threads = os.cpu_count() or 1
@@ -249,6 +432,7 @@ def run_gpu(args):
     for o, m, per in zip(objs, meshes, outs):
         batch.add(m, o["mat"], o["s"], per, order=o["order"], subdiv=o["subdiv"])
     batch.finalize()
+    launches_per_step = batch.launches_per_step
 
     def step():
         batch.run()
@@ -368,13 +552,23 @@ def run_gpu(args):
                 "launches": [{"pass": p["pass"], "ms": round(p["ms"], 3), "share": round(p["ms"] / step_ms, 4),
                               "evals": p["evals"]} for p in prof]}
 
+    # ---- other hot-path legs: history convolution, elastostatics, the request loop ----
+    extra = {}
+    if not args.value_only and args.case == "mixed24":
+        del outs, batch
+        torch.cuda.empty_cache()
+        extra["history_convolution"] = history_leg(torch, ctx, stream)
+        extra["elastostatic"] = elastostatic_leg(torch, ctx, stream)
+        if not args.no_serve:
+            extra["serving"] = serving_leg(torch, ctx)
+
     # ---- CPU baseline (rank 0, N = 1 only) ----
     cpu = None
     if rank == 0 and world == 1 and not (args.no_cpu or args.value_only):
         r, dtc, cores, sample = cpu_sample(objs, os.cpu_count() or 1)
         cpu = {"value": r, "unit": "entries/s", "cores": cores, "kind": "port", "sample": sample,
                "seconds": dtc}
-    paths = {"batched_graph": {"entries_per_s": value, "launches_per_step": batch.launches_per_step}}
+    paths = {"batched_graph": {"entries_per_s": value, "launches_per_step": launches_per_step}}
     if t_plain:
         paths["per_object_fused"] = {"entries_per_s": total_entries / t_per_object, "ms_per_step": t_per_object * 1e3}
         paths["plain_per_kind_frequency"] = {"entries_per_s": total_entries / t_plain, "ms_per_step": t_plain * 1e3}
@@ -397,7 +591,7 @@ def run_gpu(args):
                 "e2e": {"value": e2e_value, "unit": "entries/s", "h2d_bytes_per_step": h2d_bytes,
                         "d2h_bytes_per_step": d2h_bytes, "path": "sod_cqbem_assemble per (object, kind, "
                         "frequency) into pinned host memory, complex128 reference layout", "steps": e2e_steps},
-                "gpu_launches": int(launches), "clocks": clk.summary()}
+                "gpu_launches": int(launches), "clocks": clk.summary(), **extra}
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
@@ -412,6 +606,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the request-loop leg")
     ap.add_argument("--value-only", action="store_true",
                     help="profiling runs: time the batched step only (no comparison paths, e2e or CPU leg)")
     ap.add_argument("--case", default="mixed24", choices=sorted(CASES),

@@ -266,11 +266,13 @@ class HistoryBank:
         return np.ascontiguousarray(np.asarray(x, dtype=dtype))
 
     def set_weights(self, k: int, G, H) -> None:
+        """G_k, H_k (nrow x ncol, float64 or float32; host arrays or CUDA tensors).  Device inputs are
+        read in stream order on the context's stream, so they may be released right after the call
+        when they were produced on that stream."""
         G, H = self._arr(G), self._arr(H)
         dt = L.F32 if (getattr(G, "dtype", None) in (np.float32,) or str(getattr(G, "dtype", "")) == "torch.float32") \
             else L.F64
         L.check(L.load().sod_history_set_weights(self._h, k, L.ptr(G), L.ptr(H), dt))
-        self._keep = (G, H)
 
     def set_b(self, k: int, B) -> None:
         B = self._arr(B)

@@ -47,7 +47,7 @@ template <class C, class R> __device__ __forceinline__ void cfma(C &acc, C a, R 
     acc.y = fma(a.y, s, acc.y);
 }
 __device__ __forceinline__ cf crecip(cf a) {
-    const float d = 1.0f / fmaf(a.x, a.x, a.y * a.y);
+    const float d = __frcp_rn(fmaf(a.x, a.x, a.y * a.y));
     return {a.x * d, -a.y * d};
 }
 __device__ __forceinline__ cd crecip(cd a) {
@@ -70,7 +70,9 @@ __device__ __forceinline__ cf cexp_neg(cf z) {
     const float n = rintf(t);
     float f = fmaf(-z.x, 1.44269502162933350f, -n);
     f = fmaf(-z.x, 1.92596299e-8f, f);
-    const float m = (n < -126.f) ? 0.f : ldexpf(exp2f(f), (int)n);
+    // 2^n from the exponent bits (n <= 0 here: Re z >= 0); results below 2^-126 flush to zero
+    const float scale = __int_as_float(((int)n + 127) << 23);
+    const float m = (n < -126.f) ? 0.f : exp2f(f) * scale;
     return {m * cs, -m * sn};
 }
 __device__ __forceinline__ cd cexp_neg(cd z) {
@@ -124,6 +126,8 @@ template <class R> struct KConst {
     R inv4pi;            // 1/(4 pi)
     R sr, si;            // s
     R isr, isi;          // 1/s
+    R sc1r, sc1i;        // s/c1
+    R sc2r, sc2i;        // s/c2
 };
 
 template <class R, class C> struct RadialTerms {
@@ -133,8 +137,8 @@ template <class R, class C> struct RadialTerms {
 template <class R, class C>
 __device__ __forceinline__ RadialTerms<R, C> radial(R r, const KConst<R> &k) {
     RadialTerms<R, C> t;
-    t.z1 = mk(r * k.sr * k.ic1, r * k.si * k.ic1);
-    t.z2 = mk(r * k.sr * k.ic2, r * k.si * k.ic2);
+    t.z1 = mk(r * k.sc1r, r * k.sc1i);
+    t.z2 = mk(r * k.sc2r, r * k.sc2i);
     t.e1 = cexp_neg(t.z1);
     t.e2 = cexp_neg(t.z2);
     t.psi1 = psi(t.z1, t.e1);

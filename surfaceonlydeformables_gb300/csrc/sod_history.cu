@@ -43,27 +43,36 @@ namespace {
 
 constexpr int HIST_THREADS = 256;
 
-// VEC consecutive weights of one row with a single 16-byte load (4 FP32 or 8 BF16)
+// VEC consecutive weights of one row with a single 16-byte load (4 FP32 or 8 BF16), kept packed in
+// registers and unpacked per column at use
 template <class WT> struct WVec {
     static constexpr int VEC = 16 / sizeof(WT);
 };
+__device__ __forceinline__ float wget(const uint4 &q, int k, const float *) {
+    const unsigned int u = k == 0 ? q.x : k == 1 ? q.y : k == 2 ? q.z : q.w;
+    return __uint_as_float(u);
+}
+__device__ __forceinline__ float wget(const uint4 &q, int k, const __nv_bfloat16 *) {
+    const unsigned int u = (k >> 1) == 0 ? q.x : (k >> 1) == 1 ? q.y : (k >> 1) == 2 ? q.z : q.w;
+    return __uint_as_float((k & 1) ? (u & 0xffff0000u) : (u << 16));  // bf16 -> f32 is exact
+}
 __device__ __forceinline__ void load_w(const float *w, float v[4]) {
     const float4 q = __ldg(reinterpret_cast<const float4 *>(w));
     v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
 }
 __device__ __forceinline__ void load_w(const __nv_bfloat16 *w, float v[8]) {
     const uint4 q = __ldg(reinterpret_cast<const uint4 *>(w));
-    const unsigned int u[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u[k]));
-        v[2 * k] = f.x, v[2 * k + 1] = f.y;
-    }
+    for (int k = 0; k < 8; k++) v[k] = wget(q, k, w);
 }
 
 // partial[chunk][row][j] = sum over the used history of this column chunk (FP64 after the lane tree)
+// one right-hand side: enough 16-byte loads in flight per SM -- FP32 with 8 rows per warp at 2 CTAs
+// per SM, BF16 (whose weights unpack into twice the registers) with 4 rows per warp at 4 CTAs per SM
+template <int R, int RW, class WT> constexpr int hist_min_ctas() { return R == 1 ? (RW == 8 ? 2 : 4) : 1; }
+
 template <int R, int RW, class WT>
-__global__ void __launch_bounds__(HIST_THREADS) hist_conv_kernel(const WT *__restrict__ W,
+__global__ void __launch_bounds__(HIST_THREADS, hist_min_ctas<R, RW, WT>()) hist_conv_kernel(const WT *__restrict__ W,
                                                                  const float *__restrict__ scale,
                                                                  const float *__restrict__ X, int used, int head,
                                                                  int K, int nrow, int ldw, int cchunk,
@@ -96,18 +105,18 @@ __global__ void __launch_bounds__(HIST_THREADS) hist_conv_kernel(const WT *__res
 #pragma unroll
                 for (int r = 0; r < RW; r++) part[r] = 0.f;
                 for (int c = c0 + VEC * lane; c < c1; c += 32 * VEC) {
-                    float w[RW][VEC], x[VEC];
+                    uint4 wr[RW];
 #pragma unroll
-                    for (int r = 0; r < RW; r++) load_w(Wm + (size_t)rows[r] * ldw + c, w[r]);
+                    for (int r = 0; r < RW; r++) wr[r] = __ldg(reinterpret_cast<const uint4 *>(Wm + (size_t)rows[r] * ldw + c));
 #pragma unroll
-                    for (int q = 0; q < VEC; q += 4) {
-                        const float4 v = __ldg(reinterpret_cast<const float4 *>(Xm + c + q));
-                        x[q] = v.x, x[q + 1] = v.y, x[q + 2] = v.z, x[q + 3] = v.w;
+                    for (int q4 = 0; q4 < VEC; q4 += 4) {
+                        const float4 v = __ldg(reinterpret_cast<const float4 *>(Xm + c + q4));
+                        const float x[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+#pragma unroll
+                            for (int r = 0; r < RW; r++) part[r] = fmaf(wget(wr[r], q4 + q, Wm), x[q], part[r]);
                     }
-#pragma unroll
-                    for (int r = 0; r < RW; r++)
-#pragma unroll
-                        for (int q = 0; q < VEC; q++) part[r] = fmaf(w[r][q], x[q], part[r]);
                 }
 #pragma unroll
                 for (int r = 0; r < RW; r++) acc[r][0] = fmaf(part[r], sc[r], acc[r][0]);
@@ -254,7 +263,7 @@ int sod_history_create(sod_context *ctx, int nrow, int ncol, int K, int R, int w
     SOD_TRY(h->A.ensure(sizeof(double) * (size_t)K * 6 * R));
     SOD_CHECK_CUDA(cudaMemsetAsync(h->A.p, 0, h->A.bytes, ctx->stream));
     // column chunks: enough CTAs to cover the SMs several times over
-    const int RW = R == 1 ? 8 : 4;
+    const int RW = (R == 1 && weight_dtype == SOD_F32) ? 8 : 4;
     const int row_ctas = (nrow + 8 * RW - 1) / (8 * RW);
     const int want = std::max(1, (ctx->num_sms * 8 + row_ctas - 1) / row_ctas);
     const int step = weight_dtype == SOD_F32 ? 128 : 256;  // columns a warp covers per step
@@ -364,7 +373,7 @@ int sod_history_convolve(sod_history *h, double *b_out) {
     if (used > 0) {
         const bool bf = h->wdtype == SOD_BF16;
         if (h->R == 1)
-            bf ? launch_conv<1, 8, __nv_bfloat16>(h, ctx->stream, used) : launch_conv<1, 8, float>(h, ctx->stream, used);
+            bf ? launch_conv<1, 4, __nv_bfloat16>(h, ctx->stream, used) : launch_conv<1, 8, float>(h, ctx->stream, used);
         else
             bf ? launch_conv<16, 4, __nv_bfloat16>(h, ctx->stream, used) : launch_conv<16, 4, float>(h, ctx->stream, used);
         SOD_CHECK_CUDA(cudaGetLastError());
