@@ -598,6 +598,28 @@ def run_gpu(args):
     return 0
 
 
+def run_leg(args):
+    """One hot-path leg on its own, e.g. a smaller history bank for an ncu capture."""
+    import torch
+
+    from surfaceonlydeformables_gb300 import api
+    from surfaceonlydeformables_gb300 import build as B
+
+    B.build()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = api.Context(0, stream=stream)
+    if args.leg == "history":
+        out = history_leg(torch, ctx, stream, K=args.history_k, reps=args.steps)
+    elif args.leg == "elastostatic":
+        out = elastostatic_leg(torch, ctx, stream)
+    else:
+        out = serving_leg(torch, ctx)
+    print(json.dumps({"leg": args.leg, **out}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -607,6 +629,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop leg")
+    ap.add_argument("--leg", default="all", choices=["all", "history", "elastostatic", "serving"],
+                    help="run one hot-path leg alone (profiling captures) and print its JSON")
+    ap.add_argument("--history-k", type=int, default=64, help="history length of the --leg history bank")
     ap.add_argument("--value-only", action="store_true",
                     help="profiling runs: time the batched step only (no comparison paths, e2e or CPU leg)")
     ap.add_argument("--case", default="mixed24", choices=sorted(CASES),
@@ -614,6 +639,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.leg != "all":
+        return run_leg(args)
     return run_gpu(args)
 
 
