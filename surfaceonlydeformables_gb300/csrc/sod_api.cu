@@ -524,10 +524,7 @@ static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int 
                     "Laplace frequencies must be finite and non-zero");
     for (int kd = 0; kd < 4; kd++)
         if (mask & (1 << kd)) SOD_REQUIRE(outs[kd] != nullptr, "null output buffer");
-    if (method != SOD_COLLOCATION) {
-        set_error("Galerkin assembly is not available in this build");
-        return SOD_ERR_UNSUPPORTED;
-    }
+    SOD_REQUIRE(method == SOD_COLLOCATION || method == SOD_GALERKIN, "method must be collocation or Galerkin");
     SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
     const size_t esz = out_dtype == SOD_C128 ? 16 : 8;
     CollLaunch L{};
@@ -561,7 +558,7 @@ static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int 
     L.parts = parts;
     L.out_dtype = out_dtype;
     L.stream = ctx->stream;
-    SOD_TRY(launch_collocation(ctx, L));
+    SOD_TRY(method == SOD_GALERKIN ? launch_galerkin(ctx, L) : launch_collocation(ctx, L));
     if (staged) {
         for (int kd2 = 0; kd2 < 4; kd2++)
             if (host_out[kd2])

@@ -101,6 +101,13 @@ SOD_HD dd dd_recip(dd b) {
     return dd{y, 0.0f} + e * y;
 }
 SOD_HD dd operator/(dd a, dd b) { return a * dd_recip(b); }
+// square root: correctly rounded float root, then one Newton correction of the residual in dd
+SOD_HD dd dd_sqrt(dd a) {
+    if (!(a.hi > 0.0f)) return dd{0.0f, 0.0f};
+    const float s = sqrtf(a.hi);
+    const dd e = a - two_prod(s, s);
+    return fast_two_sum(s, e.hi * (0.5f / s));
+}
 
 // ---- exp ----
 // e^a for a.hi in [-87, 88]: 2^-47 relative accuracy down to a = -69; below that the low word

@@ -1,0 +1,593 @@
+// sod_galerkin.cu -- Galerkin assembly of the Laplace-domain CQBEM matrices G and H on sm_103a.
+//
+// Replaces compute_elastodynamic_{G,H}_kernel_galerkin_non_singular
+// (src/elastodynamics_cqbem_{G,H}_galerkin_non_singular.cu) and the singular face-pair integrals of
+// src/elastodynamics_cqbem_galerkin_singular.cpp (Sauter-Schwab maps, include/integrator_galerkin.hpp:42-212):
+//   U_ab = sum over face pairs (f1 containing a, f2 containing b) of
+//          int_f1 int_f2 phi_a(x) phi_b(y) K(x, y) dy dx.
+//
+// Regular pairs (no shared vertex), FP32: one CTA per (test vertex a, frequency) owns row block a in
+// shared memory.  It first stages the test quadrature points of the faces around a -- position and
+// weight w_x * area * phi_a(x) -- then walks the trial faces in colour order exactly like the
+// collocation scatter: each thread integrates one trial face f2 against every staged test face that
+// shares no vertex with f2 and adds the three trial-corner blocks without conflicts.  A face pair is
+// integrated once per test corner (three times in all) instead of scattering 9 x 9 blocks with
+// atomics: the result is deterministic and the row accumulator fits in shared memory.
+//
+// Singular pairs (coincident, edge- and vertex-adjacent), double-float: one warp per (star entry of
+// a, partner face f2, frequency); lanes share the 4-D Gauss points of the Sauter-Schwab maps and
+// the warp sums in a fixed xor tree.  An FP64 combine kernel adds the partner blocks into per-
+// (vertex, slot) 3 x 3 blocks over the two-ring of a, which the regular kernel's epilogue adds.
+#include <algorithm>
+#include <array>
+#include <set>
+
+#include "sod_dd.cuh"
+#include "sod_faces.cuh"
+#include "sod_internal.h"
+
+using namespace sod;
+
+namespace {
+
+constexpr int GAL_MAXS = 32;  // faces around a vertex
+constexpr int GAL_MAXQ = 13;  // points of the test rule (the 13-point rule is the largest)
+
+struct GalArgs {
+    int nV, nF;
+    const float4 *faces;      // trial faces, colour ordered
+    const int *color_off;
+    int ncolors;
+    const float4 *faces_nat;  // test faces, natural order
+    const int *star_off, *star_face, *star_corner;
+    void *out;
+    long long fstride;
+    int out_c64, do_regular;
+    const cd *S;  // singular blocks per (frequency, slot)
+    long long S_fstride;
+    const int *slot_off, *slot_vert;
+};
+
+__device__ __forceinline__ void store_o(void *out, int c64, long long idx, double re, double im) {
+    if (c64)
+        reinterpret_cast<float2 *>(out)[idx] = make_float2((float)re, (float)im);
+    else
+        reinterpret_cast<double2 *>(out)[idx] = make_double2(re, im);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(512, 1) gal_scatter_kernel(GalArgs a, PointTable pt,
+                                                             const __grid_constant__ FreqTable ft) {
+    constexpr int NC = KIND == SOD_G ? 6 : 9;
+    extern __shared__ float2 acc[];  // [NC][nV]
+    __shared__ float4 tp[GAL_MAXS * GAL_MAXQ];
+    __shared__ int tv[GAL_MAXS][3];
+    const int i = blockIdx.x, fq = blockIdx.y, nV = a.nV;
+    const KConst<float> k = ft.kf[fq];
+    const int s0 = a.star_off[i], ns = min(a.star_off[i + 1] - s0, GAL_MAXS);
+    const int nq = min(pt.n, GAL_MAXQ);
+    for (int t = threadIdx.x; t < ns * nq; t += blockDim.x) {
+        const int s = t / nq, q = t % nq;
+        const FaceRec fr = load_face(a.faces_nat, a.star_face[s0 + s]);
+        const int sc = a.star_corner[s0 + s];
+        const float4 P = pt.p[q];
+        const float Lsc = sc == 0 ? P.x : sc == 1 ? P.y : P.z;
+        tp[t] = make_float4(P.x * fr.y1.x + P.y * fr.y2.x + P.z * fr.y3.x, P.x * fr.y1.y + P.y * fr.y2.y + P.z * fr.y3.y,
+                            P.x * fr.y1.z + P.y * fr.y2.z + P.z * fr.y3.z, P.w * fr.area * Lsc);
+    }
+    for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+        const FaceRec fr = load_face(a.faces_nat, a.star_face[s0 + s]);
+        tv[s][0] = fr.j0, tv[s][1] = fr.j1, tv[s][2] = fr.j2;
+    }
+    for (int t = threadIdx.x; t < NC * nV; t += blockDim.x) acc[t] = make_float2(0.f, 0.f);
+    __syncthreads();
+    if (a.do_regular) {
+        for (int c = 0; c < a.ncolors; c++) {
+            const int fend = a.color_off[c + 1];
+            for (int f = a.color_off[c] + threadIdx.x; f < fend; f += blockDim.x) {
+                const FaceRec fr = load_face(a.faces, f);
+                const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
+                cf part[3][NC];
+#pragma unroll
+                for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+                    for (int cc = 0; cc < NC; cc++) part[kk][cc] = mk(0.f, 0.f);
+                for (int s = 0; s < ns; s++) {
+                    bool shared = false;
+#pragma unroll
+                    for (int u = 0; u < 3; u++) shared = shared || tv[s][u] == fr.j0 || tv[s][u] == fr.j1 || tv[s][u] == fr.j2;
+                    if (shared) continue;  // singular pair
+                    for (int ix = 0; ix < nq; ix++) {
+                        const float4 X = tp[s * nq + ix];
+                        for (int q = 0; q < pt.n; q++) {
+                            const float4 P = pt.p[q];
+                            const float dx = P.x * fr.y1.x + P.y * fr.y2.x + P.z * fr.y3.x - X.x;
+                            const float dy = P.x * fr.y1.y + P.y * fr.y2.y + P.z * fr.y3.y - X.y;
+                            const float dz = P.x * fr.y1.z + P.y * fr.y2.z + P.z * fr.y3.z - X.z;
+                            const float r2 = dx * dx + dy * dy + dz * dz;
+                            const float rinv = rsqrtf(r2);
+                            const float r = r2 * rinv;
+                            const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
+                            const RadialTerms<float, cf> t = radial<float, cf>(r, k);
+                            cf u[NC];
+                            if (KIND == SOD_G) {
+                                cf al, be;
+                                g_coeffs(t, k, rinv, al, be);
+#pragma unroll
+                                for (int p = 0; p < 3; p++)
+#pragma unroll
+                                    for (int qq = p; qq < 3; qq++) {
+                                        cf v = al * (rh[p] * rh[qq]);
+                                        if (p == qq) v = v + be;
+                                        u[sym_index(p, qq)] = v;
+                                    }
+                            } else {
+                                cf ha, hb, hd;
+                                h_coeffs(t, k, rinv * rinv, ha, hb, hd);
+                                const float rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
+                                const cf hdr = hd * rn, hbr = hb * rn;
+#pragma unroll
+                                for (int p = 0; p < 3; p++)
+#pragma unroll
+                                    for (int qq = 0; qq < 3; qq++) {
+                                        cf v = ha * (rh[p] * nn[qq]) + hb * (nn[p] * rh[qq]) + hdr * (rh[p] * rh[qq]);
+                                        if (p == qq) v = v + hbr;
+                                        u[3 * p + qq] = v;
+                                    }
+                            }
+                            const float w = P.w * fr.area * X.w;
+                            const float wl[3] = {w * P.x, w * P.y, w * P.z};
+#pragma unroll
+                            for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+                                for (int cc = 0; cc < NC; cc++) cfma(part[kk][cc], u[cc], wl[kk]);
+                        }
+                    }
+                }
+                const int jj[3] = {fr.j0, fr.j1, fr.j2};
+#pragma unroll
+                for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+                    for (int cc = 0; cc < NC; cc++) {
+                        float2 &sacc = acc[cc * nV + jj[kk]];
+                        sacc.x += part[kk][cc].x;
+                        sacc.y += part[kk][cc].y;
+                    }
+            }
+            __syncthreads();
+        }
+    }
+    // epilogue: row block 3 x 3nV, singular slot blocks added in FP64
+    const long long ld = 3LL * nV;
+    const long long base = (long long)fq * a.fstride + (long long)(3 * i) * ld;
+    for (int p = 0; p < 3; p++)
+        for (int col = threadIdx.x; col < 3 * nV; col += blockDim.x) {
+            const int j = col / 3, qq = col - 3 * j;
+            const float2 v = acc[(KIND == SOD_G ? sym_index(p, qq) : 3 * p + qq) * nV + j];
+            store_o(a.out, a.out_c64, base + p * ld + col, v.x, v.y);
+        }
+    if (a.S) {
+        __syncthreads();
+        const int b0 = a.slot_off[i], nb = a.slot_off[i + 1] - b0;
+        for (int e = threadIdx.x; e < nb * 9; e += blockDim.x) {
+            const int sl = b0 + e / 9, pq = e % 9, p = pq / 3, qq = pq % 3;
+            const int j = a.slot_vert[sl];
+            const float2 v = acc[(KIND == SOD_G ? sym_index(p, qq) : pq) * nV + j];
+            const cd sv = a.S[(long long)fq * a.S_fstride + (long long)sl * 9 + pq];
+            store_o(a.out, a.out_c64, base + p * ld + 3 * j + qq, (double)v.x + sv.x, (double)v.y + sv.y);
+        }
+    }
+}
+
+// ---- singular pairs in double-float ------------------------------------------------------------
+struct KDDg {
+    cdd sc1, sc2;
+    dd ic1s, ic2s, six_c2s, inv4pirho, inv4pi, k4m1, k2, k1m2, k12;
+};
+__device__ __forceinline__ KDDg make_kddg(const KConst<double> &k) {
+    KDDg o;
+    o.sc1 = cdd{dd_from(k.sc1r), dd_from(k.sc1i)};
+    o.sc2 = cdd{dd_from(k.sc2r), dd_from(k.sc2i)};
+    o.ic1s = dd_from(k.ic1s), o.ic2s = dd_from(k.ic2s), o.six_c2s = dd_from(k.six_c2s);
+    o.inv4pirho = dd_from(k.inv4pirho), o.inv4pi = dd_from(k.inv4pi);
+    o.k4m1 = dd_from(4.0 * k.kappa - 1.0), o.k2 = dd_from(2.0 * k.kappa), o.k1m2 = dd_from(1.0 - 2.0 * k.kappa);
+    o.k12 = dd_from(12.0 * k.kappa);
+    return o;
+}
+
+struct DuffyRule {  // 1-D Gauss-Legendre on [0,1] after subdivision, FP64
+    int n;
+    double x[40], w[40];
+};
+
+struct GalSingArgs {
+    int nent;
+    const int4 *ent;  // per entry: {f2, class, test corner, 0}, {j1[3], 0}, {j2[3], 0}, {slot[3], 0}
+    const double *V, *N;
+    double2 *R;       // [frequency][entry][3 * NCS]
+};
+
+__device__ __forceinline__ dd ddv(double x) { return dd_from(x); }
+
+template <int KIND>
+__global__ void __launch_bounds__(128) gal_sing_kernel(GalSingArgs a, const __grid_constant__ DuffyRule g,
+                                                       const __grid_constant__ FreqTable ft) {
+    constexpr int NCS = KIND == SOD_G ? 6 : 9;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= a.nent) return;
+    const int fq = blockIdx.y;
+    const KDDg k = make_kddg(ft.kd[fq]);
+    const int4 e0 = a.ent[4 * warp], ej1 = a.ent[4 * warp + 1], ej2 = a.ent[4 * warp + 2];
+    const int f2 = e0.x, cls = e0.y, ac = e0.z;
+    const int j1[3] = {ej1.x, ej1.y, ej1.z}, j2[3] = {ej2.x, ej2.y, ej2.z};
+    // parametrisation x = o + xa xh0 + xb xh1, y = o + ya yh0 + yb yh1 (FP64 set-up)
+    double P1[3][3], P2[3][3];
+    for (int c = 0; c < 3; c++)
+        for (int d = 0; d < 3; d++) P1[c][d] = a.V[3 * j1[c] + d], P2[c][d] = a.V[3 * j2[c] + d];
+    double xa[3], xb[3], ya[3], yb[3];
+    for (int d = 0; d < 3; d++) {
+        if (cls == 1) {
+            xa[d] = ya[d] = P1[1][d] - P1[0][d];
+            xb[d] = yb[d] = P1[2][d] - P1[1][d];
+        } else if (cls == 2) {
+            xa[d] = ya[d] = P1[1][d] - P1[0][d];
+            xb[d] = P1[2][d] - P1[1][d];
+            yb[d] = P2[2][d] - P1[1][d];
+        } else {
+            xa[d] = P1[1][d] - P1[0][d];
+            xb[d] = P1[2][d] - P1[1][d];
+            ya[d] = P2[1][d] - P1[0][d];
+            yb[d] = P2[2][d] - P2[1][d];
+        }
+    }
+    auto crossn = [](const double *u, const double *v) {
+        const double c0 = u[1] * v[2] - u[2] * v[1], c1 = u[2] * v[0] - u[0] * v[2], c2 = u[0] * v[1] - u[1] * v[0];
+        return sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+    };
+    const double J = crossn(xa, xb) * crossn(ya, yb);
+    const dd Xa[3] = {ddv(xa[0]), ddv(xa[1]), ddv(xa[2])}, Xb[3] = {ddv(xb[0]), ddv(xb[1]), ddv(xb[2])};
+    const dd Ya[3] = {ddv(ya[0]), ddv(ya[1]), ddv(ya[2])}, Yb[3] = {ddv(yb[0]), ddv(yb[1]), ddv(yb[2])};
+    const dd nn[3] = {ddv(a.N[3 * f2]), ddv(a.N[3 * f2 + 1]), ddv(a.N[3 * f2 + 2])};
+    cdd acc[3][NCS];
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int c = 0; c < NCS; c++) acc[b][c] = cdd{dd{0.f, 0.f}, dd{0.f, 0.f}};
+    const int n = g.n, n4 = n * n * n * n;
+    const int nmap = cls == 1 ? 6 : cls == 2 ? 5 : 2;
+    for (int pidx = lane; pidx < n4 * nmap; pidx += 32) {
+        const int m = pidx / n4, r4 = pidx % n4;
+        const int i1 = r4 / (n * n * n), i2 = (r4 / (n * n)) % n, i3 = (r4 / n) % n, i4 = r4 % n;
+        const dd e1 = ddv(g.x[i1]), e2 = ddv(g.x[i2]), e3 = ddv(g.x[i3]), xi = ddv(g.x[i4]);
+        const dd one = dd{1.f, 0.f};
+        dd w = ddv(g.w[i1] * g.w[i2] * g.w[i3] * g.w[i4]) * (xi * xi * xi);
+        dd xh0, xh1, yh0, yh1;
+        const dd e12 = e1 * e2, e123 = e12 * e3;
+        if (cls == 1) {  // coincident, 6 maps; jac = w xi^3 e1^2 e2
+            w = w * (e1 * e1) * e2;
+            switch (m) {
+            case 0: xh0 = xi, xh1 = xi * (one - e1 + e12), yh0 = xi * (one - e123), yh1 = xi * (one - e1); break;
+            case 1: xh0 = xi * (one - e123), xh1 = xi * (one - e1), yh0 = xi, yh1 = xi * (one - e1 + e12); break;
+            case 2: xh0 = xi, xh1 = xi * e1 * (one - e2 + e2 * e3), yh0 = xi * (one - e12), yh1 = xi * e1 * (one - e2); break;
+            case 3: xh0 = xi * (one - e12), xh1 = xi * e1 * (one - e2), yh0 = xi, yh1 = xi * e1 * (one - e2 + e2 * e3); break;
+            case 4: xh0 = xi * (one - e123), xh1 = xi * e1 * (one - e2 * e3), yh0 = xi, yh1 = xi * e1 * (one - e2); break;
+            default: xh0 = xi, xh1 = xi * e1 * (one - e2), yh0 = xi * (one - e123), yh1 = xi * e1 * (one - e2 * e3); break;
+            }
+        } else if (cls == 2) {  // edge adjacent, 5 maps; jac = w xi^3 e1^2 (times e2 for maps 2..5)
+            w = w * (e1 * e1);
+            switch (m) {
+            case 0: xh0 = xi, xh1 = xi * e1 * e3, yh0 = xi * (one - e12), yh1 = xi * e1 * (one - e2); break;
+            case 1: xh0 = xi, xh1 = xi * e1, yh0 = xi * (one - e123), yh1 = xi * e12 * (one - e3), w = w * e2; break;
+            case 2: xh0 = xi * (one - e12), xh1 = xi * e1 * (one - e2), yh0 = xi, yh1 = xi * e123, w = w * e2; break;
+            case 3: xh0 = xi * (one - e123), xh1 = xi * e12 * (one - e3), yh0 = xi, yh1 = xi * e1, w = w * e2; break;
+            default: xh0 = xi * (one - e123), xh1 = xi * e1 * (one - e2 * e3), yh0 = xi, yh1 = xi * e12, w = w * e2; break;
+            }
+        } else {  // vertex adjacent, 2 maps; jac = w xi^3 e2
+            w = w * e2;
+            if (m == 0) xh0 = xi, xh1 = xi * e1, yh0 = xi * e2, yh1 = xi * e2 * e3;
+            else xh0 = xi * e2, xh1 = xi * e2 * e3, yh0 = xi, yh1 = xi * e1;
+        }
+        // y - x = ya yh0 + yb yh1 - xa xh0 - xb xh1 (the common origin cancels exactly)
+        dd rv[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) rv[d] = Ya[d] * yh0 + Yb[d] * yh1 - Xa[d] * xh0 - Xb[d] * xh1;
+        const dd r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+        const dd r = dd_sqrt(r2);
+        const dd rinv = dd_recip(r);
+        const dd rh[3] = {rv[0] * rinv, rv[1] * rinv, rv[2] * rinv};
+        const dd Lx[3] = {one - xh0, xh0 - xh1, xh1}, Ly[3] = {one - yh0, yh0 - yh1, yh1};
+        const dd wa = w * Lx[ac];
+        // radial terms
+        const cdd z1 = k.sc1 * r, z2 = k.sc2 * r;
+        const cdd ez1 = cdd_exp_neg(z1), ez2 = cdd_exp_neg(z2);
+        const cdd psi1 = cdd_psi(z1, ez1), psi2 = cdd_psi(z2, ez2);
+        const cdd Y = psi1 * k.ic1s - psi2 * k.ic2s;
+        cdd u[NCS];
+        if (KIND == SOD_G) {
+            const cdd B = ez1 * k.ic1s - ez2 * k.ic2s;
+            const dd sc = k.inv4pirho * rinv;
+            const cdd al = (Y * 3.0f + B) * sc, be = (ez2 * k.ic2s - Y) * sc;
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int qq = p; qq < 3; qq++) {
+                    cdd v = al * (rh[p] * rh[qq]);
+                    if (p == qq) v = v + be;
+                    u[sym_index(p, qq)] = v;
+                }
+        } else {
+            const cdd Yc = Y * k.six_c2s;
+            const cdd z1e1 = z1 * ez1, z2e2 = z2 * ez2;
+            const dd sc = k.inv4pi * (rinv * rinv);
+            const cdd ca = (Yc + ez1 * k.k4m1 - ez2 * 2.0f - z1e1 * k.k1m2) * sc;
+            const cdd cb = (Yc + ez1 * k.k2 - ez2 * 3.0f - z2e2) * sc;
+            const cdd cdv = (Yc * (-5.0f) - ez1 * k.k12 + ez2 * 12.0f - z1e1 * k.k2 + z2e2 * 2.0f) * sc;
+            const dd rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
+            const cdd cbr = cb * rn, cdr = cdv * rn;
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int qq = 0; qq < 3; qq++) {
+                    cdd v = ca * (rh[p] * nn[qq]) + cb * (nn[p] * rh[qq]) + cdr * (rh[p] * rh[qq]);
+                    if (p == qq) v = v + cbr;
+                    u[3 * p + qq] = v;
+                }
+        }
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const dd wb = wa * Ly[b];
+#pragma unroll
+            for (int c = 0; c < NCS; c++) cdd_acc(acc[b][c], u[c], wb);
+        }
+    }
+    // fixed xor tree over the lanes, in double-float
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int c = 0; c < NCS; c++) {
+            cdd v = acc[b][c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                cdd w2;
+                w2.x.hi = __shfl_xor_sync(0xffffffffu, v.x.hi, o);
+                w2.x.lo = __shfl_xor_sync(0xffffffffu, v.x.lo, o);
+                w2.y.hi = __shfl_xor_sync(0xffffffffu, v.y.hi, o);
+                w2.y.lo = __shfl_xor_sync(0xffffffffu, v.y.lo, o);
+                v = v + w2;
+            }
+            if (lane == 0)
+                a.R[((size_t)fq * a.nent + warp) * 3 * NCS + b * NCS + c] = make_double2(dd_to(v.x) * J, dd_to(v.y) * J);
+        }
+}
+
+// S[fq][slot][9] = sum of the partner blocks of vertex i (FP64, fixed order); one warp per (i, fq)
+template <int KIND>
+__global__ void __launch_bounds__(128) gal_combine_kernel(int nV, int nent, const int *__restrict__ ent_off,
+                                                          const int4 *__restrict__ ent, const int *__restrict__ slot_off,
+                                                          const double2 *__restrict__ R, cd *__restrict__ S,
+                                                          long long S_fstride, int nf) {
+    constexpr int NCS = KIND == SOD_G ? 6 : 9;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nV * nf) return;
+    const int fq = w / nV, i = w % nV;
+    const int b0 = slot_off[i], nb = slot_off[i + 1] - b0;
+    const int e0 = ent_off[i], e1 = ent_off[i + 1];
+    for (int el = lane; el < nb * 9; el += 32) {
+        const int sl = b0 + el / 9, pq = el % 9, p = pq / 3, q = pq % 3;
+        const int comp = KIND == SOD_G ? sym_index(p, q) : pq;
+        double sx = 0.0, sy = 0.0;
+        for (int e = e0; e < e1; e++) {
+            const int4 s = ent[4 * e + 3];
+            const int sls[3] = {s.x, s.y, s.z};
+            for (int b = 0; b < 3; b++)
+                if (sls[b] == sl) {
+                    const double2 v = R[((size_t)fq * nent + e) * 3 * NCS + b * NCS + comp];
+                    sx += v.x, sy += v.y;
+                }
+        }
+        S[(size_t)fq * S_fstride + (size_t)sl * 9 + pq] = cd{sx, sy};
+    }
+}
+
+// pair classification (the singular-pair structure of include/integrator_galerkin.hpp:262-334):
+// 1 coincident, 2 edge adjacent, 3 vertex adjacent, 0 regular; permuted vertex lists j1, j2
+int classify(const int *F, int f1, int f2, int j1[3], int j2[3]) {
+    auto fv = [&](int f, int k) { return F[3 * f + k]; };
+    if (f1 == f2) {
+        for (int k = 0; k < 3; k++) j1[k] = j2[k] = fv(f1, k);
+        return 1;
+    }
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            if (fv(f1, i) == fv(f2, j) && fv(f1, (i + 1) % 3) == fv(f2, (j + 2) % 3)) {
+                j1[0] = fv(f1, i), j1[1] = fv(f1, (i + 1) % 3), j1[2] = fv(f1, (i + 2) % 3);
+                j2[0] = fv(f2, j), j2[1] = fv(f2, (j + 2) % 3), j2[2] = fv(f2, (j + 1) % 3);
+                return 2;
+            }
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            if (fv(f1, i) == fv(f2, j)) {
+                j1[0] = fv(f1, i), j1[1] = fv(f1, (i + 1) % 3), j1[2] = fv(f1, (i + 2) % 3);
+                j2[0] = fv(f2, j), j2[1] = fv(f2, (j + 1) % 3), j2[2] = fv(f2, (j + 2) % 3);
+                return 3;
+            }
+    return 0;
+}
+
+}  // namespace
+
+// ---- per-mesh Galerkin structures (built once, kept on the mesh) ----------------------------------
+static int build_gal(const sod_mesh *m, sod_mesh::GalData *g) {
+    const int nV = m->nV, nF = m->nF;
+    std::vector<std::vector<int>> vf(nV);
+    for (int f = 0; f < nF; f++)
+        for (int c = 0; c < 3; c++) vf[m->F[3 * f + c]].push_back(f);
+    std::vector<int4> ent;
+    std::vector<int> ent_off(nV + 1, 0), slot_off(nV + 1, 0), slot_vert;
+    for (int a = 0; a < nV; a++) {
+        std::vector<std::array<int, 9>> rows;  // f2, cls, ac, j1[3], j2[3]
+        for (int f1 : vf[a]) {
+            std::set<int> partners;
+            for (int c = 0; c < 3; c++)
+                for (int f2 : vf[m->F[3 * f1 + c]]) partners.insert(f2);
+            for (int f2 : partners) {
+                int j1[3], j2[3];
+                const int cls = classify(m->F.data(), f1, f2, j1, j2);
+                int ac = 0;
+                while (ac < 3 && j1[ac] != a) ac++;
+                rows.push_back({f2, cls, ac, j1[0], j1[1], j1[2], j2[0], j2[1], j2[2]});
+            }
+        }
+        std::vector<int> sl;
+        for (auto &r : rows)
+            for (int b = 0; b < 3; b++) sl.push_back(r[6 + b]);
+        std::sort(sl.begin(), sl.end());
+        sl.erase(std::unique(sl.begin(), sl.end()), sl.end());
+        const int base = (int)slot_vert.size();
+        for (auto &r : rows) {
+            int sv[3];
+            for (int b = 0; b < 3; b++) sv[b] = base + (int)(std::lower_bound(sl.begin(), sl.end(), r[6 + b]) - sl.begin());
+            ent.push_back(make_int4(r[0], r[1], r[2], 0));
+            ent.push_back(make_int4(r[3], r[4], r[5], 0));
+            ent.push_back(make_int4(r[6], r[7], r[8], 0));
+            ent.push_back(make_int4(sv[0], sv[1], sv[2], 0));
+        }
+        slot_vert.insert(slot_vert.end(), sl.begin(), sl.end());
+        ent_off[a + 1] = (int)(ent.size() / 4);
+        slot_off[a + 1] = (int)slot_vert.size();
+    }
+    g->nent = ent_off[nV];
+    g->nslots = slot_off[nV];
+    auto up = [](DevBuf &b, const void *src, size_t bytes) -> int {
+        SOD_TRY(b.ensure(std::max<size_t>(bytes, 16)));
+        if (bytes) SOD_CHECK_CUDA(cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice));
+        return SOD_OK;
+    };
+    SOD_TRY(up(g->ent, ent.data(), sizeof(int4) * ent.size()));
+    SOD_TRY(up(g->ent_off, ent_off.data(), sizeof(int) * ent_off.size()));
+    SOD_TRY(up(g->slot_off, slot_off.data(), sizeof(int) * slot_off.size()));
+    SOD_TRY(up(g->slot_vert, slot_vert.data(), sizeof(int) * slot_vert.size()));
+    return SOD_OK;
+}
+
+namespace sod {
+
+int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
+    const sod_mesh *m = L.mesh;
+    const int mask = L.kind_mask;
+    SOD_REQUIRE((mask & ~((1 << SOD_G) | (1 << SOD_H))) == 0,
+                "Galerkin assembly covers G and H in this build (B_trans / B_angular: collocation)");
+    SOD_REQUIRE(!m->has_vmap, "Galerkin assembly with traction-discontinuity splitting is not supported");
+    for (int v = 0; v < m->nV; v++)
+        SOD_REQUIRE(m->star_off[v + 1] - m->star_off[v] <= GAL_MAXS, "vertex with more than 32 faces");
+    PointTable pt;
+    SOD_TRY(make_point_table(L.order, L.subdiv, pt));
+    SOD_REQUIRE(pt.n <= GAL_MAXQ, "Galerkin test rule: at most 13 points (order <= 7, subdivision 1)");
+    SOD_REQUIRE(L.sorder >= 1 && L.sorder <= 5 && L.ssub >= 1 && L.ssub * L.sorder <= 40,
+                "singular rule: order 1..5, order x subdivision <= 40");
+    if (!m->gal) {
+        auto gd = std::make_unique<sod_mesh::GalData>();
+        SOD_TRY(build_gal(m, gd.get()));
+        const_cast<sod_mesh *>(m)->gal = std::move(gd);
+    }
+    sod_mesh::GalData *g = m->gal.get();
+    const bool sing = (L.parts & SOD_PART_SINGULAR) != 0;
+    const int chunk = std::min(L.nfreq, MAX_FREQ_PER_LAUNCH);
+    const long long nslots = g->nslots;
+    DuffyRule dr{};
+    {
+        int n = 0;
+        const double(*t)[2] = gl_rule_table(L.sorder, n);
+        dr.n = 0;
+        for (int s = 0; s < L.ssub; s++) {
+            const double lo = (double)s / L.ssub, hi = (double)(s + 1) / L.ssub;
+            for (int q = 0; q < n; q++) {
+                dr.x[dr.n] = (hi - lo) * t[q][0] / 2. + (lo + hi) / 2.;
+                dr.w[dr.n] = t[q][1] * (hi - lo) / 2.;
+                dr.n++;
+            }
+        }
+    }
+    const size_t esz = L.out_dtype == SOD_C64 ? 8 : 16;
+    for (int kd = 0; kd < 2; kd++) {
+        if (!(mask & (1 << kd))) continue;
+        int T = ctx->coll_threads > 0 ? ctx->coll_threads : 256;
+        T = std::max(32, std::min(512, (T / 32) * 32));
+        const sod_mesh::Coloured *col = nullptr;
+        SOD_TRY(const_cast<sod_mesh *>(m)->coloured_for(T, &col));
+        const size_t smem = sizeof(float2) * (kd == SOD_G ? 6 : 9) * (size_t)m->nV;
+        const void *fn = kd == SOD_G ? (const void *)gal_scatter_kernel<SOD_G> : (const void *)gal_scatter_kernel<SOD_H>;
+        cudaFuncAttributes attr;
+        SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
+        if (smem + attr.sharedSizeBytes > ctx->smem_optin) {
+            set_error("mesh too large for the shared-memory row accumulator");
+            return SOD_ERR_UNSUPPORTED;
+        }
+        SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)(ctx->smem_optin - attr.sharedSizeBytes)));
+        const int NCS = kd == SOD_G ? 6 : 9;
+        if (sing) {
+            SOD_TRY(ctx->sing.ensure(sizeof(cd) * (size_t)std::max<long long>(nslots * 9 * chunk, 1)));
+            SOD_TRY(ctx->sing_res.ensure(sizeof(double2) * (size_t)std::max<long long>((long long)g->nent * 3 * NCS * chunk, 1)));
+        }
+        for (int f0 = 0; f0 < L.nfreq; f0 += chunk) {
+            const int nf = std::min(chunk, L.nfreq - f0);
+            FreqTable ft;
+            ft.n = nf;
+            for (int l = 0; l < nf; l++) {
+                ft.kd[l] = L.kc_host[f0 + l];
+                ft.kf[l] = to_float(ft.kd[l]);
+            }
+            if (sing && g->nent > 0) {
+                GalSingArgs sa{g->nent, g->ent.as<int4>(), m->dV.as<double>(), m->dN.as<double>(),
+                               ctx->sing_res.as<double2>()};
+                const dim3 grid((g->nent * 32 + 127) / 128, nf);
+                if (kd == SOD_G)
+                    gal_sing_kernel<SOD_G><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
+                else
+                    gal_sing_kernel<SOD_H><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
+                SOD_CHECK_CUDA(cudaGetLastError());
+                ctx->count();
+                const int blocks = (int)(((long long)m->nV * nf * 32 + 127) / 128);
+                if (kd == SOD_G)
+                    gal_combine_kernel<SOD_G><<<blocks, 128, 0, L.stream>>>(
+                        m->nV, g->nent, g->ent_off.as<int>(), g->ent.as<int4>(), g->slot_off.as<int>(),
+                        ctx->sing_res.as<double2>(), ctx->sing.as<cd>(), nslots * 9, nf);
+                else
+                    gal_combine_kernel<SOD_H><<<blocks, 128, 0, L.stream>>>(
+                        m->nV, g->nent, g->ent_off.as<int>(), g->ent.as<int4>(), g->slot_off.as<int>(),
+                        ctx->sing_res.as<double2>(), ctx->sing.as<cd>(), nslots * 9, nf);
+                SOD_CHECK_CUDA(cudaGetLastError());
+                ctx->count();
+            }
+            GalArgs a{};
+            a.nV = m->nV;
+            a.nF = m->nF;
+            a.faces = col->dFaces.as<float4>();
+            a.color_off = col->dOff.as<int>();
+            a.ncolors = col->ncolors;
+            a.faces_nat = m->dFacesNat.as<float4>();
+            a.star_off = m->dStarOff.as<int>();
+            a.star_face = m->dStarFace.as<int>();
+            a.star_corner = m->dStarCorner.as<int>();
+            a.out = static_cast<char *>(L.out[kd]) + (size_t)f0 * (size_t)L.freq_stride[kd] * esz;
+            a.fstride = L.freq_stride[kd];
+            a.out_c64 = L.out_dtype == SOD_C64;
+            a.do_regular = (L.parts & SOD_PART_REGULAR) != 0;
+            a.S = sing ? ctx->sing.as<cd>() : nullptr;
+            a.S_fstride = nslots * 9;
+            a.slot_off = g->slot_off.as<int>();
+            a.slot_vert = g->slot_vert.as<int>();
+            const dim3 grid(m->nV, nf);
+            if (kd == SOD_G)
+                gal_scatter_kernel<SOD_G><<<grid, T, smem, L.stream>>>(a, pt, ft);
+            else
+                gal_scatter_kernel<SOD_H><<<grid, T, smem, L.stream>>>(a, pt, ft);
+            SOD_CHECK_CUDA(cudaGetLastError());
+            ctx->count();
+        }
+    }
+    return SOD_OK;
+}
+
+}  // namespace sod

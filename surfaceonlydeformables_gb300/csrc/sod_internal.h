@@ -147,6 +147,12 @@ struct sod_mesh {
         sod::DevBuf guig_sub; // [9][nstar] double: Cauchy principal value subtraction (times kappa / 4 pi)
     };
     std::map<std::pair<int, int>, std::unique_ptr<SingGeom>> sing_geom;
+    // Galerkin singular-pair entries per vertex and the two-ring slots of each row (sod_galerkin.cu)
+    struct GalData {
+        int nent = 0, nslots = 0;
+        sod::DevBuf ent, ent_off, slot_off, slot_vert;
+    };
+    std::unique_ptr<GalData> gal;
     int sing_geom_for(int sorder, int ssub, cudaStream_t stream, const SingGeom **out);
     // all faces in natural order (for the reduction kernels and Galerkin)
     sod::DevBuf dFacesNat, dCanonNat;
@@ -174,6 +180,8 @@ struct CollLaunch {
     cudaStream_t stream;
 };
 int launch_collocation(sod_context *ctx, const CollLaunch &L);
+// Galerkin assembly of G / H (sod_galerkin.cu); same launch description.
+int launch_galerkin(sod_context *ctx, const CollLaunch &L);
 // Singular passes in double-float (sod_singular.cu): fills the side buffers S[kind] (per kind in
 // `mask`, layout of the regular kernels' epilogue) for nf frequencies; kc is a host array.
 int launch_singular(sod_context *ctx, const sod_mesh *m, int mask, int sorder, int ssub, const KConst<double> *kc,

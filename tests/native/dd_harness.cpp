@@ -23,6 +23,13 @@ void dd_sincos_eval(const double *x, double *xin, double *s, double *c, int n) {
         c[i] = dd_to(cc);
     }
 }
+void dd_sqrt_eval(const double *x, double *xin, double *out, int n) {
+    for (int i = 0; i < n; i++) {
+        const dd a = dd_from(x[i]);
+        xin[i] = dd_to(a);
+        out[i] = dd_to(dd_sqrt(a));
+    }
+}
 void dd_recip_eval(const double *x, double *xin, double *out, int n) {
     for (int i = 0; i < n; i++) {
         const dd a = dd_from(x[i]);

@@ -53,6 +53,15 @@ def test_sincos(lib):
     assert es <= TOL and ec <= TOL, (es, ec)
 
 
+def test_sqrt(lib):
+    rng = np.random.default_rng(4)
+    x = rng.uniform(0.5, 2, 2000) * 10.0 ** rng.integers(-30, 30, 2000)
+    xin, out = np.empty_like(x), np.empty_like(x)
+    call(lib, "dd_sqrt_eval", x, xin, out, n=len(x))
+    err = max(abs(float((mp.mpf(o) - mp.sqrt(mp.mpf(v))) / mp.sqrt(mp.mpf(v)))) for v, o in zip(xin, out))
+    assert err <= TOL, err
+
+
 def test_recip_and_fma(lib):
     rng = np.random.default_rng(3)
     x = rng.uniform(0.5, 2, 2000) * 10.0 ** rng.integers(-20, 20, 2000) * rng.choice([-1, 1], 2000)
