@@ -259,6 +259,51 @@ def elastostatic_leg(torch, ctx, stream):
     return {"mesh": f"icosphere level 4, {m.nV} vertices, jittered", **res}
 
 
+def galerkin_leg(torch, ctx, stream, nfreq: int = 2, rows=(0, 517, 1280, 2561)):
+    """Galerkin G and H of the 2562-vertex jittered icosphere (configs[1]: E 1e5, nu 0.45, dt 1/200,
+    N = 64 -> 33 Laplace frequencies; 13-point rule for regular pairs, Sauter-Schwab order 5 for the
+    singular ones), timed over `nfreq` of the frequencies, with the listed rows checked against the
+    FP64 oracle (the rows of the listed vertices are exact in the row-sampled oracle)."""
+    from oracle import oracle as O
+
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+    from surfaceonlydeformables_gb300.meshes import Material, make_icosphere_mesh
+
+    m = make_icosphere_mesh(4, 0.1, jitter=0.2, seed=2)
+    dm = api.Mesh(ctx, m)
+    mat = Material(1e5, 0.45, 1000.0)
+    s, R, Lq = L.cq_frequencies(2, 1 / 200, 64)
+    sel = s[1:1 + nfreq]
+    n = 3 * m.nV
+    out = {k: torch.empty((nfreq, n, n), dtype=torch.complex64, device="cuda") for k in ("G", "H")}
+    api.assemble_frequencies(ctx, dm, "G", mat, sel[:1], order=7, sorder=5, ssub=1, method=L.GALERKIN,
+                             out=out["G"][:1], dtype=L.C64)
+    torch.cuda.synchronize()
+    res = {}
+    for kind in ("G", "H"):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        api.assemble_frequencies(ctx, dm, kind, mat, sel, order=7, sorder=5, ssub=1, method=L.GALERKIN,
+                                 out=out[kind], dtype=L.C64)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        O.build()
+        r = np.array(rows, dtype=np.int32)
+        idx = np.concatenate([np.arange(3 * v, 3 * v + 3) for v in r])
+        got = out[kind][0].cpu().numpy()[idx]
+        ref = O.galerkin(kind, m, mat, sel[0], order=7, sorder=5, ssub=1, rows=r)
+        err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        res[kind] = {"ms": round(ms, 2), "ms_per_frequency": round(ms / nfreq, 2),
+                     "entries_per_s": n * n * nfreq / (ms * 1e-3), "rel_err_vs_fp64_rows": err}
+    del out
+    torch.cuda.empty_cache()
+    return {"mesh": f"icosphere level 4 jittered (sigma 0.2 edge), {m.nV} vertices / {m.nF} faces",
+            "frequencies_timed": f"{nfreq} of {len(s)}", "rule": "13-point regular, Sauter-Schwab order 5",
+            "oracle_rows": list(rows), **res}
+
+
 def serving_requests(seed: int, n_requests: int, rate_hz: float):
     """Poisson arrivals; 30% assembly requests (objects from the mixed-size distribution), 70% time
     steps of already-submitted objects with seeded Gaussian tractions (10 Pa) and displacements."""
@@ -559,6 +604,7 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         extra["history_convolution"] = history_leg(torch, ctx, stream)
         extra["elastostatic"] = elastostatic_leg(torch, ctx, stream)
+        extra["galerkin"] = galerkin_leg(torch, ctx, stream)
         if not args.no_serve:
             extra["serving"] = serving_leg(torch, ctx)
 
@@ -614,6 +660,8 @@ def run_leg(args):
         out = history_leg(torch, ctx, stream, K=args.history_k, reps=args.steps)
     elif args.leg == "elastostatic":
         out = elastostatic_leg(torch, ctx, stream)
+    elif args.leg == "galerkin":
+        out = galerkin_leg(torch, ctx, stream)
     else:
         out = serving_leg(torch, ctx)
     print(json.dumps({"leg": args.leg, **out}))
@@ -629,7 +677,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop leg")
-    ap.add_argument("--leg", default="all", choices=["all", "history", "elastostatic", "serving"],
+    ap.add_argument("--leg", default="all", choices=["all", "history", "elastostatic", "galerkin", "serving"],
                     help="run one hot-path leg alone (profiling captures) and print its JSON")
     ap.add_argument("--history-k", type=int, default=64, help="history length of the --leg history bank")
     ap.add_argument("--value-only", action="store_true",
