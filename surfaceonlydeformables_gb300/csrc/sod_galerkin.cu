@@ -22,6 +22,7 @@
 #include <array>
 #include <set>
 
+#include "sod_bmom.cuh"
 #include "sod_dd.cuh"
 #include "sod_faces.cuh"
 #include "sod_internal.h"
@@ -32,6 +33,13 @@ namespace {
 
 constexpr int GAL_MAXS = 32;  // faces around a vertex
 constexpr int GAL_MAXQ = 13;  // points of the test rule (the 13-point rule is the largest)
+
+__device__ __forceinline__ void store_o(void *out, int c64, long long idx, double re, double im) {
+    if (c64)
+        reinterpret_cast<float2 *>(out)[idx] = make_float2((float)re, (float)im);
+    else
+        reinterpret_cast<double2 *>(out)[idx] = make_double2(re, im);
+}
 
 struct GalArgs {
     int nV, nF;
@@ -46,20 +54,47 @@ struct GalArgs {
     const cd *S;  // singular blocks per (frequency, slot)
     long long S_fstride;
     const int *slot_off, *slot_vert;
+    void *outB[2];  // B_trans [3V][3], B_angular [3V][9] (null if not requested)
+    long long fstrideB[2];
+    const cd *SB[2];  // singular B per (frequency, vertex): 9 / 27 values
+    long long SB_fstride[2];
 };
 
-__device__ __forceinline__ void store_o(void *out, int c64, long long idx, double re, double im) {
-    if (c64)
-        reinterpret_cast<float2 *>(out)[idx] = make_float2((float)re, (float)im);
-    else
-        reinterpret_cast<double2 *>(out)[idx] = make_double2(re, im);
+// B_trans / B_angular rows of test vertex i from the CTA's component sums (FP64) + singular parts
+template <int BM>
+__device__ __forceinline__ void gal_store_b(const GalArgs &a, const cd *bsum, int i, int fq) {
+    using M = BMom<BM>;
+    if (M::BT && a.outB[0]) {
+        const long long base = (long long)fq * a.fstrideB[0] + (long long)(3 * i) * 3;
+        for (int e = threadIdx.x; e < 9; e += blockDim.x) {
+            cd v = bsum[sym_index(e / 3, e % 3)];
+            if (a.SB[0]) v = v + a.SB[0][(long long)fq * a.SB_fstride[0] + (long long)i * 9 + e];
+            store_o(a.outB[0], a.out_c64, base + e, v.x, v.y);
+        }
+    }
+    if (M::BA && a.outB[1]) {
+        const long long base = (long long)fq * a.fstrideB[1] + (long long)(3 * i) * 9;
+        for (int e = threadIdx.x; e < 27; e += blockDim.x) {
+            const int p = e / 9, qq = (e / 3) % 3, kk = e % 3;
+            cd v = bsum[M::NT + 3 * sym_index(p, qq) + kk];
+            if (a.SB[1]) v = v + a.SB[1][(long long)fq * a.SB_fstride[1] + (long long)i * 27 + e];
+            store_o(a.outB[1], a.out_c64, base + e, v.x, v.y);
+        }
+    }
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(512, 1) gal_scatter_kernel(GalArgs a, PointTable pt,
-                                                             const __grid_constant__ FreqTable ft) {
+
+// With BM != 0 (G only) the pass also integrates B_trans / B_angular from the same radial terms;
+// per-thread B columns live after the row accumulator: [NC_B][blockDim] float2.
+template <int KIND, int BM> constexpr int gal_max_threads() { return (KIND == SOD_G && BM) ? 384 : 512; }
+
+template <int KIND, int BM>
+__global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_scatter_kernel(GalArgs a, PointTable pt,
+                                                                                     const __grid_constant__ FreqTable ft) {
     constexpr int NC = KIND == SOD_G ? 6 : 9;
-    extern __shared__ float2 acc[];  // [NC][nV]
+    using BMo = BMom<KIND == SOD_G ? BM : 0>;
+    constexpr int NCB = BMo::NC;
+    extern __shared__ float2 acc[];  // [NC][nV], then [NCB][blockDim]
     __shared__ float4 tp[GAL_MAXS * GAL_MAXQ];
     __shared__ int tv[GAL_MAXS][3];
     const int i = blockIdx.x, fq = blockIdx.y, nV = a.nV;
@@ -80,6 +115,9 @@ __global__ void __launch_bounds__(512, 1) gal_scatter_kernel(GalArgs a, PointTab
         tv[s][0] = fr.j0, tv[s][1] = fr.j1, tv[s][2] = fr.j2;
     }
     for (int t = threadIdx.x; t < NC * nV; t += blockDim.x) acc[t] = make_float2(0.f, 0.f);
+    float2 *accB = acc + NC * nV;
+#pragma unroll
+    for (int c = 0; c < NCB; c++) accB[c * blockDim.x + threadIdx.x] = make_float2(0.f, 0.f);
     __syncthreads();
     if (a.do_regular) {
         for (int c = 0; c < a.ncolors; c++) {
@@ -87,6 +125,8 @@ __global__ void __launch_bounds__(512, 1) gal_scatter_kernel(GalArgs a, PointTab
             for (int f = a.color_off[c] + threadIdx.x; f < fend; f += blockDim.x) {
                 const FaceRec fr = load_face(a.faces, f);
                 const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
+                BMo bm;
+                if (NCB) bm.zero();
                 cf part[3][NC];
 #pragma unroll
                 for (int kk = 0; kk < 3; kk++)
@@ -141,6 +181,7 @@ __global__ void __launch_bounds__(512, 1) gal_scatter_kernel(GalArgs a, PointTab
                             for (int kk = 0; kk < 3; kk++)
 #pragma unroll
                                 for (int cc = 0; cc < NC; cc++) cfma(part[kk][cc], u[cc], wl[kk]);
+                            if (NCB) bm.add(t, k, r, rh, nn, P.w * X.w);
                         }
                     }
                 }
@@ -153,6 +194,14 @@ __global__ void __launch_bounds__(512, 1) gal_scatter_kernel(GalArgs a, PointTab
                         sacc.x += part[kk][cc].x;
                         sacc.y += part[kk][cc].y;
                     }
+                if (NCB) {
+                    float2 *col = accB + threadIdx.x;
+                    bm.emit(nn, fr.area, [&](int cc, cf v) {
+                        float2 &sb = col[cc * blockDim.x];
+                        sb.x += v.x;
+                        sb.y += v.y;
+                    });
+                }
             }
             __syncthreads();
         }
@@ -160,13 +209,13 @@ __global__ void __launch_bounds__(512, 1) gal_scatter_kernel(GalArgs a, PointTab
     // epilogue: row block 3 x 3nV, singular slot blocks added in FP64
     const long long ld = 3LL * nV;
     const long long base = (long long)fq * a.fstride + (long long)(3 * i) * ld;
-    for (int p = 0; p < 3; p++)
+    for (int p = 0; p < 3 && a.out; p++)
         for (int col = threadIdx.x; col < 3 * nV; col += blockDim.x) {
             const int j = col / 3, qq = col - 3 * j;
             const float2 v = acc[(KIND == SOD_G ? sym_index(p, qq) : 3 * p + qq) * nV + j];
             store_o(a.out, a.out_c64, base + p * ld + col, v.x, v.y);
         }
-    if (a.S) {
+    if (a.S && a.out) {
         __syncthreads();
         const int b0 = a.slot_off[i], nb = a.slot_off[i + 1] - b0;
         for (int e = threadIdx.x; e < nb * 9; e += blockDim.x) {
@@ -177,17 +226,42 @@ __global__ void __launch_bounds__(512, 1) gal_scatter_kernel(GalArgs a, PointTab
             store_o(a.out, a.out_c64, base + p * ld + 3 * j + qq, (double)v.x + sv.x, (double)v.y + sv.y);
         }
     }
+    if (NCB) {
+        // per-thread B columns -> FP64 sums, 32 lanes per component in a fixed xor tree
+        __shared__ cd bsum[24];
+        __syncthreads();
+        const int T = blockDim.x;
+        for (int p = threadIdx.x; p < NCB * 32; p += T) {
+            const int cc = p >> 5, l = p & 31;
+            double sx = 0.0, sy = 0.0;
+            for (int j = l; j < T; j += 32) {
+                const float2 v = accB[cc * T + j];
+                sx += v.x;
+                sy += v.y;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sx += __shfl_xor_sync(0xffffffffu, sx, o);
+                sy += __shfl_xor_sync(0xffffffffu, sy, o);
+            }
+            if (l == 0) bsum[cc] = mk(sx, sy);
+        }
+        __syncthreads();
+        gal_store_b<BM>(a, bsum, i, fq);
+    }
 }
 
 // ---- singular pairs in double-float ------------------------------------------------------------
 struct KDDg {
-    cdd sc1, sc2;
-    dd ic1s, ic2s, six_c2s, inv4pirho, inv4pi, k4m1, k2, k1m2, k12;
+    cdd sc1, sc2, is;
+    dd ic1, ic2, ic1s, ic2s, six_c2s, inv4pirho, inv4pi, k4m1, k2, k1m2, k12;
 };
 __device__ __forceinline__ KDDg make_kddg(const KConst<double> &k) {
     KDDg o;
     o.sc1 = cdd{dd_from(k.sc1r), dd_from(k.sc1i)};
     o.sc2 = cdd{dd_from(k.sc2r), dd_from(k.sc2i)};
+    o.is = cdd{dd_from(k.isr), dd_from(k.isi)};
+    o.ic1 = dd_from(k.ic1), o.ic2 = dd_from(k.ic2);
     o.ic1s = dd_from(k.ic1s), o.ic2s = dd_from(k.ic2s), o.six_c2s = dd_from(k.six_c2s);
     o.inv4pirho = dd_from(k.inv4pirho), o.inv4pi = dd_from(k.inv4pi);
     o.k4m1 = dd_from(4.0 * k.kappa - 1.0), o.k2 = dd_from(2.0 * k.kappa), o.k1m2 = dd_from(1.0 - 2.0 * k.kappa);
@@ -205,14 +279,18 @@ struct GalSingArgs {
     const int4 *ent;  // per entry: {f2, class, test corner, 0}, {j1[3], 0}, {j2[3], 0}, {slot[3], 0}
     const double *V, *N;
     double2 *R;       // [frequency][entry][3 * NCS]
+    double2 *RB;      // [frequency][entry][13] B moments (G pass with B kinds)
 };
+constexpr int GAL_BMOM = 13;  // Ms[3], Md, M1[6], M0, SB, SC
 
 __device__ __forceinline__ dd ddv(double x) { return dd_from(x); }
 
-template <int KIND>
+template <int KIND, int BM>
 __global__ void __launch_bounds__(128) gal_sing_kernel(GalSingArgs a, const __grid_constant__ DuffyRule g,
                                                        const __grid_constant__ FreqTable ft) {
     constexpr int NCS = KIND == SOD_G ? 6 : 9;
+    constexpr bool DB = KIND == SOD_G && BM != 0;
+    constexpr bool BT = (BM & (1 << SOD_B_TRANS)) != 0, BA = (BM & (1 << SOD_B_ANGULAR)) != 0;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= a.nent) return;
     const int fq = blockIdx.y;
@@ -253,6 +331,9 @@ __global__ void __launch_bounds__(128) gal_sing_kernel(GalSingArgs a, const __gr
     for (int b = 0; b < 3; b++)
 #pragma unroll
         for (int c = 0; c < NCS; c++) acc[b][c] = cdd{dd{0.f, 0.f}, dd{0.f, 0.f}};
+    cdd mb[DB ? GAL_BMOM : 1];
+#pragma unroll
+    for (int c = 0; c < (DB ? GAL_BMOM : 1); c++) mb[c] = cdd{dd{0.f, 0.f}, dd{0.f, 0.f}};
     const int n = g.n, n4 = n * n * n * n;
     const int nmap = cls == 1 ? 6 : cls == 2 ? 5 : 2;
     for (int pidx = lane; pidx < n4 * nmap; pidx += 32) {
@@ -339,6 +420,28 @@ __global__ void __launch_bounds__(128) gal_sing_kernel(GalSingArgs a, const __gr
 #pragma unroll
             for (int c = 0; c < NCS; c++) cdd_acc(acc[b][c], u[c], wb);
         }
+        if (DB) {  // B moments with the test weight only (no trial shape function)
+            const dd rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
+            if (BT) {
+                const cdd ws = Y * (k.inv4pi * 0.5f);
+                const cdd di = psi2 * (k.ic2s * k.inv4pi);
+#pragma unroll
+                for (int p = 0; p < 3; p++) cdd_acc(mb[p], ws, wa * rh[p]);
+                cdd_acc(mb[3], di, wa * rn);
+            }
+            if (BA) {
+                const cdd A = Y * (r * k.inv4pi * 0.5f);
+                const cdd Bq = (ez2 * k.ic2 - ez1 * k.ic1) * k.is * (k.inv4pi * 0.5f);
+                const cdd Cq = ez2 * k.is * (k.ic2 * k.inv4pi);
+#pragma unroll
+                for (int p = 0; p < 3; p++)
+#pragma unroll
+                    for (int q = p; q < 3; q++) cdd_acc(mb[4 + sym_index(p, q)], A, wa * (rh[p] * rh[q]));
+                cdd_acc(mb[10], A, wa);
+                cdd_acc(mb[11], Bq, wa);
+                cdd_acc(mb[12], Cq, wa);
+            }
+        }
     }
     // fixed xor tree over the lanes, in double-float
 #pragma unroll
@@ -358,6 +461,61 @@ __global__ void __launch_bounds__(128) gal_sing_kernel(GalSingArgs a, const __gr
             if (lane == 0)
                 a.R[((size_t)fq * a.nent + warp) * 3 * NCS + b * NCS + c] = make_double2(dd_to(v.x) * J, dd_to(v.y) * J);
         }
+    if (DB) {
+#pragma unroll
+        for (int c = 0; c < GAL_BMOM; c++) {
+            cdd v = mb[c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                cdd w2;
+                w2.x.hi = __shfl_xor_sync(0xffffffffu, v.x.hi, o);
+                w2.x.lo = __shfl_xor_sync(0xffffffffu, v.x.lo, o);
+                w2.y.hi = __shfl_xor_sync(0xffffffffu, v.y.hi, o);
+                w2.y.lo = __shfl_xor_sync(0xffffffffu, v.y.lo, o);
+                v = v + w2;
+            }
+            if (lane == 0) a.RB[((size_t)fq * a.nent + warp) * GAL_BMOM + c] = make_double2(dd_to(v.x) * J, dd_to(v.y) * J);
+        }
+    }
+}
+
+// singular B of vertex i: sum over its partner entries of the face tensors formed from the moments
+// with the partner face's normal (FP64, fixed order); one warp per (i, frequency)
+template <int BM>
+__global__ void __launch_bounds__(128) gal_combine_b_kernel(int nV, int nent, const int *__restrict__ ent_off,
+                                                            const int4 *__restrict__ ent, const double *__restrict__ N,
+                                                            const double2 *__restrict__ RB, cd *__restrict__ SBt,
+                                                            cd *__restrict__ SBa, int nf) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nV * nf) return;
+    const int fq = w / nV, i = w % nV;
+    const int e0 = ent_off[i], e1 = ent_off[i + 1];
+    const bool bt = (BM & (1 << SOD_B_TRANS)) != 0, ba = (BM & (1 << SOD_B_ANGULAR)) != 0;
+    for (int el = lane; el < 36; el += 32) {
+        const bool isT = el < 9;
+        if ((isT && !bt) || (!isT && !ba)) continue;
+        double sx = 0.0, sy = 0.0;
+        for (int e = e0; e < e1; e++) {
+            const int f2 = ent[4 * e].x;
+            const double nv[3] = {N[3 * f2], N[3 * f2 + 1], N[3 * f2 + 2]};
+            const double2 *m = RB + ((size_t)fq * nent + e) * GAL_BMOM;
+            if (isT) {
+                const int p = el / 3, q = el % 3;
+                sx += m[p].x * nv[q] + m[q].x * nv[p] + (p == q ? m[3].x : 0.0);
+                sy += m[p].y * nv[q] + m[q].y * nv[p] + (p == q ? m[3].y : 0.0);
+            } else {
+                const int e27 = el - 9, p = e27 / 9, q = (e27 / 3) % 3, kk = e27 % 3;
+                const double2 mpk = m[4 + sym_index(p, kk)], mqk = m[4 + sym_index(q, kk)];
+                const double t2 = (q == kk ? nv[p] : 0.0) + (p == kk ? nv[q] : 0.0);
+                sx += mpk.x * nv[q] + mqk.x * nv[p] + (m[10].x + m[11].x) * t2 + (p == q ? m[12].x * nv[kk] : 0.0);
+                sy += mpk.y * nv[q] + mqk.y * nv[p] + (m[10].y + m[11].y) * t2 + (p == q ? m[12].y * nv[kk] : 0.0);
+            }
+        }
+        if (isT)
+            SBt[(size_t)fq * nV * 9 + (size_t)i * 9 + el] = cd{sx, sy};
+        else
+            SBa[(size_t)fq * nV * 27 + (size_t)i * 27 + (el - 9)] = cd{sx, sy};
+    }
 }
 
 // S[fq][slot][9] = sum of the partner blocks of vertex i (FP64, fixed order); one warp per (i, fq)
@@ -472,11 +630,20 @@ static int build_gal(const sod_mesh *m, sod_mesh::GalData *g) {
 
 namespace sod {
 
+static const void *gal_scatter_fn(int kind, int bm) {
+    constexpr int BT = 1 << SOD_B_TRANS, BA = 1 << SOD_B_ANGULAR;
+    if (kind == SOD_H) return (const void *)gal_scatter_kernel<SOD_H, 0>;
+    return bm == (BT | BA) ? (const void *)gal_scatter_kernel<SOD_G, BT | BA>
+         : bm == BT        ? (const void *)gal_scatter_kernel<SOD_G, BT>
+         : bm == BA        ? (const void *)gal_scatter_kernel<SOD_G, BA>
+                           : (const void *)gal_scatter_kernel<SOD_G, 0>;
+}
+
 int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
     const sod_mesh *m = L.mesh;
     const int mask = L.kind_mask;
-    SOD_REQUIRE((mask & ~((1 << SOD_G) | (1 << SOD_H))) == 0,
-                "Galerkin assembly covers G and H in this build (B_trans / B_angular: collocation)");
+    constexpr int BT = 1 << SOD_B_TRANS, BA = 1 << SOD_B_ANGULAR;
+    const int bm = mask & (BT | BA);
     SOD_REQUIRE(!m->has_vmap, "Galerkin assembly with traction-discontinuity splitting is not supported");
     for (int v = 0; v < m->nV; v++)
         SOD_REQUIRE(m->star_off[v + 1] - m->star_off[v] <= GAL_MAXS, "vertex with more than 32 faces");
@@ -509,16 +676,20 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
         }
     }
     const size_t esz = L.out_dtype == SOD_C64 ? 8 : 16;
+    // passes: G (with the B kinds of the mask; run for B even when G itself is not requested), H
     for (int kd = 0; kd < 2; kd++) {
-        if (!(mask & (1 << kd))) continue;
-        int T = ctx->coll_threads > 0 ? ctx->coll_threads : 256;
-        T = std::max(32, std::min(512, (T / 32) * 32));
-        const sod_mesh::Coloured *col = nullptr;
-        SOD_TRY(const_cast<sod_mesh *>(m)->coloured_for(T, &col));
-        const size_t smem = sizeof(float2) * (kd == SOD_G ? 6 : 9) * (size_t)m->nV;
-        const void *fn = kd == SOD_G ? (const void *)gal_scatter_kernel<SOD_G> : (const void *)gal_scatter_kernel<SOD_H>;
+        const bool run = kd == SOD_G ? ((mask & (1 << SOD_G)) || bm) : (mask & (1 << SOD_H)) != 0;
+        if (!run) continue;
+        const int pbm = kd == SOD_G ? bm : 0;
+        const void *fn = gal_scatter_fn(kd, pbm);
         cudaFuncAttributes attr;
         SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
+        int T = ctx->coll_threads > 0 ? ctx->coll_threads : 256;
+        T = std::max(32, std::min(attr.maxThreadsPerBlock, (T / 32) * 32));
+        const sod_mesh::Coloured *col = nullptr;
+        SOD_TRY(const_cast<sod_mesh *>(m)->coloured_for(T, &col));
+        const int ncb = (pbm & BT ? 6 : 0) + (pbm & BA ? 18 : 0);
+        const size_t smem = sizeof(float2) * ((kd == SOD_G ? 6 : 9) * (size_t)m->nV + (size_t)ncb * T);
         if (smem + attr.sharedSizeBytes > ctx->smem_optin) {
             set_error("mesh too large for the shared-memory row accumulator");
             return SOD_ERR_UNSUPPORTED;
@@ -526,10 +697,16 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
         SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)(ctx->smem_optin - attr.sharedSizeBytes)));
         const int NCS = kd == SOD_G ? 6 : 9;
+        // singular scratch: slot blocks, then per-vertex B (9 + 27); results per entry, then B moments
+        const long long s_slots = nslots * 9, s_bt = (long long)m->nV * 9, s_ba = (long long)m->nV * 27;
+        const long long r_main = (long long)g->nent * 3 * NCS, r_b = pbm ? (long long)g->nent * GAL_BMOM : 0;
         if (sing) {
-            SOD_TRY(ctx->sing.ensure(sizeof(cd) * (size_t)std::max<long long>(nslots * 9 * chunk, 1)));
-            SOD_TRY(ctx->sing_res.ensure(sizeof(double2) * (size_t)std::max<long long>((long long)g->nent * 3 * NCS * chunk, 1)));
+            SOD_TRY(ctx->sing.ensure(sizeof(cd) * (size_t)std::max<long long>((s_slots + s_bt + s_ba) * chunk, 1)));
+            SOD_TRY(ctx->sing_res.ensure(sizeof(double2) * (size_t)std::max<long long>((r_main + r_b) * chunk, 1)));
         }
+        cd *S = ctx->sing.as<cd>();
+        cd *SBt = S + s_slots * chunk, *SBa = SBt + s_bt * chunk;
+        double2 *R = ctx->sing_res.as<double2>(), *RB = R + r_main * chunk;
         for (int f0 = 0; f0 < L.nfreq; f0 += chunk) {
             const int nf = std::min(chunk, L.nfreq - f0);
             FreqTable ft;
@@ -538,28 +715,7 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
                 ft.kd[l] = L.kc_host[f0 + l];
                 ft.kf[l] = to_float(ft.kd[l]);
             }
-            if (sing && g->nent > 0) {
-                GalSingArgs sa{g->nent, g->ent.as<int4>(), m->dV.as<double>(), m->dN.as<double>(),
-                               ctx->sing_res.as<double2>()};
-                const dim3 grid((g->nent * 32 + 127) / 128, nf);
-                if (kd == SOD_G)
-                    gal_sing_kernel<SOD_G><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
-                else
-                    gal_sing_kernel<SOD_H><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
-                SOD_CHECK_CUDA(cudaGetLastError());
-                ctx->count();
-                const int blocks = (int)(((long long)m->nV * nf * 32 + 127) / 128);
-                if (kd == SOD_G)
-                    gal_combine_kernel<SOD_G><<<blocks, 128, 0, L.stream>>>(
-                        m->nV, g->nent, g->ent_off.as<int>(), g->ent.as<int4>(), g->slot_off.as<int>(),
-                        ctx->sing_res.as<double2>(), ctx->sing.as<cd>(), nslots * 9, nf);
-                else
-                    gal_combine_kernel<SOD_H><<<blocks, 128, 0, L.stream>>>(
-                        m->nV, g->nent, g->ent_off.as<int>(), g->ent.as<int4>(), g->slot_off.as<int>(),
-                        ctx->sing_res.as<double2>(), ctx->sing.as<cd>(), nslots * 9, nf);
-                SOD_CHECK_CUDA(cudaGetLastError());
-                ctx->count();
-            }
+            GalSingArgs sa{g->nent, g->ent.as<int4>(), m->dV.as<double>(), m->dN.as<double>(), R, RB};
             GalArgs a{};
             a.nV = m->nV;
             a.nF = m->nF;
@@ -570,19 +726,72 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
             a.star_off = m->dStarOff.as<int>();
             a.star_face = m->dStarFace.as<int>();
             a.star_corner = m->dStarCorner.as<int>();
-            a.out = static_cast<char *>(L.out[kd]) + (size_t)f0 * (size_t)L.freq_stride[kd] * esz;
+            a.out = L.out[kd] ? static_cast<char *>(L.out[kd]) + (size_t)f0 * (size_t)L.freq_stride[kd] * esz : nullptr;
             a.fstride = L.freq_stride[kd];
             a.out_c64 = L.out_dtype == SOD_C64;
             a.do_regular = (L.parts & SOD_PART_REGULAR) != 0;
-            a.S = sing ? ctx->sing.as<cd>() : nullptr;
-            a.S_fstride = nslots * 9;
+            a.S = sing ? S : nullptr;
+            a.S_fstride = s_slots;
             a.slot_off = g->slot_off.as<int>();
             a.slot_vert = g->slot_vert.as<int>();
+            for (int b = 0; b < 2; b++) {
+                const int kb = SOD_B_TRANS + b;
+                a.outB[b] = (pbm & (1 << kb)) && L.out[kb]
+                                ? static_cast<char *>(L.out[kb]) + (size_t)f0 * (size_t)L.freq_stride[kb] * esz
+                                : nullptr;
+                a.fstrideB[b] = L.freq_stride[kb];
+                a.SB[b] = (sing && (pbm & (1 << kb))) ? (b == 0 ? SBt : SBa) : nullptr;
+                a.SB_fstride[b] = b == 0 ? s_bt : s_ba;
+            }
+            // singular pairs, their combination, then the regular pass (which adds them)
+            if (sing && g->nent > 0) {
+                const dim3 grid((g->nent * 32 + 127) / 128, nf);
+                if (kd == SOD_H)
+                    gal_sing_kernel<SOD_H, 0><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
+                else if (pbm == (BT | BA))
+                    gal_sing_kernel<SOD_G, BT | BA><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
+                else if (pbm == BT)
+                    gal_sing_kernel<SOD_G, BT><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
+                else if (pbm == BA)
+                    gal_sing_kernel<SOD_G, BA><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
+                else
+                    gal_sing_kernel<SOD_G, 0><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
+                SOD_CHECK_CUDA(cudaGetLastError());
+                ctx->count();
+                const int blocks = (int)(((long long)m->nV * nf * 32 + 127) / 128);
+                if (kd == SOD_G)
+                    gal_combine_kernel<SOD_G><<<blocks, 128, 0, L.stream>>>(
+                        m->nV, g->nent, g->ent_off.as<int>(), g->ent.as<int4>(), g->slot_off.as<int>(), R, S, s_slots, nf);
+                else
+                    gal_combine_kernel<SOD_H><<<blocks, 128, 0, L.stream>>>(
+                        m->nV, g->nent, g->ent_off.as<int>(), g->ent.as<int4>(), g->slot_off.as<int>(), R, S, s_slots, nf);
+                SOD_CHECK_CUDA(cudaGetLastError());
+                ctx->count();
+                if (pbm) {
+                    if (pbm == (BT | BA))
+                        gal_combine_b_kernel<BT | BA><<<blocks, 128, 0, L.stream>>>(
+                            m->nV, g->nent, g->ent_off.as<int>(), g->ent.as<int4>(), m->dN.as<double>(), RB, SBt, SBa, nf);
+                    else if (pbm == BT)
+                        gal_combine_b_kernel<BT><<<blocks, 128, 0, L.stream>>>(
+                            m->nV, g->nent, g->ent_off.as<int>(), g->ent.as<int4>(), m->dN.as<double>(), RB, SBt, SBa, nf);
+                    else
+                        gal_combine_b_kernel<BA><<<blocks, 128, 0, L.stream>>>(
+                            m->nV, g->nent, g->ent_off.as<int>(), g->ent.as<int4>(), m->dN.as<double>(), RB, SBt, SBa, nf);
+                    SOD_CHECK_CUDA(cudaGetLastError());
+                    ctx->count();
+                }
+            }
             const dim3 grid(m->nV, nf);
-            if (kd == SOD_G)
-                gal_scatter_kernel<SOD_G><<<grid, T, smem, L.stream>>>(a, pt, ft);
+            if (kd == SOD_H)
+                gal_scatter_kernel<SOD_H, 0><<<grid, T, smem, L.stream>>>(a, pt, ft);
+            else if (pbm == (BT | BA))
+                gal_scatter_kernel<SOD_G, BT | BA><<<grid, T, smem, L.stream>>>(a, pt, ft);
+            else if (pbm == BT)
+                gal_scatter_kernel<SOD_G, BT><<<grid, T, smem, L.stream>>>(a, pt, ft);
+            else if (pbm == BA)
+                gal_scatter_kernel<SOD_G, BA><<<grid, T, smem, L.stream>>>(a, pt, ft);
             else
-                gal_scatter_kernel<SOD_H><<<grid, T, smem, L.stream>>>(a, pt, ft);
+                gal_scatter_kernel<SOD_G, 0><<<grid, T, smem, L.stream>>>(a, pt, ft);
             SOD_CHECK_CUDA(cudaGetLastError());
             ctx->count();
         }

@@ -26,7 +26,7 @@ def freq(sodlib, l=3):
     return s[l]
 
 
-@pytest.mark.parametrize("kind", ["G", "H"])
+@pytest.mark.parametrize("kind", ["G", "H", "B_trans", "B_angular"])
 @pytest.mark.parametrize("order", [5, 7])
 def test_galerkin_parts_vs_oracle(gpu_ctx, oracle, sodlib, small, kind, order):
     from surfaceonlydeformables_gb300 import _lib as L
@@ -69,3 +69,18 @@ def test_galerkin_G_symmetric(gpu_ctx, sodlib, small):
     assert np.linalg.norm(Ur - Ur.T) / np.linalg.norm(Ur) <= 1e-6
     U = api.assemble(gpu_ctx, dm, "G", MAT, freq(sodlib), order=7, method=L.GALERKIN)
     assert np.linalg.norm(U - U.T) / np.linalg.norm(U) <= 1e-4
+
+
+def test_galerkin_all_kinds_in_one_call(gpu_ctx, oracle, sodlib, small):
+    """G, H, B_trans and B_angular together (B fused into the G pass) match the single-kind calls."""
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    m, dm = small
+    s, R, Lq = sodlib.cq_frequencies(2, 1 / 200, 16)
+    allk = api.assemble_all(gpu_ctx, dm, MAT, s[:3], order=5, method=L.GALERKIN)
+    for kind in ("G", "H", "B_trans", "B_angular"):
+        one = api.assemble_frequencies(gpu_ctx, dm, kind, MAT, s[:3], order=5, method=L.GALERKIN)
+        assert rel_fro(allk[kind], one) <= 1e-6, kind
+        ref = oracle.galerkin(kind, m, MAT, s[2], order=5, sorder=5, ssub=1)
+        assert rel_fro(allk[kind][2], ref) <= 1e-5, kind
