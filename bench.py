@@ -197,40 +197,43 @@ def history_leg(torch, ctx, stream, n: int = 7686, K: int = 64, reps: int = 10):
 
     hbm = measured_hbm_gbs()
     rows = []
-    for wdt, name in ((L.F32, "f32"), (L.BF16, "bf16")):
-        for R in (1, 16):
-            bank = api.HistoryBank(ctx, n, n, K, R, wdt)
-            g = torch.empty((n, n), dtype=torch.float32, device="cuda")
-            gen = torch.Generator(device="cuda")
-            gen.manual_seed(7)
-            for k in range(1, K + 1):
-                g.normal_(0.0, 0.8 ** k, generator=gen)
-                bank.set_weights(k, g, g)
-            shape = (n, R) if R > 1 else (n,)
-            for _ in range(K):
-                t = torch.randn(shape, dtype=torch.float64, device="cuda", generator=gen) * 10.0
-                d = torch.randn(shape, dtype=torch.float64, device="cuda", generator=gen) * 1e-4
-                bank.push(t, d)
-            out = torch.empty(shape, dtype=torch.float64, device="cuda")
-            for _ in range(3):
-                bank.convolve(out)
+    cases = [(L.F32, "f32", 1, "cuda_cores"), (L.F32, "f32", 16, "cuda_cores"), (L.BF16, "bf16", 1, "tensor_cores"),
+             (L.BF16, "bf16", 1, "cuda_cores"), (L.BF16, "bf16", 16, "tensor_cores"), (L.BF16, "bf16", 16, "cuda_cores")]
+    for wdt, name, R, engine in cases:
+        bank = api.HistoryBank(ctx, n, n, K, R, wdt)
+        if wdt == L.BF16:
+            bank.set_engine(L.HISTORY_ENGINE_TENSOR_CORES if engine == "tensor_cores" else L.HISTORY_ENGINE_CUDA_CORES)
+        g = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(7)
+        for k in range(1, K + 1):
+            g.normal_(0.0, 0.8 ** k, generator=gen)
+            bank.set_weights(k, g, g)
+        shape = (n, R) if R > 1 else (n,)
+        for _ in range(K):
+            t = torch.randn(shape, dtype=torch.float64, device="cuda", generator=gen) * 10.0
+            d = torch.randn(shape, dtype=torch.float64, device="cuda", generator=gen) * 1e-4
+            bank.push(t, d)
+        out = torch.empty(shape, dtype=torch.float64, device="cuda")
+        for _ in range(3):
+            bank.convolve(out)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            bank.convolve(out)
+            e1.record(stream)
             torch.cuda.synchronize()
-            ts = []
-            for _ in range(reps):
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                bank.convolve(out)
-                e1.record(stream)
-                torch.cuda.synchronize()
-                ts.append(e0.elapsed_time(e1))
-            ms = float(np.median(ts))
-            wb = bank.weight_bytes
-            rows.append({"weights": name, "rhs": R, "ms": round(ms, 4), "gb_per_s": round(wb / ms / 1e6, 1),
-                         "hbm_frac": round(wb / ms / 1e6 / hbm, 4), "bytes": wb,
-                         "tflops": round(4.0 * K * n * n * R / ms / 1e9, 2)})
-            bank.close()
-            del g, out
-            torch.cuda.empty_cache()
+            ts.append(e0.elapsed_time(e1))
+        ms = float(np.median(ts))
+        wb = bank.weight_bytes
+        rows.append({"weights": name, "rhs": R, "engine": engine, "ms": round(ms, 4),
+                     "gb_per_s": round(wb / ms / 1e6, 1), "hbm_frac": round(wb / ms / 1e6 / hbm, 4), "bytes": wb,
+                     "tflops": round(4.0 * K * n * n * R / ms / 1e9, 2)})
+        bank.close()
+        del g, out
+        torch.cuda.empty_cache()
     return {"object": "3V = 7686 (2562 vertices), N = 64", "peak_gbs": hbm,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth, measured)", "cases": rows}
 

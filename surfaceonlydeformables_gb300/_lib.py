@@ -21,6 +21,7 @@ KINDS = {"G": G, "H": H, "B_trans": B_TRANS, "B_angular": B_ANGULAR}
 COLLOCATION, GALERKIN = 0, 1
 C128, C64, F64, F32, BF16 = 0, 1, 2, 3, 4
 PART_REGULAR, PART_SINGULAR, PART_ALL = 1, 2, 3
+HISTORY_ENGINE_AUTO, HISTORY_ENGINE_CUDA_CORES, HISTORY_ENGINE_TENSOR_CORES = 0, 1, 2
 
 # every function the header declares, with its ctypes signature
 _c = ctypes
@@ -75,6 +76,7 @@ _SIGS = {
     "sod_history_push": ([_P, _P, _P, _P], _c.c_int),
     "sod_history_convolve": ([_P, _P], _c.c_int),
     "sod_history_reset": ([_P], _c.c_int),
+    "sod_history_set_engine": ([_P, _c.c_int], _c.c_int),
     "sod_history_bytes": ([_P, _P], _c.c_int),
     "sod_history_destroy": ([_P], _c.c_int),
     "sod_cq_inverse_transform": ([_P, _P, _c.c_int, _c.c_int64, _c.c_int, _c.c_int, _c.c_double, _P, _c.c_int],

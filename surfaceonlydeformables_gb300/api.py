@@ -292,6 +292,11 @@ class HistoryBank:
     def reset(self) -> None:
         L.check(L.load().sod_history_reset(self._h))
 
+    def set_engine(self, engine: int) -> None:
+        """L.HISTORY_ENGINE_AUTO (tensor cores for BF16 banks), _CUDA_CORES or _TENSOR_CORES.
+        Switching engines empties the history ring."""
+        L.check(L.load().sod_history_set_engine(self._h, engine))
+
     @property
     def weight_bytes(self) -> int:
         v = ctypes.c_int64()

@@ -19,6 +19,11 @@
 // FP32 registers over all matrices, and the lanes' partial sums are combined in FP64 with a fixed
 // xor tree; a second kernel sums the column chunks in fixed order and adds the B term in FP64.
 // Results are bitwise reproducible.
+//
+// BF16 banks run on the tensor cores instead (sod_history_tc.cu): with 16 right-hand sides the work is
+// a dense contraction (32 flop per 2-byte weight), with one the tensor cores unpack the BF16 weights
+// for free.  The ring then also keeps the history as BF16 hi + lo terms, transposed for the MMA's
+// K-major B operand: [K][2][hi|lo][16][ldw] for R = 16, [K][2][16][ldw] (rows hi, lo, zeros) for R = 1.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -37,6 +42,16 @@ struct sod_history {
     DevBuf W, scale, Bw, X, A, partial, tmp;
     bool has_b = false;
     int nchunk = 0, cchunk = 0;
+    int engine = SOD_HISTORY_ENGINE_AUTO;
+    DevBuf Xt, tcpart, derr;  // tensor-core path: BF16 hi/lo history, per-segment partials, error word
+    int *err_host = nullptr;  // pinned copy of the error word (written by the finish kernel)
+    HistTcPlan plan;          // tensor maps of W and Xt
+    bool tensor_ok() const { return wdtype == SOD_BF16; }
+    bool use_tensor() const { return tensor_ok() && engine != SOD_HISTORY_ENGINE_CUDA_CORES; }
+    int xt_rows() const { return R == 16 ? 2 * 16 : 16; }  // history rows per (slot, G|H)
+    ~sod_history() {
+        if (err_host) cudaFreeHost(err_host);
+    }
 };
 
 namespace {
@@ -214,16 +229,28 @@ __global__ void hist_pack_kernel(const void *__restrict__ src, int src_f64, int 
     }
 }
 
-// newest step -> ring slot: x[slot][0] = p, x[slot][1] = u (FP32, zero padded), a[slot] = a
+// newest step -> ring slot: x[slot][0] = p, x[slot][1] = u (FP32, zero padded), a[slot] = a;
+// with Xt also the BF16 split x = hi + lo, transposed: Xt[slot][t][hi|lo][j][c] for R = 16,
+// Xt[slot][t][0 = hi | 1 = lo][c] for R = 1
 __global__ void hist_push_kernel(const double *__restrict__ p, const double *__restrict__ u,
                                  const double *__restrict__ a, int ncol, int ldw, int R, int slot,
-                                 float *__restrict__ X, double *__restrict__ A) {
+                                 float *__restrict__ X, double *__restrict__ A, __nv_bfloat16 *__restrict__ Xt) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e < ldw * R) {
-        const int c = e / R;
+        const int c = e / R, j = e % R;
         float *x = X + (size_t)slot * 2 * ldw * R;
         x[e] = c < ncol ? (float)p[e] : 0.0f;
         x[(size_t)ldw * R + e] = c < ncol ? (float)u[e] : 0.0f;
+        if (Xt) {
+            for (int t = 0; t < 2; t++) {
+                const double v = c < ncol ? (t == 0 ? p[e] : u[e]) : 0.0;
+                const __nv_bfloat16 hi = __double2bfloat16(v);
+                const __nv_bfloat16 lo = __double2bfloat16(v - (double)__bfloat162float(hi));
+                __nv_bfloat16 *xt = Xt + ((size_t)slot * 2 + t) * (R == 16 ? 32 : 16) * ldw;
+                xt[(size_t)j * ldw + c] = hi;
+                xt[(size_t)(R == 16 ? 16 + j : 1) * ldw + c] = lo;
+            }
+        }
     }
     if (e < 6 * R) A[(size_t)slot * 6 * R + e] = a ? a[e] : 0.0;
 }
@@ -272,6 +299,20 @@ int sod_history_create(sod_context *ctx, int nrow, int ncol, int K, int R, int w
     h->cchunk = ((steps + h->nchunk - 1) / h->nchunk) * step;
     h->nchunk = (h->ldw + h->cchunk - 1) / h->cchunk;
     SOD_TRY(h->partial.ensure(sizeof(double) * (size_t)h->nchunk * nrow * R));
+    if (h->tensor_ok()) {
+        SOD_TRY(h->Xt.ensure(sizeof(__nv_bfloat16) * (size_t)K * 2 * h->xt_rows() * h->ldw));
+        SOD_CHECK_CUDA(cudaMemsetAsync(h->Xt.p, 0, h->Xt.bytes, ctx->stream));
+        SOD_TRY(h->tcpart.ensure(sizeof(float) * history_tc_partial_floats(K, nrow, R)));
+        SOD_TRY(h->derr.ensure(sizeof(int)));
+        SOD_CHECK_CUDA(cudaMemsetAsync(h->derr.p, 0, sizeof(int), ctx->stream));
+        if (cudaMallocHost(&h->err_host, sizeof(int)) != cudaSuccess) {
+            h->err_host = nullptr;
+            set_error("cudaMallocHost failed for the history error word");
+            return SOD_ERR_OOM;
+        }
+        *h->err_host = 0;
+        SOD_TRY(history_tc_plan(&h->plan, h->W.p, h->Xt.p, nrow, ncol, h->ldw, K, R));
+    }
     *out = h.release();
     return SOD_OK;
 }
@@ -349,7 +390,8 @@ int sod_history_push(sod_history *h, const double *p, const double *u, const dou
     }
     const int n = h->ldw * h->R;
     hist_push_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(dp, du, da, h->ncol, h->ldw, h->R, h->head,
-                                                              h->X.as<float>(), h->A.as<double>());
+                                                              h->X.as<float>(), h->A.as<double>(),
+                                                              h->use_tensor() ? h->Xt.as<__nv_bfloat16>() : nullptr);
     SOD_CHECK_CUDA(cudaGetLastError());
     ctx->count();
     h->head = (h->head + 1) % h->K;
@@ -370,6 +412,27 @@ int sod_history_convolve(sod_history *h, double *b_out) {
         dst = ctx->staging.as<double>();
     }
     const int used = h->count;
+    if (h->use_tensor()) {
+        // a bounded wait that expired in an earlier convolution (read from the pinned copy)
+        if (*(volatile int *)h->err_host) {
+            set_error("tensor-core history convolution: a bounded mbarrier wait expired (code " +
+                      std::to_string(*(volatile int *)h->err_host) + ")");
+            return SOD_ERR_TIMEOUT;
+        }
+        SOD_TRY(launch_history_tc(ctx, &h->plan, h->scale.as<float>(), used, h->head, h->tcpart.as<float>(),
+                                  h->has_b ? h->Bw.as<double>() : nullptr, h->A.as<double>(), dst, h->derr.as<int>(),
+                                  h->err_host, ctx->stream));
+        if (host) {
+            SOD_CHECK_CUDA(cudaMemcpyAsync(b_out, dst, ob, cudaMemcpyDeviceToHost, ctx->stream));
+            SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+            if (*(volatile int *)h->err_host) {
+                set_error("tensor-core history convolution: a bounded mbarrier wait expired (code " +
+                          std::to_string(*(volatile int *)h->err_host) + ")");
+                return SOD_ERR_TIMEOUT;
+            }
+        }
+        return SOD_OK;
+    }
     if (used > 0) {
         const bool bf = h->wdtype == SOD_BF16;
         if (h->R == 1)
@@ -392,6 +455,24 @@ int sod_history_convolve(sod_history *h, double *b_out) {
         SOD_CHECK_CUDA(cudaMemcpyAsync(b_out, dst, ob, cudaMemcpyDeviceToHost, ctx->stream));
         SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
     }
+    return SOD_OK;
+}
+
+int sod_history_set_engine(sod_history *h, int engine) {
+    SOD_REQUIRE(h, "null history bank");
+    SOD_REQUIRE(engine == SOD_HISTORY_ENGINE_AUTO || engine == SOD_HISTORY_ENGINE_CUDA_CORES ||
+                    engine == SOD_HISTORY_ENGINE_TENSOR_CORES,
+                "engine must be SOD_HISTORY_ENGINE_AUTO, _CUDA_CORES or _TENSOR_CORES");
+    if (engine == SOD_HISTORY_ENGINE_TENSOR_CORES && !h->tensor_ok()) {
+        set_error("the tensor-core history convolution needs BF16 weights");
+        return SOD_ERR_UNSUPPORTED;
+    }
+    if (h->use_tensor() != (h->tensor_ok() && engine != SOD_HISTORY_ENGINE_CUDA_CORES)) {
+        // the two engines keep the history in different ring layouts: switching clears the ring
+        h->head = 0;
+        h->count = 0;
+    }
+    h->engine = engine;
     return SOD_OK;
 }
 

@@ -1,0 +1,407 @@
+// sod_history_tc.cu -- tensor-core (tcgen05) history convolution for BF16 banks on sm_103a.
+//
+// b[row][r] = sum_seg scale[seg][row] * sum_c W[seg][row][c] * x_seg[c][r]   (seg = (history i, G|-H))
+// is a tall-skinny GEMM per segment: M = nrow, N = R, K = ncol.  With BF16 weights and 16
+// right-hand sides it must move 2 bytes per weight at HBM speed while doing 32 flop per weight --
+// beyond the FP32 pipes; with one right-hand side the tensor cores still unpack the BF16 weights for
+// free, which the CUDA-core loop pays for in issue slots.  So:
+//   * TMA (cp.async.bulk.tensor, 128-byte swizzle) stages 128 x 64 weight tiles -- a 3D tensor map
+//     with the segment as z, so the rows past the end of a matrix in its last row tile are
+//     zero-filled instead of read -- and the matching history tile in a 4-stage shared-memory ring
+//     (mbarrier full / empty pairs);
+//   * one thread issues tcgen05.mma.cta_group::1.kind::f16 (M 128, K 16; BF16 x BF16 -> FP32 in
+//     tensor memory).  The history enters as two BF16 terms (hi + lo), so only the weights are
+//     rounded to BF16: R = 16 stacks the 16 hi and 16 lo columns into one N = 32 operand and the
+//     epilogue adds accumulator columns j and 16 + j; R = 1 puts hi and lo in rows 0 and 1 of an
+//     N = 16 operand (rows 2-15 zero) and adds columns 0 and 1.  Two accumulators in TMEM alternate
+//     between units;
+//   * four epilogue warps read the accumulator with tcgen05.ld (32 lanes each), apply the
+//     segment's row scale and store per-segment partial sums; a second kernel adds the segments in
+//     FP64 in fixed order (deterministic).
+// Work units are (segment, 128-row tile) in segment-major order, dealt round-robin to a grid of
+// 2 CTAs per SM: at any time the grid works on one or two segments, whose history tiles stay in L2
+// while the weights stream past.
+// Every mbarrier wait is bounded (about one second of clock); a timeout sets an error flag that the
+// host reports, and the kernel lets its copies and MMAs in flight finish (again bounded) and
+// releases its tensor memory before returning.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <mutex>
+
+#include "sod_internal.h"
+
+namespace sod {
+namespace {
+
+constexpr int TC_STAGES = 4;
+constexpr int TC_BM = 128, TC_BK = 64;
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;  // 16 KB
+// MMA N (history rows of the B operand: 16 hi + 16 lo, or hi, lo and 14 zero rows) and stage size
+template <int R> constexpr int tc_n() { return R == 16 ? 32 : 16; }
+template <int R> constexpr int tc_stage_bytes() { return TC_A_BYTES + tc_n<R>() * TC_BK * 2; }
+constexpr int TC_THREADS = 192;                     // producer, MMA, 4 epilogue warps
+constexpr int TC_TMEM_COLS = 64;                    // two FP32 accumulators of up to 32 columns
+constexpr long long TC_WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: false on timeout or when another role has already aborted
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag, int *err, int code) {
+    const long long t0 = clock64();
+    while (!mbar_try(bar, parity)) {
+        if (*abort_flag) return false;
+        if (clock64() - t0 > TC_WAIT_CYCLES) {
+            *abort_flag = 1;
+            atomicExch(err, code);
+            return false;
+        }
+    }
+    return true;
+}
+// bounded wait that ignores the abort flag (draining in-flight copies and MMAs before exit)
+__device__ __forceinline__ bool mbar_drain(uint32_t bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try(bar, parity))
+        if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+    return true;
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+// tcgen05 shared-memory matrix descriptor: K-major operand in the 128-byte swizzled layout
+// (rows of 128 B, 8-row atoms of 1024 B): start >> 4, LBO (unused here) 1, SBO 1024 >> 4,
+// descriptor version 1 (bit 46), swizzle mode 2 (128 B, bits 61-63).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+// instruction descriptor, kind::f16: D F32 (bits 4-5 = 1), A BF16 (bits 7-9 = 1), B BF16
+// (bits 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
+template <int N> constexpr uint32_t tc_idesc() {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+}
+
+template <int N> __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            d_tmem),
+        "l"(a), "l"(b), "r"(tc_idesc<N>()), "r"(accumulate));
+}
+// 16 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *v) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+struct TcArgs {
+    int nrow, ncol, used, head, K, mt, units;
+    const float *scale;  // [2K][nrow] (matrix = 2 i + t)
+    float *partial;      // [2 used][nrow][R]
+    int *err;
+};
+
+template <int R>
+__global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_constant__ CUtensorMap wmap,
+                                                                const __grid_constant__ CUtensorMap xmap,
+                                                                TcArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], acc_full[2], acc_empty[2], drain;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // 1024-byte aligned stage ring (the 128-byte swizzle atoms)
+    const uint32_t ring = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; s++) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(smem_u32(&acc_full[b]), 1);
+            mbar_init(smem_u32(&acc_empty[b]), 4);
+        }
+        mbar_init(smem_u32(&drain), 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(TC_TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base;
+    const int KT = (a.ncol + TC_BK - 1) / TC_BK;
+    volatile int *ab = &abort_flag;
+
+    if (warp == 0) {
+        // ---- producer: TMA loads of weight and history tiles ----
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            bool ok = true;
+            int issued[TC_STAGES];  // phase parity of the last load into each stage, -1 = none
+            for (int s = 0; s < TC_STAGES; s++) issued[s] = -1;
+            for (int u = blockIdx.x; u < a.units && ok; u += gridDim.x) {
+                const int seg = u / a.mt, m = u % a.mt;
+                const int i = seg >> 1, t = seg & 1;
+                const int slot = (a.head - 1 - i + 2 * a.K) % a.K;
+                for (int kt = 0; kt < KT && ok; kt++) {
+                    ok = mbar_wait(smem_u32(&empty[stage]), phase ^ 1u, ab, a.err, 1);
+                    if (!ok) break;
+                    const uint32_t fb = smem_u32(&full[stage]);
+                    mbar_expect_tx(fb, tc_stage_bytes<R>());
+                    const uint32_t sA = ring + stage * tc_stage_bytes<R>();
+                    tma_load_3d(sA, &wmap, kt * TC_BK, m * TC_BM, seg, fb);
+                    tma_load_2d(sA + TC_A_BYTES, &xmap, kt * TC_BK, (slot * 2 + t) * tc_n<R>(), fb);
+                    issued[stage] = (int)phase;
+                    if (++stage == TC_STAGES) stage = 0, phase ^= 1u;
+                }
+            }
+            if (!ok)  // aborted: let the copies in flight land before shared memory is released
+                for (int s = 0; s < TC_STAGES; s++)
+                    if (issued[s] >= 0) mbar_drain(smem_u32(&full[s]), (uint32_t)issued[s]);
+        }
+    } else if (warp == 1) {
+        // ---- MMA issue (one thread) ----
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            bool ok = true;
+            int ul = 0;
+            for (int u = blockIdx.x; u < a.units && ok; u += gridDim.x, ul++) {
+                const int buf = ul & 1;
+                const uint32_t aphase = (ul >> 1) & 1;
+                ok = mbar_wait(smem_u32(&acc_empty[buf]), aphase ^ 1u, ab, a.err, 2);
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t d = tmem + buf * 32;
+                for (int kt = 0; kt < KT && ok; kt++) {
+                    ok = mbar_wait(smem_u32(&full[stage]), phase, ab, a.err, 3);
+                    if (!ok) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t sA = ring + stage * tc_stage_bytes<R>();
+#pragma unroll
+                    for (int k = 0; k < TC_BK / 16; k++)
+                        mma_bf16<tc_n<R>()>(d, smem_desc(sA + k * 32), smem_desc(sA + TC_A_BYTES + k * 32), (kt | k) != 0);
+                    mma_commit(smem_u32(&empty[stage]));  // frees the stage when these MMAs finish
+                    if (++stage == TC_STAGES) stage = 0, phase ^= 1u;
+                }
+                if (ok) mma_commit(smem_u32(&acc_full[buf]));
+            }
+            // every MMA this thread issued has finished before tensor memory is released
+            mma_commit(smem_u32(&drain));
+            if (!mbar_drain(smem_u32(&drain), 0)) atomicExch(a.err, 5);
+        }
+    } else {
+        // ---- epilogue: TMEM -> registers -> scaled partial sums ----
+        const int q = warp & 3;  // TMEM lane quadrant this warp may access
+        int ul = 0;
+        for (int u = blockIdx.x; u < a.units; u += gridDim.x, ul++) {
+            const int buf = ul & 1;
+            const uint32_t aphase = (ul >> 1) & 1;
+            if (!mbar_wait(smem_u32(&acc_full[buf]), aphase, ab, a.err, 4)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            uint32_t v[32];
+            const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + buf * 32;
+            tmem_ld16(taddr, v);
+            if (R == 16) tmem_ld16(taddr + 16, v + 16);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&acc_empty[buf]));
+            const int seg = u / a.mt, m = u % a.mt;
+            const int row = m * TC_BM + q * 32 + lane;
+            if (row < a.nrow) {
+                const float sc = a.scale[(size_t)seg * a.nrow + row];
+                if (R == 1) {
+                    a.partial[(size_t)seg * a.nrow + row] = (__uint_as_float(v[0]) + __uint_as_float(v[1])) * sc;
+                } else {
+                    float4 *dst = reinterpret_cast<float4 *>(a.partial + ((size_t)seg * a.nrow + row) * 16);
+#pragma unroll
+                    for (int j = 0; j < 16; j += 4) {
+                        float s[4];
+#pragma unroll
+                        for (int c = 0; c < 4; c++) s[c] = (__uint_as_float(v[j + c]) + __uint_as_float(v[16 + j + c])) * sc;
+                        dst[j / 4] = make_float4(s[0], s[1], s[2], s[3]);
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
+    }
+}
+
+// b[row][r] = sum over segments of the partials (FP64, fixed order) + sum_i B_{i+1} a_slot
+// (thread 0 also mirrors the device error word into pinned host memory for the host to poll)
+__global__ void hist_tc_finish_kernel(const float *__restrict__ partial, int nseg, const double *__restrict__ Bw,
+                                      const double *__restrict__ A, int used, int head, int K, int nrow, int R,
+                                      double *__restrict__ out, const int *__restrict__ err, int *err_mirror) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e == 0 && err_mirror) *(volatile int *)err_mirror = *(volatile const int *)err;
+    if (e >= nrow * R) return;
+    const int row = e / R, j = e % R;
+    double s = 0.0;
+    for (int g = 0; g < nseg; g++) s += partial[(size_t)g * nrow * R + e];
+    if (Bw) {
+        for (int i = 0; i < used; i++) {
+            const int slot = (head - 1 - i + 2 * K) % K;
+            const double *b = Bw + ((size_t)i * nrow + row) * 6;
+            const double *x = A + (size_t)slot * 6 * R;
+            for (int c = 0; c < 6; c++) s += b[c] * x[c * R + j];
+        }
+    }
+    out[e] = s;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// BF16 tensor map of `rank` dimensions (dims innermost first, byte strides of dims 1.., box extents),
+// 128-byte swizzle, zero fill out of bounds
+int make_map(CUtensorMap *map, const void *base, int rank, const uint64_t *dims, const uint64_t *strides,
+             const uint32_t *box) {
+    auto fn = encode_fn();
+    if (!fn) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return SOD_ERR_CUDA;
+    }
+    cuuint64_t d[3], st[2];
+    cuuint32_t bx[3], estr[3] = {1, 1, 1};
+    for (int r = 0; r < rank; r++) d[r] = dims[r], bx[r] = box[r];
+    for (int r = 0; r + 1 < rank; r++) st[r] = strides[r];
+    const CUresult res = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, const_cast<void *>(base), d, st, bx,
+                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (res != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)res) + ")");
+        return SOD_ERR_CUDA;
+    }
+    return SOD_OK;
+}
+
+}  // namespace
+
+// FP32 scratch the convolution needs: per-segment partials [2K][nrow][R]
+size_t history_tc_partial_floats(int K, int nrow, int R) { return (size_t)2 * K * nrow * R; }
+
+// Tensor maps of a BF16 bank.  W: [K][2][nrow][ldw] BF16, mapped as {ncol, nrow, 2K} with 128 x 64
+// boxes; Xt: BF16 history, [K][2][hi|lo][16][ldw] for R = 16 and [K][2][16][ldw] (rows hi, lo, then
+// zeros) for R = 1, mapped as {ncol, 2K * N} with N x 64 boxes.
+int history_tc_plan(HistTcPlan *plan, const void *W, const void *Xt, int nrow, int ncol, int ldw, int K, int R) {
+    SOD_REQUIRE(ldw % 8 == 0, "tensor-core history: row pitch must be a multiple of 16 bytes");
+    SOD_REQUIRE(R == 1 || R == 16, "tensor-core history: 1 or 16 right-hand sides");
+    static_assert(sizeof(CUtensorMap) == sizeof(plan->wmap), "CUtensorMap size");
+    const int n = R == 16 ? tc_n<16>() : tc_n<1>();
+    const uint64_t wdims[3] = {(uint64_t)ncol, (uint64_t)nrow, (uint64_t)K * 2};
+    const uint64_t wstr[2] = {(uint64_t)ldw * 2, (uint64_t)nrow * ldw * 2};
+    const uint32_t wbox[3] = {TC_BK, TC_BM, 1};
+    SOD_TRY(make_map(reinterpret_cast<CUtensorMap *>(plan->wmap), W, 3, wdims, wstr, wbox));
+    const uint64_t xdims[2] = {(uint64_t)ncol, (uint64_t)K * 2 * n};
+    const uint64_t xstr[1] = {(uint64_t)ldw * 2};
+    const uint32_t xbox[2] = {TC_BK, (uint32_t)n};
+    SOD_TRY(make_map(reinterpret_cast<CUtensorMap *>(plan->xmap), Xt, 2, xdims, xstr, xbox));
+    plan->nrow = nrow, plan->ncol = ncol, plan->ldw = ldw, plan->K = K, plan->R = R;
+    plan->W = W, plan->Xt = Xt;
+    static std::once_flag attr_once;
+    static int attr_rc = SOD_OK;
+    std::call_once(attr_once, [] {
+        const int s16 = TC_STAGES * tc_stage_bytes<16>() + 1024, s1 = TC_STAGES * tc_stage_bytes<1>() + 1024;
+        if (cudaFuncSetAttribute(hist_tc_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, s16) != cudaSuccess ||
+            cudaFuncSetAttribute(hist_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1) != cudaSuccess)
+            attr_rc = SOD_ERR_CUDA;
+    });
+    if (attr_rc != SOD_OK) {
+        set_error("cudaFuncSetAttribute failed for the tensor-core history kernel");
+        return attr_rc;
+    }
+    plan->ready = true;
+    return SOD_OK;
+}
+
+// Convolution of the `used` most recent steps; partial: FP32 scratch of history_tc_partial_floats().
+int launch_history_tc(sod_context *ctx, const HistTcPlan *plan, const float *scale, int used, int head,
+                      float *partial, const double *Bw, const double *A, double *out, int *err, int *err_mirror,
+                      cudaStream_t stream) {
+    SOD_REQUIRE(plan && plan->ready, "tensor-core history: plan not built");
+    const int nrow = plan->nrow, K = plan->K, R = plan->R;
+    const CUtensorMap &wmap = *reinterpret_cast<const CUtensorMap *>(plan->wmap);
+    const CUtensorMap &xmap = *reinterpret_cast<const CUtensorMap *>(plan->xmap);
+    TcArgs a;
+    a.nrow = nrow, a.ncol = plan->ncol, a.used = used, a.head = head, a.K = K;
+    a.mt = (nrow + TC_BM - 1) / TC_BM;
+    a.units = 2 * used * a.mt;
+    a.scale = scale;
+    a.partial = partial;
+    a.err = err;
+    const size_t smem = (size_t)TC_STAGES * (R == 16 ? tc_stage_bytes<16>() : tc_stage_bytes<1>()) + 1024;
+    auto kern = R == 16 ? hist_tc_kernel<16> : hist_tc_kernel<1>;
+    const int grid = std::min(a.units, 2 * ctx->num_sms);
+    if (a.units > 0) {
+        kern<<<grid, TC_THREADS, smem, stream>>>(wmap, xmap, a);
+        SOD_CHECK_CUDA(cudaGetLastError());
+        ctx->count();
+    }
+    const int n = nrow * R;
+    hist_tc_finish_kernel<<<(n + 255) / 256, 256, 0, stream>>>(partial, 2 * used, Bw, A, used, head, K, nrow, R, out,
+                                                               err, err_mirror);
+    SOD_CHECK_CUDA(cudaGetLastError());
+    ctx->count();
+    return SOD_OK;
+}
+
+}  // namespace sod

@@ -3,7 +3,9 @@ src/elastodynamics_cqbem_object.cpp:44-48.
 
 Tolerances (relative Frobenius norm of b):
   FP32 weights : <= 2e-6 (FP32 rounding of weights and history vectors);
-  BF16 weights : <= 4e-3 (8-bit significand of the weights; per-row power-of-two scales)."""
+  BF16 weights : <= 4e-3 (8-bit significand of the weights; per-row power-of-two scales);
+  BF16, tensor cores against CUDA cores on the same bank: <= 3e-5 (the tensor-core path carries the
+  history as two BF16 terms, a 16-bit significand, and accumulates in FP32 in another order)."""
 import numpy as np
 import pytest
 
@@ -22,7 +24,7 @@ def decaying_bank(rng, K, n, m):
     return G, H
 
 
-def run(gpu_ctx, oracle, n, m, K, R, wdt, nsteps, with_b, seed=0):
+def run(gpu_ctx, oracle, n, m, K, R, wdt, nsteps, with_b, seed=0, engine=0):
     from surfaceonlydeformables_gb300 import _lib as L
     from surfaceonlydeformables_gb300 import api
 
@@ -30,6 +32,7 @@ def run(gpu_ctx, oracle, n, m, K, R, wdt, nsteps, with_b, seed=0):
     G, H = decaying_bank(rng, K, n, m)
     B = rng.normal(size=(K + 1, n, 6)) * 1e-3 if with_b else None
     bank = api.HistoryBank(gpu_ctx, n, m, K, R, wdt)
+    bank.set_engine(engine)
     for k in range(1, K + 1):
         bank.set_weights(k, G[k], H[k])
         if with_b:
@@ -69,6 +72,41 @@ def test_history_bf16(gpu_ctx, oracle, R):
     got, ref, bank = run(gpu_ctx, oracle, 126, 130, 8, R, L.BF16, 9, with_b=False, seed=3)
     assert rel_fro(got, ref) <= 4e-3
     assert bank.weight_bytes == 8 * 2 * 126 * 136 * 2 + 8 * 2 * 126 * 4
+
+
+@pytest.mark.parametrize("R", [1, 16])
+@pytest.mark.parametrize("n,m,K,nsteps", [(126, 130, 8, 9), (300, 200, 4, 2), (1926, 1926, 24, 30)])
+def test_history_bf16_tensor_cores(gpu_ctx, oracle, n, m, K, nsteps, R):
+    """tcgen05 path: row counts that are not a multiple of the 128-row tile, column counts that are
+    not a multiple of the 64-column K tile, a partly filled and a wrapped ring, the B term."""
+    from surfaceonlydeformables_gb300 import _lib as L
+
+    tc, ref, bank = run(gpu_ctx, oracle, n, m, K, R, L.BF16, nsteps, with_b=True, seed=7,
+                        engine=L.HISTORY_ENGINE_TENSOR_CORES)
+    cc, _, _ = run(gpu_ctx, oracle, n, m, K, R, L.BF16, nsteps, with_b=True, seed=7,
+                   engine=L.HISTORY_ENGINE_CUDA_CORES)
+    assert rel_fro(tc, ref) <= 4e-3
+    assert rel_fro(tc, cc) <= 3e-5
+    again = bank.convolve()
+    assert np.array_equal(tc.view(np.uint8), again.view(np.uint8))  # bitwise reproducible
+
+
+def test_history_engine_selection(gpu_ctx):
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    f32 = api.HistoryBank(gpu_ctx, 10, 10, 2, 16, L.F32)
+    with pytest.raises(L.SodError) as e:
+        f32.set_engine(L.HISTORY_ENGINE_TENSOR_CORES)
+    assert e.value.code == L.SOD_ERR_UNSUPPORTED
+    bf = api.HistoryBank(gpu_ctx, 10, 10, 2, 16, L.BF16)
+    bf.set_weights(1, np.eye(10), np.zeros((10, 10)))
+    bf.push(np.ones((10, 16)), np.zeros((10, 16)))
+    assert np.allclose(bf.convolve(), 1.0)
+    bf.set_engine(L.HISTORY_ENGINE_CUDA_CORES)  # the ring is emptied
+    assert np.all(bf.convolve() == 0.0)
+    with pytest.raises(L.SodError):
+        bf.set_engine(7)
 
 
 def test_history_larger_object(gpu_ctx, oracle):
