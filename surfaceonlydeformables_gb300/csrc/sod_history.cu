@@ -302,7 +302,7 @@ int sod_history_create(sod_context *ctx, int nrow, int ncol, int K, int R, int w
     if (h->tensor_ok()) {
         SOD_TRY(h->Xt.ensure(sizeof(__nv_bfloat16) * (size_t)K * 2 * h->xt_rows() * h->ldw));
         SOD_CHECK_CUDA(cudaMemsetAsync(h->Xt.p, 0, h->Xt.bytes, ctx->stream));
-        SOD_TRY(h->tcpart.ensure(sizeof(float) * history_tc_partial_floats(K, nrow, R)));
+        SOD_TRY(h->tcpart.ensure(sizeof(float) * history_tc_partial_floats(ctx->num_sms, nrow, R)));
         SOD_TRY(h->derr.ensure(sizeof(int)));
         SOD_CHECK_CUDA(cudaMemsetAsync(h->derr.p, 0, sizeof(int), ctx->stream));
         if (cudaMallocHost(&h->err_host, sizeof(int)) != cudaSuccess) {

@@ -16,11 +16,13 @@
 //     N = 16 operand (rows 2-15 zero) and adds columns 0 and 1.  Two accumulators in TMEM alternate
 //     between units;
 //   * four epilogue warps read the accumulator with tcgen05.ld (32 lanes each), apply the
-//     segment's row scale and store per-segment partial sums; a second kernel adds the segments in
-//     FP64 in fixed order (deterministic).
-// Work units are (segment, 128-row tile) in segment-major order, dealt round-robin to a grid of
-// 2 CTAs per SM: at any time the grid works on one or two segments, whose history tiles stay in L2
-// while the weights stream past.
+//     segment's row scale and add it to the CTA's running FP32 sum for its row tile.
+// The grid is a multiple of the row-tile count, G = k * mt (k = floor(2 SMs / mt), at most the
+// segment count): CTA b keeps row tile m = b % mt and takes segments c, c + k, c + 2k, ...
+// (c = b / mt), so it stores one partial tile at the end, and at any time the whole grid works on
+// k neighbouring segments, whose history tiles stay in L2 while the weights stream past.  A second
+// kernel adds a row tile's k partials in FP64 in fixed order (deterministic).  Banks with more row
+// tiles than 2 CTAs per SM (nrow > 2 SMs x 128) run with k = 1 in several waves.
 // Every mbarrier wait is bounded (about one second of clock); a timeout sets an error flag that the
 // host reports, and the kernel lets its copies and MMAs in flight finish (again bounded) and
 // releases its tensor memory before returning.
@@ -131,9 +133,9 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 }
 
 struct TcArgs {
-    int nrow, ncol, used, head, K, mt, units;
+    int nrow, ncol, used, head, K, mt, nseg, k;
     const float *scale;  // [2K][nrow] (matrix = 2 i + t)
-    float *partial;      // [2 used][nrow][R]
+    float *partial;      // [G = k mt][128][R]
     int *err;
 };
 
@@ -172,6 +174,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
     const uint32_t tmem = tmem_base;
     const int KT = (a.ncol + TC_BK - 1) / TC_BK;
     volatile int *ab = &abort_flag;
+    const int m = blockIdx.x % a.mt, seg0 = blockIdx.x / a.mt;  // this CTA's row tile and first segment
 
     if (warp == 0) {
         // ---- producer: TMA loads of weight and history tiles ----
@@ -181,8 +184,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
             bool ok = true;
             int issued[TC_STAGES];  // phase parity of the last load into each stage, -1 = none
             for (int s = 0; s < TC_STAGES; s++) issued[s] = -1;
-            for (int u = blockIdx.x; u < a.units && ok; u += gridDim.x) {
-                const int seg = u / a.mt, m = u % a.mt;
+            for (int seg = seg0; seg < a.nseg && ok; seg += a.k) {
                 const int i = seg >> 1, t = seg & 1;
                 const int slot = (a.head - 1 - i + 2 * a.K) % a.K;
                 for (int kt = 0; kt < KT && ok; kt++) {
@@ -208,7 +210,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
             uint32_t phase = 0;
             bool ok = true;
             int ul = 0;
-            for (int u = blockIdx.x; u < a.units && ok; u += gridDim.x, ul++) {
+            for (int seg = seg0; seg < a.nseg && ok; seg += a.k, ul++) {
                 const int buf = ul & 1;
                 const uint32_t aphase = (ul >> 1) & 1;
                 ok = mbar_wait(smem_u32(&acc_empty[buf]), aphase ^ 1u, ab, a.err, 2);
@@ -233,10 +235,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
             if (!mbar_drain(smem_u32(&drain), 0)) atomicExch(a.err, 5);
         }
     } else {
-        // ---- epilogue: TMEM -> registers -> scaled partial sums ----
+        // ---- epilogue: TMEM -> registers -> scaled sum over the CTA's segments ----
         const int q = warp & 3;  // TMEM lane quadrant this warp may access
+        const int row = m * TC_BM + q * 32 + lane;
+        float acc[R];
+#pragma unroll
+        for (int j = 0; j < R; j++) acc[j] = 0.f;
         int ul = 0;
-        for (int u = blockIdx.x; u < a.units; u += gridDim.x, ul++) {
+        for (int seg = seg0; seg < a.nseg; seg += a.k, ul++) {
             const int buf = ul & 1;
             const uint32_t aphase = (ul >> 1) & 1;
             if (!mbar_wait(smem_u32(&acc_full[buf]), aphase, ab, a.err, 4)) break;
@@ -249,23 +255,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
             asm volatile("tcgen05.fence::before_thread_sync;");
             __syncwarp();
             if (lane == 0) mbar_arrive(smem_u32(&acc_empty[buf]));
-            const int seg = u / a.mt, m = u % a.mt;
-            const int row = m * TC_BM + q * 32 + lane;
-            if (row < a.nrow) {
-                const float sc = a.scale[(size_t)seg * a.nrow + row];
-                if (R == 1) {
-                    a.partial[(size_t)seg * a.nrow + row] = (__uint_as_float(v[0]) + __uint_as_float(v[1])) * sc;
-                } else {
-                    float4 *dst = reinterpret_cast<float4 *>(a.partial + ((size_t)seg * a.nrow + row) * 16);
+            const float sc = row < a.nrow ? a.scale[(size_t)seg * a.nrow + row] : 0.f;  // a power of two
+            if (R == 1) {
+                acc[0] = fmaf(__uint_as_float(v[0]) + __uint_as_float(v[1]), sc, acc[0]);
+            } else {
 #pragma unroll
-                    for (int j = 0; j < 16; j += 4) {
-                        float s[4];
-#pragma unroll
-                        for (int c = 0; c < 4; c++) s[c] = (__uint_as_float(v[j + c]) + __uint_as_float(v[16 + j + c])) * sc;
-                        dst[j / 4] = make_float4(s[0], s[1], s[2], s[3]);
-                    }
-                }
+                for (int j = 0; j < R; j++) acc[j] = fmaf(__uint_as_float(v[j]) + __uint_as_float(v[16 + j]), sc, acc[j]);
             }
+        }
+        float *dst = a.partial + ((size_t)blockIdx.x * TC_BM + q * 32 + lane) * R;
+        if (R == 1) {
+            dst[0] = acc[0];
+        } else {
+#pragma unroll
+            for (int j = 0; j < R; j += 4)
+                *reinterpret_cast<float4 *>(dst + j) = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -276,17 +280,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
     }
 }
 
-// b[row][r] = sum over segments of the partials (FP64, fixed order) + sum_i B_{i+1} a_slot
+// b[row][r] = sum of the row tile's k partials (FP64, fixed order) + sum_i B_{i+1} a_slot
 // (thread 0 also mirrors the device error word into pinned host memory for the host to poll)
-__global__ void hist_tc_finish_kernel(const float *__restrict__ partial, int nseg, const double *__restrict__ Bw,
+__global__ void hist_tc_finish_kernel(const float *__restrict__ partial, int k, int mt, const double *__restrict__ Bw,
                                       const double *__restrict__ A, int used, int head, int K, int nrow, int R,
                                       double *__restrict__ out, const int *__restrict__ err, int *err_mirror) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e == 0 && err_mirror) *(volatile int *)err_mirror = *(volatile const int *)err;
     if (e >= nrow * R) return;
     const int row = e / R, j = e % R;
+    const int m = row / TC_BM;
     double s = 0.0;
-    for (int g = 0; g < nseg; g++) s += partial[(size_t)g * nrow * R + e];
+    for (int c = 0; c < k; c++) s += partial[((size_t)(c * mt + m) * TC_BM + row % TC_BM) * R + j];
     if (Bw) {
         for (int i = 0; i < used; i++) {
             const int slot = (head - 1 - i + 2 * K) % K;
@@ -336,8 +341,16 @@ int make_map(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
 
 }  // namespace
 
-// FP32 scratch the convolution needs: per-segment partials [2K][nrow][R]
-size_t history_tc_partial_floats(int K, int nrow, int R) { return (size_t)2 * K * nrow * R; }
+namespace {
+// segment groups per row tile: fill the 2-CTAs-per-SM grid with whole multiples of the row tiles
+int tc_groups(int num_sms, int mt, int nseg) { return std::max(1, std::min(2 * num_sms / mt, nseg)); }
+}  // namespace
+
+// FP32 scratch the convolution needs: partial tiles [G][128][R], G = k * mt <= max(2 SMs, mt)
+size_t history_tc_partial_floats(int num_sms, int nrow, int R) {
+    const int mt = (nrow + TC_BM - 1) / TC_BM;
+    return (size_t)std::max(2 * num_sms, mt) * TC_BM * R;
+}
 
 // Tensor maps of a BF16 bank.  W: [K][2][nrow][ldw] BF16, mapped as {ncol, nrow, 2K} with 128 x 64
 // boxes; Xt: BF16 history, [K][2][hi|lo][16][ldw] for R = 16 and [K][2][16][ldw] (rows hi, lo, then
@@ -384,20 +397,21 @@ int launch_history_tc(sod_context *ctx, const HistTcPlan *plan, const float *sca
     TcArgs a;
     a.nrow = nrow, a.ncol = plan->ncol, a.used = used, a.head = head, a.K = K;
     a.mt = (nrow + TC_BM - 1) / TC_BM;
-    a.units = 2 * used * a.mt;
+    a.nseg = 2 * used;
+    a.k = used > 0 ? tc_groups(ctx->num_sms, a.mt, a.nseg) : 0;
     a.scale = scale;
     a.partial = partial;
     a.err = err;
     const size_t smem = (size_t)TC_STAGES * (R == 16 ? tc_stage_bytes<16>() : tc_stage_bytes<1>()) + 1024;
     auto kern = R == 16 ? hist_tc_kernel<16> : hist_tc_kernel<1>;
-    const int grid = std::min(a.units, 2 * ctx->num_sms);
-    if (a.units > 0) {
+    const int grid = a.k * a.mt;
+    if (grid > 0) {
         kern<<<grid, TC_THREADS, smem, stream>>>(wmap, xmap, a);
         SOD_CHECK_CUDA(cudaGetLastError());
         ctx->count();
     }
     const int n = nrow * R;
-    hist_tc_finish_kernel<<<(n + 255) / 256, 256, 0, stream>>>(partial, 2 * used, Bw, A, used, head, K, nrow, R, out,
+    hist_tc_finish_kernel<<<(n + 255) / 256, 256, 0, stream>>>(partial, a.k, a.mt, Bw, A, used, head, K, nrow, R, out,
                                                                err, err_mirror);
     SOD_CHECK_CUDA(cudaGetLastError());
     ctx->count();

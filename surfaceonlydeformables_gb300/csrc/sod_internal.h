@@ -240,7 +240,7 @@ struct HistTcPlan {
     const void *W = nullptr, *Xt = nullptr;
     bool ready = false;
 };
-size_t history_tc_partial_floats(int K, int nrow, int R);
+size_t history_tc_partial_floats(int num_sms, int nrow, int R);
 int history_tc_plan(HistTcPlan *plan, const void *W, const void *Xt, int nrow, int ncol, int ldw, int K, int R);
 // err: device error word (first expired wait); err_mirror: pinned host word the finish kernel copies it to
 int launch_history_tc(sod_context *ctx, const HistTcPlan *plan, const float *scale, int used, int head,
