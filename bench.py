@@ -70,8 +70,16 @@ def make_single(level: int = 3):
                  order=5, subdiv=1)]
 
 
+def make_single_2f():
+    """The 2562-vertex object of make_single(4) with two of its 17 frequencies (l = 4 and 12): the
+    scatter kernels at full mesh size with ~2 GB of outputs, small enough for an ncu --set full capture."""
+    objs = make_single(4)
+    objs[0]["fsel"] = (4, 12)
+    return objs
+
+
 CASES = {"mixed24": make_workload, "coll642": lambda: make_single(3), "coll2562": lambda: make_single(4),
-         "coll162": lambda: make_single(2)}
+         "coll162": lambda: make_single(2), "coll2562_2f": make_single_2f}
 
 
 def entries(nV: int, nfreq: int) -> int:
@@ -462,6 +470,8 @@ def run_gpu(args):
     freqs = []
     for o in objs:
         s, R, Lq = L.cq_frequencies(o["bdf"], o["dt"], o["N"])
+        if "fsel" in o:
+            s = s[list(o["fsel"])].copy()
         o["s"], o["R"], o["L"] = s, R, Lq
     total_entries = sum(entries(o["mesh"].nV, len(o["s"])) for o in objs)
     # device outputs, complex64, one buffer per (object, kind)
