@@ -243,7 +243,11 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
 }
 
 // Fused G + B variants are limited to 384 threads so that they may use up to 170 registers.
-template <int KIND, int BM> constexpr int scatter_max_threads() { return (KIND == SOD_G && BM) ? 384 : 512; }
+// CTA size bound of the scatter variants.  It also sets the register budget, 65536 / 512 = 128 per
+// thread: measured on the 2562-vertex object, a 384 bound (165 registers, 12 warps per SM) made the
+// G + B pass 18% slower, and a 640 bound (96 registers, with spills) made both passes ~10% slower.
+constexpr int SCATTER_MAX_THREADS = 512;
+template <int KIND, int BM> constexpr int scatter_max_threads() { return SCATTER_MAX_THREADS; }
 
 template <int KIND, int BM>
 __global__ void __launch_bounds__(scatter_max_threads<KIND, BM>(), 1) coll_scatter_kernel(CollArgs a, PointTable pt,
@@ -707,7 +711,7 @@ int autotune_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int bm, in
     SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, scatter_fn(kind, bm, false)));
     double best = 1e300;
     int bestT = 0;
-    for (int T = 32; T <= std::min(512, attr.maxThreadsPerBlock); T += 32) {
+    for (int T = 32; T <= std::min(SCATTER_MAX_THREADS, attr.maxThreadsPerBlock); T += 32) {
         const size_t smem = scatter_smem_bytes(kind, bm, m->nV, T);
         int per_sm = 0;
         SOD_TRY(scatter_occupancy(ctx, kind, bm, false, T, smem, &per_sm));
@@ -768,7 +772,7 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
         if (T <= 0) SOD_TRY(autotune_scatter_threads(ctx, const_cast<sod_mesh *>(m), kd, bm, &T));
         cudaFuncAttributes attr;
         SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, scatter_fn(kd, bm, false)));
-        T = std::max(32, std::min(std::min(512, attr.maxThreadsPerBlock), (T / 32) * 32));
+        T = std::max(32, std::min(std::min(SCATTER_MAX_THREADS, attr.maxThreadsPerBlock), (T / 32) * 32));
         threads[kd] = T;
         SOD_TRY(const_cast<sod_mesh *>(m)->coloured_for(T, &col[kd]));
         smem[kd] = scatter_smem_bytes(kd, bm, m->nV, T);
