@@ -180,6 +180,17 @@ static bool is_device_ptr(const void *p) {
 
 bool is_device_pointer(const void *p) { return is_device_ptr(p); }
 
+// Device address of a page-locked host buffer (cudaHostAlloc / cudaHostRegister, mapped into the
+// device address space), or null for device, managed or pageable memory.
+static void *mapped_host_ptr(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 template <class T> static int upload(DevBuf &b, const std::vector<T> &v) {
     SOD_TRY(b.ensure(sizeof(T) * std::max<size_t>(v.size(), 1)));
     if (!v.empty()) SOD_CHECK_CUDA(cudaMemcpy(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
@@ -508,6 +519,9 @@ static size_t kind_elems(int kind, int nV) {
 }
 
 // Shared driver: validates, stages host outputs through device memory, launches, copies back.
+// Page-locked host outputs of the collocation path skip the staging: its kernels only store to
+// their outputs, so they write the rows straight into host memory over the CPU-GPU link while
+// other rows are still being computed, and the call returns once the stream has drained.
 static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int method, double c1, double c2,
                           double rho, const double *s, int nfreq, int order, int subdiv, int sorder, int ssub,
                           int parts, void *const outs[4], int out_dtype) {
@@ -533,20 +547,24 @@ static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int 
     L.nfreq = nfreq;
     // host outputs are staged in one device buffer, kinds back to back
     bool host_out[4] = {false, false, false, false};
+    void *direct[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t staged = 0, off[4] = {0, 0, 0, 0};
+    bool any_host = false;
     for (int kd = 0; kd < 4; kd++) {
         if (!(mask & (1 << kd))) continue;
-        host_out[kd] = !is_device_ptr(outs[kd]);
-        if (host_out[kd]) {
-            off[kd] = staged;
-            staged += kind_elems(kd, mesh->nV) * nfreq * esz;
-        }
+        if (is_device_ptr(outs[kd])) continue;
+        any_host = true;
+        if (method == SOD_COLLOCATION) direct[kd] = mapped_host_ptr(outs[kd]);
+        if (direct[kd]) continue;
+        host_out[kd] = true;
+        off[kd] = staged;
+        staged += kind_elems(kd, mesh->nV) * nfreq * esz;
     }
     if (staged) SOD_TRY(ctx->staging.ensure(staged));
     for (int kd = 0; kd < 4; kd++) {
         L.freq_stride[kd] = (long long)kind_elems(kd, mesh->nV);
         if (!(mask & (1 << kd))) continue;
-        L.out[kd] = host_out[kd] ? ctx->staging.as<char>() + off[kd] : outs[kd];
+        L.out[kd] = direct[kd] ? direct[kd] : host_out[kd] ? ctx->staging.as<char>() + off[kd] : outs[kd];
     }
     std::vector<KConst<double>> kd(nfreq);
     for (int l = 0; l < nfreq; l++) kd[l] = make_kconst(c1, c2, rho, s[2 * l], s[2 * l + 1]);
@@ -559,7 +577,7 @@ static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int 
     L.out_dtype = out_dtype;
     L.stream = ctx->stream;
     SOD_TRY(method == SOD_GALERKIN ? launch_galerkin(ctx, L) : launch_collocation(ctx, L));
-    if (staged) {
+    if (any_host) {
         for (int kd2 = 0; kd2 < 4; kd2++)
             if (host_out[kd2])
                 SOD_CHECK_CUDA(cudaMemcpyAsync(outs[kd2], L.out[kd2], kind_elems(kd2, mesh->nV) * nfreq * esz,

@@ -206,3 +206,32 @@ def test_assemble_all_matches_per_kind(gpu_ctx, dev_meshes, meshes, oracle, sodl
         assert rel_fro(allk[kind][2], ref) <= 1e-5, kind
     part = api.assemble_all(gpu_ctx, dev_meshes[2], MAT, s, kinds=("G", "B_angular"))
     assert set(part) == {"G", "B_angular"} and rel_fro(part["G"], allk["G"]) < 1e-6
+
+
+@pytest.mark.parametrize("dtype_name", ["C128", "C64"])
+def test_pinned_host_output_written_in_place(gpu_ctx, dev_meshes, freqs, dtype_name):
+    """Page-locked host outputs are written by the kernels directly (no staging copy); the result
+    must be bit-identical to a pageable host buffer and to a device buffer, for every kind and for
+    the multi-frequency call."""
+    import torch
+
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    dt = getattr(L, dtype_name)
+    tdt = torch.complex128 if dt == L.C128 else torch.complex64
+    m = dev_meshes[2]
+    for kind in KINDS:
+        shape = api.out_shape(L.KINDS[kind], m.nV)
+        pageable = api.assemble(gpu_ctx, m, kind, MAT, freqs[1], dtype=dt)
+        pinned = torch.full(shape, complex(np.nan, np.nan), dtype=tdt).pin_memory()
+        api.assemble(gpu_ctx, m, kind, MAT, freqs[1], out=pinned.numpy(), dtype=dt)
+        dev = torch.empty(shape, dtype=tdt, device="cuda")
+        api.assemble(gpu_ctx, m, kind, MAT, freqs[1], out=dev, dtype=dt)
+        torch.cuda.synchronize()
+        assert np.array_equal(pinned.numpy().view(np.uint8), pageable.view(np.uint8)), kind
+        assert np.array_equal(dev.cpu().numpy().view(np.uint8), pageable.view(np.uint8)), kind
+        many = torch.full((len(freqs),) + shape, complex(np.nan, np.nan), dtype=tdt).pin_memory()
+        api.assemble_frequencies(gpu_ctx, m, kind, MAT, freqs, out=many.numpy(), dtype=dt)
+        ref = api.assemble_frequencies(gpu_ctx, m, kind, MAT, freqs, dtype=dt)
+        assert np.array_equal(many.numpy().view(np.uint8), ref.view(np.uint8)), kind
