@@ -83,153 +83,130 @@ __device__ __forceinline__ void gal_store_b(const GalArgs &a, const cd *bsum, in
     }
 }
 
+// Regular pairs, pass 1: one CTA per (test point x, frequency).  Test point t = f1 * nq + ix is point
+// ix of the test rule on test face f1.  The CTA integrates every trial face f2 that shares no vertex
+// with f1 -- the collocation scatter with x as the field point -- into the unweighted row
+//     R(x)[c][b] = sum_f2 int_f2 K_c(x, y) phi_b(y) dy      (c: tensor component, b: trial vertex)
+// in shared memory (colour order, conflict-free, deterministic) and stores it to scratch, with the
+// B_trans / B_angular sums of x when BM != 0.  Each kernel evaluation is done once per point pair.
+struct GalTpArgs {
+    int nV, nq, t0;            // vertices, test points per face, first test point of this launch
+    const float4 *faces;       // trial faces, colour ordered
+    const int *color_off;
+    int ncolors;
+    const float4 *faces_nat;   // test faces, natural order
+    float2 *rows;              // [fq][t - t0][NC][nV]
+    long long rows_fstride;
+    cd *bsum;                  // [fq][t - t0][NCB] (BM != 0)
+    long long b_fstride;
+};
 
-// With BM != 0 (G only) the pass also integrates B_trans / B_angular from the same radial terms;
-// per-thread B columns live after the row accumulator: [NC_B][blockDim] float2.
-template <int KIND, int BM> constexpr int gal_max_threads() { return (KIND == SOD_G && BM) ? 384 : 512; }
+template <int KIND, int BM> constexpr int gal_max_threads() { return 512; }
 
 template <int KIND, int BM>
-__global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_scatter_kernel(GalArgs a, PointTable pt,
-                                                                                     const __grid_constant__ FreqTable ft) {
+__global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_tp_kernel(GalTpArgs a, PointTable pt,
+                                                                                const __grid_constant__ FreqTable ft) {
     constexpr int NC = KIND == SOD_G ? 6 : 9;
     using BMo = BMom<KIND == SOD_G ? BM : 0>;
     constexpr int NCB = BMo::NC;
     extern __shared__ float2 acc[];  // [NC][nV], then [NCB][blockDim]
-    __shared__ float4 tp[GAL_MAXS * GAL_MAXQ];
-    __shared__ int tv[GAL_MAXS][3];
-    const int i = blockIdx.x, fq = blockIdx.y, nV = a.nV;
+    const int tl = blockIdx.x, t = a.t0 + tl, fq = blockIdx.y, nV = a.nV;
     const KConst<float> k = ft.kf[fq];
-    const int s0 = a.star_off[i], ns = min(a.star_off[i + 1] - s0, GAL_MAXS);
-    const int nq = min(pt.n, GAL_MAXQ);
-    for (int t = threadIdx.x; t < ns * nq; t += blockDim.x) {
-        const int s = t / nq, q = t % nq;
-        const FaceRec fr = load_face(a.faces_nat, a.star_face[s0 + s]);
-        const int sc = a.star_corner[s0 + s];
-        const float4 P = pt.p[q];
-        const float Lsc = sc == 0 ? P.x : sc == 1 ? P.y : P.z;
-        tp[t] = make_float4(P.x * fr.y1.x + P.y * fr.y2.x + P.z * fr.y3.x, P.x * fr.y1.y + P.y * fr.y2.y + P.z * fr.y3.y,
-                            P.x * fr.y1.z + P.y * fr.y2.z + P.z * fr.y3.z, P.w * fr.area * Lsc);
-    }
-    for (int s = threadIdx.x; s < ns; s += blockDim.x) {
-        const FaceRec fr = load_face(a.faces_nat, a.star_face[s0 + s]);
-        tv[s][0] = fr.j0, tv[s][1] = fr.j1, tv[s][2] = fr.j2;
-    }
-    for (int t = threadIdx.x; t < NC * nV; t += blockDim.x) acc[t] = make_float2(0.f, 0.f);
+    const int f1 = t / a.nq, ix = t - f1 * a.nq;
+    const FaceRec tf = load_face(a.faces_nat, f1);
+    const float4 PX = pt.p[ix];
+    const float3 x = make_float3(PX.x * tf.y1.x + PX.y * tf.y2.x + PX.z * tf.y3.x,
+                                 PX.x * tf.y1.y + PX.y * tf.y2.y + PX.z * tf.y3.y,
+                                 PX.x * tf.y1.z + PX.y * tf.y2.z + PX.z * tf.y3.z);
+    for (int e = threadIdx.x; e < NC * nV; e += blockDim.x) acc[e] = make_float2(0.f, 0.f);
     float2 *accB = acc + NC * nV;
 #pragma unroll
     for (int c = 0; c < NCB; c++) accB[c * blockDim.x + threadIdx.x] = make_float2(0.f, 0.f);
     __syncthreads();
-    if (a.do_regular) {
-        for (int c = 0; c < a.ncolors; c++) {
-            const int fend = a.color_off[c + 1];
-            for (int f = a.color_off[c] + threadIdx.x; f < fend; f += blockDim.x) {
-                const FaceRec fr = load_face(a.faces, f);
-                const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
-                BMo bm;
-                if (NCB) bm.zero();
-                cf part[3][NC];
+    for (int c = 0; c < a.ncolors; c++) {
+        const int fend = a.color_off[c + 1];
+        for (int f = a.color_off[c] + threadIdx.x; f < fend; f += blockDim.x) {
+            const FaceRec fr = load_face(a.faces, f);
+            const bool touch = fr.j0 == tf.j0 || fr.j0 == tf.j1 || fr.j0 == tf.j2 || fr.j1 == tf.j0 || fr.j1 == tf.j1 ||
+                               fr.j1 == tf.j2 || fr.j2 == tf.j0 || fr.j2 == tf.j1 || fr.j2 == tf.j2;
+            if (touch) continue;  // singular pair (coincident, edge- or vertex-adjacent)
+            const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
+            cf part[3][NC];
 #pragma unroll
-                for (int kk = 0; kk < 3; kk++)
+            for (int kk = 0; kk < 3; kk++)
 #pragma unroll
-                    for (int cc = 0; cc < NC; cc++) part[kk][cc] = mk(0.f, 0.f);
-                for (int s = 0; s < ns; s++) {
-                    bool shared = false;
+                for (int cc = 0; cc < NC; cc++) part[kk][cc] = mk(0.f, 0.f);
+            BMo bm;
+            if (NCB) bm.zero();
+            for (int q = 0; q < pt.n; q++) {
+                const float4 P = pt.p[q];
+                const float dx = P.x * fr.y1.x + P.y * fr.y2.x + P.z * fr.y3.x - x.x;
+                const float dy = P.x * fr.y1.y + P.y * fr.y2.y + P.z * fr.y3.y - x.y;
+                const float dz = P.x * fr.y1.z + P.y * fr.y2.z + P.z * fr.y3.z - x.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                const float rinv = rsqrtf(r2);
+                const float r = r2 * rinv;
+                const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
+                const RadialTerms<float, cf> rt = radial<float, cf>(r, k);
+                cf u[NC];
+                if (KIND == SOD_G) {
+                    cf al, be;
+                    g_coeffs(rt, k, rinv, al, be);
 #pragma unroll
-                    for (int u = 0; u < 3; u++) shared = shared || tv[s][u] == fr.j0 || tv[s][u] == fr.j1 || tv[s][u] == fr.j2;
-                    if (shared) continue;  // singular pair
-                    for (int ix = 0; ix < nq; ix++) {
-                        const float4 X = tp[s * nq + ix];
-                        for (int q = 0; q < pt.n; q++) {
-                            const float4 P = pt.p[q];
-                            const float dx = P.x * fr.y1.x + P.y * fr.y2.x + P.z * fr.y3.x - X.x;
-                            const float dy = P.x * fr.y1.y + P.y * fr.y2.y + P.z * fr.y3.y - X.y;
-                            const float dz = P.x * fr.y1.z + P.y * fr.y2.z + P.z * fr.y3.z - X.z;
-                            const float r2 = dx * dx + dy * dy + dz * dz;
-                            const float rinv = rsqrtf(r2);
-                            const float r = r2 * rinv;
-                            const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                            const RadialTerms<float, cf> t = radial<float, cf>(r, k);
-                            cf u[NC];
-                            if (KIND == SOD_G) {
-                                cf al, be;
-                                g_coeffs(t, k, rinv, al, be);
+                    for (int p = 0; p < 3; p++)
 #pragma unroll
-                                for (int p = 0; p < 3; p++)
-#pragma unroll
-                                    for (int qq = p; qq < 3; qq++) {
-                                        cf v = al * (rh[p] * rh[qq]);
-                                        if (p == qq) v = v + be;
-                                        u[sym_index(p, qq)] = v;
-                                    }
-                            } else {
-                                cf ha, hb, hd;
-                                h_coeffs(t, k, rinv * rinv, ha, hb, hd);
-                                const float rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
-                                const cf hdr = hd * rn, hbr = hb * rn;
-#pragma unroll
-                                for (int p = 0; p < 3; p++)
-#pragma unroll
-                                    for (int qq = 0; qq < 3; qq++) {
-                                        cf v = ha * (rh[p] * nn[qq]) + hb * (nn[p] * rh[qq]) + hdr * (rh[p] * rh[qq]);
-                                        if (p == qq) v = v + hbr;
-                                        u[3 * p + qq] = v;
-                                    }
-                            }
-                            const float w = P.w * fr.area * X.w;
-                            const float wl[3] = {w * P.x, w * P.y, w * P.z};
-#pragma unroll
-                            for (int kk = 0; kk < 3; kk++)
-#pragma unroll
-                                for (int cc = 0; cc < NC; cc++) cfma(part[kk][cc], u[cc], wl[kk]);
-                            if (NCB) bm.add(t, k, r, rh, nn, P.w * X.w);
+                        for (int qq = p; qq < 3; qq++) {
+                            cf v = al * (rh[p] * rh[qq]);
+                            if (p == qq) v = v + be;
+                            u[sym_index(p, qq)] = v;
                         }
-                    }
+                } else {
+                    cf ha, hb, hd;
+                    h_coeffs(rt, k, rinv * rinv, ha, hb, hd);
+                    const float rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
+                    const cf hdr = hd * rn, hbr = hb * rn;
+#pragma unroll
+                    for (int p = 0; p < 3; p++)
+#pragma unroll
+                        for (int qq = 0; qq < 3; qq++) {
+                            cf v = ha * (rh[p] * nn[qq]) + hb * (nn[p] * rh[qq]) + hdr * (rh[p] * rh[qq]);
+                            if (p == qq) v = v + hbr;
+                            u[3 * p + qq] = v;
+                        }
                 }
-                const int jj[3] = {fr.j0, fr.j1, fr.j2};
+                const float w = P.w * fr.area;
+                const float wl[3] = {w * P.x, w * P.y, w * P.z};
 #pragma unroll
                 for (int kk = 0; kk < 3; kk++)
 #pragma unroll
-                    for (int cc = 0; cc < NC; cc++) {
-                        float2 &sacc = acc[cc * nV + jj[kk]];
-                        sacc.x += part[kk][cc].x;
-                        sacc.y += part[kk][cc].y;
-                    }
-                if (NCB) {
-                    float2 *col = accB + threadIdx.x;
-                    bm.emit(nn, fr.area, [&](int cc, cf v) {
-                        float2 &sb = col[cc * blockDim.x];
-                        sb.x += v.x;
-                        sb.y += v.y;
-                    });
-                }
+                    for (int cc = 0; cc < NC; cc++) cfma(part[kk][cc], u[cc], wl[kk]);
+                if (NCB) bm.add(rt, k, r, rh, nn, P.w);
             }
-            __syncthreads();
+            const int jj[3] = {fr.j0, fr.j1, fr.j2};
+#pragma unroll
+            for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+                for (int cc = 0; cc < NC; cc++) {
+                    float2 &sacc = acc[cc * nV + jj[kk]];
+                    sacc.x += part[kk][cc].x;
+                    sacc.y += part[kk][cc].y;
+                }
+            if (NCB) {
+                float2 *col = accB + threadIdx.x;
+                bm.emit(nn, fr.area, [&](int cc, cf v) {
+                    float2 &sb = col[cc * blockDim.x];
+                    sb.x += v.x;
+                    sb.y += v.y;
+                });
+            }
         }
-    }
-    // epilogue: row block 3 x 3nV, singular slot blocks added in FP64
-    const long long ld = 3LL * nV;
-    const long long base = (long long)fq * a.fstride + (long long)(3 * i) * ld;
-    for (int p = 0; p < 3 && a.out; p++)
-        for (int col = threadIdx.x; col < 3 * nV; col += blockDim.x) {
-            const int j = col / 3, qq = col - 3 * j;
-            const float2 v = acc[(KIND == SOD_G ? sym_index(p, qq) : 3 * p + qq) * nV + j];
-            store_o(a.out, a.out_c64, base + p * ld + col, v.x, v.y);
-        }
-    if (a.S && a.out) {
         __syncthreads();
-        const int b0 = a.slot_off[i], nb = a.slot_off[i + 1] - b0;
-        for (int e = threadIdx.x; e < nb * 9; e += blockDim.x) {
-            const int sl = b0 + e / 9, pq = e % 9, p = pq / 3, qq = pq % 3;
-            const int j = a.slot_vert[sl];
-            const float2 v = acc[(KIND == SOD_G ? sym_index(p, qq) : pq) * nV + j];
-            const cd sv = a.S[(long long)fq * a.S_fstride + (long long)sl * 9 + pq];
-            store_o(a.out, a.out_c64, base + p * ld + 3 * j + qq, (double)v.x + sv.x, (double)v.y + sv.y);
-        }
     }
+    // the row, unweighted, to scratch (coalesced)
+    float2 *dst = a.rows + (long long)fq * a.rows_fstride + (long long)tl * NC * nV;
+    for (int e = threadIdx.x; e < NC * nV; e += blockDim.x) dst[e] = acc[e];
     if (NCB) {
         // per-thread B columns -> FP64 sums, 32 lanes per component in a fixed xor tree
-        __shared__ cd bsum[24];
-        __syncthreads();
         const int T = blockDim.x;
         for (int p = threadIdx.x; p < NCB * 32; p += T) {
             const int cc = p >> 5, l = p & 31;
@@ -244,10 +221,108 @@ __global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_scatter_ke
                 sx += __shfl_xor_sync(0xffffffffu, sx, o);
                 sy += __shfl_xor_sync(0xffffffffu, sy, o);
             }
-            if (l == 0) bsum[cc] = mk(sx, sy);
+            if (l == 0) a.bsum[(long long)fq * a.b_fstride + (long long)tl * NCB + cc] = mk(sx, sy);
+        }
+    }
+}
+
+// Regular pairs, pass 2: one CTA per (test vertex a, frequency) combines the rows of the test points
+// on the faces around a, U[a] = sum_x phi_a(x) w_x area(f1) R(x), in fixed order (star face, then
+// test point) with compensated FP32 sums (TwoSum, error ~ 1 ulp of the result: FP64 arithmetic runs
+// at a small fraction of the FP32 rate here), and adds the singular blocks of a's two-ring slots
+// (FP64) and the singular B parts.
+struct Comp2 {  // compensated FP32 complex sum
+    float sx = 0.f, cx = 0.f, sy = 0.f, cy = 0.f;
+    __device__ __forceinline__ static void add1(float &s, float &c, float p) {
+        const float t = s + p, bp = t - s;
+        c += (s - (t - bp)) + (p - bp);
+        s = t;
+    }
+    __device__ __forceinline__ void add(float w, float2 v) {
+        add1(sx, cx, w * v.x);
+        add1(sy, cy, w * v.y);
+    }
+    __device__ __forceinline__ cd value() const { return mk((double)sx + (double)cx, (double)sy + (double)cy); }
+};
+struct GalGatherArgs {
+    GalArgs g;                 // outputs, singular blocks and slots
+    int nq, do_regular;
+    const float2 *rows;        // [fq][t][NC][nV] (all test points of the mesh)
+    long long rows_fstride;
+    const cd *bsum;            // [fq][t][NCB]
+    long long b_fstride;
+};
+
+template <int KIND, int BM>
+__global__ void __launch_bounds__(256) gal_gather_kernel(GalGatherArgs ga, PointTable pt) {
+    constexpr int NC = KIND == SOD_G ? 6 : 9;
+    using BMo = BMom<KIND == SOD_G ? BM : 0>;
+    constexpr int NCB = BMo::NC;
+    const GalArgs &a = ga.g;
+    __shared__ float wt[GAL_MAXS * GAL_MAXQ];
+    __shared__ int tt[GAL_MAXS * GAL_MAXQ];
+    __shared__ cd bs[24];
+    const int i = blockIdx.x, fq = blockIdx.y, nV = a.nV, nq = ga.nq;
+    const int s0 = a.star_off[i], ns = min(a.star_off[i + 1] - s0, GAL_MAXS);
+    const int np = ns * nq;
+    for (int e = threadIdx.x; e < np; e += blockDim.x) {
+        const int s = e / nq, q = e - s * nq;
+        const int f1 = a.star_face[s0 + s], sc = a.star_corner[s0 + s];
+        const FaceRec fr = load_face(a.faces_nat, f1);
+        const float4 P = pt.p[q];
+        const float L = sc == 0 ? P.x : sc == 1 ? P.y : P.z;
+        wt[e] = P.w * fr.area * L;
+        tt[e] = f1 * nq + q;
+    }
+    __syncthreads();
+    const float2 *R = ga.rows + (long long)fq * ga.rows_fstride;
+    auto row_sum = [&](int c, int j) {
+        Comp2 acc;
+        if (ga.do_regular)
+#pragma unroll 4
+            for (int e = 0; e < np; e++) acc.add(wt[e], __ldg(R + ((long long)tt[e] * NC + c) * nV + j));
+        return acc.value();
+    };
+    const long long ld = 3LL * nV;
+    const long long base = (long long)fq * a.fstride + (long long)(3 * i) * ld;
+    if (a.out) {
+        // one thread per (component, trial vertex): coalesced reads of the rows
+        for (int e = threadIdx.x; e < NC * nV; e += blockDim.x) {
+            const int c = e / nV, j = e - c * nV;
+            const cd v = row_sum(c, j);
+            if (KIND == SOD_G) {
+                const int p = c < 3 ? 0 : (c < 5 ? 1 : 2), qq = c < 3 ? c : (c < 5 ? c - 2 : 2);
+                store_o(a.out, a.out_c64, base + p * ld + 3 * j + qq, v.x, v.y);
+                if (p != qq) store_o(a.out, a.out_c64, base + qq * ld + 3 * j + p, v.x, v.y);
+            } else {
+                store_o(a.out, a.out_c64, base + (c / 3) * ld + 3 * j + c % 3, v.x, v.y);
+            }
+        }
+        if (a.S) {
+            __syncthreads();
+            const int b0 = a.slot_off[i], nb = a.slot_off[i + 1] - b0;
+            for (int e = threadIdx.x; e < nb * 9; e += blockDim.x) {
+                const int sl = b0 + e / 9, pq = e % 9, p = pq / 3, qq = pq % 3;
+                const int j = a.slot_vert[sl];
+                const cd v = row_sum(KIND == SOD_G ? sym_index(p, qq) : pq, j);
+                const cd sv = a.S[(long long)fq * a.S_fstride + (long long)sl * 9 + pq];
+                store_o(a.out, a.out_c64, base + p * ld + 3 * j + qq, v.x + sv.x, v.y + sv.y);
+            }
+        }
+    }
+    if (NCB) {
+        for (int c = threadIdx.x; c < NCB; c += blockDim.x) {
+            double sx = 0.0, sy = 0.0;  // FP64: 24 components per vertex, negligible
+            if (ga.do_regular)
+                for (int e = 0; e < np; e++) {
+                    const cd v = ga.bsum[(long long)fq * ga.b_fstride + (long long)tt[e] * NCB + c];
+                    sx = fma((double)wt[e], v.x, sx);
+                    sy = fma((double)wt[e], v.y, sy);
+                }
+            bs[c] = mk(sx, sy);
         }
         __syncthreads();
-        gal_store_b<BM>(a, bsum, i, fq);
+        gal_store_b<BM>(a, bs, i, fq);
     }
 }
 
@@ -630,17 +705,59 @@ static int build_gal(const sod_mesh *m, sod_mesh::GalData *g) {
 
 namespace sod {
 
-static const void *gal_scatter_fn(int kind, int bm) {
+static const void *gal_tp_fn(int kind, int bm) {
     constexpr int BT = 1 << SOD_B_TRANS, BA = 1 << SOD_B_ANGULAR;
-    if (kind == SOD_H) return (const void *)gal_scatter_kernel<SOD_H, 0>;
-    return bm == (BT | BA) ? (const void *)gal_scatter_kernel<SOD_G, BT | BA>
-         : bm == BT        ? (const void *)gal_scatter_kernel<SOD_G, BT>
-         : bm == BA        ? (const void *)gal_scatter_kernel<SOD_G, BA>
-                           : (const void *)gal_scatter_kernel<SOD_G, 0>;
+    if (kind == SOD_H) return (const void *)gal_tp_kernel<SOD_H, 0>;
+    return bm == (BT | BA) ? (const void *)gal_tp_kernel<SOD_G, BT | BA>
+         : bm == BT        ? (const void *)gal_tp_kernel<SOD_G, BT>
+         : bm == BA        ? (const void *)gal_tp_kernel<SOD_G, BA>
+                           : (const void *)gal_tp_kernel<SOD_G, 0>;
 }
+
+// CTA size of the test-point kernel: the collocation scatter's cost model (colours x T / occupancy,
+// occupancy from the CUDA occupancy calculator), cached on the mesh.
+static int gal_tp_threads(sod_context *ctx, sod_mesh *m, int kind, int bm, const void *fn, int *threads) {
+    const int key = 4096 + kind * 16 + bm;
+    auto it = m->tuned.find(key);
+    if (it != m->tuned.end()) {
+        *threads = it->second;
+        return SOD_OK;
+    }
+    cudaFuncAttributes attr;
+    SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
+    SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(ctx->smem_optin - attr.sharedSizeBytes)));
+    const int nc = kind == SOD_G ? 6 : 9;
+    const int ncb = (bm & (1 << SOD_B_TRANS) ? 6 : 0) + (bm & (1 << SOD_B_ANGULAR) ? 18 : 0);
+    double best = 1e300;
+    int bestT = 0;
+    for (int T = 32; T <= attr.maxThreadsPerBlock; T += 32) {
+        const size_t smem = sizeof(float2) * ((size_t)nc * m->nV + (size_t)ncb * T);
+        if (smem + attr.sharedSizeBytes > ctx->smem_optin) continue;
+        int per_sm = 0;
+        SOD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, T, smem));
+        if (per_sm <= 0) continue;
+        const sod_mesh::Coloured *col = nullptr;
+        SOD_TRY(m->coloured_for(T, &col));
+        const double occ = std::min(1.0, (double)per_sm * T / 32.0 / 24.0);
+        const double cost = (double)col->ncolors * T / occ;
+        if (cost < best * 0.999) best = cost, bestT = T;
+    }
+    if (bestT == 0) {
+        set_error("mesh too large for the shared-memory row accumulator (" + std::to_string(m->nV) + " vertices)");
+        return SOD_ERR_UNSUPPORTED;
+    }
+    m->tuned[key] = bestT;
+    *threads = bestT;
+    return SOD_OK;
+}
+
+// Bytes of test-point row scratch a Galerkin pass may hold at once (frequencies are chunked to fit)
+constexpr size_t GAL_ROWS_BUDGET = (size_t)16 << 30;
 
 int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
     const sod_mesh *m = L.mesh;
+    sod_mesh *mm = const_cast<sod_mesh *>(m);
     const int mask = L.kind_mask;
     constexpr int BT = 1 << SOD_B_TRANS, BA = 1 << SOD_B_ANGULAR;
     const int bm = mask & (BT | BA);
@@ -655,12 +772,14 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
     if (!m->gal) {
         auto gd = std::make_unique<sod_mesh::GalData>();
         SOD_TRY(build_gal(m, gd.get()));
-        const_cast<sod_mesh *>(m)->gal = std::move(gd);
+        mm->gal = std::move(gd);
     }
     sod_mesh::GalData *g = m->gal.get();
     const bool sing = (L.parts & SOD_PART_SINGULAR) != 0;
-    const int chunk = std::min(L.nfreq, MAX_FREQ_PER_LAUNCH);
+    const bool reg = (L.parts & SOD_PART_REGULAR) != 0;
     const long long nslots = g->nslots;
+    const int nq = pt.n;
+    const long long ntp = (long long)m->nF * nq;  // test points
     DuffyRule dr{};
     {
         int n = 0;
@@ -681,22 +800,39 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
         const bool run = kd == SOD_G ? ((mask & (1 << SOD_G)) || bm) : (mask & (1 << SOD_H)) != 0;
         if (!run) continue;
         const int pbm = kd == SOD_G ? bm : 0;
-        const void *fn = gal_scatter_fn(kd, pbm);
-        cudaFuncAttributes attr;
-        SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
-        int T = ctx->coll_threads > 0 ? ctx->coll_threads : 256;
-        T = std::max(32, std::min(attr.maxThreadsPerBlock, (T / 32) * 32));
-        const sod_mesh::Coloured *col = nullptr;
-        SOD_TRY(const_cast<sod_mesh *>(m)->coloured_for(T, &col));
-        const int ncb = (pbm & BT ? 6 : 0) + (pbm & BA ? 18 : 0);
-        const size_t smem = sizeof(float2) * ((kd == SOD_G ? 6 : 9) * (size_t)m->nV + (size_t)ncb * T);
-        if (smem + attr.sharedSizeBytes > ctx->smem_optin) {
-            set_error("mesh too large for the shared-memory row accumulator");
-            return SOD_ERR_UNSUPPORTED;
-        }
-        SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)(ctx->smem_optin - attr.sharedSizeBytes)));
         const int NCS = kd == SOD_G ? 6 : 9;
+        const int ncb = (pbm & BT ? 6 : 0) + (pbm & BA ? 18 : 0);
+        const void *fn = gal_tp_fn(kd, pbm);
+        int T = 0;
+        if (ctx->gal_threads > 0) {
+            cudaFuncAttributes attr;
+            SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
+            T = std::max(32, std::min(attr.maxThreadsPerBlock, (ctx->gal_threads / 32) * 32));
+        } else if (reg) {
+            SOD_TRY(gal_tp_threads(ctx, mm, kd, pbm, fn, &T));
+        }
+        const sod_mesh::Coloured *col = nullptr;
+        size_t smem = 0;
+        if (reg) {
+            SOD_TRY(mm->coloured_for(T, &col));
+            cudaFuncAttributes attr;
+            SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
+            smem = sizeof(float2) * ((size_t)NCS * m->nV + (size_t)ncb * T);
+            if (smem + attr.sharedSizeBytes > ctx->smem_optin) {
+                set_error("mesh too large for the shared-memory row accumulator");
+                return SOD_ERR_UNSUPPORTED;
+            }
+            SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)(ctx->smem_optin - attr.sharedSizeBytes)));
+        }
+        // frequency chunk: singular scratch limit and the test-point row scratch budget
+        const size_t rows_per_f = (size_t)ntp * NCS * m->nV * sizeof(float2), b_per_f = (size_t)ntp * ncb * sizeof(cd);
+        int chunk = std::min(L.nfreq, MAX_FREQ_PER_LAUNCH);
+        if (reg) chunk = std::max(1, std::min<int>(chunk, (int)(GAL_ROWS_BUDGET / (rows_per_f + b_per_f))));
+        if (reg) {
+            SOD_TRY(ctx->gal_rows.ensure(rows_per_f * chunk));
+            if (ncb) SOD_TRY(ctx->gal_bsum.ensure(b_per_f * chunk));
+        }
         // singular scratch: slot blocks, then per-vertex B (9 + 27); results per entry, then B moments
         const long long s_slots = nslots * 9, s_bt = (long long)m->nV * 9, s_ba = (long long)m->nV * 27;
         const long long r_main = (long long)g->nent * 3 * NCS, r_b = pbm ? (long long)g->nent * GAL_BMOM : 0;
@@ -719,9 +855,9 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
             GalArgs a{};
             a.nV = m->nV;
             a.nF = m->nF;
-            a.faces = col->dFaces.as<float4>();
-            a.color_off = col->dOff.as<int>();
-            a.ncolors = col->ncolors;
+            a.faces = reg ? col->dFaces.as<float4>() : nullptr;
+            a.color_off = reg ? col->dOff.as<int>() : nullptr;
+            a.ncolors = reg ? col->ncolors : 0;
             a.faces_nat = m->dFacesNat.as<float4>();
             a.star_off = m->dStarOff.as<int>();
             a.star_face = m->dStarFace.as<int>();
@@ -729,7 +865,7 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
             a.out = L.out[kd] ? static_cast<char *>(L.out[kd]) + (size_t)f0 * (size_t)L.freq_stride[kd] * esz : nullptr;
             a.fstride = L.freq_stride[kd];
             a.out_c64 = L.out_dtype == SOD_C64;
-            a.do_regular = (L.parts & SOD_PART_REGULAR) != 0;
+            a.do_regular = reg;
             a.S = sing ? S : nullptr;
             a.S_fstride = s_slots;
             a.slot_off = g->slot_off.as<int>();
@@ -743,7 +879,7 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
                 a.SB[b] = (sing && (pbm & (1 << kb))) ? (b == 0 ? SBt : SBa) : nullptr;
                 a.SB_fstride[b] = b == 0 ? s_bt : s_ba;
             }
-            // singular pairs, their combination, then the regular pass (which adds them)
+            // singular pairs and their combination into slot blocks
             if (sing && g->nent > 0) {
                 const dim3 grid((g->nent * 32 + 127) / 128, nf);
                 if (kd == SOD_H)
@@ -781,17 +917,54 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
                     ctx->count();
                 }
             }
+            // regular pairs: rows of every test point, then the per-vertex combination (which also
+            // adds the singular blocks)
+            GalGatherArgs ga{};
+            ga.g = a;
+            ga.nq = nq;
+            ga.do_regular = reg;
+            ga.rows_fstride = ntp * NCS * m->nV;
+            ga.b_fstride = ntp * ncb;
+            if (reg) {
+                GalTpArgs ta{};
+                ta.nV = m->nV;
+                ta.nq = nq;
+                ta.t0 = 0;
+                ta.faces = col->dFaces.as<float4>();
+                ta.color_off = col->dOff.as<int>();
+                ta.ncolors = col->ncolors;
+                ta.faces_nat = m->dFacesNat.as<float4>();
+                ta.rows = ctx->gal_rows.as<float2>();
+                ta.rows_fstride = ga.rows_fstride;
+                ta.bsum = ncb ? ctx->gal_bsum.as<cd>() : nullptr;
+                ta.b_fstride = ga.b_fstride;
+                const dim3 grid((unsigned)ntp, nf);
+                if (kd == SOD_H)
+                    gal_tp_kernel<SOD_H, 0><<<grid, T, smem, L.stream>>>(ta, pt, ft);
+                else if (pbm == (BT | BA))
+                    gal_tp_kernel<SOD_G, BT | BA><<<grid, T, smem, L.stream>>>(ta, pt, ft);
+                else if (pbm == BT)
+                    gal_tp_kernel<SOD_G, BT><<<grid, T, smem, L.stream>>>(ta, pt, ft);
+                else if (pbm == BA)
+                    gal_tp_kernel<SOD_G, BA><<<grid, T, smem, L.stream>>>(ta, pt, ft);
+                else
+                    gal_tp_kernel<SOD_G, 0><<<grid, T, smem, L.stream>>>(ta, pt, ft);
+                SOD_CHECK_CUDA(cudaGetLastError());
+                ctx->count();
+                ga.rows = ta.rows;
+                ga.bsum = ta.bsum;
+            }
             const dim3 grid(m->nV, nf);
             if (kd == SOD_H)
-                gal_scatter_kernel<SOD_H, 0><<<grid, T, smem, L.stream>>>(a, pt, ft);
+                gal_gather_kernel<SOD_H, 0><<<grid, 256, 0, L.stream>>>(ga, pt);
             else if (pbm == (BT | BA))
-                gal_scatter_kernel<SOD_G, BT | BA><<<grid, T, smem, L.stream>>>(a, pt, ft);
+                gal_gather_kernel<SOD_G, BT | BA><<<grid, 256, 0, L.stream>>>(ga, pt);
             else if (pbm == BT)
-                gal_scatter_kernel<SOD_G, BT><<<grid, T, smem, L.stream>>>(a, pt, ft);
+                gal_gather_kernel<SOD_G, BT><<<grid, 256, 0, L.stream>>>(ga, pt);
             else if (pbm == BA)
-                gal_scatter_kernel<SOD_G, BA><<<grid, T, smem, L.stream>>>(a, pt, ft);
+                gal_gather_kernel<SOD_G, BA><<<grid, 256, 0, L.stream>>>(ga, pt);
             else
-                gal_scatter_kernel<SOD_G, 0><<<grid, T, smem, L.stream>>>(a, pt, ft);
+                gal_gather_kernel<SOD_G, 0><<<grid, 256, 0, L.stream>>>(ga, pt);
             SOD_CHECK_CUDA(cudaGetLastError());
             ctx->count();
         }

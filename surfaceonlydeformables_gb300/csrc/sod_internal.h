@@ -112,6 +112,8 @@ struct sod_context {
     sod::DevBuf twiddle;   // inverse-transform twiddles
     sod::DevBuf freqbuf;   // Laplace-domain intermediates of the precompute
     sod::DevBuf small;     // small per-call tables (free terms, adjacency)
+    sod::DevBuf gal_rows;  // Galerkin: unweighted rows of every test point (per frequency chunk)
+    sod::DevBuf gal_bsum;  // Galerkin: B_trans / B_angular sums of every test point
     void count(int n = 1) { launches += n; }
 };
 
