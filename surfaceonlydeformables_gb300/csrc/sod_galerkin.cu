@@ -20,6 +20,7 @@
 // (vertex, slot) 3 x 3 blocks over the two-ring of a, which the regular kernel's epilogue adds.
 #include <algorithm>
 #include <array>
+#include <map>
 #include <set>
 
 #include "sod_bmom.cuh"
@@ -350,29 +351,53 @@ struct DuffyRule {  // 1-D Gauss-Legendre on [0,1] after subdivision, FP64
 };
 
 struct GalSingArgs {
-    int nent;
-    const int4 *ent;  // per entry: {f2, class, test corner, 0}, {j1[3], 0}, {j2[3], 0}, {slot[3], 0}
+    int nent, npairs;
+    const int4 *pairs;  // per pair: {f2, class}, {j1[3]}, {j2[3]}, {entry of test corner 0, 1, 2}
     const double *V, *N;
-    double2 *R;       // [frequency][entry][3 * NCS]
-    double2 *RB;      // [frequency][entry][13] B moments (G pass with B kinds)
+    double2 *R;         // [frequency][entry][3 * NCS]
+    double2 *RB;        // [frequency][entry][13] B moments (G pass with B kinds)
 };
 constexpr int GAL_BMOM = 13;  // Ms[3], Md, M1[6], M0, SB, SC
 
 __device__ __forceinline__ dd ddv(double x) { return dd_from(x); }
 
+// shared-memory floats per warp of the singular kernel: kernel tensor (NCS cdd), B moment values
+// (13 cdd, G pass with B kinds) and the test / trial shape functions (6 dd) of 32 points
+template <int KIND, int BM> constexpr int sing_warp_floats() {
+    return 32 * ((KIND == SOD_G ? 6 : 9) * 4 + ((KIND == SOD_G && BM != 0) ? GAL_BMOM * 4 : 0) + 12);
+}
+__device__ __forceinline__ void st_cdd(float *p, const cdd &v) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v.x.hi, v.x.lo, v.y.hi, v.y.lo);
+}
+__device__ __forceinline__ cdd ld_cdd(const float *p) {
+    const float4 q = *reinterpret_cast<const float4 *>(p);
+    return cdd{dd{q.x, q.y}, dd{q.z, q.w}};
+}
+
+// One warp per (distinct singular face pair, frequency).  The three entries of a pair (test corners
+// of f1) share every kernel evaluation, so the warp integrates the pair once: in batches of 32
+// Sauter-Schwab points, each lane first evaluates the kernel tensor (times the point weight) at one
+// point into shared memory, then each lane adds the 32 points into the few (test corner, trial
+// corner, component) sums it owns, in point order -- every sum is owned by one lane, so no cross-lane
+// reduction is needed and the order is fixed.
 template <int KIND, int BM>
 __global__ void __launch_bounds__(128) gal_sing_kernel(GalSingArgs a, const __grid_constant__ DuffyRule g,
                                                        const __grid_constant__ FreqTable ft) {
     constexpr int NCS = KIND == SOD_G ? 6 : 9;
     constexpr bool DB = KIND == SOD_G && BM != 0;
     constexpr bool BT = (BM & (1 << SOD_B_TRANS)) != 0, BA = (BM & (1 << SOD_B_ANGULAR)) != 0;
+    constexpr int NA = 9 * NCS + (DB ? 3 * GAL_BMOM : 0), PER = (NA + 31) / 32;
+    constexpr int OFF_V = 32 * NCS * 4, OFF_L = OFF_V + (DB ? 32 * GAL_BMOM * 4 : 0);
+    extern __shared__ float smem_sing[];
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= a.nent) return;
+    if (warp >= a.npairs) return;
+    float *sw = smem_sing + (threadIdx.x >> 5) * sing_warp_floats<KIND, BM>();
     const int fq = blockIdx.y;
     const KDDg k = make_kddg(ft.kd[fq]);
-    const int4 e0 = a.ent[4 * warp], ej1 = a.ent[4 * warp + 1], ej2 = a.ent[4 * warp + 2];
-    const int f2 = e0.x, cls = e0.y, ac = e0.z;
-    const int j1[3] = {ej1.x, ej1.y, ej1.z}, j2[3] = {ej2.x, ej2.y, ej2.z};
+    const int4 e0 = a.pairs[4 * warp], ej1 = a.pairs[4 * warp + 1], ej2 = a.pairs[4 * warp + 2],
+               ee = a.pairs[4 * warp + 3];
+    const int f2 = e0.x, cls = e0.y;
+    const int j1[3] = {ej1.x, ej1.y, ej1.z}, j2[3] = {ej2.x, ej2.y, ej2.z}, ent[3] = {ee.x, ee.y, ee.z};
     // parametrisation x = o + xa xh0 + xb xh1, y = o + ya yh0 + yb yh1 (FP64 set-up)
     double P1[3][3], P2[3][3];
     for (int c = 0; c < 3; c++)
@@ -401,155 +426,168 @@ __global__ void __launch_bounds__(128) gal_sing_kernel(GalSingArgs a, const __gr
     const dd Xa[3] = {ddv(xa[0]), ddv(xa[1]), ddv(xa[2])}, Xb[3] = {ddv(xb[0]), ddv(xb[1]), ddv(xb[2])};
     const dd Ya[3] = {ddv(ya[0]), ddv(ya[1]), ddv(ya[2])}, Yb[3] = {ddv(yb[0]), ddv(yb[1]), ddv(yb[2])};
     const dd nn[3] = {ddv(a.N[3 * f2]), ddv(a.N[3 * f2 + 1]), ddv(a.N[3 * f2 + 2])};
-    cdd acc[3][NCS];
+    cdd acc[PER];
 #pragma unroll
-    for (int b = 0; b < 3; b++)
-#pragma unroll
-        for (int c = 0; c < NCS; c++) acc[b][c] = cdd{dd{0.f, 0.f}, dd{0.f, 0.f}};
-    cdd mb[DB ? GAL_BMOM : 1];
-#pragma unroll
-    for (int c = 0; c < (DB ? GAL_BMOM : 1); c++) mb[c] = cdd{dd{0.f, 0.f}, dd{0.f, 0.f}};
+    for (int t = 0; t < PER; t++) acc[t] = cdd{dd{0.f, 0.f}, dd{0.f, 0.f}};
     const int n = g.n, n4 = n * n * n * n;
     const int nmap = cls == 1 ? 6 : cls == 2 ? 5 : 2;
-    for (int pidx = lane; pidx < n4 * nmap; pidx += 32) {
-        const int m = pidx / n4, r4 = pidx % n4;
-        const int i1 = r4 / (n * n * n), i2 = (r4 / (n * n)) % n, i3 = (r4 / n) % n, i4 = r4 % n;
-        const dd e1 = ddv(g.x[i1]), e2 = ddv(g.x[i2]), e3 = ddv(g.x[i3]), xi = ddv(g.x[i4]);
-        const dd one = dd{1.f, 0.f};
-        dd w = ddv(g.w[i1] * g.w[i2] * g.w[i3] * g.w[i4]) * (xi * xi * xi);
-        dd xh0, xh1, yh0, yh1;
-        const dd e12 = e1 * e2, e123 = e12 * e3;
-        if (cls == 1) {  // coincident, 6 maps; jac = w xi^3 e1^2 e2
-            w = w * (e1 * e1) * e2;
-            switch (m) {
-            case 0: xh0 = xi, xh1 = xi * (one - e1 + e12), yh0 = xi * (one - e123), yh1 = xi * (one - e1); break;
-            case 1: xh0 = xi * (one - e123), xh1 = xi * (one - e1), yh0 = xi, yh1 = xi * (one - e1 + e12); break;
-            case 2: xh0 = xi, xh1 = xi * e1 * (one - e2 + e2 * e3), yh0 = xi * (one - e12), yh1 = xi * e1 * (one - e2); break;
-            case 3: xh0 = xi * (one - e12), xh1 = xi * e1 * (one - e2), yh0 = xi, yh1 = xi * e1 * (one - e2 + e2 * e3); break;
-            case 4: xh0 = xi * (one - e123), xh1 = xi * e1 * (one - e2 * e3), yh0 = xi, yh1 = xi * e1 * (one - e2); break;
-            default: xh0 = xi, xh1 = xi * e1 * (one - e2), yh0 = xi * (one - e123), yh1 = xi * e1 * (one - e2 * e3); break;
-            }
-        } else if (cls == 2) {  // edge adjacent, 5 maps; jac = w xi^3 e1^2 (times e2 for maps 2..5)
-            w = w * (e1 * e1);
-            switch (m) {
-            case 0: xh0 = xi, xh1 = xi * e1 * e3, yh0 = xi * (one - e12), yh1 = xi * e1 * (one - e2); break;
-            case 1: xh0 = xi, xh1 = xi * e1, yh0 = xi * (one - e123), yh1 = xi * e12 * (one - e3), w = w * e2; break;
-            case 2: xh0 = xi * (one - e12), xh1 = xi * e1 * (one - e2), yh0 = xi, yh1 = xi * e123, w = w * e2; break;
-            case 3: xh0 = xi * (one - e123), xh1 = xi * e12 * (one - e3), yh0 = xi, yh1 = xi * e1, w = w * e2; break;
-            default: xh0 = xi * (one - e123), xh1 = xi * e1 * (one - e2 * e3), yh0 = xi, yh1 = xi * e12, w = w * e2; break;
-            }
-        } else {  // vertex adjacent, 2 maps; jac = w xi^3 e2
-            w = w * e2;
-            if (m == 0) xh0 = xi, xh1 = xi * e1, yh0 = xi * e2, yh1 = xi * e2 * e3;
-            else xh0 = xi * e2, xh1 = xi * e2 * e3, yh0 = xi, yh1 = xi * e1;
-        }
-        // y - x = ya yh0 + yb yh1 - xa xh0 - xb xh1 (the common origin cancels exactly)
-        dd rv[3];
-#pragma unroll
-        for (int d = 0; d < 3; d++) rv[d] = Ya[d] * yh0 + Yb[d] * yh1 - Xa[d] * xh0 - Xb[d] * xh1;
-        const dd r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
-        const dd r = dd_sqrt(r2);
-        const dd rinv = dd_recip(r);
-        const dd rh[3] = {rv[0] * rinv, rv[1] * rinv, rv[2] * rinv};
-        const dd Lx[3] = {one - xh0, xh0 - xh1, xh1}, Ly[3] = {one - yh0, yh0 - yh1, yh1};
-        const dd wa = w * Lx[ac];
-        // radial terms
-        const cdd z1 = k.sc1 * r, z2 = k.sc2 * r;
-        const cdd ez1 = cdd_exp_neg(z1), ez2 = cdd_exp_neg(z2);
-        const cdd psi1 = cdd_psi(z1, ez1), psi2 = cdd_psi(z2, ez2);
-        const cdd Y = psi1 * k.ic1s - psi2 * k.ic2s;
+    const int total = n4 * nmap;
+    const dd zero = dd{0.f, 0.f};
+    for (int base = 0; base < total; base += 32) {
+        // ---- phase A: this lane's point -> kernel tensor, B moment values and shape functions ----
+        const int pidx = base + lane;
         cdd u[NCS];
-        if (KIND == SOD_G) {
-            const cdd B = ez1 * k.ic1s - ez2 * k.ic2s;
-            const dd sc = k.inv4pirho * rinv;
-            const cdd al = (Y * 3.0f + B) * sc, be = (ez2 * k.ic2s - Y) * sc;
+        cdd mv[DB ? GAL_BMOM : 1];
+        dd Lx[3] = {zero, zero, zero}, Ly[3] = {zero, zero, zero};
 #pragma unroll
-            for (int p = 0; p < 3; p++)
+        for (int c = 0; c < NCS; c++) u[c] = cdd{zero, zero};
 #pragma unroll
-                for (int qq = p; qq < 3; qq++) {
-                    cdd v = al * (rh[p] * rh[qq]);
-                    if (p == qq) v = v + be;
-                    u[sym_index(p, qq)] = v;
+        for (int c = 0; c < (DB ? GAL_BMOM : 1); c++) mv[c] = cdd{zero, zero};
+        if (pidx < total) {
+            const int m = pidx / n4, r4 = pidx % n4;
+            const int i1 = r4 / (n * n * n), i2 = (r4 / (n * n)) % n, i3 = (r4 / n) % n, i4 = r4 % n;
+            const dd e1 = ddv(g.x[i1]), e2 = ddv(g.x[i2]), e3 = ddv(g.x[i3]), xi = ddv(g.x[i4]);
+            const dd one = dd{1.f, 0.f};
+            dd w = ddv(g.w[i1] * g.w[i2] * g.w[i3] * g.w[i4]) * (xi * xi * xi);
+            dd xh0, xh1, yh0, yh1;
+            const dd e12 = e1 * e2, e123 = e12 * e3;
+            if (cls == 1) {  // coincident, 6 maps; jac = w xi^3 e1^2 e2
+                w = w * (e1 * e1) * e2;
+                switch (m) {
+                case 0: xh0 = xi, xh1 = xi * (one - e1 + e12), yh0 = xi * (one - e123), yh1 = xi * (one - e1); break;
+                case 1: xh0 = xi * (one - e123), xh1 = xi * (one - e1), yh0 = xi, yh1 = xi * (one - e1 + e12); break;
+                case 2: xh0 = xi, xh1 = xi * e1 * (one - e2 + e2 * e3), yh0 = xi * (one - e12), yh1 = xi * e1 * (one - e2); break;
+                case 3: xh0 = xi * (one - e12), xh1 = xi * e1 * (one - e2), yh0 = xi, yh1 = xi * e1 * (one - e2 + e2 * e3); break;
+                case 4: xh0 = xi * (one - e123), xh1 = xi * e1 * (one - e2 * e3), yh0 = xi, yh1 = xi * e1 * (one - e2); break;
+                default: xh0 = xi, xh1 = xi * e1 * (one - e2), yh0 = xi * (one - e123), yh1 = xi * e1 * (one - e2 * e3); break;
                 }
-        } else {
-            const cdd Yc = Y * k.six_c2s;
-            const cdd z1e1 = z1 * ez1, z2e2 = z2 * ez2;
-            const dd sc = k.inv4pi * (rinv * rinv);
-            const cdd ca = (Yc + ez1 * k.k4m1 - ez2 * 2.0f - z1e1 * k.k1m2) * sc;
-            const cdd cb = (Yc + ez1 * k.k2 - ez2 * 3.0f - z2e2) * sc;
-            const cdd cdv = (Yc * (-5.0f) - ez1 * k.k12 + ez2 * 12.0f - z1e1 * k.k2 + z2e2 * 2.0f) * sc;
-            const dd rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
-            const cdd cbr = cb * rn, cdr = cdv * rn;
-#pragma unroll
-            for (int p = 0; p < 3; p++)
-#pragma unroll
-                for (int qq = 0; qq < 3; qq++) {
-                    cdd v = ca * (rh[p] * nn[qq]) + cb * (nn[p] * rh[qq]) + cdr * (rh[p] * rh[qq]);
-                    if (p == qq) v = v + cbr;
-                    u[3 * p + qq] = v;
+            } else if (cls == 2) {  // edge adjacent, 5 maps; jac = w xi^3 e1^2 (times e2 for maps 2..5)
+                w = w * (e1 * e1);
+                switch (m) {
+                case 0: xh0 = xi, xh1 = xi * e1 * e3, yh0 = xi * (one - e12), yh1 = xi * e1 * (one - e2); break;
+                case 1: xh0 = xi, xh1 = xi * e1, yh0 = xi * (one - e123), yh1 = xi * e12 * (one - e3), w = w * e2; break;
+                case 2: xh0 = xi * (one - e12), xh1 = xi * e1 * (one - e2), yh0 = xi, yh1 = xi * e123, w = w * e2; break;
+                case 3: xh0 = xi * (one - e123), xh1 = xi * e12 * (one - e3), yh0 = xi, yh1 = xi * e1, w = w * e2; break;
+                default: xh0 = xi * (one - e123), xh1 = xi * e1 * (one - e2 * e3), yh0 = xi, yh1 = xi * e12, w = w * e2; break;
                 }
-        }
-#pragma unroll
-        for (int b = 0; b < 3; b++) {
-            const dd wb = wa * Ly[b];
-#pragma unroll
-            for (int c = 0; c < NCS; c++) cdd_acc(acc[b][c], u[c], wb);
-        }
-        if (DB) {  // B moments with the test weight only (no trial shape function)
-            const dd rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
-            if (BT) {
-                const cdd ws = Y * (k.inv4pi * 0.5f);
-                const cdd di = psi2 * (k.ic2s * k.inv4pi);
-#pragma unroll
-                for (int p = 0; p < 3; p++) cdd_acc(mb[p], ws, wa * rh[p]);
-                cdd_acc(mb[3], di, wa * rn);
+            } else {  // vertex adjacent, 2 maps; jac = w xi^3 e2
+                w = w * e2;
+                if (m == 0) xh0 = xi, xh1 = xi * e1, yh0 = xi * e2, yh1 = xi * e2 * e3;
+                else xh0 = xi * e2, xh1 = xi * e2 * e3, yh0 = xi, yh1 = xi * e1;
             }
-            if (BA) {
-                const cdd A = Y * (r * k.inv4pi * 0.5f);
-                const cdd Bq = (ez2 * k.ic2 - ez1 * k.ic1) * k.is * (k.inv4pi * 0.5f);
-                const cdd Cq = ez2 * k.is * (k.ic2 * k.inv4pi);
+            // y - x = ya yh0 + yb yh1 - xa xh0 - xb xh1 (the common origin cancels exactly)
+            dd rv[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) rv[d] = Ya[d] * yh0 + Yb[d] * yh1 - Xa[d] * xh0 - Xb[d] * xh1;
+            const dd r2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+            const dd r = dd_sqrt(r2);
+            const dd rinv = dd_recip(r);
+            const dd rh[3] = {rv[0] * rinv, rv[1] * rinv, rv[2] * rinv};
+            Lx[0] = one - xh0, Lx[1] = xh0 - xh1, Lx[2] = xh1;
+            Ly[0] = one - yh0, Ly[1] = yh0 - yh1, Ly[2] = yh1;
+            // radial terms
+            const cdd z1 = k.sc1 * r, z2 = k.sc2 * r;
+            const cdd ez1 = cdd_exp_neg(z1), ez2 = cdd_exp_neg(z2);
+            const cdd psi1 = cdd_psi(z1, ez1), psi2 = cdd_psi(z2, ez2);
+            const cdd Y = psi1 * k.ic1s - psi2 * k.ic2s;
+            if (KIND == SOD_G) {
+                const cdd B = ez1 * k.ic1s - ez2 * k.ic2s;
+                const dd sc = k.inv4pirho * rinv * w;
+                const cdd al = (Y * 3.0f + B) * sc, be = (ez2 * k.ic2s - Y) * sc;
 #pragma unroll
                 for (int p = 0; p < 3; p++)
 #pragma unroll
-                    for (int q = p; q < 3; q++) cdd_acc(mb[4 + sym_index(p, q)], A, wa * (rh[p] * rh[q]));
-                cdd_acc(mb[10], A, wa);
-                cdd_acc(mb[11], Bq, wa);
-                cdd_acc(mb[12], Cq, wa);
+                    for (int qq = p; qq < 3; qq++) {
+                        cdd v = al * (rh[p] * rh[qq]);
+                        if (p == qq) v = v + be;
+                        u[sym_index(p, qq)] = v;
+                    }
+            } else {
+                const cdd Yc = Y * k.six_c2s;
+                const cdd z1e1 = z1 * ez1, z2e2 = z2 * ez2;
+                const dd sc = k.inv4pi * (rinv * rinv) * w;
+                const cdd ca = (Yc + ez1 * k.k4m1 - ez2 * 2.0f - z1e1 * k.k1m2) * sc;
+                const cdd cb = (Yc + ez1 * k.k2 - ez2 * 3.0f - z2e2) * sc;
+                const cdd cdv = (Yc * (-5.0f) - ez1 * k.k12 + ez2 * 12.0f - z1e1 * k.k2 + z2e2 * 2.0f) * sc;
+                const dd rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
+                const cdd cbr = cb * rn, cdr = cdv * rn;
+#pragma unroll
+                for (int p = 0; p < 3; p++)
+#pragma unroll
+                    for (int qq = 0; qq < 3; qq++) {
+                        cdd v = ca * (rh[p] * nn[qq]) + cb * (nn[p] * rh[qq]) + cdr * (rh[p] * rh[qq]);
+                        if (p == qq) v = v + cbr;
+                        u[3 * p + qq] = v;
+                    }
+            }
+            if (DB) {  // B moment values with the point weight (the test corner weight comes later)
+                const dd rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
+                if (BT) {
+                    const cdd ws = Y * (k.inv4pi * 0.5f);
+                    const cdd di = psi2 * (k.ic2s * k.inv4pi);
+#pragma unroll
+                    for (int p = 0; p < 3; p++) mv[p] = ws * (w * rh[p]);
+                    mv[3] = di * (w * rn);
+                }
+                if (BA) {
+                    const cdd A = Y * (r * k.inv4pi * 0.5f);
+                    const cdd Bq = (ez2 * k.ic2 - ez1 * k.ic1) * k.is * (k.inv4pi * 0.5f);
+                    const cdd Cq = ez2 * k.is * (k.ic2 * k.inv4pi);
+#pragma unroll
+                    for (int p = 0; p < 3; p++)
+#pragma unroll
+                        for (int q = p; q < 3; q++) mv[4 + sym_index(p, q)] = A * (w * (rh[p] * rh[q]));
+                    mv[10] = A * w;
+                    mv[11] = Bq * w;
+                    mv[12] = Cq * w;
+                }
             }
         }
+#pragma unroll
+        for (int c = 0; c < NCS; c++) st_cdd(sw + (lane * NCS + c) * 4, u[c]);
+        if (DB)
+#pragma unroll
+            for (int c = 0; c < GAL_BMOM; c++) st_cdd(sw + OFF_V + (lane * GAL_BMOM + c) * 4, mv[c]);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            sw[OFF_L + lane * 12 + 2 * c] = Lx[c].hi, sw[OFF_L + lane * 12 + 2 * c + 1] = Lx[c].lo;
+            sw[OFF_L + lane * 12 + 6 + 2 * c] = Ly[c].hi, sw[OFF_L + lane * 12 + 6 + 2 * c + 1] = Ly[c].lo;
+        }
+        __syncwarp();
+        // ---- phase B: the sums this lane owns, over the batch's 32 points in order ----
+#pragma unroll
+        for (int t = 0; t < PER; t++) {
+            const int q = lane + 32 * t;
+            if (q >= NA) continue;
+            if (q < 9 * NCS) {
+                const int ac = q / (3 * NCS), b = (q / NCS) % 3, c = q % NCS;
+                for (int pt = 0; pt < 32; pt++) {
+                    const float *L = sw + OFF_L + pt * 12;
+                    const dd wgt = dd{L[2 * ac], L[2 * ac + 1]} * dd{L[6 + 2 * b], L[6 + 2 * b + 1]};
+                    cdd_acc(acc[t], ld_cdd(sw + (pt * NCS + c) * 4), wgt);
+                }
+            } else if (DB) {
+                const int qm = q - 9 * NCS, ac = qm / GAL_BMOM, c = qm % GAL_BMOM;
+                for (int pt = 0; pt < 32; pt++) {
+                    const float *L = sw + OFF_L + pt * 12;
+                    cdd_acc(acc[t], ld_cdd(sw + OFF_V + (pt * GAL_BMOM + c) * 4), dd{L[2 * ac], L[2 * ac + 1]});
+                }
+            }
+        }
+        __syncwarp();
     }
-    // fixed xor tree over the lanes, in double-float
+    // each sum belongs to one lane: scale by the map Jacobian and store per entry
 #pragma unroll
-    for (int b = 0; b < 3; b++)
-#pragma unroll
-        for (int c = 0; c < NCS; c++) {
-            cdd v = acc[b][c];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                cdd w2;
-                w2.x.hi = __shfl_xor_sync(0xffffffffu, v.x.hi, o);
-                w2.x.lo = __shfl_xor_sync(0xffffffffu, v.x.lo, o);
-                w2.y.hi = __shfl_xor_sync(0xffffffffu, v.y.hi, o);
-                w2.y.lo = __shfl_xor_sync(0xffffffffu, v.y.lo, o);
-                v = v + w2;
-            }
-            if (lane == 0)
-                a.R[((size_t)fq * a.nent + warp) * 3 * NCS + b * NCS + c] = make_double2(dd_to(v.x) * J, dd_to(v.y) * J);
-        }
-    if (DB) {
-#pragma unroll
-        for (int c = 0; c < GAL_BMOM; c++) {
-            cdd v = mb[c];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                cdd w2;
-                w2.x.hi = __shfl_xor_sync(0xffffffffu, v.x.hi, o);
-                w2.x.lo = __shfl_xor_sync(0xffffffffu, v.x.lo, o);
-                w2.y.hi = __shfl_xor_sync(0xffffffffu, v.y.hi, o);
-                w2.y.lo = __shfl_xor_sync(0xffffffffu, v.y.lo, o);
-                v = v + w2;
-            }
-            if (lane == 0) a.RB[((size_t)fq * a.nent + warp) * GAL_BMOM + c] = make_double2(dd_to(v.x) * J, dd_to(v.y) * J);
+    for (int t = 0; t < PER; t++) {
+        const int q = lane + 32 * t;
+        if (q >= NA) continue;
+        const double2 v = make_double2(dd_to(acc[t].x) * J, dd_to(acc[t].y) * J);
+        if (q < 9 * NCS) {
+            const int ac = q / (3 * NCS), bc = q % (3 * NCS);
+            a.R[((size_t)fq * a.nent + ent[ac]) * 3 * NCS + bc] = v;
+        } else if (DB) {
+            const int qm = q - 9 * NCS, ac = qm / GAL_BMOM, c = qm % GAL_BMOM;
+            a.RB[((size_t)fq * a.nent + ent[ac]) * GAL_BMOM + c] = v;
         }
     }
 }
@@ -657,8 +695,13 @@ static int build_gal(const sod_mesh *m, sod_mesh::GalData *g) {
         for (int c = 0; c < 3; c++) vf[m->F[3 * f + c]].push_back(f);
     std::vector<int4> ent;
     std::vector<int> ent_off(nV + 1, 0), slot_off(nV + 1, 0), slot_vert;
+    // distinct pairs (f1, f2): the three entries of a pair (one per test corner of f1) share every
+    // kernel evaluation, so the singular kernel integrates a pair once for all three
+    std::map<std::pair<int, int>, int> pair_id;
+    std::vector<int4> pairs;
     for (int a = 0; a < nV; a++) {
         std::vector<std::array<int, 9>> rows;  // f2, cls, ac, j1[3], j2[3]
+        std::vector<int> rf1;                  // f1 of each row
         for (int f1 : vf[a]) {
             std::set<int> partners;
             for (int c = 0; c < 3; c++)
@@ -669,6 +712,7 @@ static int build_gal(const sod_mesh *m, sod_mesh::GalData *g) {
                 int ac = 0;
                 while (ac < 3 && j1[ac] != a) ac++;
                 rows.push_back({f2, cls, ac, j1[0], j1[1], j1[2], j2[0], j2[1], j2[2]});
+                rf1.push_back(f1);
             }
         }
         std::vector<int> sl;
@@ -677,7 +721,18 @@ static int build_gal(const sod_mesh *m, sod_mesh::GalData *g) {
         std::sort(sl.begin(), sl.end());
         sl.erase(std::unique(sl.begin(), sl.end()), sl.end());
         const int base = (int)slot_vert.size();
-        for (auto &r : rows) {
+        for (size_t ri = 0; ri < rows.size(); ri++) {
+            auto &r = rows[ri];
+            const int f1 = rf1[ri], eidx = (int)(ent.size() / 4);
+            auto ins = pair_id.emplace(std::make_pair(f1, r[0]), (int)(pairs.size() / 4));
+            if (ins.second) {
+                pairs.push_back(make_int4(r[0], r[1], 0, 0));
+                pairs.push_back(make_int4(r[3], r[4], r[5], 0));
+                pairs.push_back(make_int4(r[6], r[7], r[8], 0));
+                pairs.push_back(make_int4(-1, -1, -1, 0));
+            }
+            int4 &pe = pairs[4 * ins.first->second + 3];
+            (r[2] == 0 ? pe.x : r[2] == 1 ? pe.y : pe.z) = eidx;
             int sv[3];
             for (int b = 0; b < 3; b++) sv[b] = base + (int)(std::lower_bound(sl.begin(), sl.end(), r[6 + b]) - sl.begin());
             ent.push_back(make_int4(r[0], r[1], r[2], 0));
@@ -691,6 +746,14 @@ static int build_gal(const sod_mesh *m, sod_mesh::GalData *g) {
     }
     g->nent = ent_off[nV];
     g->nslots = slot_off[nV];
+    g->npairs = (int)(pairs.size() / 4);
+    for (int q = 0; q < g->npairs; q++) {
+        const int4 pe = pairs[4 * q + 3];
+        if (pe.x < 0 || pe.y < 0 || pe.z < 0) {
+            set_error("Galerkin set-up: a singular face pair without all three test corners");
+            return SOD_ERR_INVALID_ARG;
+        }
+    }
     auto up = [](DevBuf &b, const void *src, size_t bytes) -> int {
         SOD_TRY(b.ensure(std::max<size_t>(bytes, 16)));
         if (bytes) SOD_CHECK_CUDA(cudaMemcpy(b.p, src, bytes, cudaMemcpyHostToDevice));
@@ -700,6 +763,7 @@ static int build_gal(const sod_mesh *m, sod_mesh::GalData *g) {
     SOD_TRY(up(g->ent_off, ent_off.data(), sizeof(int) * ent_off.size()));
     SOD_TRY(up(g->slot_off, slot_off.data(), sizeof(int) * slot_off.size()));
     SOD_TRY(up(g->slot_vert, slot_vert.data(), sizeof(int) * slot_vert.size()));
+    SOD_TRY(up(g->pairs, pairs.data(), sizeof(int4) * pairs.size()));
     return SOD_OK;
 }
 
@@ -851,7 +915,7 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
                 ft.kd[l] = L.kc_host[f0 + l];
                 ft.kf[l] = to_float(ft.kd[l]);
             }
-            GalSingArgs sa{g->nent, g->ent.as<int4>(), m->dV.as<double>(), m->dN.as<double>(), R, RB};
+            GalSingArgs sa{g->nent, g->npairs, g->pairs.as<int4>(), m->dV.as<double>(), m->dN.as<double>(), R, RB};
             GalArgs a{};
             a.nV = m->nV;
             a.nF = m->nF;
@@ -881,17 +945,18 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
             }
             // singular pairs and their combination into slot blocks
             if (sing && g->nent > 0) {
-                const dim3 grid((g->nent * 32 + 127) / 128, nf);
+                const dim3 grid((g->npairs * 32 + 127) / 128, nf);
                 if (kd == SOD_H)
-                    gal_sing_kernel<SOD_H, 0><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
+                    gal_sing_kernel<SOD_H, 0><<<grid, 128, 4 * 4 * sing_warp_floats<SOD_H, 0>(), L.stream>>>(sa, dr, ft);
                 else if (pbm == (BT | BA))
-                    gal_sing_kernel<SOD_G, BT | BA><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
+                    gal_sing_kernel<SOD_G, BT | BA>
+                        <<<grid, 128, 4 * 4 * sing_warp_floats<SOD_G, BT | BA>(), L.stream>>>(sa, dr, ft);
                 else if (pbm == BT)
-                    gal_sing_kernel<SOD_G, BT><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
+                    gal_sing_kernel<SOD_G, BT><<<grid, 128, 4 * 4 * sing_warp_floats<SOD_G, BT>(), L.stream>>>(sa, dr, ft);
                 else if (pbm == BA)
-                    gal_sing_kernel<SOD_G, BA><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
+                    gal_sing_kernel<SOD_G, BA><<<grid, 128, 4 * 4 * sing_warp_floats<SOD_G, BA>(), L.stream>>>(sa, dr, ft);
                 else
-                    gal_sing_kernel<SOD_G, 0><<<grid, 128, 0, L.stream>>>(sa, dr, ft);
+                    gal_sing_kernel<SOD_G, 0><<<grid, 128, 4 * 4 * sing_warp_floats<SOD_G, 0>(), L.stream>>>(sa, dr, ft);
                 SOD_CHECK_CUDA(cudaGetLastError());
                 ctx->count();
                 const int blocks = (int)(((long long)m->nV * nf * 32 + 127) / 128);

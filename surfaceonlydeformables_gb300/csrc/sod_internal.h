@@ -151,8 +151,9 @@ struct sod_mesh {
     std::map<std::pair<int, int>, std::unique_ptr<SingGeom>> sing_geom;
     // Galerkin singular-pair entries per vertex and the two-ring slots of each row (sod_galerkin.cu)
     struct GalData {
-        int nent = 0, nslots = 0;
+        int nent = 0, nslots = 0, npairs = 0;
         sod::DevBuf ent, ent_off, slot_off, slot_vert;
+        sod::DevBuf pairs;  // per distinct singular face pair: {f2, class}, j1, j2, {entry of test corner 0..2}
     };
     std::unique_ptr<GalData> gal;
     int sing_geom_for(int sorder, int ssub, cudaStream_t stream, const SingGeom **out);
