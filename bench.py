@@ -205,12 +205,12 @@ def history_leg(torch, ctx, stream, n: int = 7686, K: int = 64, reps: int = 10):
 
     hbm = measured_hbm_gbs()
     rows = []
-    cases = [(L.F32, "f32", 1, "cuda_cores"), (L.F32, "f32", 16, "cuda_cores"), (L.BF16, "bf16", 1, "tensor_cores"),
-             (L.BF16, "bf16", 1, "cuda_cores"), (L.BF16, "bf16", 16, "tensor_cores"), (L.BF16, "bf16", 16, "cuda_cores")]
+    cases = [(L.F32, "f32", 1, "cuda_cores"), (L.F32, "f32", 16, "tensor_cores"), (L.F32, "f32", 16, "cuda_cores"),
+             (L.BF16, "bf16", 1, "tensor_cores"), (L.BF16, "bf16", 1, "cuda_cores"), (L.BF16, "bf16", 16, "tensor_cores"),
+             (L.BF16, "bf16", 16, "cuda_cores")]
     for wdt, name, R, engine in cases:
         bank = api.HistoryBank(ctx, n, n, K, R, wdt)
-        if wdt == L.BF16:
-            bank.set_engine(L.HISTORY_ENGINE_TENSOR_CORES if engine == "tensor_cores" else L.HISTORY_ENGINE_CUDA_CORES)
+        bank.set_engine(L.HISTORY_ENGINE_TENSOR_CORES if engine == "tensor_cores" else L.HISTORY_ENGINE_CUDA_CORES)
         g = torch.empty((n, n), dtype=torch.float32, device="cuda")
         gen = torch.Generator(device="cuda")
         gen.manual_seed(7)

@@ -205,9 +205,10 @@ int sod_history_push(sod_history *bank, const double *p, const double *u, const 
 /* b for the next step from the pushed history (the min(n, K) most recent steps). */
 int sod_history_convolve(sod_history *bank, double *b);
 int sod_history_reset(sod_history *bank);
-/* Engine for the convolution: AUTO (tensor cores for BF16 banks, CUDA cores for FP32 banks),
- * CUDA_CORES, or TENSOR_CORES (BF16 banks only, else SOD_ERR_UNSUPPORTED).  A change of engine
- * empties the history ring (the engines keep it in different layouts). */
+/* Engine for the convolution: AUTO (tensor cores for BF16 banks and for FP32 banks with R = 16,
+ * CUDA cores for FP32 banks with R = 1), CUDA_CORES, or TENSOR_CORES.  FP32 banks on the tensor
+ * cores use a 3xTF32 split (FP32 accuracy).  A change of engine empties the history ring (the
+ * engines keep it in different layouts). */
 enum { SOD_HISTORY_ENGINE_AUTO = 0, SOD_HISTORY_ENGINE_CUDA_CORES = 1, SOD_HISTORY_ENGINE_TENSOR_CORES = 2 };
 int sod_history_set_engine(sod_history *bank, int engine);
 int sod_history_bytes(const sod_history *bank, int64_t *weight_bytes);

@@ -293,7 +293,8 @@ class HistoryBank:
         L.check(L.load().sod_history_reset(self._h))
 
     def set_engine(self, engine: int) -> None:
-        """L.HISTORY_ENGINE_AUTO (tensor cores for BF16 banks), _CUDA_CORES or _TENSOR_CORES.
+        """L.HISTORY_ENGINE_AUTO (tensor cores for BF16 banks and FP32 banks with R = 16), _CUDA_CORES or
+        _TENSOR_CORES (FP32 banks there use a 3xTF32 split with FP32 accuracy).
         Switching engines empties the history ring."""
         L.check(L.load().sod_history_set_engine(self._h, engine))
 

@@ -20,9 +20,10 @@
 // xor tree; a second kernel sums the column chunks in fixed order and adds the B term in FP64.
 // Results are bitwise reproducible.
 //
-// BF16 banks run on the tensor cores instead (sod_history_tc.cu): with 16 right-hand sides the work is
-// a dense contraction (32 flop per 2-byte weight), with one the tensor cores unpack the BF16 weights
-// for free.  The ring then also keeps the history as BF16 hi + lo terms, transposed for the MMA's
+// BF16 banks, and FP32 banks with 16 right-hand sides, run on the tensor cores instead
+// (sod_history_tc.cu): with 16 right-hand sides the work is a dense contraction (32 flop per
+// weight), and with one the tensor cores unpack the BF16 weights for free.  The ring then also keeps
+// the history as hi + lo terms (BF16, or FP32 with a TF32-exact hi), transposed for the MMA's
 // K-major B operand: [K][2][hi|lo][16][ldw] for R = 16, [K][2][16][ldw] (rows hi, lo, zeros) for R = 1.
 #include <cuda_bf16.h>
 
@@ -46,8 +47,11 @@ struct sod_history {
     DevBuf Xt, tcpart, derr;  // tensor-core path: BF16 hi/lo history, per-segment partials, error word
     int *err_host = nullptr;  // pinned copy of the error word (written by the finish kernel)
     HistTcPlan plan;          // tensor maps of W and Xt
-    bool tensor_ok() const { return wdtype == SOD_BF16; }
-    bool use_tensor() const { return tensor_ok() && engine != SOD_HISTORY_ENGINE_CUDA_CORES; }
+    bool use_tensor() const {
+        if (engine == SOD_HISTORY_ENGINE_AUTO) return wdtype == SOD_BF16 || R == 16;
+        return engine == SOD_HISTORY_ENGINE_TENSOR_CORES;
+    }
+    size_t xt_esz() const { return wdtype == SOD_BF16 ? 2 : 4; }
     int xt_rows() const { return R == 16 ? 2 * 16 : 16; }  // history rows per (slot, G|H)
     ~sod_history() {
         if (err_host) cudaFreeHost(err_host);
@@ -229,12 +233,24 @@ __global__ void hist_pack_kernel(const void *__restrict__ src, int src_f64, int 
     }
 }
 
+// hi + lo split of one history value for the tensor cores: BF16 terms, or FP32 terms whose hi keeps
+// the top 19 bits (exact in TF32; the tensor core reads only those bits of lo as well)
+__device__ __forceinline__ void split_x(double v, __nv_bfloat16 *h, __nv_bfloat16 *l) {
+    *h = __double2bfloat16(v);
+    *l = __double2bfloat16(v - (double)__bfloat162float(*h));
+}
+__device__ __forceinline__ void split_x(double v, float *h, float *l) {
+    *h = __uint_as_float(__float_as_uint((float)v) & 0xffffe000u);
+    *l = (float)(v - (double)*h);
+}
+
 // newest step -> ring slot: x[slot][0] = p, x[slot][1] = u (FP32, zero padded), a[slot] = a;
-// with Xt also the BF16 split x = hi + lo, transposed: Xt[slot][t][hi|lo][j][c] for R = 16,
+// with Xt also the split x = hi + lo, transposed: Xt[slot][t][hi|lo][j][c] for R = 16,
 // Xt[slot][t][0 = hi | 1 = lo][c] for R = 1
+template <class XT>
 __global__ void hist_push_kernel(const double *__restrict__ p, const double *__restrict__ u,
                                  const double *__restrict__ a, int ncol, int ldw, int R, int slot,
-                                 float *__restrict__ X, double *__restrict__ A, __nv_bfloat16 *__restrict__ Xt) {
+                                 float *__restrict__ X, double *__restrict__ A, XT *__restrict__ Xt) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e < ldw * R) {
         const int c = e / R, j = e % R;
@@ -244,9 +260,9 @@ __global__ void hist_push_kernel(const double *__restrict__ p, const double *__r
         if (Xt) {
             for (int t = 0; t < 2; t++) {
                 const double v = c < ncol ? (t == 0 ? p[e] : u[e]) : 0.0;
-                const __nv_bfloat16 hi = __double2bfloat16(v);
-                const __nv_bfloat16 lo = __double2bfloat16(v - (double)__bfloat162float(hi));
-                __nv_bfloat16 *xt = Xt + ((size_t)slot * 2 + t) * (R == 16 ? 32 : 16) * ldw;
+                XT hi, lo;
+                split_x(v, &hi, &lo);
+                XT *xt = Xt + ((size_t)slot * 2 + t) * (R == 16 ? 32 : 16) * ldw;
                 xt[(size_t)j * ldw + c] = hi;
                 xt[(size_t)(R == 16 ? 16 + j : 1) * ldw + c] = lo;
             }
@@ -299,8 +315,8 @@ int sod_history_create(sod_context *ctx, int nrow, int ncol, int K, int R, int w
     h->cchunk = ((steps + h->nchunk - 1) / h->nchunk) * step;
     h->nchunk = (h->ldw + h->cchunk - 1) / h->cchunk;
     SOD_TRY(h->partial.ensure(sizeof(double) * (size_t)h->nchunk * nrow * R));
-    if (h->tensor_ok()) {
-        SOD_TRY(h->Xt.ensure(sizeof(__nv_bfloat16) * (size_t)K * 2 * h->xt_rows() * h->ldw));
+    {  // tensor-core path (either engine can be selected later)
+        SOD_TRY(h->Xt.ensure(h->xt_esz() * (size_t)K * 2 * h->xt_rows() * h->ldw));
         SOD_CHECK_CUDA(cudaMemsetAsync(h->Xt.p, 0, h->Xt.bytes, ctx->stream));
         SOD_TRY(h->tcpart.ensure(sizeof(float) * history_tc_partial_floats(ctx->num_sms, nrow, R)));
         SOD_TRY(h->derr.ensure(sizeof(int)));
@@ -311,7 +327,7 @@ int sod_history_create(sod_context *ctx, int nrow, int ncol, int K, int R, int w
             return SOD_ERR_OOM;
         }
         *h->err_host = 0;
-        SOD_TRY(history_tc_plan(&h->plan, h->W.p, h->Xt.p, nrow, ncol, h->ldw, K, R));
+        SOD_TRY(history_tc_plan(&h->plan, h->W.p, h->Xt.p, nrow, ncol, h->ldw, K, R, weight_dtype == SOD_F32));
     }
     *out = h.release();
     return SOD_OK;
@@ -389,9 +405,14 @@ int sod_history_push(sod_history *h, const double *p, const double *u, const dou
         }
     }
     const int n = h->ldw * h->R;
-    hist_push_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(dp, du, da, h->ncol, h->ldw, h->R, h->head,
-                                                              h->X.as<float>(), h->A.as<double>(),
-                                                              h->use_tensor() ? h->Xt.as<__nv_bfloat16>() : nullptr);
+    if (h->wdtype == SOD_BF16)
+        hist_push_kernel<__nv_bfloat16><<<(n + 255) / 256, 256, 0, ctx->stream>>>(
+            dp, du, da, h->ncol, h->ldw, h->R, h->head, h->X.as<float>(), h->A.as<double>(),
+            h->use_tensor() ? h->Xt.as<__nv_bfloat16>() : nullptr);
+    else
+        hist_push_kernel<float><<<(n + 255) / 256, 256, 0, ctx->stream>>>(
+            dp, du, da, h->ncol, h->ldw, h->R, h->head, h->X.as<float>(), h->A.as<double>(),
+            h->use_tensor() ? h->Xt.as<float>() : nullptr);
     SOD_CHECK_CUDA(cudaGetLastError());
     ctx->count();
     h->head = (h->head + 1) % h->K;
@@ -419,7 +440,7 @@ int sod_history_convolve(sod_history *h, double *b_out) {
                       std::to_string(*(volatile int *)h->err_host) + ")");
             return SOD_ERR_TIMEOUT;
         }
-        SOD_TRY(launch_history_tc(ctx, &h->plan, h->scale.as<float>(), used, h->head, h->tcpart.as<float>(),
+        SOD_TRY(launch_history_tc(ctx, &h->plan, h->wdtype == SOD_BF16 ? h->scale.as<float>() : nullptr, used, h->head, h->tcpart.as<float>(),
                                   h->has_b ? h->Bw.as<double>() : nullptr, h->A.as<double>(), dst, h->derr.as<int>(),
                                   h->err_host, ctx->stream));
         if (host) {
@@ -463,16 +484,13 @@ int sod_history_set_engine(sod_history *h, int engine) {
     SOD_REQUIRE(engine == SOD_HISTORY_ENGINE_AUTO || engine == SOD_HISTORY_ENGINE_CUDA_CORES ||
                     engine == SOD_HISTORY_ENGINE_TENSOR_CORES,
                 "engine must be SOD_HISTORY_ENGINE_AUTO, _CUDA_CORES or _TENSOR_CORES");
-    if (engine == SOD_HISTORY_ENGINE_TENSOR_CORES && !h->tensor_ok()) {
-        set_error("the tensor-core history convolution needs BF16 weights");
-        return SOD_ERR_UNSUPPORTED;
-    }
-    if (h->use_tensor() != (h->tensor_ok() && engine != SOD_HISTORY_ENGINE_CUDA_CORES)) {
+    const bool before = h->use_tensor();
+    h->engine = engine;
+    if (h->use_tensor() != before) {
         // the two engines keep the history in different ring layouts: switching clears the ring
         h->head = 0;
         h->count = 0;
     }
-    h->engine = engine;
     return SOD_OK;
 }
 

@@ -1,4 +1,4 @@
-// sod_history_tc.cu -- tensor-core (tcgen05) history convolution for BF16 banks on sm_103a.
+// sod_history_tc.cu -- tensor-core (tcgen05) history convolution on sm_103a.
 //
 // b[row][r] = sum_seg scale[seg][row] * sum_c W[seg][row][c] * x_seg[c][r]   (seg = (history i, G|-H))
 // is a tall-skinny GEMM per segment: M = nrow, N = R, K = ncol.  With BF16 weights and 16
@@ -23,6 +23,11 @@
 // k neighbouring segments, whose history tiles stay in L2 while the weights stream past.  A second
 // kernel adds a row tile's k partials in FP64 in fixed order (deterministic).  Banks with more row
 // tiles than 2 CTAs per SM (nrow > 2 SMs x 128) run with k = 1 in several waves.
+// FP32 banks (16 right-hand sides) run the same pipeline with 3xTF32 arithmetic and FP32 accuracy:
+// 128 x 32 FP32 weight tiles arrive by TMA; four transform warps split each into w_hi (top 19 bits,
+// exact in TF32) in place and w_lo = w - w_hi into a second tile; the history comes as x_hi + x_lo
+// (x_hi TF32-exact); tcgen05.mma.kind::tf32 accumulates w_hi [x_hi | x_lo] (N = 32) and w_lo x_hi
+// (N = 16, same accumulator columns), dropping only w_lo x_lo (~2^-22 relative).
 // Every mbarrier wait is bounded (about one second of clock); a timeout sets an error flag that the
 // host reports, and the kernel lets its copies and MMAs in flight finish (again bounded) and
 // releases its tensor memory before returning.
@@ -37,14 +42,23 @@
 namespace sod {
 namespace {
 
-constexpr int TC_STAGES = 4;
-constexpr int TC_BM = 128, TC_BK = 64;
-constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;  // 16 KB
-// MMA N (history rows of the B operand: 16 hi + 16 lo, or hi, lo and 14 zero rows) and stage size
+constexpr int TC_MAX_STAGES = 4;
+constexpr int TC_BM = 128;
+constexpr int TC_A_BYTES = TC_BM * 128;  // 128 weight rows of 128 bytes: 16 KB
+// elements per 128-byte row (the K extent of a stage): 64 BF16 or 32 FP32
+template <bool F32> constexpr int tc_bk() { return F32 ? 32 : 64; }
+// MMA N (history rows of the B operand: 16 hi + 16 lo, or hi, lo and 14 zero rows)
 template <int R> constexpr int tc_n() { return R == 16 ? 32 : 16; }
-template <int R> constexpr int tc_stage_bytes() { return TC_A_BYTES + tc_n<R>() * TC_BK * 2; }
-constexpr int TC_THREADS = 192;                     // producer, MMA, 4 epilogue warps
-constexpr int TC_TMEM_COLS = 64;                    // two FP32 accumulators of up to 32 columns
+// stage: weight tile (+ its lo part for FP32) and history tile; 20 / 18 KB BF16, 36 / 34 KB FP32
+template <int R, bool F32> constexpr int tc_stage_bytes() { return TC_A_BYTES * (F32 ? 2 : 1) + tc_n<R>() * 128; }
+template <bool F32> constexpr int tc_stages() { return F32 ? 3 : 4; }  // 2 CTAs per SM either way
+// producer, MMA, 4 epilogue warps (+ 4 warps that split FP32 weight tiles)
+template <bool F32> constexpr int tc_threads() { return F32 ? 320 : 192; }
+template <int R, bool F32> constexpr int tc_smem() { return tc_stages<F32>() * tc_stage_bytes<R, F32>() + 1024; }
+// accumulators per unit: FP32 banks spread the K tiles round-robin over 4 accumulators (shorter
+// accumulation chains inside the tensor core), summed in the epilogue; two units in flight
+template <bool F32> constexpr int tc_ngroups() { return F32 ? 4 : 1; }
+template <bool F32> constexpr int tc_tmem_cols() { return 2 * tc_ngroups<F32>() * 32; }  // 256 / 64
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -107,17 +121,27 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
     return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
            ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
-// instruction descriptor, kind::f16: D F32 (bits 4-5 = 1), A BF16 (bits 7-9 = 1), B BF16
-// (bits 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
-template <int N> constexpr uint32_t tc_idesc() {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+// instruction descriptor: D F32 (bits 4-5 = 1), A and B format at bits 7-9 / 10-12 (kind::f16: BF16 = 1;
+// kind::tf32: TF32 = 2), both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
+template <int N, bool F32> constexpr uint32_t tc_idesc() {
+    return (1u << 4) | ((F32 ? 2u : 1u) << 7) | ((F32 ? 2u : 1u) << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(TC_BM >> 4) << 24);
 }
 
-template <int N> __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-            d_tmem),
-        "l"(a), "l"(b), "r"(tc_idesc<N>()), "r"(accumulate));
+// one MMA, M 128 x N x K 16 (BF16) or K 8 (TF32: FP32 operands of which the tensor core uses the top
+// 19 bits), FP32 accumulate in tensor memory
+template <int N, bool F32>
+__device__ __forceinline__ void mma_tc(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    if constexpr (F32)
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                d_tmem),
+            "l"(a), "l"(b), "r"(tc_idesc<N, true>()), "r"(accumulate));
+    else
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                d_tmem),
+            "l"(a), "l"(b), "r"(tc_idesc<N, false>()), "r"(accumulate));
 }
 // 16 consecutive FP32 columns of this thread's TMEM lane
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *v) {
@@ -134,26 +158,30 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 
 struct TcArgs {
     int nrow, ncol, used, head, K, mt, nseg, k;
-    const float *scale;  // [2K][nrow] (matrix = 2 i + t)
+    const float *scale;  // [2K][nrow] (matrix = 2 i + t); null for FP32 banks
     float *partial;      // [G = k mt][128][R]
     int *err;
 };
 
-template <int R>
-__global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_constant__ CUtensorMap wmap,
-                                                                const __grid_constant__ CUtensorMap xmap,
-                                                                TcArgs a) {
+template <int R, bool F32>
+__global__ void __launch_bounds__(tc_threads<F32>(), 2) hist_tc_kernel(const __grid_constant__ CUtensorMap wmap,
+                                                                       const __grid_constant__ CUtensorMap xmap,
+                                                                       TcArgs a) {
+    constexpr int STAGES = tc_stages<F32>(), BK = tc_bk<F32>(), SB = tc_stage_bytes<R, F32>();
+    constexpr int B_OFF = TC_A_BYTES * (F32 ? 2 : 1);  // history tile offset in a stage (after A and A_lo)
     extern __shared__ uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], acc_full[2], acc_empty[2], drain;
+    __shared__ __align__(8) uint64_t full[TC_MAX_STAGES], empty[TC_MAX_STAGES], ready[TC_MAX_STAGES], acc_full[2],
+        acc_empty[2], drain;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // 1024-byte aligned stage ring (the 128-byte swizzle atoms)
     const uint32_t ring = (smem_u32(smem_raw) + 1023u) & ~1023u;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < TC_STAGES; s++) {
+        for (int s = 0; s < STAGES; s++) {
             mbar_init(smem_u32(&full[s]), 1);
             mbar_init(smem_u32(&empty[s]), 1);
+            mbar_init(smem_u32(&ready[s]), 128);  // FP32: the 128 transform threads
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(smem_u32(&acc_full[b]), 1);
@@ -165,14 +193,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                     "r"(TC_TMEM_COLS));
+                     "r"(tc_tmem_cols<F32>()));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_base;
-    const int KT = (a.ncol + TC_BK - 1) / TC_BK;
+    const int KT = (a.ncol + BK - 1) / BK;
     volatile int *ab = &abort_flag;
     const int m = blockIdx.x % a.mt, seg0 = blockIdx.x / a.mt;  // this CTA's row tile and first segment
 
@@ -182,8 +210,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
             int stage = 0;
             uint32_t phase = 0;
             bool ok = true;
-            int issued[TC_STAGES];  // phase parity of the last load into each stage, -1 = none
-            for (int s = 0; s < TC_STAGES; s++) issued[s] = -1;
+            int issued[TC_MAX_STAGES];  // phase parity of the last load into each stage, -1 = none
+            for (int s = 0; s < STAGES; s++) issued[s] = -1;
             for (int seg = seg0; seg < a.nseg && ok; seg += a.k) {
                 const int i = seg >> 1, t = seg & 1;
                 const int slot = (a.head - 1 - i + 2 * a.K) % a.K;
@@ -191,16 +219,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
                     ok = mbar_wait(smem_u32(&empty[stage]), phase ^ 1u, ab, a.err, 1);
                     if (!ok) break;
                     const uint32_t fb = smem_u32(&full[stage]);
-                    mbar_expect_tx(fb, tc_stage_bytes<R>());
-                    const uint32_t sA = ring + stage * tc_stage_bytes<R>();
-                    tma_load_3d(sA, &wmap, kt * TC_BK, m * TC_BM, seg, fb);
-                    tma_load_2d(sA + TC_A_BYTES, &xmap, kt * TC_BK, (slot * 2 + t) * tc_n<R>(), fb);
+                    mbar_expect_tx(fb, TC_A_BYTES + tc_n<R>() * 128);
+                    const uint32_t sA = ring + stage * SB;
+                    tma_load_3d(sA, &wmap, kt * BK, m * TC_BM, seg, fb);
+                    tma_load_2d(sA + B_OFF, &xmap, kt * BK, (slot * 2 + t) * tc_n<R>(), fb);
                     issued[stage] = (int)phase;
-                    if (++stage == TC_STAGES) stage = 0, phase ^= 1u;
+                    if (++stage == STAGES) stage = 0, phase ^= 1u;
                 }
             }
             if (!ok)  // aborted: let the copies in flight land before shared memory is released
-                for (int s = 0; s < TC_STAGES; s++)
+                for (int s = 0; s < STAGES; s++)
                     if (issued[s] >= 0) mbar_drain(smem_u32(&full[s]), (uint32_t)issued[s]);
         }
     } else if (warp == 1) {
@@ -216,17 +244,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
                 ok = mbar_wait(smem_u32(&acc_empty[buf]), aphase ^ 1u, ab, a.err, 2);
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t d = tmem + buf * 32;
+                constexpr int NG = tc_ngroups<F32>();
                 for (int kt = 0; kt < KT && ok; kt++) {
-                    ok = mbar_wait(smem_u32(&full[stage]), phase, ab, a.err, 3);
+                    // BF16: the TMA tiles; FP32: the tiles after the transform warps split the weights
+                    ok = mbar_wait(smem_u32(F32 ? &ready[stage] : &full[stage]), phase, ab, a.err, 3);
                     if (!ok) break;
                     asm volatile("tcgen05.fence::after_thread_sync;");
-                    const uint32_t sA = ring + stage * tc_stage_bytes<R>();
+                    const uint32_t sA = ring + stage * SB;
+                    // 4 K steps of 32 bytes: K 16 (BF16) or K 8 (TF32) each
 #pragma unroll
-                    for (int k = 0; k < TC_BK / 16; k++)
-                        mma_bf16<tc_n<R>()>(d, smem_desc(sA + k * 32), smem_desc(sA + TC_A_BYTES + k * 32), (kt | k) != 0);
+                    for (int k = 0; k < 4; k++) {
+                        // accumulator of this K tile; the first MMA into it overwrites
+                        const uint32_t d = tmem + (buf * NG + kt % NG) * 32;
+                        mma_tc<tc_n<R>(), F32>(d, smem_desc(sA + k * 32), smem_desc(sA + B_OFF + k * 32),
+                                               (kt >= NG) || (k > 0));
+                        // FP32: W_lo x (x_hi rows; for R = 1 the whole hi/lo tile)
+                        if (F32) mma_tc<16, F32>(d, smem_desc(sA + TC_A_BYTES + k * 32), smem_desc(sA + B_OFF + k * 32), 1u);
+                    }
                     mma_commit(smem_u32(&empty[stage]));  // frees the stage when these MMAs finish
-                    if (++stage == TC_STAGES) stage = 0, phase ^= 1u;
+                    if (++stage == STAGES) stage = 0, phase ^= 1u;
                 }
                 if (ok) mma_commit(smem_u32(&acc_full[buf]));
             }
@@ -234,6 +270,35 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
             mma_commit(smem_u32(&drain));
             if (!mbar_drain(smem_u32(&drain), 0)) atomicExch(a.err, 5);
         }
+    } else if (F32 && warp >= 6) {
+        // ---- FP32 weights: split each tile into w_hi (top 19 bits, exact in TF32) and w_lo = w - w_hi,
+        // in place and into the stage's second weight tile (elementwise, so the swizzle is irrelevant)
+        const int tt = threadIdx.x - 192;
+        int stage = 0;
+        uint32_t phase = 0;
+        bool ok = true;
+        for (int seg = seg0; seg < a.nseg && ok; seg += a.k)
+            for (int kt = 0; kt < KT && ok; kt++) {
+                ok = mbar_wait(smem_u32(&full[stage]), phase, ab, a.err, 6);
+                if (!ok) break;
+                float4 *hi = reinterpret_cast<float4 *>(smem_raw + (ring - smem_u32(smem_raw)) + stage * SB);
+                float4 *lo = hi + TC_A_BYTES / 16;
+#pragma unroll
+                for (int e = tt; e < TC_A_BYTES / 16; e += 128) {
+                    const float4 v = hi[e];
+                    float4 h, l;
+                    h.x = __uint_as_float(__float_as_uint(v.x) & 0xffffe000u), l.x = v.x - h.x;
+                    h.y = __uint_as_float(__float_as_uint(v.y) & 0xffffe000u), l.y = v.y - h.y;
+                    h.z = __uint_as_float(__float_as_uint(v.z) & 0xffffe000u), l.z = v.z - h.z;
+                    h.w = __uint_as_float(__float_as_uint(v.w) & 0xffffe000u), l.w = v.w - h.w;
+                    hi[e] = h;
+                    lo[e] = l;
+                }
+                // make the generic-proxy writes visible to the tensor core (async proxy), then signal
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive(smem_u32(&ready[stage]));
+                if (++stage == STAGES) stage = 0, phase ^= 1u;
+            }
     } else {
         // ---- epilogue: TMEM -> registers -> scaled sum over the CTA's segments ----
         const int q = warp & 3;  // TMEM lane quadrant this warp may access
@@ -247,20 +312,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
             const uint32_t aphase = (ul >> 1) & 1;
             if (!mbar_wait(smem_u32(&acc_full[buf]), aphase, ab, a.err, 4)) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            uint32_t v[32];
-            const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + buf * 32;
-            tmem_ld16(taddr, v);
-            if (R == 16) tmem_ld16(taddr + 16, v + 16);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            constexpr int NG = tc_ngroups<F32>();
+            const int ng = min(NG, KT);  // accumulators this unit wrote
+            float vs[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++) vs[j] = 0.f;
+            for (int gi = 0; gi < ng; gi++) {  // fixed order
+                uint32_t v[32];
+                const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (buf * NG + gi) * 32;
+                tmem_ld16(taddr, v);
+                if (R == 16) tmem_ld16(taddr + 16, v + 16);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int j = 0; j < (R == 16 ? 32 : 16); j++) vs[j] += __uint_as_float(v[j]);
+            }
             asm volatile("tcgen05.fence::before_thread_sync;");
             __syncwarp();
             if (lane == 0) mbar_arrive(smem_u32(&acc_empty[buf]));
-            const float sc = row < a.nrow ? a.scale[(size_t)seg * a.nrow + row] : 0.f;  // a power of two
+            // BF16: the row's power-of-two scale; FP32: unscaled
+            const float sc = row < a.nrow ? (a.scale ? a.scale[(size_t)seg * a.nrow + row] : 1.f) : 0.f;
             if (R == 1) {
-                acc[0] = fmaf(__uint_as_float(v[0]) + __uint_as_float(v[1]), sc, acc[0]);
+                acc[0] = fmaf(vs[0] + vs[1], sc, acc[0]);
             } else {
 #pragma unroll
-                for (int j = 0; j < R; j++) acc[j] = fmaf(__uint_as_float(v[j]) + __uint_as_float(v[16 + j]), sc, acc[j]);
+                for (int j = 0; j < R; j++) acc[j] = fmaf(vs[j] + vs[16 + j], sc, acc[j]);
             }
         }
         float *dst = a.partial + ((size_t)blockIdx.x * TC_BM + q * 32 + lane) * R;
@@ -276,7 +351,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) hist_tc_kernel(const __grid_con
     __syncthreads();
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tc_tmem_cols<F32>()));
     }
 }
 
@@ -316,9 +391,9 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// BF16 tensor map of `rank` dimensions (dims innermost first, byte strides of dims 1.., box extents),
-// 128-byte swizzle, zero fill out of bounds
-int make_map(CUtensorMap *map, const void *base, int rank, const uint64_t *dims, const uint64_t *strides,
+// BF16 or FP32 tensor map of `rank` dimensions (dims innermost first, byte strides of dims 1.., box
+// extents), 128-byte swizzle, zero fill out of bounds
+int make_map(CUtensorMap *map, bool f32, const void *base, int rank, const uint64_t *dims, const uint64_t *strides,
              const uint32_t *box) {
     auto fn = encode_fn();
     if (!fn) {
@@ -329,7 +404,8 @@ int make_map(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
     cuuint32_t bx[3], estr[3] = {1, 1, 1};
     for (int r = 0; r < rank; r++) d[r] = dims[r], bx[r] = box[r];
     for (int r = 0; r + 1 < rank; r++) st[r] = strides[r];
-    const CUresult res = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, const_cast<void *>(base), d, st, bx,
+    const CUresult res = fn(map, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                            (cuuint32_t)rank, const_cast<void *>(base), d, st, bx,
                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (res != CUDA_SUCCESS) {
@@ -352,30 +428,36 @@ size_t history_tc_partial_floats(int num_sms, int nrow, int R) {
     return (size_t)std::max(2 * num_sms, mt) * TC_BM * R;
 }
 
-// Tensor maps of a BF16 bank.  W: [K][2][nrow][ldw] BF16, mapped as {ncol, nrow, 2K} with 128 x 64
-// boxes; Xt: BF16 history, [K][2][hi|lo][16][ldw] for R = 16 and [K][2][16][ldw] (rows hi, lo, then
-// zeros) for R = 1, mapped as {ncol, 2K * N} with N x 64 boxes.
-int history_tc_plan(HistTcPlan *plan, const void *W, const void *Xt, int nrow, int ncol, int ldw, int K, int R) {
+// Tensor maps of a bank.  W: [K][2][nrow][ldw] BF16 or FP32, mapped as {ncol, nrow, 2K} with boxes
+// of 128 rows x 128 bytes; Xt: the history split into hi + lo (BF16, or FP32 with a TF32-exact hi),
+// [K][2][hi|lo][16][ldw] for R = 16 and [K][2][16][ldw] (rows hi, lo, then zeros) for R = 1, mapped
+// as {ncol, 2K * N} with N x 128-byte boxes.
+int history_tc_plan(HistTcPlan *plan, const void *W, const void *Xt, int nrow, int ncol, int ldw, int K, int R,
+                    bool f32) {
     SOD_REQUIRE(ldw % 8 == 0, "tensor-core history: row pitch must be a multiple of 16 bytes");
     SOD_REQUIRE(R == 1 || R == 16, "tensor-core history: 1 or 16 right-hand sides");
     static_assert(sizeof(CUtensorMap) == sizeof(plan->wmap), "CUtensorMap size");
     const int n = R == 16 ? tc_n<16>() : tc_n<1>();
+    const uint64_t esz = f32 ? 4 : 2;
+    const uint32_t bk = f32 ? tc_bk<true>() : tc_bk<false>();
     const uint64_t wdims[3] = {(uint64_t)ncol, (uint64_t)nrow, (uint64_t)K * 2};
-    const uint64_t wstr[2] = {(uint64_t)ldw * 2, (uint64_t)nrow * ldw * 2};
-    const uint32_t wbox[3] = {TC_BK, TC_BM, 1};
-    SOD_TRY(make_map(reinterpret_cast<CUtensorMap *>(plan->wmap), W, 3, wdims, wstr, wbox));
+    const uint64_t wstr[2] = {(uint64_t)ldw * esz, (uint64_t)nrow * ldw * esz};
+    const uint32_t wbox[3] = {bk, TC_BM, 1};
+    SOD_TRY(make_map(reinterpret_cast<CUtensorMap *>(plan->wmap), f32, W, 3, wdims, wstr, wbox));
     const uint64_t xdims[2] = {(uint64_t)ncol, (uint64_t)K * 2 * n};
-    const uint64_t xstr[1] = {(uint64_t)ldw * 2};
-    const uint32_t xbox[2] = {TC_BK, (uint32_t)n};
-    SOD_TRY(make_map(reinterpret_cast<CUtensorMap *>(plan->xmap), Xt, 2, xdims, xstr, xbox));
-    plan->nrow = nrow, plan->ncol = ncol, plan->ldw = ldw, plan->K = K, plan->R = R;
+    const uint64_t xstr[1] = {(uint64_t)ldw * esz};
+    const uint32_t xbox[2] = {bk, (uint32_t)n};
+    SOD_TRY(make_map(reinterpret_cast<CUtensorMap *>(plan->xmap), f32, Xt, 2, xdims, xstr, xbox));
+    plan->nrow = nrow, plan->ncol = ncol, plan->ldw = ldw, plan->K = K, plan->R = R, plan->f32 = f32;
     plan->W = W, plan->Xt = Xt;
     static std::once_flag attr_once;
     static int attr_rc = SOD_OK;
     std::call_once(attr_once, [] {
-        const int s16 = TC_STAGES * tc_stage_bytes<16>() + 1024, s1 = TC_STAGES * tc_stage_bytes<1>() + 1024;
-        if (cudaFuncSetAttribute(hist_tc_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, s16) != cudaSuccess ||
-            cudaFuncSetAttribute(hist_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, s1) != cudaSuccess)
+        const auto A = cudaFuncAttributeMaxDynamicSharedMemorySize;
+        if (cudaFuncSetAttribute(hist_tc_kernel<16, false>, A, tc_smem<16, false>()) != cudaSuccess ||
+            cudaFuncSetAttribute(hist_tc_kernel<1, false>, A, tc_smem<1, false>()) != cudaSuccess ||
+            cudaFuncSetAttribute(hist_tc_kernel<16, true>, A, tc_smem<16, true>()) != cudaSuccess ||
+            cudaFuncSetAttribute(hist_tc_kernel<1, true>, A, tc_smem<1, true>()) != cudaSuccess)
             attr_rc = SOD_ERR_CUDA;
     });
     if (attr_rc != SOD_OK) {
@@ -402,11 +484,15 @@ int launch_history_tc(sod_context *ctx, const HistTcPlan *plan, const float *sca
     a.scale = scale;
     a.partial = partial;
     a.err = err;
-    const size_t smem = (size_t)TC_STAGES * (R == 16 ? tc_stage_bytes<16>() : tc_stage_bytes<1>()) + 1024;
-    auto kern = R == 16 ? hist_tc_kernel<16> : hist_tc_kernel<1>;
+    const bool f = plan->f32;
+    const size_t smem = f ? (R == 16 ? tc_smem<16, true>() : tc_smem<1, true>())
+                          : (R == 16 ? tc_smem<16, false>() : tc_smem<1, false>());
+    auto kern = f ? (R == 16 ? hist_tc_kernel<16, true> : hist_tc_kernel<1, true>)
+                  : (R == 16 ? hist_tc_kernel<16, false> : hist_tc_kernel<1, false>);
+    const int threads = f ? tc_threads<true>() : tc_threads<false>();
     const int grid = a.k * a.mt;
     if (grid > 0) {
-        kern<<<grid, TC_THREADS, smem, stream>>>(wmap, xmap, a);
+        kern<<<grid, threads, smem, stream>>>(wmap, xmap, a);
         SOD_CHECK_CUDA(cudaGetLastError());
         ctx->count();
     }

@@ -234,17 +234,19 @@ int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, i
                              double R, void *out, int out_dtype, cudaStream_t stream);
 KConst<double> make_kconst(double c1, double c2, double rho, double sr, double si);
 KConst<float> to_float(const KConst<double> &k);
-// tensor-core (tcgen05) history convolution of a BF16 bank (1 or 16 right-hand sides).  The plan
+// tensor-core (tcgen05) history convolution of a BF16 or FP32 bank (1 or 16 right-hand sides).  The plan
 // holds the two TMA tensor maps (CUtensorMap, 128 bytes each), encoded once per bank.
 struct HistTcPlan {
     alignas(64) unsigned char wmap[128];
     alignas(64) unsigned char xmap[128];
     int nrow = 0, ncol = 0, ldw = 0, K = 0, R = 0;
     const void *W = nullptr, *Xt = nullptr;
+    bool f32 = false;  // FP32 bank (3xTF32) or BF16 bank
     bool ready = false;
 };
 size_t history_tc_partial_floats(int num_sms, int nrow, int R);
-int history_tc_plan(HistTcPlan *plan, const void *W, const void *Xt, int nrow, int ncol, int ldw, int K, int R);
+int history_tc_plan(HistTcPlan *plan, const void *W, const void *Xt, int nrow, int ncol, int ldw, int K, int R,
+                    bool f32);
 // err: device error word (first expired wait); err_mirror: pinned host word the finish kernel copies it to
 int launch_history_tc(sod_context *ctx, const HistTcPlan *plan, const float *scale, int used, int head,
                       float *partial, const double *Bw, const double *A, double *out, int *err, int *err_mirror,

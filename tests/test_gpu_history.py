@@ -5,7 +5,9 @@ Tolerances (relative Frobenius norm of b):
   FP32 weights : <= 2e-6 (FP32 rounding of weights and history vectors);
   BF16 weights : <= 4e-3 (8-bit significand of the weights; per-row power-of-two scales);
   BF16, tensor cores against CUDA cores on the same bank: <= 3e-5 (the tensor-core path carries the
-  history as two BF16 terms, a 16-bit significand, and accumulates in FP32 in another order)."""
+  history as two BF16 terms, a 16-bit significand, and accumulates in FP32 in another order);
+  FP32 on the tensor cores (3xTF32: w_hi x_hi + w_hi x_lo + w_lo x_hi, 22-bit split operands):
+  the FP32 tolerance, <= 2e-6."""
 import numpy as np
 import pytest
 
@@ -91,14 +93,32 @@ def test_history_bf16_tensor_cores(gpu_ctx, oracle, n, m, K, nsteps, R):
     assert np.array_equal(tc.view(np.uint8), again.view(np.uint8))  # bitwise reproducible
 
 
+@pytest.mark.parametrize("R", [1, 16])
+@pytest.mark.parametrize("n,m,K,nsteps", [(126, 130, 8, 9), (300, 200, 4, 2), (1926, 1926, 24, 30)])
+def test_history_fp32_tensor_cores(gpu_ctx, oracle, n, m, K, nsteps, R):
+    """3xTF32 path for FP32 banks: same shapes as the BF16 case, FP32 tolerance against the oracle."""
+    from surfaceonlydeformables_gb300 import _lib as L
+
+    tc, ref, bank = run(gpu_ctx, oracle, n, m, K, R, L.F32, nsteps, with_b=True, seed=9,
+                        engine=L.HISTORY_ENGINE_TENSOR_CORES)
+    cc, _, _ = run(gpu_ctx, oracle, n, m, K, R, L.F32, nsteps, with_b=True, seed=9,
+                   engine=L.HISTORY_ENGINE_CUDA_CORES)
+    assert rel_fro(tc, ref) <= 2e-6, rel_fro(tc, ref)
+    assert rel_fro(cc, ref) <= 2e-6
+    again = bank.convolve()
+    assert np.array_equal(tc.view(np.uint8), again.view(np.uint8))  # bitwise reproducible
+
+
 def test_history_engine_selection(gpu_ctx):
     from surfaceonlydeformables_gb300 import _lib as L
     from surfaceonlydeformables_gb300 import api
 
-    f32 = api.HistoryBank(gpu_ctx, 10, 10, 2, 16, L.F32)
-    with pytest.raises(L.SodError) as e:
-        f32.set_engine(L.HISTORY_ENGINE_TENSOR_CORES)
-    assert e.value.code == L.SOD_ERR_UNSUPPORTED
+    f32 = api.HistoryBank(gpu_ctx, 10, 10, 2, 16, L.F32)  # AUTO: tensor cores (3xTF32)
+    f32.set_weights(1, 2.0 * np.eye(10), np.zeros((10, 10)))
+    f32.push(np.ones((10, 16)), np.zeros((10, 16)))
+    assert np.allclose(f32.convolve(), 2.0)
+    f32.set_engine(L.HISTORY_ENGINE_TENSOR_CORES)  # same engine as AUTO here: the ring is kept
+    assert np.allclose(f32.convolve(), 2.0)
     bf = api.HistoryBank(gpu_ctx, 10, 10, 2, 16, L.BF16)
     bf.set_weights(1, np.eye(10), np.zeros((10, 10)))
     bf.push(np.ones((10, 16)), np.zeros((10, 16)))
