@@ -258,16 +258,18 @@ def elastostatic_leg(torch, ctx, stream):
     mat = Material(1e5, 0.45, 1000.0)
     out = torch.empty((3 * m.nV, 3 * m.nV), dtype=torch.float64, device="cuda")
     res = {}
-    for kind in ("G", "H"):
-        api.elastostatic(ctx, dm, kind, mat, out=out)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        api.elastostatic(ctx, dm, kind, mat, out=out)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        res[kind] = {"ms": round(e0.elapsed_time(e1), 3), "entries_per_s": (3 * m.nV) ** 2 / (e0.elapsed_time(e1) * 1e-3)}
-    return {"mesh": f"icosphere level 4, {m.nV} vertices, jittered", **res}
+    for method, tag in ((L.COLLOCATION, ""), (L.GALERKIN, "galerkin_")):
+        for kind in ("G", "H"):
+            api.elastostatic(ctx, dm, kind, mat, method=method, out=out)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            api.elastostatic(ctx, dm, kind, mat, method=method, out=out)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            res[tag + kind] = {"ms": round(ms, 3), "entries_per_s": (3 * m.nV) ** 2 / (ms * 1e-3)}
+    return {"mesh": f"icosphere level 4, {m.nV} vertices, jittered", "rule": "7-point regular, singular order 5", **res}
 
 
 def galerkin_leg(torch, ctx, stream, nfreq: int = 2, rows=(0, 517, 1280, 2561)):

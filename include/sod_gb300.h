@@ -178,11 +178,13 @@ int sod_batch_profile(sod_batch *batch, int cap, int *which, double *evals, floa
 int sod_batch_destroy(sod_batch *batch);
 
 /* ---- elastostatic BEM matrices ----------------------------------------------------------------- */
-/* Replaces ElasticsBEMMatrixCollection::compute_elastostatic_{G,H}_matrix_collocation
- * (src/elastics_bem_matrix_collection.cpp:43-243): the Kelvin single- and double-layer matrices,
- * 3nV x 3nV row-major, H with the rigid-mode diagonal correction H_ii = -sum_{j != i} H_ij.
- * Regular faces in FP32, singular faces and the correction in FP64.  out: SOD_F64 or SOD_F32, host
- * or device.  method: SOD_COLLOCATION. */
+/* Replaces ElasticsBEMMatrixCollection::compute_elastostatic_{G,H}_matrix_{collocation,galerkin}
+ * (src/elastics_bem_matrix_collection.cpp:43-385): the Kelvin single- and double-layer matrices,
+ * 3nV x 3nV row-major, H with the rigid-mode diagonal correction H_ii = -sum_{j != i} H_ij (Galerkin
+ * H also with the mass matrix C added first, as the reference does).  Regular faces / face pairs in
+ * FP32, singular ones and the correction in FP64 (double-float Sauter-Schwab pairs for Galerkin;
+ * the reference integrates those with the regular order: pass sorder = order, ssub = subdiv for
+ * parity).  out: SOD_F64 or SOD_F32, host or device.  method: SOD_COLLOCATION or SOD_GALERKIN. */
 int sod_elastostatic_assemble(sod_context *ctx, const sod_mesh *mesh, int kind, int method, double nu, double mu,
                               int order, int subdiv, int sorder, int ssub, void *out, int out_dtype);
 

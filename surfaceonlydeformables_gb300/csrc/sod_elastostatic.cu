@@ -1,7 +1,7 @@
-// sod_elastostatic.cu -- elastostatic (Kelvin) collocation BEM matrices G and H on sm_103a.
+// sod_elastostatic.cu -- elastostatic (Kelvin) BEM matrices G and H on sm_103a.
 //
-// Replaces ElasticsBEMMatrixCollection::compute_elastostatic_{G,H}_matrix_collocation
-// (src/elastics_bem_matrix_collection.cpp:43-243):
+// Replaces ElasticsBEMMatrixCollection::compute_elastostatic_{G,H}_matrix_{collocation,galerkin}
+// (src/elastics_bem_matrix_collection.cpp:43-385):
 //   u*_pq = [(3 - 4 nu) d_pq + rh_p rh_q] / (16 pi (1 - nu) mu r)
 //   p*_pq = C [(rh_p n_q - rh_q n_p) - (d_pq + 3 rh_p rh_q / (1 - 2 nu)) rh.n] / r^2,
 //           C = (1 - 2 nu) / (8 pi (1 - nu))
@@ -11,6 +11,15 @@
 // walked in colour order (no two faces of a colour share a vertex: conflict-free, fixed order).
 // Singular faces: FP64 polar / Guiggiani rules from the mesh's geometry tables (sod_singular.cu),
 // added in the epilogue.  The diagonal correction sums the finished row in FP64 in fixed order.
+//
+// Galerkin: the Laplace-domain kernels at s = 0 are exactly the Kelvin kernels -- with rho = 1,
+// c2^2 = mu, c1^2 = lambda + 2 mu, G's alpha = 1/(16 pi mu (1 - nu) r), beta = (3 - 4 nu) alpha and
+// H's a = kappa, b = -kappa, d = -3 (1 - kappa) over 4 pi r^2 (kappa = c2^2 / c1^2) -- and at
+// z = 0 the psi series gives exactly -1/2 and e^-z exactly 1.  So the Galerkin path
+// (sod_galerkin.cu: test-point rows, fixed-order gather, pair-shared double-float singular pairs)
+// runs at s = 0 into a complex128 scratch matrix, and a finishing kernel takes the real part, adds
+// the Galerkin mass matrix C (:372-373, 447-467) to H and applies H_ii = -sum_{j != i} H_ij
+// (:375-382) in FP64 in fixed order.
 #include <algorithm>
 
 #include "sod_faces.cuh"
@@ -170,7 +179,106 @@ __global__ void __launch_bounds__(512) static_scatter_kernel(StaticArgs a, Point
     }
 }
 
+// Galerkin finish: one warp per row r = 3 i + p of the 3V x 3V matrix.  out = Re(scratch); for H,
+// the off-diagonal mass-matrix entries C[3i+p][3j+p] = sum of A_f / 48 over the faces f holding
+// both i and j (A_f: twice the face area, as igl::doublearea) are added, and the diagonal block
+// becomes minus the sum of the row's off-diagonal blocks (C's diagonal entries are overwritten
+// there, as in the reference).
+template <int KIND>
+__global__ void __launch_bounds__(256) static_gal_finish_kernel(const double2 *__restrict__ scr, int nV,
+                                                                const double *__restrict__ V,
+                                                                const int *__restrict__ F,
+                                                                const int *__restrict__ star_off,
+                                                                const int *__restrict__ star_face, void *out,
+                                                                int out_f32) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const long long n3 = 3LL * nV;
+    if (warp >= n3) return;
+    const int r = warp, i = r / 3, p = r % 3;
+    const double2 *row = scr + (long long)r * n3;
+    const long long base = (long long)r * n3;
+    double d[3] = {0.0, 0.0, 0.0};  // sums over j != i of the row's column q = 3 j + qq entries
+    for (long long c = lane; c < n3; c += 32) {
+        const int j = (int)(c / 3), qq = (int)(c % 3);
+        const double v = row[c].x;
+        if (KIND == SOD_H && j == i) continue;
+        put(out, out_f32, base + c, v);
+        if (KIND == SOD_H) d[qq] += v;
+    }
+    if (KIND == SOD_H) {
+#pragma unroll
+        for (int q = 0; q < 3; q++)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) d[q] += __shfl_xor_sync(0xffffffffu, d[q], o);
+        __syncwarp();  // the lanes' stores above come before lane 0 rewrites the mass-matrix entries
+        if (lane == 0) {
+            // mass matrix: the row's off-diagonal entries 3 j + p for j in a face with i
+            const int s0 = star_off[i], s1 = star_off[i + 1];
+            double cdiag = 0.0;
+            for (int s = s0; s < s1; s++) {
+                const int f = star_face[s];
+                for (int c = 0; c < 3; c++) {
+                    const int j = F[3 * f + c];
+                    if (j == i) continue;
+                    double cij = 0.0;  // all faces of i's star holding j, in star order
+                    for (int t = s0; t < s1; t++) {
+                        const int g = star_face[t];
+                        if (F[3 * g] != j && F[3 * g + 1] != j && F[3 * g + 2] != j) continue;
+                        const double *a = V + 3 * F[3 * g], *b = V + 3 * F[3 * g + 1], *e = V + 3 * F[3 * g + 2];
+                        const double u0 = b[0] - a[0], u1 = b[1] - a[1], u2 = b[2] - a[2];
+                        const double w0 = e[0] - a[0], w1 = e[1] - a[1], w2 = e[2] - a[2];
+                        const double x = u1 * w2 - u2 * w1, y = u2 * w0 - u0 * w2, z = u0 * w1 - u1 * w0;
+                        cij += sqrt(x * x + y * y + z * z) / 48.0;
+                    }
+                    put(out, out_f32, base + 3LL * j + p, row[3LL * j + p].x + cij);
+                }
+                const double *a = V + 3 * F[3 * f], *b = V + 3 * F[3 * f + 1], *e = V + 3 * F[3 * f + 2];
+                const double u0 = b[0] - a[0], u1 = b[1] - a[1], u2 = b[2] - a[2];
+                const double w0 = e[0] - a[0], w1 = e[1] - a[1], w2 = e[2] - a[2];
+                const double x = u1 * w2 - u2 * w1, y = u2 * w0 - u0 * w2, z = u0 * w1 - u1 * w0;
+                cdiag += 2.0 * sqrt(x * x + y * y + z * z) / 48.0;  // the two other corners of f
+            }
+            for (int q = 0; q < 3; q++) put(out, out_f32, base + 3LL * i + q, -(d[q] + (q == p ? cdiag : 0.0)));
+        }
+    }
+}
+
 }  // namespace
+
+// Galerkin elastostatic G or H (see the file comment).
+static int elastostatic_galerkin(sod_context *ctx, const sod_mesh *m, int kind, double nu, double mu, int order,
+                                 int subdiv, int sorder, int ssub, void *dst, int out_dtype) {
+    const int nV = m->nV;
+    const long long n3 = 3LL * nV;
+    SOD_TRY(ctx->freqbuf.ensure(sizeof(double2) * (size_t)(n3 * n3)));
+    const double lam = 2.0 * nu * mu / (1.0 - 2.0 * nu);
+    KConst<double> k0 = make_kconst(std::sqrt(lam + 2.0 * mu), std::sqrt(mu), 1.0, 0.0, 0.0);
+    k0.isr = k0.isi = 0.0;  // 1/s: used by B_angular only
+    CollLaunch L{};
+    L.mesh = m;
+    L.kind_mask = 1 << kind;
+    L.nfreq = 1;
+    L.kc_host = &k0;
+    L.order = order, L.subdiv = subdiv, L.sorder = sorder, L.ssub = ssub;
+    L.parts = SOD_PART_ALL;
+    L.out[kind] = ctx->freqbuf.p;
+    L.out_dtype = SOD_C128;
+    for (int kd = 0; kd < 4; kd++) L.freq_stride[kd] = kd <= SOD_H ? n3 * n3 : 0;
+    L.stream = ctx->stream;
+    SOD_TRY(launch_galerkin(ctx, L));
+    const int blocks = (int)((n3 * 32 + 255) / 256);
+    if (kind == SOD_G)
+        static_gal_finish_kernel<SOD_G><<<blocks, 256, 0, ctx->stream>>>(
+            ctx->freqbuf.as<double2>(), nV, m->dV.as<double>(), m->dF.as<int>(), m->dStarOff.as<int>(),
+            m->dStarFace.as<int>(), dst, out_dtype == SOD_F32);
+    else
+        static_gal_finish_kernel<SOD_H><<<blocks, 256, 0, ctx->stream>>>(
+            ctx->freqbuf.as<double2>(), nV, m->dV.as<double>(), m->dF.as<int>(), m->dStarOff.as<int>(),
+            m->dStarFace.as<int>(), dst, out_dtype == SOD_F32);
+    SOD_CHECK_CUDA(cudaGetLastError());
+    ctx->count();
+    return SOD_OK;
+}
 
 extern "C" int sod_elastostatic_assemble(sod_context *ctx, const sod_mesh *m, int kind, int method, double nu,
                                          double mu, int order, int subdiv, int sorder, int ssub, void *out,
@@ -181,11 +289,23 @@ extern "C" int sod_elastostatic_assemble(sod_context *ctx, const sod_mesh *m, in
     SOD_REQUIRE(out_dtype == SOD_F64 || out_dtype == SOD_F32, "output dtype must be SOD_F64 or SOD_F32");
     SOD_REQUIRE(nu > -1.0 && nu < 0.5 && mu > 0.0 && std::isfinite(mu), "need -1 < nu < 1/2 and mu > 0");
     SOD_REQUIRE(sorder >= 1 && sorder <= 5 && ssub >= 1 && ssub <= 8, "singular quadrature order must be 1..5, subdivision 1..8");
-    if (method != SOD_COLLOCATION) {
-        set_error("Galerkin elastostatic assembly is not available in this build");
-        return SOD_ERR_UNSUPPORTED;
-    }
+    SOD_REQUIRE(method == SOD_COLLOCATION || method == SOD_GALERKIN, "method must be collocation or Galerkin");
     SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
+    if (method == SOD_GALERKIN) {
+        const bool host = !is_device_pointer(out);
+        const size_t esz = out_dtype == SOD_F64 ? 8 : 4, bytes = esz * 9 * (size_t)m->nV * m->nV;
+        void *dst = out;
+        if (host) {
+            SOD_TRY(ctx->staging.ensure(bytes));
+            dst = ctx->staging.p;
+        }
+        SOD_TRY(elastostatic_galerkin(ctx, m, kind, nu, mu, order, subdiv, sorder, ssub, dst, out_dtype));
+        if (host) {
+            SOD_CHECK_CUDA(cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+            SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+        }
+        return SOD_OK;
+    }
     PointTable pt;
     SOD_TRY(make_point_table(order, subdiv, pt));
     const int nV = m->nV;
