@@ -70,3 +70,31 @@ def test_precompute_accuracy_vs_fp64(oracle, setup):
         print(f"{k}: GPU stacked err {e:.2e}, reference-mixed {rel_fro(mix[k], ref[k]):.2e}")
         assert e <= 3 * fp32_level, (k, e, fp32_level)
         assert rel_fro(got[k][0], ref[k][0]) <= 1e-5, k
+
+
+def test_precompute_galerkin_pipeline_exact(gpu_ctx, oracle, sodlib):
+    """Galerkin path: H_0 gets the Galerkin mass matrix (src/elastodynamics_cqbem_H.cu:184-186,
+    src/elastics_bem_matrix_collection.cpp:447-467); the pipeline on the GPU's own Galerkin
+    Laplace-domain matrices agrees to <= 1e-10."""
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    m = make_icosphere_mesh(1, 0.1)
+    dm = api.Mesh(gpu_ctx, m)
+    N, dt = 8, 0.01
+    s, R, Lq = sodlib.cq_frequencies(2, dt, N)
+    cm = (0.0, 0.0, 0.0)
+    got = {k: v.cpu().numpy() for k, v in api.precompute(gpu_ctx, dm, MAT, 2, dt, N, order=4, sorder=4,
+                                                         method=L.GALERKIN, cm=cm).items()}
+    # the same all-kinds call the precompute makes (same fused passes, so the same FP32 sums)
+    X = api.assemble_all(gpu_ctx, dm, MAT, s, order=4, sorder=4, method=L.GALERKIN)
+    X["B_angular"] = X["B_angular"].reshape(len(s), 3 * m.nV, 3, 3)
+    nV = m.nV
+    ref = {k: oracle.inverse_transform(X[k], Lq, R) for k in KINDS}
+    ref["H"][0] += oracle.c_matrix_galerkin(m)
+    Ba = ref["B_angular"].reshape(Lq, 3 * nV, 3, 3)
+    Ba = np.stack([oracle.b_angular_shift(Ba[n], ref["B_trans"][n], m.V, np.asarray(cm)) for n in range(Lq)])
+    ref["B_angular"] = Ba
+    ref["B_euler"] = np.stack([oracle.b_euler(Ba[n]) for n in range(Lq)])
+    for k in ("G", "H", "B_trans", "B_angular", "B_euler"):
+        assert rel_fro(got[k], ref[k]) <= 1e-10, (k, rel_fro(got[k], ref[k]))
