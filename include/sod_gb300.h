@@ -216,6 +216,21 @@ int sod_history_set_engine(sod_history *bank, int engine);
 int sod_history_bytes(const sod_history *bank, int64_t *weight_bytes);
 int sod_history_destroy(sod_history *bank);
 
+/* ---- the reference's matrix files ------------------------------------------------------------ */
+/* Eigen::save_matrix / load_matrix format (include/matrix_io.hpp:14-61): int64 rows, int64 cols,
+ * then the row-major doubles.  data: host or device, SOD_F64 or SOD_F32 (written as doubles).
+ * sod_mat_read reads into FP64 (host or device) and checks the dimensions.  ctx may be NULL when
+ * data is host memory. */
+int sod_mat_write(sod_context *ctx, const char *path, const void *data, int64_t rows, int64_t cols, int dtype);
+int sod_mat_read(sod_context *ctx, const char *path, void *data, int64_t rows, int64_t cols);
+/* The time-domain cache of ElastodynamicsCQBEMMatrixCollection::init
+ * (src/elastodynamics_cqbem_matrix_collection.cpp:76-176) in `folder`: G_k.mat, H_k.mat (3V x 3V,
+ * H as computed, before the reference's negation at load) and B_k.mat = [B_trans_k | B_euler_k]
+ * (3V x 6), k = 0..L-1, from sod_cqbem_precompute's outputs ([L][...], host or device, SOD_F64 or
+ * SOD_F32).  Any of G, H, (B_trans, B_euler) may be NULL.  The folder must exist. */
+int sod_cqbem_write_cache(sod_context *ctx, const char *folder, int nV, int L, const void *G, const void *H,
+                          const void *B_trans, const void *B_euler, int dtype);
+
 /* ---- request loop (continuous batching) ------------------------------------------------------ */
 /* A server owns `slots` assembly contexts and one step context on `device`.  Assembly requests
  * build a resident object (CQ precompute of G_k, H_k, k = 1..N, into an FP32 history bank, BDF

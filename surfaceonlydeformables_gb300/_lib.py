@@ -76,6 +76,9 @@ _SIGS = {
     "sod_history_push": ([_P, _P, _P, _P], _c.c_int),
     "sod_history_convolve": ([_P, _P], _c.c_int),
     "sod_history_reset": ([_P], _c.c_int),
+    "sod_mat_write": ([_P, _c.c_char_p, _P, _c.c_int64, _c.c_int64, _c.c_int], _c.c_int),
+    "sod_mat_read": ([_P, _c.c_char_p, _P, _c.c_int64, _c.c_int64], _c.c_int),
+    "sod_cqbem_write_cache": ([_P, _c.c_char_p, _c.c_int, _c.c_int, _P, _P, _P, _P, _c.c_int], _c.c_int),
     "sod_history_set_engine": ([_P, _c.c_int], _c.c_int),
     "sod_history_bytes": ([_P, _P], _c.c_int),
     "sod_history_destroy": ([_P], _c.c_int),

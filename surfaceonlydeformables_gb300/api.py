@@ -250,6 +250,31 @@ def elastostatic(ctx: Context, mesh: Mesh, kind: str, mat: Material, order: int 
     return out
 
 
+def mat_write(ctx, path: str, M) -> None:
+    """Matrix (2-D numpy array or CUDA tensor, float64/float32) to the reference's .mat file format.
+    ctx may be None for host arrays."""
+    M = M if hasattr(M, "data_ptr") else np.ascontiguousarray(M)
+    dt = L.F32 if str(M.dtype) in ("float32", "torch.float32") else L.F64
+    L.check(L.load().sod_mat_write(ctx.handle if ctx else None, path.encode(), L.ptr(M), M.shape[0], M.shape[1], dt))
+
+
+def mat_read(ctx, path: str, rows: int, cols: int) -> np.ndarray:
+    out = np.empty((rows, cols), dtype=np.float64)
+    L.check(L.load().sod_mat_read(ctx.handle if ctx else None, path.encode(), L.ptr(out), rows, cols))
+    return out
+
+
+def write_cache(ctx: Context, folder: str, nV: int, weights: dict) -> None:
+    """sod_cqbem_write_cache: `weights` as returned by precompute() (G, H, B_trans, B_euler; any
+    subset, B_trans with B_euler)."""
+    ref = next(iter(weights.values()))
+    dt = L.F32 if str(ref.dtype) in ("float32", "torch.float32") else L.F64
+    L_ = ref.shape[0]
+    p = {k: (L.ptr(weights[k]) if k in weights else None) for k in ("G", "H", "B_trans", "B_euler")}
+    L.check(L.load().sod_cqbem_write_cache(ctx.handle, folder.encode(), nV, L_, p["G"], p["H"], p["B_trans"],
+                                           p["B_euler"], dt))
+
+
 class HistoryBank:
     """Device-resident history convolution of one object (sod_history): G_k, -H_k (k = 1..K) as FP32
     or BF16 + per-row scales, a ring of the last K steps' vectors, b = sum G p - H u + B a."""

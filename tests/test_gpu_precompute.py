@@ -98,3 +98,23 @@ def test_precompute_galerkin_pipeline_exact(gpu_ctx, oracle, sodlib):
     ref["B_euler"] = np.stack([oracle.b_euler(Ba[n]) for n in range(Lq)])
     for k in ("G", "H", "B_trans", "B_angular", "B_euler"):
         assert rel_fro(got[k], ref[k]) <= 1e-10, (k, rel_fro(got[k], ref[k]))
+
+
+def test_write_cache_matches_precompute(gpu_ctx, setup, tmp_path):
+    """sod_cqbem_write_cache writes the reference's cache files (G_k, H_k, B_k = [B_trans | B_euler],
+    src/elastodynamics_cqbem_matrix_collection.cpp:76-176) from device-resident precompute outputs."""
+    from surfaceonlydeformables_gb300 import api
+
+    m, dm, s, R, L, cm, got = setup
+    import torch
+
+    w = {k: torch.from_numpy(got[k]).cuda() for k in ("G", "H", "B_trans", "B_euler")}
+    api.write_cache(gpu_ctx, str(tmp_path), m.nV, w)
+    n3 = 3 * m.nV
+    for k in (0, L // 2, L - 1):
+        for name in ("G", "H"):
+            raw = open(tmp_path / f"{name}_{k}.mat", "rb").read()
+            assert np.frombuffer(raw[:16], dtype=np.int64).tolist() == [n3, n3]
+            assert np.array_equal(np.frombuffer(raw[16:], dtype=np.float64).reshape(n3, n3), got[name][k])
+        B = api.mat_read(gpu_ctx, str(tmp_path / f"B_{k}.mat"), n3, 6)
+        assert np.array_equal(B[:, :3], got["B_trans"][k]) and np.array_equal(B[:, 3:], got["B_euler"][k])

@@ -65,3 +65,24 @@ def test_no_device_fails_loudly(sodlib):
 
     with pytest.raises(sodlib.SodError):
         Context(0)
+
+
+def test_mat_file_format_roundtrip(sodlib, tmp_path):
+    """sod_mat_write / sod_mat_read use Eigen::save_matrix's layout (include/matrix_io.hpp:14-61):
+    int64 rows, int64 cols, row-major doubles (the reference's matrices are row-major)."""
+    import numpy as np
+
+    from surfaceonlydeformables_gb300 import api
+
+    rng = np.random.default_rng(1)
+    M = rng.normal(size=(7, 5))
+    p = str(tmp_path / "M.mat")
+    api.mat_write(None, p, M)
+    raw = open(p, "rb").read()
+    assert np.frombuffer(raw[:16], dtype=np.int64).tolist() == [7, 5]
+    assert np.array_equal(np.frombuffer(raw[16:], dtype=np.float64).reshape(7, 5), M)
+    assert np.array_equal(api.mat_read(None, p, 7, 5), M)
+    api.mat_write(None, p, M.astype(np.float32))  # FP32 input is written as doubles
+    assert np.array_equal(api.mat_read(None, p, 7, 5), M.astype(np.float32).astype(np.float64))
+    with pytest.raises(sodlib.SodError):
+        api.mat_read(None, p, 5, 7)  # wrong dimensions are rejected
