@@ -272,6 +272,79 @@ def elastostatic_leg(torch, ctx, stream):
     return {"mesh": f"icosphere level 4, {m.nV} vertices, jittered", "rule": "7-point regular, singular order 5", **res}
 
 
+def solve_leg(torch, ctx, stream, n: int = 7686, K: int = 8):
+    """Dense FP64 solves of the 2562-vertex object's size (3V = 7686): the H_0 LU, u_p = H_0^-1 G'
+    (3V right-hand sides), the explicit inverse, and one served step u = H_0^-1 b fused after a
+    K-step FP32 history convolution (1 and 16 right-hand sides).  Synthetic, well-conditioned
+    matrices of that size stand in for H_0 and G'."""
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(5)
+    A = torch.randn((n, n), dtype=torch.float64, device="cuda", generator=gen) + n ** 0.5 * torch.eye(
+        n, dtype=torch.float64, device="cuda")
+    G = torch.randn((n, n), dtype=torch.float64, device="cuda", generator=gen)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), r
+
+    try:
+        api.Solver(ctx, torch.eye(8, dtype=torch.float64, device="cuda")).close()  # library load, handles
+        ms_lu, S = timed(lambda: api.Solver(ctx, A))
+    except L.SodError as e:
+        return {"unavailable": str(e)}
+    X = torch.empty_like(G)
+    S.solve(G, out=X)
+    ms_up, _ = timed(lambda: S.solve(G, out=X))
+    ms_inv, _ = timed(lambda: S.inverse(out=X))
+    res = {"n": n, "lu_ms": round(ms_lu, 2), "lu_tflops_fp64": round(2 / 3 * n ** 3 / ms_lu / 1e9, 3),
+           "u_p_solve_ms": round(ms_up, 2), "inverse_ms": round(ms_inv, 2)}
+    del X, G
+    for R in (1, 16):
+        bank = api.HistoryBank(ctx, n, n, K, R, L.F32)
+        w = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        for k in range(1, K + 1):
+            w.normal_(0.0, 0.8 ** k, generator=gen)
+            bank.set_weights(k, w, w)
+        shape = (n, R) if R > 1 else (n,)
+        for _ in range(K):
+            bank.push(torch.randn(shape, dtype=torch.float64, device="cuda", generator=gen),
+                      torch.randn(shape, dtype=torch.float64, device="cuda", generator=gen))
+        out = torch.empty(shape, dtype=torch.float64, device="cuda")
+        bank.convolve_solve(S, out)
+        ms_c, _ = timed(lambda: bank.convolve(out))
+        ms_cs, _ = timed(lambda: bank.convolve_solve(S, out))
+        res[f"step_rhs{R}"] = {"convolve_ms": round(ms_c, 3), "convolve_lu_solve_ms": round(ms_cs, 3)}
+        bank.close()
+        del w, out
+    S.keep_inverse()
+    for R in (1, 16):
+        bank = api.HistoryBank(ctx, n, n, K, R, L.F32)
+        w = torch.empty((n, n), dtype=torch.float32, device="cuda")
+        for k in range(1, K + 1):
+            w.normal_(0.0, 0.8 ** k, generator=gen)
+            bank.set_weights(k, w, w)
+        shape = (n, R) if R > 1 else (n,)
+        for _ in range(K):
+            bank.push(torch.randn(shape, dtype=torch.float64, device="cuda", generator=gen),
+                      torch.randn(shape, dtype=torch.float64, device="cuda", generator=gen))
+        out = torch.empty(shape, dtype=torch.float64, device="cuda")
+        bank.convolve_solve(S, out)
+        ms_ci, _ = timed(lambda: bank.convolve_solve(S, out))
+        res[f"step_rhs{R}"]["convolve_inverse_gemv_ms"] = round(ms_ci, 3)
+        bank.close()
+        del w, out
+    S.close()
+    return res
+
+
 def galerkin_leg(torch, ctx, stream, nfreq: int = 2, rows=(0, 517, 1280, 2561)):
     """Galerkin G and H of the 2562-vertex jittered icosphere (configs[1]: E 1e5, nu 0.45, dt 1/200,
     N = 64 -> 33 Laplace frequencies; 13-point rule for regular pairs, Sauter-Schwab order 5 for the
@@ -620,6 +693,7 @@ def run_gpu(args):
         extra["history_convolution"] = history_leg(torch, ctx, stream)
         extra["elastostatic"] = elastostatic_leg(torch, ctx, stream)
         extra["galerkin"] = galerkin_leg(torch, ctx, stream)
+        extra["dense_solve"] = solve_leg(torch, ctx, stream)
         if not args.no_serve:
             extra["serving"] = serving_leg(torch, ctx)
 
@@ -677,6 +751,8 @@ def run_leg(args):
         out = elastostatic_leg(torch, ctx, stream)
     elif args.leg == "galerkin":
         out = galerkin_leg(torch, ctx, stream)
+    elif args.leg == "solve":
+        out = solve_leg(torch, ctx, stream)
     else:
         out = serving_leg(torch, ctx)
     print(json.dumps({"leg": args.leg, **out}))
@@ -692,7 +768,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop leg")
-    ap.add_argument("--leg", default="all", choices=["all", "history", "elastostatic", "galerkin", "serving"],
+    ap.add_argument("--leg", default="all", choices=["all", "history", "elastostatic", "galerkin", "serving", "solve"],
                     help="run one hot-path leg alone (profiling captures) and print its JSON")
     ap.add_argument("--history-k", type=int, default=64, help="history length of the --leg history bank")
     ap.add_argument("--value-only", action="store_true",

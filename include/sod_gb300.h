@@ -216,6 +216,27 @@ int sod_history_set_engine(sod_history *bank, int engine);
 int sod_history_bytes(const sod_history *bank, int64_t *weight_bytes);
 int sod_history_destroy(sod_history *bank);
 
+/* ---- dense solves downstream of the assembly ------------------------------------------------- */
+/* Replace the Eigen::PartialPivLU uses of ElastodynamicsCQBEMMatrixCollection::init
+ * (src/elastodynamics_cqbem_matrix_collection.cpp:200-214: H_inv.compute(H_0), u_p = H_inv.solve(G'),
+ * H_inv_B_trans / H_inv_B_euler, H_inv.inverse()) and the per-step H_inv.solve(b)
+ * (src/elastodynamics_cqbem_object.cpp:63): LU with partial pivoting in FP64 on the device
+ * (cuSOLVER, loaded at first use: SOD_ERR_UNSUPPORTED if it is not installed).  All matrices are
+ * row-major FP64, host or device.  A singular matrix gives SOD_ERR_INVALID_ARG. */
+typedef struct sod_solver sod_solver;
+int sod_solver_create(sod_context *ctx, int n, const double *A, sod_solver **solver);
+/* X = A^-1 B, B and X n x nrhs (X may alias B). */
+int sod_solver_solve(sod_solver *solver, int nrhs, const double *B, double *X);
+/* A^-1, n x n. */
+int sod_solver_inverse(sod_solver *solver, double *Ainv);
+/* Keeps A^-1 on the device (n^2 doubles), as the reference's H_inv.inverse(): the per-step
+ * sod_history_convolve_solve then applies it as one FP64 GEMV instead of two triangular solves. */
+int sod_solver_keep_inverse(sod_solver *solver);
+int sod_solver_destroy(sod_solver *solver);
+/* One served time step on the device: u = A^-1 b with b = sod_history_convolve's result ([nrow][R]);
+ * the solver's n must equal the bank's nrow. */
+int sod_history_convolve_solve(sod_history *bank, sod_solver *solver, double *u);
+
 /* ---- the reference's matrix files ------------------------------------------------------------ */
 /* Eigen::save_matrix / load_matrix format (include/matrix_io.hpp:14-61): int64 rows, int64 cols,
  * then the row-major doubles.  data: host or device, SOD_F64 or SOD_F32 (written as doubles).

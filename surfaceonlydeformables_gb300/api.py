@@ -250,6 +250,46 @@ def elastostatic(ctx: Context, mesh: Mesh, kind: str, mat: Material, order: int 
     return out
 
 
+class Solver:
+    """Dense LU (partial pivoting, FP64) of a row-major n x n matrix on the device (sod_solver): the
+    H_0 factorisation of the reference's matrix collection and its solves."""
+
+    def __init__(self, ctx: Context, A):
+        A = A if hasattr(A, "data_ptr") else np.ascontiguousarray(np.asarray(A, dtype=np.float64))
+        self.ctx, self.n = ctx, A.shape[0]
+        self._h = ctypes.c_void_p()
+        L.check(L.load().sod_solver_create(ctx.handle, self.n, L.ptr(A), ctypes.byref(self._h)))
+
+    def solve(self, B, out=None):
+        B = B if hasattr(B, "data_ptr") else np.ascontiguousarray(np.asarray(B, dtype=np.float64))
+        nrhs = 1 if B.ndim == 1 else B.shape[1]
+        if out is None:
+            out = np.empty(B.shape, dtype=np.float64)
+        L.check(L.load().sod_solver_solve(self._h, nrhs, L.ptr(B), L.ptr(out)))
+        return out
+
+    def inverse(self, out=None):
+        if out is None:
+            out = np.empty((self.n, self.n), dtype=np.float64)
+        L.check(L.load().sod_solver_inverse(self._h, L.ptr(out)))
+        return out
+
+    def keep_inverse(self) -> None:
+        """Keep A^-1 resident: the per-step HistoryBank.convolve_solve becomes one FP64 GEMV."""
+        L.check(L.load().sod_solver_keep_inverse(self._h))
+
+    def close(self) -> None:
+        if self._h:
+            L.load().sod_solver_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def mat_write(ctx, path: str, M) -> None:
     """Matrix (2-D numpy array or CUDA tensor, float64/float32) to the reference's .mat file format.
     ctx may be None for host arrays."""
@@ -316,6 +356,13 @@ class HistoryBank:
 
     def reset(self) -> None:
         L.check(L.load().sod_history_reset(self._h))
+
+    def convolve_solve(self, solver: "Solver", out=None):
+        """u = A^-1 b for the solver's A, with b this step's convolution (one device round trip)."""
+        if out is None:
+            out = np.empty((self.nrow, self.R) if self.R > 1 else (self.nrow,), dtype=np.float64)
+        L.check(L.load().sod_history_convolve_solve(self._h, solver._h, L.ptr(out)))
+        return out
 
     def set_engine(self, engine: int) -> None:
         """L.HISTORY_ENGINE_AUTO (tensor cores for BF16 banks and FP32 banks with R = 16), _CUDA_CORES or

@@ -44,7 +44,8 @@ struct sod_history {
     bool has_b = false;
     int nchunk = 0, cchunk = 0;
     int engine = SOD_HISTORY_ENGINE_AUTO;
-    DevBuf Xt, tcpart, derr;  // tensor-core path: BF16 hi/lo history, per-segment partials, error word
+    DevBuf Xt, tcpart, derr;
+    DevBuf bsolve;            // b of the fused per-step solve  // tensor-core path: BF16 hi/lo history, per-segment partials, error word
     int *err_host = nullptr;  // pinned copy of the error word (written by the finish kernel)
     HistTcPlan plan;          // tensor maps of W and Xt
     bool use_tensor() const {
@@ -474,6 +475,24 @@ int sod_history_convolve(sod_history *h, double *b_out) {
     ctx->count();
     if (host) {
         SOD_CHECK_CUDA(cudaMemcpyAsync(b_out, dst, ob, cudaMemcpyDeviceToHost, ctx->stream));
+        SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    return SOD_OK;
+}
+
+int sod_history_convolve_solve(sod_history *h, sod_solver *s, double *u_out) {
+    SOD_REQUIRE(h && s && u_out, "null argument");
+    SOD_REQUIRE(solver_size(s) == h->nrow, "the solver's matrix size must equal the bank's row count");
+    sod_context *ctx = h->ctx;
+    SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
+    const size_t bytes = sizeof(double) * (size_t)h->nrow * h->R;
+    SOD_TRY(h->bsolve.ensure(2 * bytes));
+    double *b = h->bsolve.as<double>(), *u = b + (size_t)h->nrow * h->R;
+    SOD_TRY(sod_history_convolve(h, b));  // device output: no synchronisation
+    const bool host = !is_device_pointer(u_out);
+    SOD_TRY(solver_apply_device(s, h->R, b, host ? u : u_out));
+    if (host) {
+        SOD_CHECK_CUDA(cudaMemcpyAsync(u_out, u, bytes, cudaMemcpyDeviceToHost, ctx->stream));
         SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
     }
     return SOD_OK;

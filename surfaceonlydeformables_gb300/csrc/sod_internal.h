@@ -252,4 +252,10 @@ int launch_history_tc(sod_context *ctx, const HistTcPlan *plan, const float *sca
                       float *partial, const double *Bw, const double *A, double *out, int *err, int *err_mirror,
                       cudaStream_t stream);
 
+// dense LU solves (sod_solve.cu); X = A^-1 B, row-major device buffers, X may alias B
+int solver_size(const sod_solver *s);
+int solver_solve_device(sod_solver *s, int nrhs, const double *B, double *X);
+// per-step form: GEMV with the kept inverse when there is one, else the LU solve (X must not alias B)
+int solver_apply_device(sod_solver *s, int nrhs, const double *B, double *X);
+
 }  // namespace sod
