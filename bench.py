@@ -345,18 +345,20 @@ def solve_leg(torch, ctx, stream, n: int = 7686, K: int = 8):
     return res
 
 
-def galerkin_leg(torch, ctx, stream, nfreq: int = 2, rows=(0, 517, 1280, 2561)):
-    """Galerkin G and H of the 2562-vertex jittered icosphere (configs[1]: E 1e5, nu 0.45, dt 1/200,
-    N = 64 -> 33 Laplace frequencies; 13-point rule for regular pairs, Sauter-Schwab order 5 for the
-    singular ones), timed over `nfreq` of the frequencies, with the listed rows checked against the
-    FP64 oracle (the rows of the listed vertices are exact in the row-sampled oracle)."""
+def galerkin_leg(torch, ctx, stream, nfreq: int = 2, level: int = 4):
+    """Galerkin G and H of the jittered icosphere (level 4 = 2562 vertices, configs[1]: E 1e5, nu 0.45,
+    dt 1/200, N = 64 -> 33 Laplace frequencies; 13-point rule for regular pairs, Sauter-Schwab order 5
+    for the singular ones), timed over `nfreq` of the frequencies, with four rows checked against the
+    FP64 oracle (the rows of the listed vertices are exact in the row-sampled oracle).  Level 3
+    (642 vertices) is the small case for profiling captures."""
     from oracle import oracle as O
 
     from surfaceonlydeformables_gb300 import _lib as L
     from surfaceonlydeformables_gb300 import api
     from surfaceonlydeformables_gb300.meshes import Material, make_icosphere_mesh
 
-    m = make_icosphere_mesh(4, 0.1, jitter=0.2, seed=2)
+    m = make_icosphere_mesh(level, 0.1, jitter=0.2, seed=2)
+    rows = (0, m.nV // 5, m.nV // 2, m.nV - 1)
     dm = api.Mesh(ctx, m)
     mat = Material(1e5, 0.45, 1000.0)
     s, R, Lq = L.cq_frequencies(2, 1 / 200, 64)
@@ -385,7 +387,7 @@ def galerkin_leg(torch, ctx, stream, nfreq: int = 2, rows=(0, 517, 1280, 2561)):
                      "entries_per_s": n * n * nfreq / (ms * 1e-3), "rel_err_vs_fp64_rows": err}
     del out
     torch.cuda.empty_cache()
-    return {"mesh": f"icosphere level 4 jittered (sigma 0.2 edge), {m.nV} vertices / {m.nF} faces",
+    return {"mesh": f"icosphere level {level} jittered (sigma 0.2 edge), {m.nV} vertices / {m.nF} faces",
             "frequencies_timed": f"{nfreq} of {len(s)}", "rule": "13-point regular, Sauter-Schwab order 5",
             "oracle_rows": list(rows), **res}
 
@@ -750,7 +752,7 @@ def run_leg(args):
     elif args.leg == "elastostatic":
         out = elastostatic_leg(torch, ctx, stream)
     elif args.leg == "galerkin":
-        out = galerkin_leg(torch, ctx, stream)
+        out = galerkin_leg(torch, ctx, stream, level=args.galerkin_level)
     elif args.leg == "solve":
         out = solve_leg(torch, ctx, stream)
     else:
@@ -771,6 +773,8 @@ def main():
     ap.add_argument("--leg", default="all", choices=["all", "history", "elastostatic", "galerkin", "serving", "solve"],
                     help="run one hot-path leg alone (profiling captures) and print its JSON")
     ap.add_argument("--history-k", type=int, default=64, help="history length of the --leg history bank")
+    ap.add_argument("--galerkin-level", type=int, default=4, choices=[3, 4],
+                    help="icosphere level of the --leg galerkin mesh (3: the small profiling case)")
     ap.add_argument("--value-only", action="store_true",
                     help="profiling runs: time the batched step only (no comparison paths, e2e or CPU leg)")
     ap.add_argument("--case", default="mixed24", choices=sorted(CASES),
