@@ -362,9 +362,10 @@ constexpr int GAL_BMOM = 13;  // Ms[3], Md, M1[6], M0, SB, SC
 __device__ __forceinline__ dd ddv(double x) { return dd_from(x); }
 
 // shared-memory floats per warp of the singular kernel: kernel tensor (NCS cdd), B moment values
-// (13 cdd, G pass with B kinds) and the test / trial shape functions (6 dd) of 32 points
+// (13 cdd, G pass with B kinds), the test shape functions (3 dd) and the test x trial shape-function
+// products (9 dd) of 32 points
 template <int KIND, int BM> constexpr int sing_warp_floats() {
-    return 32 * ((KIND == SOD_G ? 6 : 9) * 4 + ((KIND == SOD_G && BM != 0) ? GAL_BMOM * 4 : 0) + 12);
+    return 32 * ((KIND == SOD_G ? 6 : 9) * 4 + ((KIND == SOD_G && BM != 0) ? GAL_BMOM * 4 : 0) + 24);
 }
 __device__ __forceinline__ void st_cdd(float *p, const cdd &v) {
     *reinterpret_cast<float4 *>(p) = make_float4(v.x.hi, v.x.lo, v.y.hi, v.y.lo);
@@ -550,8 +551,13 @@ __global__ void __launch_bounds__(128) gal_sing_kernel(GalSingArgs a, const __gr
             for (int c = 0; c < GAL_BMOM; c++) st_cdd(sw + OFF_V + (lane * GAL_BMOM + c) * 4, mv[c]);
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            sw[OFF_L + lane * 12 + 2 * c] = Lx[c].hi, sw[OFF_L + lane * 12 + 2 * c + 1] = Lx[c].lo;
-            sw[OFF_L + lane * 12 + 6 + 2 * c] = Ly[c].hi, sw[OFF_L + lane * 12 + 6 + 2 * c + 1] = Ly[c].lo;
+            sw[OFF_L + lane * 24 + 2 * c] = Lx[c].hi, sw[OFF_L + lane * 24 + 2 * c + 1] = Lx[c].lo;
+#pragma unroll
+            for (int b = 0; b < 3; b++) {  // the weights of the 9 (test corner, trial corner) sums
+                const dd wab = Lx[c] * Ly[b];
+                sw[OFF_L + lane * 24 + 6 + 2 * (3 * c + b)] = wab.hi;
+                sw[OFF_L + lane * 24 + 6 + 2 * (3 * c + b) + 1] = wab.lo;
+            }
         }
         __syncwarp();
         // ---- phase B: the sums this lane owns, over the batch's 32 points in order ----
@@ -562,14 +568,13 @@ __global__ void __launch_bounds__(128) gal_sing_kernel(GalSingArgs a, const __gr
             if (q < 9 * NCS) {
                 const int ac = q / (3 * NCS), b = (q / NCS) % 3, c = q % NCS;
                 for (int pt = 0; pt < 32; pt++) {
-                    const float *L = sw + OFF_L + pt * 12;
-                    const dd wgt = dd{L[2 * ac], L[2 * ac + 1]} * dd{L[6 + 2 * b], L[6 + 2 * b + 1]};
-                    cdd_acc(acc[t], ld_cdd(sw + (pt * NCS + c) * 4), wgt);
+                    const float *L = sw + OFF_L + pt * 24 + 6 + 2 * (3 * ac + b);
+                    cdd_acc(acc[t], ld_cdd(sw + (pt * NCS + c) * 4), dd{L[0], L[1]});
                 }
             } else if (DB) {
                 const int qm = q - 9 * NCS, ac = qm / GAL_BMOM, c = qm % GAL_BMOM;
                 for (int pt = 0; pt < 32; pt++) {
-                    const float *L = sw + OFF_L + pt * 12;
+                    const float *L = sw + OFF_L + pt * 24;
                     cdd_acc(acc[t], ld_cdd(sw + OFF_V + (pt * GAL_BMOM + c) * 4), dd{L[2 * ac], L[2 * ac + 1]});
                 }
             }
@@ -945,6 +950,15 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
             }
             // singular pairs and their combination into slot blocks
             if (sing && g->nent > 0) {
+                static bool attr_done[64] = {};  // per device: the G + B variants need more than 48 KB
+                if (ctx->device < 0 || ctx->device >= 64 || !attr_done[ctx->device]) {
+                    const void *fns[3] = {(const void *)gal_sing_kernel<SOD_G, BT | BA>,
+                                          (const void *)gal_sing_kernel<SOD_G, BT>, (const void *)gal_sing_kernel<SOD_G, BA>};
+                    for (const void *f : fns)
+                        SOD_CHECK_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                            4 * 4 * sing_warp_floats<SOD_G, BT | BA>()));
+                    if (ctx->device >= 0 && ctx->device < 64) attr_done[ctx->device] = true;
+                }
                 const dim3 grid((g->npairs * 32 + 127) / 128, nf);
                 if (kd == SOD_H)
                     gal_sing_kernel<SOD_H, 0><<<grid, 128, 4 * 4 * sing_warp_floats<SOD_H, 0>(), L.stream>>>(sa, dr, ft);
