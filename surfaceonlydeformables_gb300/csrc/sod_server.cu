@@ -448,6 +448,17 @@ int sod_server_create(int device, int64_t hbm_cap_bytes, int slots, int max_vert
     s->cap = hbm_cap_bytes;
     s->vmax_n = 3 * max_vertices;
     SOD_TRY(sod_context_create(device, &s->step_ctx));
+    {
+        // time steps run on the device's highest-priority stream: the block scheduler hands them SMs
+        // as soon as CTAs of the assembly kernels (regular grids, short CTAs) retire, instead of
+        // queueing them behind whole assemblies
+        int lo = 0, hi = 0;
+        SOD_CHECK_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        cudaStream_t hs = nullptr;
+        SOD_CHECK_CUDA(cudaStreamCreateWithPriority(&hs, cudaStreamNonBlocking, hi));
+        SOD_CHECK_CUDA(cudaStreamDestroy(s->step_ctx->own_stream));
+        s->step_ctx->own_stream = s->step_ctx->stream = hs;
+    }
     constexpr int RING = 32;
     s->ring.resize(RING);
     for (int k = 0; k < RING; k++) {
