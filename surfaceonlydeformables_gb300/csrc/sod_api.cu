@@ -378,6 +378,11 @@ int sod_context_destroy(sod_context *ctx) {
         cudaStreamSynchronize(ctx->own_stream);
         cudaStreamDestroy(ctx->own_stream);
     }
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+    }
+    for (cudaEvent_t e : ctx->chunk_events) cudaEventDestroy(e);
     delete ctx;
     return SOD_OK;
 }
@@ -519,9 +524,10 @@ static size_t kind_elems(int kind, int nV) {
 }
 
 // Shared driver: validates, stages host outputs through device memory, launches, copies back.
-// Page-locked host outputs of the collocation path skip the staging: its kernels only store to
-// their outputs, so they write the rows straight into host memory over the CPU-GPU link while
-// other rows are still being computed, and the call returns once the stream has drained.
+// Collocation host outputs: large ones (>= 16 MB) are staged and copied in row chunks on a copy
+// stream while later rows compute (the copy engine moves ~190 GB/s over the CPU-GPU link, about
+// twice what kernel stores into host memory reach); small page-locked ones are written in place by
+// the kernels through their device-mapped address (no copy launch at all).
 static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int method, double c1, double c2,
                           double rho, const double *s, int nfreq, int order, int subdiv, int sorder, int ssub,
                           int parts, void *const outs[4], int out_dtype) {
@@ -550,11 +556,15 @@ static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int 
     void *direct[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t staged = 0, off[4] = {0, 0, 0, 0};
     bool any_host = false;
+    size_t host_bytes = 0;
+    for (int kd = 0; kd < 4; kd++)
+        if ((mask & (1 << kd)) && !is_device_ptr(outs[kd])) host_bytes += kind_elems(kd, mesh->nV) * nfreq * esz;
+    const bool pipelined = method == SOD_COLLOCATION && host_bytes >= ((size_t)16 << 20);
     for (int kd = 0; kd < 4; kd++) {
         if (!(mask & (1 << kd))) continue;
         if (is_device_ptr(outs[kd])) continue;
         any_host = true;
-        if (method == SOD_COLLOCATION) direct[kd] = mapped_host_ptr(outs[kd]);
+        if (method == SOD_COLLOCATION && !pipelined) direct[kd] = mapped_host_ptr(outs[kd]);
         if (direct[kd]) continue;
         host_out[kd] = true;
         off[kd] = staged;
@@ -576,10 +586,12 @@ static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int 
     L.parts = parts;
     L.out_dtype = out_dtype;
     L.stream = ctx->stream;
+    if (pipelined)
+        for (int kd = 0; kd < 4; kd++) L.host[kd] = host_out[kd] ? outs[kd] : nullptr;
     SOD_TRY(method == SOD_GALERKIN ? launch_galerkin(ctx, L) : launch_collocation(ctx, L));
     if (any_host) {
         for (int kd2 = 0; kd2 < 4; kd2++)
-            if (host_out[kd2])
+            if (host_out[kd2] && !pipelined)
                 SOD_CHECK_CUDA(cudaMemcpyAsync(outs[kd2], L.out[kd2], kind_elems(kd2, mesh->nV) * nfreq * esz,
                                                cudaMemcpyDeviceToHost, ctx->stream));
         SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -40,6 +40,7 @@ struct CollArgs {
     const int4 *canonF;    // canonical corner ids per face record, or null
     const int *color_off;  // ncolors+1 (scatter kernels)
     int ncolors;
+    int i0;                // first field vertex of the plain kernels' grid (row chunks)
     const float *Vf;       // nV x 3
     const int *canonV;     // canonical id per vertex, or null
     void *out[4];          // per kind (G, H, B_trans, B_angular)
@@ -253,7 +254,7 @@ template <int KIND, int BM>
 __global__ void __launch_bounds__(scatter_max_threads<KIND, BM>(), 1) coll_scatter_kernel(CollArgs a, PointTable pt,
                                                                const __grid_constant__ FreqTable ft) {
     extern __shared__ float2 acc[];
-    scatter_body<KIND, BM>(a, pt, ft.kf[blockIdx.y], blockIdx.x, blockIdx.y, acc);
+    scatter_body<KIND, BM>(a, pt, ft.kf[blockIdx.y], a.i0 + blockIdx.x, blockIdx.y, acc);
 }
 
 // -------------------------------------------------------------------------------------------
@@ -320,7 +321,7 @@ __device__ __forceinline__ void reduce_body(const CollArgs &a, const PointTable 
 template <int MASK>
 __global__ void __launch_bounds__(256) coll_reduce_kernel(CollArgs a, PointTable pt,
                                                           const __grid_constant__ FreqTable ft) {
-    reduce_body<MASK>(a, pt, ft.kf[blockIdx.y], blockIdx.x, blockIdx.y);
+    reduce_body<MASK>(a, pt, ft.kf[blockIdx.y], a.i0 + blockIdx.x, blockIdx.y);
 }
 
 // -------------------------------------------------------------------------------------------
@@ -784,6 +785,28 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
         }
     }
     const size_t esz = L.out_dtype == SOD_C64 ? 8 : 16;
+    // host destinations: row chunks of whole waves of the scatter grid, each chunk's rows copied on
+    // the copy stream while the next chunk computes
+    const bool to_host = L.host[0] || L.host[1] || L.host[2] || L.host[3];
+    int vchunk = m->nV;
+    if (to_host) {
+        int wave = ctx->num_sms;
+        for (int kd = 0; kd < 2; kd++)
+            if (mask & (1 << kd)) {
+                int per_sm = 1;
+                SOD_TRY(scatter_occupancy(ctx, kd, kd == SOD_G ? bmG : 0, false, threads[kd], smem[kd], &per_sm));
+                wave = std::max(wave, ctx->num_sms * std::max(per_sm, 1));
+            }
+        const int target = (m->nV + 5) / 6;  // about six chunks
+        vchunk = std::min(m->nV, std::max(wave, (target + wave - 1) / wave * wave));
+        if (!ctx->copy_stream) SOD_CHECK_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        const size_t need = (size_t)((m->nV + vchunk - 1) / vchunk) + 1;
+        while (ctx->chunk_events.size() < need) {
+            cudaEvent_t e;
+            SOD_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            ctx->chunk_events.push_back(e);
+        }
+    }
     for (int f0 = 0; f0 < L.nfreq; f0 += chunk) {
         const int nf = std::min(chunk, L.nfreq - f0);
         FreqTable ft;
@@ -792,7 +815,6 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
             ft.kd[l] = L.kc_host[f0 + l];
             ft.kf[l] = to_float(ft.kd[l]);
         }
-        const dim3 grid(m->nV, nf);
         SingArgs sa{};
         sa.nV = m->nV;
         sa.V = m->dV.as<double>();
@@ -825,38 +847,64 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
             a.S[kd] = sa.S[kd];
             a.S_fstride[kd] = sfs[kd];
         }
-        for (int kd = 0; kd < 2; kd++) {
-            if (!(mask & (1 << kd))) continue;
-            a.faces = col[kd]->dFaces.as<float4>();
-            a.canonF = m->has_vmap ? col[kd]->dCanonF.as<int4>() : nullptr;
-            a.color_off = col[kd]->dOff.as<int>();
-            a.ncolors = col[kd]->ncolors;
-            if (kd == SOD_H)
-                coll_scatter_kernel<SOD_H, 0><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
-            else if (bmG == KM_BT)
-                coll_scatter_kernel<SOD_G, KM_BT><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
-            else if (bmG == KM_BA)
-                coll_scatter_kernel<SOD_G, KM_BA><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
-            else if (bmG)
-                coll_scatter_kernel<SOD_G, KM_BT | KM_BA><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
-            else
-                coll_scatter_kernel<SOD_G, 0><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
-            SOD_CHECK_CUDA(cudaGetLastError());
-            ctx->count();
+        for (int v0 = 0, ci = 0; v0 < m->nV; v0 += vchunk, ci++) {
+            const int v1 = std::min(m->nV, v0 + vchunk);
+            const dim3 grid(v1 - v0, nf);
+            a.i0 = v0;
+            for (int kd = 0; kd < 2; kd++) {
+                if (!(mask & (1 << kd))) continue;
+                a.faces = col[kd]->dFaces.as<float4>();
+                a.canonF = m->has_vmap ? col[kd]->dCanonF.as<int4>() : nullptr;
+                a.color_off = col[kd]->dOff.as<int>();
+                a.ncolors = col[kd]->ncolors;
+                if (kd == SOD_H)
+                    coll_scatter_kernel<SOD_H, 0><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
+                else if (bmG == KM_BT)
+                    coll_scatter_kernel<SOD_G, KM_BT><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
+                else if (bmG == KM_BA)
+                    coll_scatter_kernel<SOD_G, KM_BA><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
+                else if (bmG)
+                    coll_scatter_kernel<SOD_G, KM_BT | KM_BA><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
+                else
+                    coll_scatter_kernel<SOD_G, 0><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
+                SOD_CHECK_CUDA(cudaGetLastError());
+                ctx->count();
+            }
+            const int rm = (mask & KM_G) ? 0 : (mask & (KM_BT | KM_BA));
+            if (rm) {
+                a.faces = m->dFacesNat.as<float4>();
+                a.canonF = m->has_vmap ? m->dCanonNat.as<int4>() : nullptr;
+                if (rm == KM_BT)
+                    coll_reduce_kernel<KM_BT><<<grid, 256, 0, L.stream>>>(a, pt, ft);
+                else if (rm == KM_BA)
+                    coll_reduce_kernel<KM_BA><<<grid, 256, 0, L.stream>>>(a, pt, ft);
+                else
+                    coll_reduce_kernel<KM_BT | KM_BA><<<grid, 256, 0, L.stream>>>(a, pt, ft);
+                SOD_CHECK_CUDA(cudaGetLastError());
+                ctx->count();
+            }
+            if (to_host) {  // this chunk's rows (vertices v0..v1-1) of every kind and frequency to the host
+                cudaEvent_t e = ctx->chunk_events[ci];
+                SOD_CHECK_CUDA(cudaEventRecord(e, L.stream));
+                SOD_CHECK_CUDA(cudaStreamWaitEvent(ctx->copy_stream, e, 0));
+                for (int kd = 0; kd < 4; kd++) {
+                    if (!L.host[kd]) continue;
+                    const size_t ncol = kd <= SOD_H ? 3 * (size_t)m->nV : (kd == SOD_B_TRANS ? 3 : 9);
+                    for (int f = 0; f < nf; f++) {
+                        const size_t off = ((size_t)(f0 + f) * (size_t)L.freq_stride[kd] + 3 * (size_t)v0 * ncol) * esz;
+                        SOD_CHECK_CUDA(cudaMemcpyAsync(static_cast<char *>(L.host[kd]) + off,
+                                                       static_cast<const char *>(L.out[kd]) + off,
+                                                       3 * (size_t)(v1 - v0) * ncol * esz, cudaMemcpyDeviceToHost,
+                                                       ctx->copy_stream));
+                    }
+                }
+            }
         }
-        const int rm = (mask & KM_G) ? 0 : (mask & (KM_BT | KM_BA));
-        if (rm) {
-            a.faces = m->dFacesNat.as<float4>();
-            a.canonF = m->has_vmap ? m->dCanonNat.as<int4>() : nullptr;
-            if (rm == KM_BT)
-                coll_reduce_kernel<KM_BT><<<grid, 256, 0, L.stream>>>(a, pt, ft);
-            else if (rm == KM_BA)
-                coll_reduce_kernel<KM_BA><<<grid, 256, 0, L.stream>>>(a, pt, ft);
-            else
-                coll_reduce_kernel<KM_BT | KM_BA><<<grid, 256, 0, L.stream>>>(a, pt, ft);
-            SOD_CHECK_CUDA(cudaGetLastError());
-            ctx->count();
-        }
+    }
+    if (to_host) {  // the caller's stream sees the copies complete
+        cudaEvent_t e = ctx->chunk_events.back();
+        SOD_CHECK_CUDA(cudaEventRecord(e, ctx->copy_stream));
+        SOD_CHECK_CUDA(cudaStreamWaitEvent(L.stream, e, 0));
     }
     return SOD_OK;
 }

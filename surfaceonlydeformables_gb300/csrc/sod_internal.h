@@ -113,6 +113,8 @@ struct sod_context {
     sod::DevBuf freqbuf;   // Laplace-domain intermediates of the precompute
     sod::DevBuf small;     // small per-call tables (free terms, adjacency)
     sod::DevBuf gal_rows;  // Galerkin: unweighted rows of every test point (per frequency chunk)
+    cudaStream_t copy_stream = nullptr;    // device-to-host copies overlapped with compute
+    std::vector<cudaEvent_t> chunk_events;  // row-chunk completion markers (reused)
     sod::DevBuf gal_bsum;  // Galerkin: B_trans / B_angular sums of every test point
     void count(int n = 1) { launches += n; }
 };
@@ -181,6 +183,10 @@ struct CollLaunch {
     int out_dtype;
     long long freq_stride[4];  // elements between consecutive frequencies of out[kind]
     cudaStream_t stream;
+    // collocation only: host destinations of out[kind] (device staging).  When set, the scatter runs
+    // in row chunks and each chunk's rows are copied to the host on the context's copy stream while
+    // the next chunk computes; `stream` waits for the copies at the end.
+    void *host[4];
 };
 int launch_collocation(sod_context *ctx, const CollLaunch &L);
 // Galerkin assembly of G / H (sod_galerkin.cu); same launch description.
