@@ -342,6 +342,34 @@ def solve_leg(torch, ctx, stream, n: int = 7686, K: int = 8):
         bank.close()
         del w, out
     S.close()
+    # B_trans_inv.solve(H_0): minimum-norm least squares with a tall 3V x 3 matrix (one pass over Y)
+    Bt = torch.randn((n, 3), dtype=torch.float64, device="cuda", generator=gen)
+    Y = torch.randn((n, n), dtype=torch.float64, device="cuda", generator=gen)
+    X3 = torch.empty((3, n), dtype=torch.float64, device="cuda")
+    ms_f, C = timed(lambda: api.LeastSquares(ctx, Bt))
+    C.solve(Y, out=X3)
+    ms_s, _ = timed(lambda: C.solve(Y, out=X3))
+    res["lstsq_3col"] = {"factor_ms": round(ms_f, 3), "solve_ms": round(ms_s, 3),
+                         "solve_gbs": round(n * n * 8 / ms_s / 1e6, 1)}
+    C.close()
+    del Y, X3
+    if n % 3 == 0 and n // 3 in (12, 42, 162, 642, 2562):
+        # elastostatic u_p from the icosphere's own Kelvin H and G (collocation)
+        from surfaceonlydeformables_gb300.meshes import Material, make_icosphere_mesh
+
+        level = (12, 42, 162, 642, 2562).index(n // 3)
+        dm = api.Mesh(ctx, make_icosphere_mesh(level, 0.1))
+        mat = Material(1e5, 0.3, 1000.0)
+        H = torch.empty((n, n), dtype=torch.float64, device="cuda")
+        Gs = torch.empty_like(H)
+        api.elastostatic(ctx, dm, "H", mat, out=H)
+        api.elastostatic(ctx, dm, "G", mat, out=Gs)
+        up = torch.empty_like(H)
+        ms_up2, _ = timed(lambda: api.elastostatic_u_p(ctx, dm, H, Gs, out=up))
+        flop = 2 * n ** 3 + n ** 3 + n ** 3 / 3 + 2 * n ** 3  # GEMM, SYRK, Cholesky, n-RHS solve
+        res["elastostatic_u_p"] = {"ms": round(ms_up2, 1), "fp64_tflops": round(flop / ms_up2 / 1e9, 3)}
+        dm.close()
+        del H, Gs, up
     return res
 
 

@@ -237,6 +237,35 @@ int sod_solver_destroy(sod_solver *solver);
  * the solver's n must equal the bank's nrow. */
 int sod_history_convolve_solve(sod_history *bank, sod_solver *solver, double *u);
 
+/* Replace the Eigen::CompleteOrthogonalDecomposition objects B_trans_inv / B_euler_inv
+ * (include/elastodynamics_cqbem_matrix_collection.hpp:43, src/elastodynamics_cqbem_matrix_collection.cpp:
+ * 184-191: B_trans_inv.solve(H), .solve(G'), B_euler_inv.solve(B_trans), ...): the minimum-norm
+ * least-squares solution X = B^+ Y of a tall B (m x k, m >= k, 1 <= k <= 8; 3V x 3 in the reference).
+ * Column-pivoted Householder QR, numerical rank by Eigen's default threshold
+ * (|R_ii| > eps * k * max |R_ii|), and for a rank-deficient B the complete orthogonal decomposition.
+ * FP64 on the device; B, Y (m x ncols) and X (k x ncols) row-major, host or device. */
+typedef struct sod_lstsq sod_lstsq;
+int sod_lstsq_create(sod_context *ctx, int m, int k, const double *B, sod_lstsq **lstsq);
+int sod_lstsq_rank(const sod_lstsq *lstsq, int *rank);
+int sod_lstsq_solve(sod_lstsq *lstsq, int ncols, const double *Y, double *X);
+/* B^+ itself, k x m. */
+int sod_lstsq_pinv(sod_lstsq *lstsq, double *P);
+int sod_lstsq_destroy(sod_lstsq *lstsq);
+
+/* Replaces the u_p computation of ElastostaticsBEMMatrixCollection::init
+ * (src/elastostatics_bem_matrix_collection.cpp:58-89): with H, G the elastostatic matrices of
+ * sod_elastostatic_assemble (3nV x 3nV row-major FP64, host or device) and T the area-weighted
+ * rigid modes of the mesh,
+ *   u_p = (H^T H + (tr H / 3nV)^2 T^T T)^-1 H^T G (I - T^T (T T^T)^-1 T).
+ * The symmetric positive definite system is factored by Cholesky (the reference's LDL^T); FP64 on
+ * the device (cuBLAS and cuSOLVER, loaded at first use).  u_p: 3nV x 3nV row-major, host or device.
+ * SOD_ERR_INVALID_ARG if the regularised matrix is not positive definite. */
+int sod_elastostatic_u_p(sod_context *ctx, const sod_mesh *mesh, const double *H, const double *G, double *u_p);
+/* T (6 x 3nV row-major, host or device): rows 0-2 translations (A_e / 6 per face corner), rows 3-5
+ * rotations (A_e / 24 [v_0 + v_1 + v_2 + v_i]_x), A_e the doubled face area
+ * (src/elastostatics_bem_matrix_collection.cpp:61-79). */
+int sod_elastostatic_rigid_modes(sod_context *ctx, const sod_mesh *mesh, double *T);
+
 /* ---- the reference's matrix files ------------------------------------------------------------ */
 /* Eigen::save_matrix / load_matrix format (include/matrix_io.hpp:14-61): int64 rows, int64 cols,
  * then the row-major doubles.  data: host or device, SOD_F64 or SOD_F32 (written as doubles).

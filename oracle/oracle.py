@@ -166,3 +166,77 @@ def history_convolution(G, H, p_hist, u_hist, B=None, a_hist=None):
         if B is not None:
             b += B[k] @ a_hist[k - 1]
     return b
+
+
+def cod_solve(B: np.ndarray, Y: np.ndarray) -> np.ndarray:
+    """Minimum-norm least squares X = B^+ Y by the complete orthogonal decomposition, the algorithm
+    of Eigen::CompleteOrthogonalDecomposition that the reference's B_trans_inv / B_euler_inv use
+    (include/elastodynamics_cqbem_matrix_collection.hpp:43, src/elastodynamics_cqbem_matrix_collection.cpp:
+    184-191): Householder QR with column pivoting (largest remaining column norm, first on ties),
+    rank = leading |R_ii| > eps * min(m, k) * max |R_ii|, for rank r < k the R12 block removed by
+    Householder reflections from the right, then x = P Z^T [T^-1 (Q^T y)_{1..r}; 0].  B: (m, k), m >= k."""
+    A = np.array(B, dtype=np.float64)
+    m, k = A.shape
+    Y2 = np.asarray(Y, dtype=np.float64).reshape(m, -1).copy()
+    perm = list(range(k))
+    R = np.zeros((k, k))
+    for j in range(k):
+        norms = (A[j:, j:] ** 2).sum(axis=0)
+        p = j + int(np.argmax(norms))
+        A[:, [j, p]] = A[:, [p, j]]
+        perm[j], perm[p] = perm[p], perm[j]
+        x = A[j:, j].copy()
+        sigma = float((x[1:] ** 2).sum())
+        if sigma <= np.finfo(float).tiny:
+            beta, tau, v = x[0], 0.0, np.zeros_like(x)
+        else:
+            beta = np.sqrt(x[0] ** 2 + sigma) * (-1.0 if x[0] >= 0 else 1.0)
+            v = x / (x[0] - beta)
+            tau = (beta - x[0]) / beta
+        v[0] = 1.0
+        A[j:, j] = 0.0
+        A[j, j] = beta
+        A[j:, j + 1:] -= tau * np.outer(v, v @ A[j:, j + 1:])
+        Y2[j:] -= tau * np.outer(v, v @ Y2[j:])  # Q^T y, one reflector at a time
+    R = np.triu(A[:k, :k])
+    d = np.abs(np.diag(R))
+    thr = d.max() * np.finfo(float).eps * k
+    r = 0
+    while r < k and d[r] > thr:
+        r += 1
+    X = np.zeros((k, Y2.shape[1]))
+    if r == 0:
+        return X.reshape((k,) + np.shape(Y)[1:])
+    W = R[:r].copy()
+    zs = []
+    for i in range(r - 1, -1, -1):  # [R11 R12] = [T 0] Z
+        idx = [i] + list(range(r, k))
+        x = W[i, idx].copy()
+        sigma = float((x[1:] ** 2).sum())
+        if sigma <= np.finfo(float).tiny:
+            zs.append((idx, 0.0, np.zeros_like(x)))
+            continue
+        beta = np.sqrt(x[0] ** 2 + sigma) * (-1.0 if x[0] >= 0 else 1.0)
+        v = x / (x[0] - beta)
+        v[0] = 1.0
+        tau = (beta - x[0]) / beta
+        W[:i + 1, idx] -= tau * np.outer(W[:i + 1, idx] @ v, v)
+        zs.append((idx, tau, v))
+    z = np.zeros((k, Y2.shape[1]))
+    z[:r] = np.linalg.solve(np.triu(W[:r, :r]), Y2[:r])  # T^-1 c
+    for idx, tau, v in reversed(zs):  # Z^T = H_{r-1} ... H_0: H_0 first
+        z[idx] -= tau * np.outer(v, v @ z[idx])
+    X[perm] = z
+    return X.reshape((k,) + np.shape(Y)[1:])
+
+
+def elastostatic_u_p(H: np.ndarray, G: np.ndarray, T: np.ndarray) -> np.ndarray:
+    """u_p of ElastostaticsBEMMatrixCollection::init (src/elastostatics_bem_matrix_collection.cpp:58-89):
+    H' = H^T H + (tr H / 3V)^2 T^T T, G' = H^T G (I - A^T (A A^T)^-1 A) with A = T, u_p = H'^-1 G'
+    (the reference factors the symmetric H' by LDL^T; here LAPACK's symmetric-indefinite LDL^T solve)."""
+    import scipy.linalg as sl
+
+    n = H.shape[0]
+    Hr = H.T @ H + (np.trace(H) / n) ** 2 * (T.T @ T)
+    Gp = H.T @ G @ (np.eye(n) - T.T @ np.linalg.solve(T @ T.T, T))
+    return sl.solve(Hr, Gp, assume_a="sym")

@@ -82,6 +82,13 @@ _SIGS = {
     "sod_solver_destroy": ([_P], _c.c_int),
     "sod_solver_keep_inverse": ([_P], _c.c_int),
     "sod_history_convolve_solve": ([_P, _P, _P], _c.c_int),
+    "sod_lstsq_create": ([_P, _c.c_int, _c.c_int, _P, _P], _c.c_int),
+    "sod_lstsq_rank": ([_P, _P], _c.c_int),
+    "sod_lstsq_solve": ([_P, _c.c_int, _P, _P], _c.c_int),
+    "sod_lstsq_pinv": ([_P, _P], _c.c_int),
+    "sod_lstsq_destroy": ([_P], _c.c_int),
+    "sod_elastostatic_u_p": ([_P, _P, _P, _P, _P], _c.c_int),
+    "sod_elastostatic_rigid_modes": ([_P, _P, _P], _c.c_int),
     "sod_mat_write": ([_P, _c.c_char_p, _P, _c.c_int64, _c.c_int64, _c.c_int], _c.c_int),
     "sod_mat_read": ([_P, _c.c_char_p, _P, _c.c_int64, _c.c_int64], _c.c_int),
     "sod_cqbem_write_cache": ([_P, _c.c_char_p, _c.c_int, _c.c_int, _P, _P, _P, _P, _c.c_int], _c.c_int),

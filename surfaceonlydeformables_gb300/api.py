@@ -290,6 +290,67 @@ class Solver:
             pass
 
 
+class LeastSquares:
+    """Minimum-norm least squares with a tall m x k matrix B (sod_lstsq): the reference's
+    CompleteOrthogonalDecomposition B_trans_inv / B_euler_inv.  solve(Y) = B^+ Y."""
+
+    def __init__(self, ctx: Context, B):
+        B = B if hasattr(B, "data_ptr") else np.ascontiguousarray(np.asarray(B, dtype=np.float64))
+        self.ctx, self.m, self.k = ctx, B.shape[0], B.shape[1]
+        self._h = ctypes.c_void_p()
+        L.check(L.load().sod_lstsq_create(ctx.handle, self.m, self.k, L.ptr(B), ctypes.byref(self._h)))
+
+    @property
+    def rank(self) -> int:
+        r = ctypes.c_int()
+        L.check(L.load().sod_lstsq_rank(self._h, ctypes.byref(r)))
+        return r.value
+
+    def solve(self, Y, out=None):
+        Y = Y if hasattr(Y, "data_ptr") else np.ascontiguousarray(np.asarray(Y, dtype=np.float64))
+        ncols = 1 if Y.ndim == 1 else Y.shape[1]
+        if out is None:
+            out = np.empty((self.k,) if Y.ndim == 1 else (self.k, ncols), dtype=np.float64)
+        L.check(L.load().sod_lstsq_solve(self._h, ncols, L.ptr(Y), L.ptr(out)))
+        return out
+
+    def pinv(self, out=None):
+        if out is None:
+            out = np.empty((self.k, self.m), dtype=np.float64)
+        L.check(L.load().sod_lstsq_pinv(self._h, L.ptr(out)))
+        return out
+
+    def close(self) -> None:
+        if self._h:
+            L.load().sod_lstsq_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def elastostatic_u_p(ctx: Context, mesh: Mesh, H, G, out=None):
+    """u_p of the elastostatic matrix collection: the regularised, force-free-projected solve of
+    src/elastostatics_bem_matrix_collection.cpp:58-89 (FP64, 3nV x 3nV)."""
+    H = H if hasattr(H, "data_ptr") else np.ascontiguousarray(np.asarray(H, dtype=np.float64))
+    G = G if hasattr(G, "data_ptr") else np.ascontiguousarray(np.asarray(G, dtype=np.float64))
+    if out is None:
+        out = np.empty((3 * mesh.nV, 3 * mesh.nV), dtype=np.float64)
+    L.check(L.load().sod_elastostatic_u_p(ctx.handle, mesh.handle, L.ptr(H), L.ptr(G), L.ptr(out)))
+    return out
+
+
+def rigid_modes(ctx: Context, mesh: Mesh, out=None):
+    """Area-weighted rigid modes T (6 x 3nV) of the elastostatic regularisation."""
+    if out is None:
+        out = np.empty((6, 3 * mesh.nV), dtype=np.float64)
+    L.check(L.load().sod_elastostatic_rigid_modes(ctx.handle, mesh.handle, L.ptr(out)))
+    return out
+
+
 def mat_write(ctx, path: str, M) -> None:
     """Matrix (2-D numpy array or CUDA tensor, float64/float32) to the reference's .mat file format.
     ctx may be None for host arrays."""

@@ -11,55 +11,64 @@
 // depend on it).  Matrices are row-major at the interface; a row-major A is the column-major A^T, so
 // the buffer is factored as it is (P A^T = L U) and solves use the transposed form, A X = B.
 // Right-hand sides are transposed to column-major and back by a tiled shared-memory kernel.
-#include <cublas_api.h>
-#include <cusolverDn.h>
 #include <dlfcn.h>
 
 #include <mutex>
 #include <string>
 
-#include "sod_internal.h"
+#include "sod_dense.h"
 
 using namespace sod;
 
-namespace {
+namespace sod {
 
-struct DnApi {
-    cusolverStatus_t (*create)(cusolverDnHandle_t *) = nullptr;
-    cusolverStatus_t (*destroy)(cusolverDnHandle_t) = nullptr;
-    cusolverStatus_t (*set_stream)(cusolverDnHandle_t, cudaStream_t) = nullptr;
-    cusolverStatus_t (*getrf_buf)(cusolverDnHandle_t, int, int, double *, int, int *) = nullptr;
-    cusolverStatus_t (*getrf)(cusolverDnHandle_t, int, int, double *, int, double *, int *, int *) = nullptr;
-    cusolverStatus_t (*getrs)(cusolverDnHandle_t, cublasOperation_t, int, int, const double *, int, const int *,
-                              double *, int, int *) = nullptr;
-    bool ok = false;
-    std::string why;
-};
-
-const DnApi &dn_api() {
-    static DnApi api;
+const DenseApi &dense_api() {
+    static DenseApi api;
     static std::once_flag once;
     std::call_once(once, [] {
-        const char *names[] = {"libcusolver.so.12", "libcusolver.so", "/usr/local/cuda/lib64/libcusolver.so.12"};
-        void *h = nullptr;
-        for (const char *n : names)
-            if ((h = dlopen(n, RTLD_NOW | RTLD_LOCAL))) break;
-        if (!h) {
-            api.why = std::string("cuSOLVER not found (") + dlerror() + ")";
-            return;
+        auto open = [](const char *const *names, int n) -> void * {
+            for (int i = 0; i < n; i++)
+                if (void *h = dlopen(names[i], RTLD_NOW | RTLD_LOCAL)) return h;
+            return nullptr;
+        };
+        const char *sol[] = {"libcusolver.so.12", "libcusolver.so", "/usr/local/cuda/lib64/libcusolver.so.12"};
+        if (void *h = open(sol, 3)) {
+            auto sym = [&](const char *s) { return dlsym(h, s); };
+            api.dn_create = reinterpret_cast<decltype(api.dn_create)>(sym("cusolverDnCreate"));
+            api.dn_destroy = reinterpret_cast<decltype(api.dn_destroy)>(sym("cusolverDnDestroy"));
+            api.dn_set_stream = reinterpret_cast<decltype(api.dn_set_stream)>(sym("cusolverDnSetStream"));
+            api.getrf_buf = reinterpret_cast<decltype(api.getrf_buf)>(sym("cusolverDnDgetrf_bufferSize"));
+            api.getrf = reinterpret_cast<decltype(api.getrf)>(sym("cusolverDnDgetrf"));
+            api.getrs = reinterpret_cast<decltype(api.getrs)>(sym("cusolverDnDgetrs"));
+            api.potrf_buf = reinterpret_cast<decltype(api.potrf_buf)>(sym("cusolverDnDpotrf_bufferSize"));
+            api.potrf = reinterpret_cast<decltype(api.potrf)>(sym("cusolverDnDpotrf"));
+            api.potrs = reinterpret_cast<decltype(api.potrs)>(sym("cusolverDnDpotrs"));
+            api.solver_ok = api.dn_create && api.dn_destroy && api.dn_set_stream && api.getrf_buf && api.getrf &&
+                            api.getrs && api.potrf_buf && api.potrf && api.potrs;
+            if (!api.solver_ok) api.why_solver = "cuSOLVER is missing dense LU / Cholesky entry points";
+        } else {
+            api.why_solver = std::string("cuSOLVER not found (") + dlerror() + ")";
         }
-        auto sym = [&](const char *s) { return dlsym(h, s); };
-        api.create = reinterpret_cast<decltype(api.create)>(sym("cusolverDnCreate"));
-        api.destroy = reinterpret_cast<decltype(api.destroy)>(sym("cusolverDnDestroy"));
-        api.set_stream = reinterpret_cast<decltype(api.set_stream)>(sym("cusolverDnSetStream"));
-        api.getrf_buf = reinterpret_cast<decltype(api.getrf_buf)>(sym("cusolverDnDgetrf_bufferSize"));
-        api.getrf = reinterpret_cast<decltype(api.getrf)>(sym("cusolverDnDgetrf"));
-        api.getrs = reinterpret_cast<decltype(api.getrs)>(sym("cusolverDnDgetrs"));
-        api.ok = api.create && api.destroy && api.set_stream && api.getrf_buf && api.getrf && api.getrs;
-        if (!api.ok) api.why = "cuSOLVER is missing dense LU entry points";
+        const char *blas[] = {"libcublas.so.13", "libcublas.so", "/usr/local/cuda/lib64/libcublas.so.13"};
+        if (void *h = open(blas, 3)) {
+            auto sym = [&](const char *s) { return dlsym(h, s); };
+            api.blas_create = reinterpret_cast<decltype(api.blas_create)>(sym("cublasCreate_v2"));
+            api.blas_destroy = reinterpret_cast<decltype(api.blas_destroy)>(sym("cublasDestroy_v2"));
+            api.blas_set_stream = reinterpret_cast<decltype(api.blas_set_stream)>(sym("cublasSetStream_v2"));
+            api.dgemm = reinterpret_cast<decltype(api.dgemm)>(sym("cublasDgemm_v2"));
+            api.dsyrk = reinterpret_cast<decltype(api.dsyrk)>(sym("cublasDsyrk_v2"));
+            api.blas_ok = api.blas_create && api.blas_destroy && api.blas_set_stream && api.dgemm && api.dsyrk;
+            if (!api.blas_ok) api.why_blas = "cuBLAS is missing FP64 GEMM entry points";
+        } else {
+            api.why_blas = std::string("cuBLAS not found (") + dlerror() + ")";
+        }
     });
     return api;
 }
+
+}  // namespace sod
+
+namespace {
 
 // out[c][r] = in[r][c] for an R x C row-major matrix (32 x 32 tiles through shared memory)
 __global__ void transpose_kernel(const double *__restrict__ in, int R, int C, double *__restrict__ out) {
@@ -76,13 +85,6 @@ __global__ void transpose_kernel(const double *__restrict__ in, int R, int C, do
     }
 }
 
-int transpose(sod_context *ctx, const double *in, int R, int C, double *out) {
-    const dim3 grid((C + 31) / 32, (R + 31) / 32), block(32, 8);
-    transpose_kernel<<<grid, block, 0, ctx->stream>>>(in, R, C, out);
-    SOD_CHECK_CUDA(cudaGetLastError());
-    ctx->count();
-    return SOD_OK;
-}
 
 // X[r][j] = sum_c Ai[r][c] B[c][j] (FP64): one warp per row, lanes over the columns in a fixed
 // stride, FP64 xor tree over the lanes (deterministic).  B (n x R) stays in L2.
@@ -116,6 +118,14 @@ __global__ void identity_kernel(double *I, int n) {
 
 }  // namespace
 
+int sod::transpose_f64(sod_context *ctx, const double *in, int R, int C, double *out) {
+    const dim3 grid((C + 31) / 32, (R + 31) / 32), block(32, 8);
+    transpose_kernel<<<grid, block, 0, ctx->stream>>>(in, R, C, out);
+    SOD_CHECK_CUDA(cudaGetLastError());
+    ctx->count();
+    return SOD_OK;
+}
+
 struct sod_solver {
     sod_context *ctx = nullptr;
     int n = 0;
@@ -124,7 +134,7 @@ struct sod_solver {
     DevBuf inv;         // A^-1 (row-major) once sod_solver_keep_inverse ran
     bool has_inv = false;
     ~sod_solver() {
-        if (h) dn_api().destroy(h);
+        if (h) dense_api().dn_destroy(h);
     }
 };
 
@@ -148,14 +158,14 @@ int solver_apply_device(sod_solver *s, int nrhs, const double *B, double *X) {
 int solver_solve_device(sod_solver *s, int nrhs, const double *B, double *X) {
     sod_context *ctx = s->ctx;
     const int n = s->n;
-    const DnApi &api = dn_api();
+    const DenseApi &api = dense_api();
     const size_t bytes = sizeof(double) * (size_t)n * nrhs;
     SOD_TRY(s->rhs.ensure(bytes));
     double *cm = s->rhs.as<double>();
     if (nrhs == 1) {
         if (cm != B) SOD_CHECK_CUDA(cudaMemcpyAsync(cm, B, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     } else {
-        SOD_TRY(transpose(ctx, B, n, nrhs, cm));  // -> column-major n x nrhs
+        SOD_TRY(transpose_f64(ctx, B, n, nrhs, cm));  // -> column-major n x nrhs
     }
     if (api.getrs(s->h, CUBLAS_OP_T, n, nrhs, s->lu.as<double>(), n, s->ipiv.as<int>(), cm, n, s->info.as<int>()) !=
         CUSOLVER_STATUS_SUCCESS) {
@@ -166,7 +176,7 @@ int solver_solve_device(sod_solver *s, int nrhs, const double *B, double *X) {
     if (nrhs == 1) {
         if (X != cm) SOD_CHECK_CUDA(cudaMemcpyAsync(X, cm, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     } else {
-        SOD_TRY(transpose(ctx, cm, nrhs, n, X));  // column-major n x nrhs is row-major nrhs x n
+        SOD_TRY(transpose_f64(ctx, cm, nrhs, n, X));  // column-major n x nrhs is row-major nrhs x n
     }
     return SOD_OK;
 }
@@ -177,16 +187,16 @@ extern "C" {
 int sod_solver_create(sod_context *ctx, int n, const double *A, sod_solver **out) {
     SOD_REQUIRE(ctx && A && out, "null argument");
     SOD_REQUIRE(n >= 1, "matrix size must be >= 1");
-    const DnApi &api = dn_api();
-    if (!api.ok) {
-        set_error(api.why);
+    const DenseApi &api = dense_api();
+    if (!api.solver_ok) {
+        set_error(api.why_solver);
         return SOD_ERR_UNSUPPORTED;
     }
     SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
     auto s = std::make_unique<sod_solver>();
     s->ctx = ctx;
     s->n = n;
-    if (api.create(&s->h) != CUSOLVER_STATUS_SUCCESS || api.set_stream(s->h, ctx->stream) != CUSOLVER_STATUS_SUCCESS) {
+    if (api.dn_create(&s->h) != CUSOLVER_STATUS_SUCCESS || api.dn_set_stream(s->h, ctx->stream) != CUSOLVER_STATUS_SUCCESS) {
         s->h = nullptr;
         set_error("cusolverDnCreate failed");
         return SOD_ERR_CUDA;

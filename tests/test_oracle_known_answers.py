@@ -145,3 +145,39 @@ def test_mixed_mode_close_to_fp64(oracle):
         a = oracle.collocation(kind, m, mat, s, mode=oracle.FP64)
         b = oracle.collocation(kind, m, mat, s, mode=oracle.MIXED)
         assert np.linalg.norm(a - b) / np.linalg.norm(a) < 2e-6, kind
+
+
+@pytest.mark.parametrize("k,rank", [(3, 3), (3, 2), (6, 4), (3, 0)])
+def test_cod_solve_is_minimum_norm_least_squares(oracle, k, rank):
+    """The restated complete orthogonal decomposition gives the minimum-norm least-squares solution:
+    numpy's lstsq for full column rank, the pseudo-inverse for planted dependencies."""
+    rng = np.random.default_rng(10 * k + rank)
+    m = 200
+    B = rng.normal(size=(m, k)) if rank else np.zeros((m, k))
+    for c in range(rank, k):
+        if rank:
+            B[:, c] = 2.0 * B[:, c - rank] - B[:, (c + 1) % rank]
+    Y = rng.normal(size=(m, 5))
+    X = oracle.cod_solve(B, Y)
+    ref = np.linalg.lstsq(B, Y, rcond=None)[0] if rank == k else np.linalg.pinv(B, rcond=1e-10) @ Y
+    assert np.linalg.norm(X - ref) <= 1e-12 * max(np.linalg.norm(ref), 1.0)
+    assert oracle.cod_solve(B, Y[:, 0]).shape == (k,)
+
+
+def test_elastostatic_u_p_restatement(oracle):
+    """u_p = H'^-1 G' with H' = H^T H + c^2 T^T T and G' = H^T G P is the least-squares solution of
+    [H; c T] u = [G P; 0]; computed that way (QR, no normal equations) it agrees within the
+    conditioning of H'.  P removes rigid tractions: T P = 0, so u_p T^T = 0."""
+    m = make_icosphere_mesh(1, 0.1)
+    mat = Material(1e5, 0.3, 1000.0)
+    H = oracle.elastostatic("H", m, mat)
+    G = oracle.elastostatic("G", m, mat)
+    T = oracle.rigid_modes(m)
+    up = oracle.elastostatic_u_p(H, G, T)
+    n = H.shape[0]
+    c = np.trace(H) / n
+    P = np.eye(n) - T.T @ np.linalg.solve(T @ T.T, T)
+    assert np.abs(T @ P).max() < 1e-12 * np.abs(T).max()
+    stacked = np.linalg.lstsq(np.vstack([H, c * T]), np.vstack([G @ P, np.zeros((6, n))]), rcond=None)[0]
+    assert np.linalg.norm(up - stacked) / np.linalg.norm(stacked) < 1e-8
+    assert np.linalg.norm(up @ T.T) < 1e-9 * np.linalg.norm(up) * np.linalg.norm(T)
