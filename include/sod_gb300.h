@@ -213,6 +213,24 @@ int sod_history_reset(sod_history *bank);
  * engines keep it in different layouts). */
 enum { SOD_HISTORY_ENGINE_AUTO = 0, SOD_HISTORY_ENGINE_CUDA_CORES = 1, SOD_HISTORY_ENGINE_TENSOR_CORES = 2 };
 int sod_history_set_engine(sod_history *bank, int engine);
+/* Wavelet-compressed bank: replaces CompressedMatrix<1> / CompressedVector<1> of the compressed
+ * history (include/wavelets.hpp:337-436, src/elastodynamics_cqbem_object.cpp:31-41, 217-226,
+ * src/elastodynamics_cqbem_matrix_collection.cpp:95-131).  Square 3nV x 3nV weights, one right-hand
+ * side.  sod_history_set_weights then permutes each matrix (dof i -> i / 3 + (i % 3) nV), takes the
+ * non-standard Haar decomposition of the zero-padded matrix (size Np = 2^ceil(log2 3nV); FP64,
+ * bit-identical to a plain FP64 evaluation in the reference's order) and keeps the (int)(9 nV^2 ratio)
+ * coefficients of largest magnitude (all nonzero ones if that is 0; ties at the threshold in (row,
+ * column) order).  push, convolve, reset and the B terms work as for a dense bank; the per-step
+ * product is one sparse pass over all kept coefficients plus the inverse transform.  3nV <= 16384.
+ * sod_history_bytes reports the kept coefficients (12 bytes each). */
+int sod_history_create_compressed(sod_context *ctx, int nV, int K, double ratio, sod_history **bank);
+/* Kept coefficients of G_k (which = 0) or -H_k (which = 1) as CSR of the (2Np - 2)^2 matrix (columns
+ * ascending; row_ptr has 2Np - 1 entries).  Pass NULL arrays to get nnz only.  Host arrays. */
+int sod_history_compressed_matrix(sod_history *bank, int k, int which, int64_t *nnz, int32_t *row_ptr,
+                                  int32_t *col, double *val);
+/* The same matrix as the reference's .cpmat file (save_compressed_matrix, include/wavelets.hpp:474-502),
+ * so the original simulator loads it unchanged (its cache names are H_k_<ratio>.cpmat / G_k_<ratio>.cpmat). */
+int sod_history_write_cpmat(sod_history *bank, int k, int which, const char *path);
 int sod_history_bytes(const sod_history *bank, int64_t *weight_bytes);
 int sod_history_destroy(sod_history *bank);
 

@@ -240,3 +240,133 @@ def elastostatic_u_p(H: np.ndarray, G: np.ndarray, T: np.ndarray) -> np.ndarray:
     Hr = H.T @ H + (np.trace(H) / n) ** 2 * (T.T @ T)
     Gp = H.T @ G @ (np.eye(n) - T.T @ np.linalg.solve(T @ T.T, T))
     return sl.solve(Hr, Gp, assume_a="sym")
+
+
+# ---- wavelet-compressed history (Haar, the reference's CompressedMatrix<1>) ----------------------
+HAAR = 0.70710678118654752440  # M_SQRT1_2: h = (HAAR, HAAR), g = (HAAR, -HAAR) (include/wavelets.hpp:15-17)
+
+
+def _haar_perm(nV: int) -> np.ndarray:
+    """Permuted position of dof i: (i / 3) + (i % 3) nV (src/elastics_bem_matrix_collection.cpp:25-29)."""
+    i = np.arange(3 * nV)
+    return i // 3 + (i % 3) * nV
+
+
+def _pow2(N: int) -> int:
+    return 1 << max(1, int(np.ceil(np.log2(N))))
+
+
+def wavelet_compress(M: np.ndarray, nV: int, ratio: float, sign: float = 1.0):
+    """CompressedMatrix<1>(P (sign M) P^T, ratio) (include/wavelets.hpp:163-226, 402-420): the Haar
+    non-standard form of the zero-padded permuted matrix (alpha = gg, beta = gh, gamma = hg blocks
+    per level, the last scale coefficient at (2Np-3, 2Np-3)), keeping the (int)(N^2 ratio) entries of
+    largest magnitude (all nonzero entries if that is <= 0).  Sums in the reference's order (k outer,
+    m inner; (f_k f_m) s added to a running sum from 0).  Ties at the threshold are kept in (row,
+    column) order (the reference's heap keeps an arbitrary subset of them).
+    Returns (row_ptr, col, val) of the (2Np-2)^2 matrix, entries sorted by (row, column)."""
+    N = 3 * nV
+    Np = _pow2(N)
+    sig = _haar_perm(nV)
+    S = np.zeros((Np, Np))
+    S[np.ix_(sig, sig)] = sign * np.asarray(M, dtype=np.float64)
+    h, g = (HAAR, HAAR), (HAAR, -HAAR)
+
+    def comb(fk, fm, s00, s01, s10, s11):
+        a = 0.0 + (fk[0] * fm[0]) * s00
+        a = a + (fk[0] * fm[1]) * s01
+        a = a + (fk[1] * fm[0]) * s10
+        return a + (fk[1] * fm[1]) * s11
+
+    vals, cols, counts = [], [], []
+    size, offset = Np // 2, 0
+    while size >= 1:
+        q = (S[0::2, 0::2], S[0::2, 1::2], S[1::2, 0::2], S[1::2, 1::2])
+        alpha, beta, gamma, new_s = comb(g, g, *q), comb(g, h, *q), comb(h, g, *q), comb(h, h, *q)
+        vals.append(np.hstack([alpha, beta]).ravel())
+        cols.append(np.tile(offset + np.arange(2 * size), size))
+        counts += [2 * size] * size
+        vals.append(gamma.ravel())
+        cols.append(np.tile(offset + np.arange(size), size))
+        counts += [size] * size
+        offset += 2 * size
+        size //= 2
+        S = new_s
+    vals.append(np.array([S[0, 0]]))
+    cols.append(np.array([offset - 1]))
+    counts[-1] += 1  # the last gamma row also holds the final scale coefficient
+    v = np.concatenate(vals)
+    c = np.concatenate(cols)
+    rows = np.repeat(np.arange(len(counts)), counts)
+    a = np.abs(v)
+    keep = int(N * N * ratio)
+    if keep <= 0 or np.count_nonzero(a) <= keep:
+        sel = a > 0
+    else:
+        t = np.partition(a, a.size - keep)[a.size - keep]  # keep-th largest magnitude
+        sel = a > t
+        eq = np.flatnonzero(a == t)
+        sel[eq[:keep - int(sel.sum())]] = True
+    L = 2 * Np - 2
+    row_ptr = np.zeros(L + 1, dtype=np.int64)
+    np.add.at(row_ptr, rows[sel] + 1, 1)
+    return np.cumsum(row_ptr), c[sel].astype(np.int64), v[sel]
+
+
+def wavelet_vector(x: np.ndarray, nV: int) -> np.ndarray:
+    """CompressedVector<1>(P x) (include/wavelets.hpp:228-256, 383-399): per level the detail (g)
+    then the scale (h) coefficients, 2Np-2 values."""
+    N = 3 * nV
+    Np = _pow2(N)
+    s = np.zeros(Np)
+    s[_haar_perm(nV)] = x
+    out = np.zeros(2 * Np - 2)
+    size, offset = Np // 2, 0
+    while size >= 1:
+        a, b = s[0::2], s[1::2]
+        d = (0.0 + HAAR * a) + (-HAAR) * b
+        ns = (0.0 + HAAR * a) + HAAR * b
+        out[offset:offset + size] = d
+        out[offset + size:offset + 2 * size] = ns
+        s = ns
+        offset += 2 * size
+        size //= 2
+    return out
+
+
+def wavelet_reconstruct(y: np.ndarray, nV: int) -> np.ndarray:
+    """CompressedMatrixVectorProduct<1> -> vector (include/wavelets.hpp:258-283, 372-376), then the
+    inverse permutation: result[i] = reconstructed[(i / 3) + (i % 3) nV]."""
+    Np = (len(y) + 2) // 2
+    res = np.zeros(Np)
+    size, offset = 1, -2
+    while size <= Np // 2:
+        base = 2 * Np - 2 + offset
+        d = y[base:base + size]
+        s = y[base + size:base + 2 * size] + res[:size]
+        res[:2 * size] = 0.0
+        res[0:2 * size:2] = 0.0 + (HAAR * s + HAAR * d)
+        res[1:2 * size:2] = 0.0 + (HAAR * s + (-HAAR) * d)
+        offset -= 4 * size
+        size *= 2
+    return res[_haar_perm(nV)]
+
+
+def wavelet_history_convolution(Gc, Hc, p_hist, u_hist, nV, B=None, a_hist=None):
+    """Compressed history of ElastodynamicsCQBEMObject::estimate_next_state
+    (src/elastodynamics_cqbem_object.cpp:31-41): b = P^T reconstruct(sum_k D(-H_k) w(u_{n-k}) +
+    D(G_k) w(p_{n-k})) + sum_k B_k a_{n-k}.  Gc[k], Hc[k] (k = 1..K): wavelet_compress of G_k and of
+    H_k with sign -1; p_hist/u_hist: (K, 3V), index 0 the most recent step."""
+    import scipy.sparse as sp
+
+    N = 3 * nV
+    Np = _pow2(N)
+    L = 2 * Np - 2
+    y = np.zeros(L)
+    for k in range(1, p_hist.shape[0] + 1):
+        for D, x in ((Hc[k], u_hist[k - 1]), (Gc[k], p_hist[k - 1])):
+            y += sp.csr_matrix((D[2], D[1], D[0]), shape=(L, L)) @ wavelet_vector(x, nV)
+    b = wavelet_reconstruct(y, nV)
+    if B is not None:
+        for k in range(1, p_hist.shape[0] + 1):
+            b = b + B[k] @ a_hist[k - 1]
+    return b

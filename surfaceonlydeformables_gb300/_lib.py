@@ -93,6 +93,9 @@ _SIGS = {
     "sod_mat_read": ([_P, _c.c_char_p, _P, _c.c_int64, _c.c_int64], _c.c_int),
     "sod_cqbem_write_cache": ([_P, _c.c_char_p, _c.c_int, _c.c_int, _P, _P, _P, _P, _c.c_int], _c.c_int),
     "sod_history_set_engine": ([_P, _c.c_int], _c.c_int),
+    "sod_history_create_compressed": ([_P, _c.c_int, _c.c_int, _c.c_double, _P], _c.c_int),
+    "sod_history_compressed_matrix": ([_P, _c.c_int, _c.c_int, _P, _P, _P, _P], _c.c_int),
+    "sod_history_write_cpmat": ([_P, _c.c_int, _c.c_int, _c.c_char_p], _c.c_int),
     "sod_history_bytes": ([_P, _P], _c.c_int),
     "sod_history_destroy": ([_P], _c.c_int),
     "sod_cq_inverse_transform": ([_P, _P, _c.c_int, _c.c_int64, _c.c_int, _c.c_int, _c.c_double, _P, _c.c_int],

@@ -437,6 +437,34 @@ class HistoryBank:
         L.check(L.load().sod_history_bytes(self._h, ctypes.byref(v)))
         return int(v.value)
 
+    @classmethod
+    def compressed(cls, ctx: Context, nV: int, K: int, ratio: float) -> "HistoryBank":
+        """Wavelet-compressed bank (sod_history_create_compressed): the reference's compressed
+        history with CompressedMatrix<1> (Haar) at `ratio` (fraction of the 9 nV^2 entries kept)."""
+        self = cls.__new__(cls)
+        self.ctx, self.nrow, self.ncol, self.K, self.R = ctx, 3 * nV, 3 * nV, K, 1
+        self._h = ctypes.c_void_p()
+        L.check(L.load().sod_history_create_compressed(ctx.handle, nV, K, ratio, ctypes.byref(self._h)))
+        return self
+
+    def compressed_matrix(self, k: int, which: int):
+        """(row_ptr, col, val) of the kept coefficients of G_k (which 0) or -H_k (which 1)."""
+        nnz = ctypes.c_int64()
+        L.check(L.load().sod_history_compressed_matrix(self._h, k, which, ctypes.byref(nnz), None, None, None))
+        Np = 2
+        while Np < self.nrow:
+            Np *= 2
+        rp = np.empty(2 * Np - 1, dtype=np.int32)
+        col = np.empty(nnz.value, dtype=np.int32)
+        val = np.empty(nnz.value, dtype=np.float64)
+        L.check(L.load().sod_history_compressed_matrix(self._h, k, which, ctypes.byref(nnz), L.ptr(rp), L.ptr(col),
+                                                       L.ptr(val)))
+        return rp, col, val
+
+    def write_cpmat(self, k: int, which: int, path: str) -> None:
+        """The reference's .cpmat file of G_k (which 0) or -H_k (which 1)."""
+        L.check(L.load().sod_history_write_cpmat(self._h, k, which, path.encode()))
+
     def close(self) -> None:
         if self._h:
             L.load().sod_history_destroy(self._h)

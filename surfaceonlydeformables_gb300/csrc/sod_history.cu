@@ -28,6 +28,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <memory>
 #include <vector>
 
@@ -48,6 +49,7 @@ struct sod_history {
     DevBuf bsolve;            // b of the fused per-step solve  // tensor-core path: BF16 hi/lo history, per-segment partials, error word
     int *err_host = nullptr;  // pinned copy of the error word (written by the finish kernel)
     HistTcPlan plan;          // tensor maps of W and Xt
+    WaveletBank *wav = nullptr;  // wavelet-compressed weights (sod_history_create_compressed)
     bool use_tensor() const {
         if (engine == SOD_HISTORY_ENGINE_AUTO) return wdtype == SOD_BF16 || R == 16;
         return engine == SOD_HISTORY_ENGINE_TENSOR_CORES;
@@ -56,6 +58,7 @@ struct sod_history {
     int xt_rows() const { return R == 16 ? 2 * 16 : 16; }  // history rows per (slot, G|H)
     ~sod_history() {
         if (err_host) cudaFreeHost(err_host);
+        wavelet_bank_free(wav);
     }
 };
 
@@ -343,6 +346,18 @@ int sod_history_set_weights(sod_history *h, int k, const void *G_k, const void *
     SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
     const size_t isz = in_dtype == SOD_F64 ? 8 : 4, bytes = isz * (size_t)h->nrow * h->ncol;
     const void *src[2] = {G_k, H_k};
+    if (h->wav) {
+        for (int t = 0; t < 2; t++) {
+            const void *d = src[t];
+            if (!is_device_pointer(d)) {
+                SOD_TRY(h->tmp.ensure(bytes));
+                SOD_CHECK_CUDA(cudaMemcpyAsync(h->tmp.p, d, bytes, cudaMemcpyHostToDevice, ctx->stream));
+                d = h->tmp.p;
+            }
+            SOD_TRY(wavelet_set_block(ctx, h->wav, 2 * (k - 1) + t, d, in_dtype == SOD_F64, t == 0 ? 1.0 : -1.0));
+        }
+        return SOD_OK;
+    }
     for (int t = 0; t < 2; t++) {
         const void *d = src[t];
         if (!is_device_pointer(d)) {
@@ -406,7 +421,9 @@ int sod_history_push(sod_history *h, const double *p, const double *u, const dou
         }
     }
     const int n = h->ldw * h->R;
-    if (h->wdtype == SOD_BF16)
+    if (h->wav)
+        SOD_TRY(wavelet_push(ctx, h->wav, dp, du, da, h->head, h->A.as<double>() + (size_t)h->head * 6));
+    else if (h->wdtype == SOD_BF16)
         hist_push_kernel<__nv_bfloat16><<<(n + 255) / 256, 256, 0, ctx->stream>>>(
             dp, du, da, h->ncol, h->ldw, h->R, h->head, h->X.as<float>(), h->A.as<double>(),
             h->use_tensor() ? h->Xt.as<__nv_bfloat16>() : nullptr);
@@ -434,7 +451,9 @@ int sod_history_convolve(sod_history *h, double *b_out) {
         dst = ctx->staging.as<double>();
     }
     const int used = h->count;
-    if (h->use_tensor()) {
+    if (h->wav) {
+        SOD_TRY(wavelet_convolve(ctx, h->wav, used, h->head, h->partial.as<double>()));
+    } else if (h->use_tensor()) {
         // a bounded wait that expired in an earlier convolution (read from the pinned copy)
         if (*(volatile int *)h->err_host) {
             set_error("tensor-core history convolution: a bounded mbarrier wait expired (code " +
@@ -454,8 +473,7 @@ int sod_history_convolve(sod_history *h, double *b_out) {
             }
         }
         return SOD_OK;
-    }
-    if (used > 0) {
+    } else if (used > 0) {
         const bool bf = h->wdtype == SOD_BF16;
         if (h->R == 1)
             bf ? launch_conv<1, 4, __nv_bfloat16>(h, ctx->stream, used) : launch_conv<1, 8, float>(h, ctx->stream, used);
@@ -503,6 +521,11 @@ int sod_history_set_engine(sod_history *h, int engine) {
     SOD_REQUIRE(engine == SOD_HISTORY_ENGINE_AUTO || engine == SOD_HISTORY_ENGINE_CUDA_CORES ||
                     engine == SOD_HISTORY_ENGINE_TENSOR_CORES,
                 "engine must be SOD_HISTORY_ENGINE_AUTO, _CUDA_CORES or _TENSOR_CORES");
+    if (h->wav) {
+        SOD_REQUIRE(engine != SOD_HISTORY_ENGINE_TENSOR_CORES,
+                    "a wavelet-compressed bank runs its sparse products on the CUDA cores");
+        return SOD_OK;
+    }
     const bool before = h->use_tensor();
     h->engine = engine;
     if (h->use_tensor() != before) {
@@ -522,7 +545,68 @@ int sod_history_reset(sod_history *h) {
 
 int sod_history_bytes(const sod_history *h, int64_t *weight_bytes) {
     SOD_REQUIRE(h && weight_bytes, "null argument");
-    *weight_bytes = (int64_t)(h->W.bytes + h->scale.bytes);
+    *weight_bytes = h->wav ? wavelet_bytes(h->wav) : (int64_t)(h->W.bytes + h->scale.bytes);
+    return SOD_OK;
+}
+
+int sod_history_create_compressed(sod_context *ctx, int nV, int K, double ratio, sod_history **out) {
+    SOD_REQUIRE(ctx && out, "null argument");
+    SOD_REQUIRE(nV >= 1 && K >= 1, "compressed history bank needs nV, K >= 1");
+    SOD_REQUIRE(ratio > 0.0 && ratio <= 1.0, "compression ratio must be in (0, 1]");
+    SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
+    *out = nullptr;
+    auto h = std::make_unique<sod_history>();
+    h->ctx = ctx;
+    h->nrow = h->ncol = 3 * nV, h->K = K, h->R = 1, h->wdtype = SOD_F64;
+    h->ldw = h->ncol;
+    h->engine = SOD_HISTORY_ENGINE_CUDA_CORES;
+    SOD_TRY(wavelet_bank_create(ctx, nV, K, ratio, &h->wav));
+    SOD_TRY(h->A.ensure(sizeof(double) * (size_t)K * 6));
+    SOD_CHECK_CUDA(cudaMemsetAsync(h->A.p, 0, h->A.bytes, ctx->stream));
+    h->nchunk = 1;  // the reconstructed product is the finish kernel's single partial
+    SOD_TRY(h->partial.ensure(sizeof(double) * (size_t)h->nrow));
+    *out = h.release();
+    return SOD_OK;
+}
+
+int sod_history_compressed_matrix(sod_history *h, int k, int which, int64_t *nnz, int32_t *row_ptr, int32_t *col,
+                                  double *val) {
+    SOD_REQUIRE(h && nnz, "null argument");
+    SOD_REQUIRE(h->wav, "not a compressed history bank");
+    SOD_REQUIRE(k >= 1 && k <= h->K && (which == 0 || which == 1), "k must be in 1..K and which 0 (G) or 1 (H)");
+    SOD_CHECK_CUDA(cudaSetDevice(h->ctx->device));
+    return wavelet_block(h->wav, 2 * (k - 1) + which, nnz, row_ptr, col, val, h->ctx->stream);
+}
+
+int sod_history_write_cpmat(sod_history *h, int k, int which, const char *path) {
+    SOD_REQUIRE(h && path, "null argument");
+    SOD_REQUIRE(h->wav, "not a compressed history bank");
+    SOD_REQUIRE(k >= 1 && k <= h->K && (which == 0 || which == 1), "k must be in 1..K and which 0 (G) or 1 (H)");
+    SOD_CHECK_CUDA(cudaSetDevice(h->ctx->device));
+    int N = 0, L = 0;
+    wavelet_dims(h->wav, &N, &L);
+    int64_t nnz = 0;
+    SOD_TRY(wavelet_block(h->wav, 2 * (k - 1) + which, &nnz, nullptr, nullptr, nullptr, h->ctx->stream));
+    std::vector<int32_t> rp(L + 1), col(nnz);
+    std::vector<double> val(nnz);
+    SOD_TRY(wavelet_block(h->wav, 2 * (k - 1) + which, &nnz, rp.data(), col.data(), val.data(), h->ctx->stream));
+    // save_compressed_matrix (include/wavelets.hpp:474-502): int N; int64 rows, cols, nonZeros,
+    // outerSize, innerSize; values; the outerSize row starts; column indices
+    FILE *f = fopen(path, "wb");
+    if (!f) {
+        set_error(std::string("cannot open for writing: ") + path);
+        return SOD_ERR_INVALID_ARG;
+    }
+    const int64_t hdr[5] = {L, L, nnz, L, L};
+    bool ok = fwrite(&N, sizeof(int), 1, f) == 1 && fwrite(hdr, sizeof(int64_t), 5, f) == 5 &&
+              fwrite(val.data(), sizeof(double), nnz, f) == (size_t)nnz &&
+              fwrite(rp.data(), sizeof(int32_t), L, f) == (size_t)L &&
+              fwrite(col.data(), sizeof(int32_t), nnz, f) == (size_t)nnz;
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) {
+        set_error(std::string("write failed: ") + path);
+        return SOD_ERR_INVALID_ARG;
+    }
     return SOD_OK;
 }
 

@@ -258,6 +258,21 @@ int launch_history_tc(sod_context *ctx, const HistTcPlan *plan, const float *sca
                       float *partial, const double *Bw, const double *A, double *out, int *err, int *err_mirror,
                       cudaStream_t stream);
 
+// wavelet-compressed history weights (sod_wavelet.cu): Haar non-standard form of P W P^T per block
+// b = 2 (k - 1) + {0: G, 1: -H}, top-(N^2 ratio) coefficients as CSR, merged for the per-step SpMV
+struct WaveletBank;
+int wavelet_bank_create(sod_context *ctx, int nV, int K, double ratio, WaveletBank **out);
+void wavelet_bank_free(WaveletBank *w);
+int wavelet_set_block(sod_context *ctx, WaveletBank *w, int b, const void *W, bool f64, double sign);
+// ring slot `slot` <- wavelet vectors of p and u; aslot (6 doubles) <- a or zeros
+int wavelet_push(sod_context *ctx, WaveletBank *w, const double *p, const double *u, const double *a, int slot,
+                 double *aslot);
+// out (3nV) = P^T reconstruct(sum over the `used` most recent steps); head = ring slot of the next push
+int wavelet_convolve(sod_context *ctx, WaveletBank *w, int used, int head, double *out);
+int64_t wavelet_bytes(const WaveletBank *w);
+int wavelet_block(const WaveletBank *w, int b, int64_t *nnz, int *row_ptr, int *col, double *val, cudaStream_t st);
+int wavelet_dims(const WaveletBank *w, int *N, int *L);
+
 // dense LU solves (sod_solve.cu); X = A^-1 B, row-major device buffers, X may alias B
 int solver_size(const sod_solver *s);
 int solver_solve_device(sod_solver *s, int nrhs, const double *B, double *X);

@@ -181,3 +181,43 @@ def test_elastostatic_u_p_restatement(oracle):
     stacked = np.linalg.lstsq(np.vstack([H, c * T]), np.vstack([G @ P, np.zeros((6, n))]), rcond=None)[0]
     assert np.linalg.norm(up - stacked) / np.linalg.norm(stacked) < 1e-8
     assert np.linalg.norm(up @ T.T) < 1e-9 * np.linalg.norm(up) * np.linalg.norm(T)
+
+
+def test_wavelet_history_lossless_and_selection(oracle):
+    """Keeping every coefficient, the compressed history (Haar non-standard form, the reference's
+    CompressedMatrix<1>) reproduces the dense convolution; with a ratio, exactly (int)(N^2 ratio)
+    coefficients are kept and none dropped is larger than any kept."""
+    rng = np.random.default_rng(7)
+    nV, K = 14, 3
+    N = 3 * nV
+    G = [np.zeros((N, N))] + [rng.normal(size=(N, N)) * 0.5 ** k for k in range(1, K + 1)]
+    H = [np.zeros((N, N))] + [rng.normal(size=(N, N)) * 0.5 ** k for k in range(1, K + 1)]
+    p, u = rng.normal(size=(K, N)), rng.normal(size=(K, N))
+    B = [np.zeros((N, 6))] + [rng.normal(size=(N, 6)) for _ in range(K)]
+    a = rng.normal(size=(K, 6))
+    dense = oracle.history_convolution(np.stack(G), np.stack(H), p, u, np.stack(B), a)
+    Gc = {k: oracle.wavelet_compress(G[k], nV, 1e-12) for k in range(1, K + 1)}
+    Hc = {k: oracle.wavelet_compress(H[k], nV, 1e-12, -1.0) for k in range(1, K + 1)}
+    b = oracle.wavelet_history_convolution(Gc, Hc, p, u, nV, np.stack(B), a)
+    assert np.linalg.norm(b - dense) / np.linalg.norm(dense) < 1e-13
+    full = oracle.wavelet_compress(G[1], nV, 1e-12)
+    part = oracle.wavelet_compress(G[1], nV, 0.1)
+    assert len(part[2]) == int(N * N * 0.1)
+    dropped = np.setdiff1d(np.abs(full[2]), np.abs(part[2]))
+    assert np.abs(part[2]).min() >= dropped.max()
+    assert np.all(np.diff(part[0]) >= 0) and part[0][-1] == len(part[2])
+
+
+def test_wavelet_vector_and_reconstruct_invert(oracle):
+    """The scale coefficients of the vector transform are what the reconstruction consumes: feeding
+    the non-standard product of the identity (D = the decomposed identity) returns the vector."""
+    rng = np.random.default_rng(8)
+    nV = 11
+    N = 3 * nV
+    x = rng.normal(size=N)
+    D = oracle.wavelet_compress(np.eye(N), nV, 1e-12)
+    import scipy.sparse as sp
+
+    L = len(D[0]) - 1
+    y = sp.csr_matrix((D[2], D[1], D[0]), shape=(L, L)) @ oracle.wavelet_vector(x, nV)
+    assert np.abs(oracle.wavelet_reconstruct(y, nV) - x).max() < 1e-14
