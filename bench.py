@@ -243,10 +243,22 @@ def history_leg(torch, ctx, stream, n: int = 7686, K: int = 64, reps: int = 10):
         del g, out
         torch.cuda.empty_cache()
     # wavelet-compressed bank (Haar non-standard form, 10% of the 9 nV^2 coefficients kept per matrix,
-    # the ratio of the reference's compressed-history scenes); bytes = kept coefficients x 12 B
+    # the ratio of the reference's compressed-history scenes)
+    rows.append(wavelet_case(torch, ctx, stream, n // 3, K, 0.1, reps, hbm))
+    return {"object": "3V = 7686 (2562 vertices), N = 64", "peak_gbs": hbm,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth, measured)", "cases": rows}
+
+
+def wavelet_case(torch, ctx, stream, nV: int, K: int, ratio: float, reps: int, hbm: float) -> dict:
+    """Per-step convolution of a wavelet-compressed bank (3 nV rows, K steps, `ratio` of the
+    coefficients kept), synthetic FP32 weights as the dense cases; algorithmic bytes = the kept
+    coefficients x 12 B (FP64 value + packed column)."""
     import time
 
-    bank = api.HistoryBank.compressed(ctx, n // 3, K, 0.1)
+    from surfaceonlydeformables_gb300 import api
+
+    n = 3 * nV
+    bank = api.HistoryBank.compressed(ctx, nV, K, ratio)
     g = torch.empty((n, n), dtype=torch.float32, device="cuda")
     gen = torch.Generator(device="cuda")
     gen.manual_seed(7)
@@ -274,14 +286,12 @@ def history_leg(torch, ctx, stream, n: int = 7686, K: int = 64, reps: int = 10):
         ts.append(e0.elapsed_time(e1))
     ms = float(np.median(ts))
     wb = bank.weight_bytes
-    rows.append({"weights": "haar_ratio_0.1", "rhs": 1, "engine": "sparse_cuda_cores", "ms": round(ms, 4),
-                 "gb_per_s": round(wb / ms / 1e6, 1), "hbm_frac": round(wb / ms / 1e6 / hbm, 4), "bytes": wb,
-                 "setup_s": round(setup_s, 2)})
     bank.close()
     del g, out
     torch.cuda.empty_cache()
-    return {"object": "3V = 7686 (2562 vertices), N = 64", "peak_gbs": hbm,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth, measured)", "cases": rows}
+    return {"weights": f"haar_ratio_{ratio}", "rows": n, "K": K, "rhs": 1, "engine": "sparse_cuda_cores",
+            "ms": round(ms, 4), "gb_per_s": round(wb / ms / 1e6, 1), "hbm_frac": round(wb / ms / 1e6 / hbm, 4),
+            "bytes": wb, "setup_s": round(setup_s, 2)}
 
 
 def elastostatic_leg(torch, ctx, stream):
@@ -821,6 +831,8 @@ def run_leg(args):
         out = galerkin_leg(torch, ctx, stream, level=args.galerkin_level)
     elif args.leg == "solve":
         out = solve_leg(torch, ctx, stream)
+    elif args.leg == "wavelet":
+        out = wavelet_case(torch, ctx, stream, args.wavelet_nv, args.history_k, 0.1, args.steps, measured_hbm_gbs())
     else:
         out = serving_leg(torch, ctx)
     print(json.dumps({"leg": args.leg, **out}))
@@ -836,9 +848,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop leg")
-    ap.add_argument("--leg", default="all", choices=["all", "history", "elastostatic", "galerkin", "serving", "solve"],
+    ap.add_argument("--leg", default="all", choices=["all", "history", "elastostatic", "galerkin", "serving", "solve", "wavelet"],
                     help="run one hot-path leg alone (profiling captures) and print its JSON")
     ap.add_argument("--history-k", type=int, default=64, help="history length of the --leg history bank")
+    ap.add_argument("--wavelet-nv", type=int, default=2562,
+                    help="vertices of the --leg wavelet compressed bank (642 = the small profiling case)")
     ap.add_argument("--galerkin-level", type=int, default=4, choices=[3, 4],
                     help="icosphere level of the --leg galerkin mesh (3: the small profiling case)")
     ap.add_argument("--value-only", action="store_true",

@@ -31,6 +31,8 @@
 //         column), so one SpMV over fixed-size chunks of every row reads each weight once; chunk
 //         sums and row sums run in a fixed order.  One CTA then reconstructs the vector level by
 //         level and applies P^T; the B terms are added by the history bank's finish kernel.
+// The product is one FP64 FMA per 12 bytes of kept coefficients: at the HBM rate that is about the
+// whole FP64 FMA rate of GB300, so the FP64 pipe, not HBM, bounds this kernel.
 #include <cmath>
 #include <vector>
 
@@ -214,23 +216,63 @@ __global__ void __launch_bounds__(1024) wav_push_kernel(const double *__restrict
     }
 }
 
-// partial[c] = sum over chunk c's nonzeros of v * x (blocks beyond the `used` history steps skipped)
+// partial[c] = sum over chunk c's nonzeros of v * x.  Each CTA first tabulates, per block
+// b = 2 (k - 1) + t, the ring offset of its history vector (-1 beyond the `used` steps).  Each lane
+// takes 4 nonzeros 32 apart per batch, with the next batch's columns and values in flight while the
+// current batch gathers x; 2 accumulators, fixed order.
+constexpr int SPMV_UNROLL = 4;
 __global__ void __launch_bounds__(256) wav_spmv_kernel(const longlong2 *__restrict__ chunks, int nchunk,
                                                        const unsigned int *__restrict__ mcol,
                                                        const double *__restrict__ mval,
                                                        const double *__restrict__ xring, int L, int K, int used,
-                                                       int head, double *__restrict__ partial) {
+                                                       int head, int nblk, double *__restrict__ partial) {
+    extern __shared__ long long xoff[];
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+        const int k = b / 2 + 1;
+        xoff[b] = k <= used ? ((long long)((head - k + 2 * K) % K) * 2 + (b & 1)) * L : -1LL;
+    }
+    __syncthreads();
     const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (c >= nchunk) return;
     const longlong2 ch = chunks[c];
-    double acc = 0.0;
-    for (long long e = ch.x + lane; e < ch.y; e += 32) {
-        const unsigned w = __ldg(mcol + e);
-        const int b = (int)(w >> COL_BITS), k = b / 2 + 1;
-        if (k > used) continue;
-        const int slot = (head - k + 2 * K) % K;
-        acc = fma(__ldg(mval + e), xring[((size_t)slot * 2 + (b & 1)) * L + (w & ((1u << COL_BITS) - 1))], acc);
+    double acc0 = 0.0, acc1 = 0.0;
+    constexpr unsigned MASK = (1u << COL_BITS) - 1u;
+    unsigned w[SPMV_UNROLL];
+    double v[SPMV_UNROLL];
+    long long e = ch.x + lane;
+#pragma unroll
+    for (int j = 0; j < SPMV_UNROLL; j++) {
+        const long long i = e + 32 * j;
+        w[j] = i < ch.y ? __ldg(mcol + i) : 0u;
+        v[j] = i < ch.y ? __ldg(mval + i) : 0.0;
     }
+    for (; e < ch.y; e += 32 * SPMV_UNROLL) {
+        unsigned wn[SPMV_UNROLL];
+        double vn[SPMV_UNROLL];
+#pragma unroll
+        for (int j = 0; j < SPMV_UNROLL; j++) {
+            const long long i = e + 32 * (SPMV_UNROLL + j);
+            wn[j] = i < ch.y ? __ldg(mcol + i) : 0u;
+            vn[j] = i < ch.y ? __ldg(mval + i) : 0.0;
+        }
+        double x[SPMV_UNROLL];
+#pragma unroll
+        for (int j = 0; j < SPMV_UNROLL; j++) {
+            const long long o = xoff[w[j] >> COL_BITS];
+            x[j] = (o >= 0 && e + 32 * j < ch.y) ? xring[o + (w[j] & MASK)] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < SPMV_UNROLL; j += 2) {
+            acc0 = fma(v[j], x[j], acc0);
+            acc1 = fma(v[j + 1], x[j + 1], acc1);
+        }
+#pragma unroll
+        for (int j = 0; j < SPMV_UNROLL; j++) {
+            w[j] = wn[j];
+            v[j] = vn[j];
+        }
+    }
+    double acc = acc0 + acc1;
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) partial[c] = acc;
 }
@@ -244,10 +286,12 @@ __global__ void wav_rowsum_kernel(const double *__restrict__ partial, const int 
     y[r] = s;
 }
 
-// reconstruction (include/wavelets.hpp:258-283), coarse to fine, then out[i] = res[P(i)]
+// reconstruction (include/wavelets.hpp:258-283), coarse to fine in shared memory (res: Np values,
+// sb: Np / 2), then out[i] = res[P(i)]
 __global__ void __launch_bounds__(1024) wav_reconstruct_kernel(const double *__restrict__ y, int nV, int Np,
-                                                               double *__restrict__ res, double *__restrict__ sb,
                                                                double *__restrict__ out) {
+    extern __shared__ double shm[];
+    double *res = shm, *sb = shm + Np;
     int offset = -2;
     for (int size = 1; size <= Np / 2; size *= 2) {
         const int base = 2 * Np - 2 + offset;
@@ -283,7 +327,7 @@ struct WaveletBank {
     std::vector<long long> cand_ptr;  // per row of D: first candidate (L + 1)
     DevBuf dcand, dcol0, coef, sA, sB, hist, gt, eq, eqb, xring;
     // merged CSR and the SpMV chunks
-    DevBuf mptr, mcol, mval, chunks, chunk_ptr, partial, y, res, sbuf, dblk;
+    DevBuf mptr, mcol, mval, chunks, chunk_ptr, partial, y, dblk;
     int nchunk = 0;
     long long nnz = 0;
     bool dirty = true;
@@ -299,7 +343,7 @@ int wavelet_bank_create(sod_context *ctx, int nV, int K, double ratio, WaveletBa
     w->Np = 2;
     while (w->Np < w->N) w->Np *= 2;
     SOD_REQUIRE(w->Np <= (1 << (COL_BITS - 1)), "compressed history supports 3 nV <= 16384");
-    SOD_REQUIRE((long long)2 * K < (1LL << (32 - COL_BITS)), "compressed history: K too large");
+    SOD_REQUIRE(K <= 2048, "compressed history supports K <= 2048");  // ring offsets per block in shared memory
     w->L = 2 * w->Np - 2;
     w->K = K;
     w->ratio = ratio;
@@ -329,8 +373,6 @@ int wavelet_bank_create(sod_context *ctx, int nV, int K, double ratio, WaveletBa
     SOD_TRY(w->xring.ensure(sizeof(double) * (size_t)K * 2 * w->L));
     SOD_CHECK_CUDA(cudaMemsetAsync(w->xring.p, 0, w->xring.bytes, ctx->stream));
     SOD_TRY(w->y.ensure(sizeof(double) * w->L));
-    SOD_TRY(w->res.ensure(sizeof(double) * w->Np));
-    SOD_TRY(w->sbuf.ensure(sizeof(double) * w->Np));
     SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));  // host tables above go out of scope
     *out = w.release();
     return SOD_OK;
@@ -505,15 +547,19 @@ int wavelet_convolve(sod_context *ctx, WaveletBank *w, int used, int head, doubl
     if (w->dirty) SOD_TRY(wavelet_merge(ctx, w));
     cudaStream_t st = ctx->stream;
     if (w->nchunk > 0) {
-        wav_spmv_kernel<<<(unsigned)(((size_t)w->nchunk * 32 + 255) / 256), 256, 0, st>>>(
+        const int nblk = 2 * w->K;
+        wav_spmv_kernel<<<(unsigned)(((size_t)w->nchunk * 32 + 255) / 256), 256, sizeof(long long) * nblk, st>>>(
             w->chunks.as<longlong2>(), w->nchunk, w->mcol.as<unsigned int>(), w->mval.as<double>(),
-            w->xring.as<double>(), w->L, w->K, used, head, w->partial.as<double>());
+            w->xring.as<double>(), w->L, w->K, used, head, nblk, w->partial.as<double>());
         SOD_CHECK_CUDA(cudaGetLastError());
     }
     wav_rowsum_kernel<<<(w->L + 255) / 256, 256, 0, st>>>(w->partial.as<double>(), w->chunk_ptr.as<int>(), w->L,
                                                          w->y.as<double>());
-    wav_reconstruct_kernel<<<1, 1024, 0, st>>>(w->y.as<double>(), w->nV, w->Np, w->res.as<double>(),
-                                               w->sbuf.as<double>(), out);
+    const size_t rsmem = sizeof(double) * (size_t)w->Np * 3 / 2;
+    if (rsmem > 48 * 1024)
+        SOD_CHECK_CUDA(cudaFuncSetAttribute(wav_reconstruct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)rsmem));
+    wav_reconstruct_kernel<<<1, 1024, rsmem, st>>>(w->y.as<double>(), w->nV, w->Np, out);
     SOD_CHECK_CUDA(cudaGetLastError());
     ctx->count(3);
     return SOD_OK;
