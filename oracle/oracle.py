@@ -17,7 +17,7 @@ _LIB_PATH = os.path.join(_HERE, "_build", "libsod_oracle.so")
 _lib = None
 
 KIND = {"G": 0, "H": 1, "B_trans": 2, "B_angular": 3}
-FP64, MIXED = 0, 1
+FP64, MIXED, LITERAL64 = 0, 1, 3  # accuracy oracle, reference-mixed baseline, FP64 with the literal formulas
 
 
 def build(force: bool = False) -> str:

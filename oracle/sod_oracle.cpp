@@ -11,13 +11,16 @@
  * they can be checked by known-answer tests (quadrature exactness, closed-form CQ weights,
  * static limits, symmetries, rigid-mode null spaces) instead.
  *
- * Two precision modes:
- *   mode 0  FP64 everywhere                              -> the accuracy oracle
+ * Precision modes:
+ *   mode 0  FP64 everywhere, kernels in their cancellation-free form (the reference's formulas
+ *           lose up to ~9 digits in FP64 as |s| r -> 0; see psi_stable)  -> the accuracy oracle
  *   mode 1  "reference-mixed": the scalar types the reference picks per kernel
  *           (FP32 regular G/B_trans/B_angular collocation, FP64 regular H collocation,
  *           FP32 Galerkin non-singular, FP64 singular integrals, FP32 B row accumulators)
  *           -> the restated reference CPU path, used as the timed CPU baseline.
  *   mode 2  FP32 for every regular (non-singular) integral including H  -> precision study only.
+ *   mode 3  FP64 everywhere with the reference's literal kernel formulas  -> precision study only
+ *           (agrees with mode 0 wherever |s| r is not small).
  *
  * The loop structure (per-component singular integration, per-k B_angular passes, per-face
  * accumulation then scatter) follows the reference so that the baseline's cost is
@@ -173,11 +176,86 @@ void for_each_subtriangle(const V3<T> &x0, const V3<T> &x1, const V3<T> &x2, int
 template <class T> struct Mat {
     T c1, c2, rho;
     cplx<T> s;
+    bool stable = false;  // FP64 accuracy mode: the cancellation-free forms below
 };
 template <class T> inline T kd(int i, int j) { return i == j ? T(1) : T(0); }
 
+// ---- cancellation-free forms of the four kernels (the FP64 accuracy mode) -------------------------
+// The reference's formulas subtract terms of size 1/(s r)^2 (and c^2 / r^2 times that in p_hat) that
+// cancel to O(1) as s r -> 0; in FP64 the innermost singular quadrature points (s r ~ 1e-4) lose
+// about 9 digits there.  The same functions are evaluated through
+//   psi(z) = ((1 + z) e^-z - 1) / z^2,  z_a = s r / c_a,  e_a = e^-z_a,
+//   Y = psi(z1)/c1^2 - psi(z2)/c2^2,    kappa = c2^2 / c1^2,
+// using the exact identities X / r^2 = Y (X of r_u_hat), X2 - X1 = -r^2 Y and
+// 1/s^2 - X2 = -(r^2 / c2^2) psi(z2) (tests/test_kernel_identities.py checks each rearranged kernel
+// against the literal one to 1e-36 in 40-digit arithmetic).
+// psi: 25-term series below |z| = 1 (truncation < 1e-26), closed form above (loss <= 2 eps/|z|^2).
+template <class T> cplx<T> psi_stable(cplx<T> z, cplx<T> ez) {
+    if (std::abs(z) < T(1)) {
+        // -sum_{m>=0} (-1)^m (m+1) z^m / (m+2)!, Horner from m = 24
+        double fact = 1.0;  // (m+2)! for m = 24
+        for (int t = 2; t <= 26; t++) fact *= t;
+        cplx<T> acc(0);
+        for (int m = 24; m >= 0; m--) {
+            const T c = T(((m % 2) ? 1.0 : -1.0) * (m + 1) / fact);
+            acc = acc * z + c;
+            fact /= (m + 2);
+        }
+        return acc;
+    }
+    return ((T(1) + z) * ez - T(1)) / (z * z);
+}
+template <class T> struct Radial {
+    cplx<T> z1, z2, e1, e2, psi1, psi2, Y;
+};
+template <class T> Radial<T> radial_stable(T r, const Mat<T> &m) {
+    Radial<T> t;
+    t.z1 = m.s * (r / m.c1);
+    t.z2 = m.s * (r / m.c2);
+    t.e1 = std::exp(-t.z1);
+    t.e2 = std::exp(-t.z2);
+    t.psi1 = psi_stable(t.z1, t.e1);
+    t.psi2 = psi_stable(t.z2, t.e2);
+    t.Y = t.psi1 / (m.c1 * m.c1) - t.psi2 / (m.c2 * m.c2);
+    return t;
+}
+// r u_hat = [(3Y + e1/c1^2 - e2/c2^2) rh_i rh_j + (e2/c2^2 - Y) d_ij] / (4 pi rho)
+template <class T> cplx<T> r_u_hat_stable(const V3<T> &rh, T r, int i, int j, const Mat<T> &m) {
+    const Radial<T> t = radial_stable(r, m);
+    const cplx<T> B = t.e1 / (m.c1 * m.c1) - t.e2 / (m.c2 * m.c2), C = t.e2 / (m.c2 * m.c2);
+    return (T(1. / (4. * PI)) / m.rho) * ((T(3) * t.Y + B) * (rh[i] * rh[j]) + (C - t.Y) * kd<T>(i, j));
+}
+// p_hat = [a rh_i n_j + b (n_i rh_j + rn d_ij) + d rn rh_i rh_j] / (4 pi r^2)
+template <class T> cplx<T> p_hat_stable(const V3<T> &rh, T r, const V3<T> &n, int i, int j, const Mat<T> &m) {
+    const Radial<T> t = radial_stable(r, m);
+    const T kp = (m.c2 * m.c2) / (m.c1 * m.c1), rn = dot(rh, n);
+    const cplx<T> Yc = t.Y * (T(6) * m.c2 * m.c2), z1e1 = t.z1 * t.e1, z2e2 = t.z2 * t.e2;
+    const cplx<T> a = Yc + t.e1 * (T(4) * kp - T(1)) - t.e2 * T(2) - z1e1 * (T(1) - T(2) * kp);
+    const cplx<T> b = Yc + t.e1 * (T(2) * kp) - t.e2 * T(3) - z2e2;
+    const cplx<T> d = Yc * T(-5) - t.e1 * (T(12) * kp) + t.e2 * T(12) - z1e1 * (T(2) * kp) + z2e2 * T(2);
+    return (T(1. / (4. * PI)) / (r * r)) *
+           (a * (rh[i] * n[j]) + b * (n[i] * rh[j] + kd<T>(i, j) * rn) + d * (rn * rh[i] * rh[j]));
+}
+// r b_trans_hat = r [(Y/2)(rh_i n_j + rh_j n_i) + psi2/c2^2 rn d_ij] / (4 pi)
+template <class T> cplx<T> r_b_trans_stable(const V3<T> &rh, T r, const V3<T> &n, int i, int j, const Mat<T> &m) {
+    const Radial<T> t = radial_stable(r, m);
+    return (r * T(1. / (4. * PI))) *
+           ((t.Y / T(2)) * (rh[i] * n[j] + rh[j] * n[i]) + (t.psi2 / (m.c2 * m.c2)) * (dot(rh, n) * kd<T>(i, j)));
+}
+// r b_ang_hat = r [(r Y/2) T1 + T2 (e2/c2 - e1/c1)/(2s) + d_ij n_k e2/(c2 s)] / (4 pi),
+//   T1 = rh_i rh_k n_j + rh_j rh_k n_i + d_jk n_i + d_ik n_j, T2 = d_jk n_i + d_ik n_j
+template <class T>
+cplx<T> r_b_ang_stable(const V3<T> &rh, T r, const V3<T> &n, int i, int j, int k, const Mat<T> &m) {
+    const Radial<T> t = radial_stable(r, m);
+    const T T2 = kd<T>(j, k) * n[i] + kd<T>(i, k) * n[j];
+    const T T1 = rh[i] * rh[k] * n[j] + rh[j] * rh[k] * n[i] + T2;
+    return (r * T(1. / (4. * PI))) * ((r * t.Y / T(2)) * T1 + (t.e2 / m.c2 - t.e1 / m.c1) / (T(2) * m.s) * T2 +
+                                      kd<T>(i, j) * n[k] * t.e2 / (m.c2 * m.s));
+}
+
 // r * u_hat_ij, elastodynamic single layer (src/elastodynamics_cqbem_G_collocation.cu:44-60)
 template <class T> cplx<T> r_u_hat(const V3<T> &rh, T r, int i, int j, const Mat<T> &m) {
+    if (m.stable) return r_u_hat_stable(rh, r, i, j, m);
     const cplx<T> s = m.s;
     const cplx<T> e1 = std::exp(-r * s / m.c1), e2 = std::exp(-r * s / m.c2);
     const cplx<T> X = ((s * r / m.c1 + T(1)) / (s * s)) * e1 - ((s * r / m.c2 + T(1)) / (s * s)) * e2;
@@ -188,6 +266,7 @@ template <class T> cplx<T> r_u_hat(const V3<T> &rh, T r, int i, int j, const Mat
 
 // p_hat_ij, elastodynamic double layer (src/elastodynamics_cqbem_H_collocation.cu:45-76)
 template <class T> cplx<T> p_hat(const V3<T> &rh, T r, const V3<T> &n, int i, int j, const Mat<T> &m) {
+    if (m.stable) return p_hat_stable(rh, r, n, i, j, m);
     const cplx<T> s = m.s;
     const T c1 = m.c1, c2 = m.c2;
     const cplx<T> e1 = std::exp(-r * s / c1), e2 = std::exp(-r * s / c2);
@@ -212,6 +291,7 @@ template <class T> T p_hat_sing(const V3<T> &rh, T r, const V3<T> &n, int i, int
 
 // r * b_hat_ij, rigid-translation coupling (src/elastodynamics_cqbem_B_trans_collocation.cu:41-58)
 template <class T> cplx<T> r_b_trans(const V3<T> &rh, T r, const V3<T> &n, int i, int j, const Mat<T> &m) {
+    if (m.stable) return r_b_trans_stable(rh, r, n, i, j, m);
     const cplx<T> s = m.s;
     const cplx<T> e1 = std::exp(-r * s / m.c1), e2 = std::exp(-r * s / m.c2);
     const cplx<T> X2 = ((s * r / m.c2 + T(1)) / (s * s)) * e2, X1 = ((s * r / m.c1 + T(1)) / (s * s)) * e1;
@@ -222,6 +302,7 @@ template <class T> cplx<T> r_b_trans(const V3<T> &rh, T r, const V3<T> &n, int i
 // r * b_hat_ijk, rigid-rotation coupling (src/elastodynamics_cqbem_B_angular_collocation.cu:44-63)
 template <class T>
 cplx<T> r_b_ang(const V3<T> &rh, T r, const V3<T> &n, int i, int j, int k, const Mat<T> &m) {
+    if (m.stable) return r_b_ang_stable(rh, r, n, i, j, k, m);
     const cplx<T> s = m.s;
     const cplx<T> e1 = std::exp(-r * s / m.c1), e2 = std::exp(-r * s / m.c2);
     const cplx<T> X2 = ((s * r / m.c2 + T(1)) / (s * s)) * e2, X1 = ((s * r / m.c1 + T(1)) / (s * s)) * e1;
@@ -253,15 +334,17 @@ template <class T> void bary_clamped(const V3<T> &P, const V3<T> &A, const V3<T>
 template <int NC, class F>
 void weakly_singular(const V3<double> &y1, const V3<double> &y2, const V3<double> &y3, int order, int subdiv,
                      F integrand, cplx<double> res[NC]) {
-    auto clampd = [](double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); };
     const V3<double> v1 = y2 - y1, v2 = y3 - y1;
     const V3<double> v1n = normalized(v1), v2n = normalized(v2);
     const V3<double> xh = v1n;
     const V3<double> yh = normalized(cross(cross(xh, v2n), xh));
     const V3<double> v12 = v1 + dot(v1, normalized(v1 - v2)) * normalized(v2 - v1);
     const double a = norm(v12);
-    const double alpha = std::acos(dot(v1n, v2n));
-    const double beta = std::acos(clampd(dot(normalized(v12), v1n), -1.0, 1.0));
+    // the angles as atan2(|u x v|, u . v): the reference's acos(u . v) loses half the digits near 0
+    // and pi (beta = 0 exactly for a right angle at y2, ~1.5e-8 rad of rounding noise with acos)
+    const double alpha = std::atan2(norm(cross(v1n, v2n)), dot(v1n, v2n));
+    const V3<double> v12n = normalized(v12);
+    const double beta = std::atan2(norm(cross(v12n, v1n)), dot(v12n, v1n));
     const GLRule g = gl_rule(order);
     for (int c = 0; c < NC; c++) res[c] = 0.0;
     for (int ts = 0; ts < subdiv; ts++) {
@@ -370,7 +453,7 @@ int singular_corner(const Mesh &m, long i, long face) {
 template <class T>
 void coll_G_row(const Mesh &m, long i, const Mat<double> &md, int order, int subdiv, int sorder, int ssub,
                 int parts, cplx<double> *U, long ld) {
-    const Mat<T> mt{(T)md.c1, (T)md.c2, (T)md.rho, cplx<T>(md.s)};
+    const Mat<T> mt{(T)md.c1, (T)md.c2, (T)md.rho, cplx<T>(md.s), md.stable && sizeof(T) == sizeof(double)};
     const TriRule rule = tri_rule(order);
     const V3<T> x = load<T>(m.V, i);
     for (long f = 0; f < m.nF; f++) {
@@ -434,7 +517,7 @@ void coll_G_row(const Mesh &m, long i, const Mat<double> &md, int order, int sub
 template <class T>
 void coll_H_row(const Mesh &m, long i, const Mat<double> &md, int order, int subdiv, int sorder, int ssub,
                 int parts, cplx<double> *P, long ld) {
-    const Mat<T> mt{(T)md.c1, (T)md.c2, (T)md.rho, cplx<T>(md.s)};
+    const Mat<T> mt{(T)md.c1, (T)md.c2, (T)md.rho, cplx<T>(md.s), md.stable && sizeof(T) == sizeof(double)};
     const TriRule rule = tri_rule(order);
     const V3<T> x = load<T>(m.V, i);
     for (long f = 0; f < m.nF; f++) {
@@ -489,7 +572,7 @@ void coll_H_row(const Mesh &m, long i, const Mat<double> &md, int order, int sub
 template <class T>
 void coll_Bt_row(const Mesh &m, long i, const Mat<double> &md, int order, int subdiv, int sorder, int ssub,
                  int parts, cplx<double> *B) {
-    const Mat<T> mt{(T)md.c1, (T)md.c2, (T)md.rho, cplx<T>(md.s)};
+    const Mat<T> mt{(T)md.c1, (T)md.c2, (T)md.rho, cplx<T>(md.s), md.stable && sizeof(T) == sizeof(double)};
     const TriRule rule = tri_rule(order);
     const V3<T> x = load<T>(m.V, i);
     cplx<T> Bi[3][3] = {};  // row accumulator in the kernel precision (B_trans_collocation.cu:39)
@@ -546,7 +629,7 @@ void coll_Bt_row(const Mesh &m, long i, const Mat<double> &md, int order, int su
 template <class T>
 void coll_Ba_row(const Mesh &m, long i, const Mat<double> &md, int order, int subdiv, int sorder, int ssub,
                  int parts, cplx<double> *B) {
-    const Mat<T> mt{(T)md.c1, (T)md.c2, (T)md.rho, cplx<T>(md.s)};
+    const Mat<T> mt{(T)md.c1, (T)md.c2, (T)md.rho, cplx<T>(md.s), md.stable && sizeof(T) == sizeof(double)};
     const TriRule rule = tri_rule(order);
     const V3<T> x = load<T>(m.V, i);
     cplx<T> Bi[27] = {};  // [p][q][k] row-major (B_angular_collocation.cu:37-42)
@@ -792,7 +875,8 @@ template <class T>
 void galerkin_pair_regular(const Mesh &m, int kind, long f1, long f2, const Mat<double> &md, int order, int subdiv,
                            cplx<double> *blk /* 9 x NCOL */) {
     const int NC = 9 * galerkin_ncol(kind);
-    GalerkinEval<T> ev{kind, {(T)md.c1, (T)md.c2, (T)md.rho, cplx<T>(md.s)}, load<T>(m.N, f2)};
+    GalerkinEval<T> ev{kind, {(T)md.c1, (T)md.c2, (T)md.rho, cplx<T>(md.s), md.stable && sizeof(T) == sizeof(double)},
+                       load<T>(m.N, f2)};
     const V3<T> x0 = load<T>(m.V, m.f(f1, 0)), x1 = load<T>(m.V, m.f(f1, 1)), x2 = load<T>(m.V, m.f(f1, 2));
     const V3<T> y0 = load<T>(m.V, m.f(f2, 0)), y1 = load<T>(m.V, m.f(f2, 1)), y2 = load<T>(m.V, m.f(f2, 2));
     const V3<T> ax = x1 - x0, bx = x2 - x0, ay = y1 - y0, by = y2 - y0;
@@ -912,14 +996,15 @@ int oracle_cq_frequencies(int bdf, double dt, int N, double *s_out, double *R_ou
 }
 
 // Collocation assembly of the rows of the listed field vertices for one Laplace frequency s.
-// kind: 0=G 1=H 2=B_trans 3=B_angular;  mode: 0 FP64, 1 reference-mixed;  parts: 1 regular, 2 singular, 3 both.
+// kind: 0=G 1=H 2=B_trans 3=B_angular;  mode: 0 FP64, 1 reference-mixed, 2 FP32 regular, 3 FP64 literal;
+// parts: 1 regular, 2 singular, 3 both.
 // out: complex128 interleaved, (3*nrows) x ncols (ncols = 3V, 3V, 3, 9).  rows=NULL -> all vertices.
 int oracle_collocation(int kind, int mode, const double *V, int nV, const int *F, int nF, const double *N,
                        const int *vmap, double c1, double c2, double rho, double s_re, double s_im, int order,
                        int subdiv, int sorder, int ssub, const int *rows, int nrows, int parts, double *out) {
     if (!tri_rule(order).n || !gl_rule(sorder).n || subdiv < 1 || ssub < 1) return 1;
     Mesh m{V, nV, F, nF, N, vmap};
-    Mat<double> md{c1, c2, rho, {s_re, s_im}};
+    Mat<double> md{c1, c2, rho, {s_re, s_im}, mode == 0};
     const long ncol = (kind <= 1) ? 3L * nV : (kind == 2 ? 3 : 9);
     const int nr = rows ? nrows : nV;
     cplx<double> *O = reinterpret_cast<cplx<double> *>(out);
@@ -928,7 +1013,7 @@ int oracle_collocation(int kind, int mode, const double *V, int nV, const int *F
     for (int r = 0; r < nr; r++) {
         const long i = rows ? rows[r] : r;
         cplx<double> *row = O + 3L * r * ncol;
-        const bool mixed = mode >= 1;
+        const bool mixed = mode == 1 || mode == 2;
         switch (kind) {
         case 0:
             if (mixed) coll_G_row<float>(m, i, md, order, subdiv, sorder, ssub, parts, row, ncol);
@@ -959,7 +1044,7 @@ int oracle_galerkin(int kind, int mode, const double *V, int nV, const int *F, i
                     int subdiv, int sorder, int ssub, const int *rows, int nrows, int parts, double *out) {
     if (!tri_rule(order).n || !gl_rule(sorder).n || subdiv < 1 || ssub < 1) return 1;
     Mesh m{V, nV, F, nF, N, vmap};
-    Mat<double> md{c1, c2, rho, {s_re, s_im}};
+    Mat<double> md{c1, c2, rho, {s_re, s_im}, mode == 0};
     const long ncol = (kind <= 1) ? 3L * nV : (kind == 2 ? 3 : 9);
     const int nr = rows ? nrows : nV;
     std::vector<int> slot(nV, -1);
@@ -1074,7 +1159,7 @@ int oracle_c_matrix_collocation(const double *V, int nV, const int *F, int nF, c
         const V3<double> r = normalized(load<double>(V, a) - load<double>(V, b));
         const double sx = dot(cross(n1, n2), r);
         const double sg = std::abs(sx) < 1e-12 ? 0.0 : (sx > 0 ? 1.0 : -1.0);
-        const double w = (1. / (4. * PI)) * sg * std::acos(std::min(1.0, std::max(-1.0, dot(n1, n2))));
+        const double w = (1. / (4. * PI)) * sg * std::atan2(norm(cross(n1, n2)), dot(n1, n2));  // dihedral angle
         for (int d = 0; d < 3; d++) {
             out[9 * a + 4 * d] += w;
             out[9 * b + 4 * d] += w;

@@ -43,8 +43,13 @@ __device__ __forceinline__ Polar polar_setup(double3 y1, double3 y2, double3 y3)
     g.yh = nrmz(cross3(cross3(g.xh, v2n), g.xh));
     const double3 v12 = v1 + nrmz(v2 - v1) * dot3(v1, nrmz(v1 - v2));
     g.a = norm3(v12);
-    g.alpha = acos(dot3(v1n, v2n));
-    g.beta = acos(fmin(1.0, fmax(-1.0, dot3(nrmz(v12), v1n))));
+    // The angles of include/integrator_collocation.hpp:35-36 are acos of dot products, which loses
+    // half the digits when the angle is near 0 or pi: beta is exactly 0 when the triangle has its
+    // right angle at y2 (common on structured meshes), and acos then turns one ulp of the dot
+    // product into ~1.5e-8 rad.  The same angles as atan2(|u x v|, u . v) are well conditioned.
+    g.alpha = atan2(norm3(cross3(v1n, v2n)), dot3(v1n, v2n));
+    const double3 v12n = nrmz(v12);
+    g.beta = atan2(norm3(cross3(v12n, v1n)), dot3(v12n, v1n));
     return g;
 }
 

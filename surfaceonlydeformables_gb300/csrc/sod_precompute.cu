@@ -58,8 +58,8 @@ static void c_matrix_collocation(const sod_mesh *m, double nu, std::vector<doubl
         const double cx[3] = {n1[1] * n2[2] - n1[2] * n2[1], n1[2] * n2[0] - n1[0] * n2[2], n1[0] * n2[1] - n1[1] * n2[0]};
         const double sx = cx[0] * r[0] + cx[1] * r[1] + cx[2] * r[2];
         const double sg = std::abs(sx) < 1e-12 ? 0.0 : (sx > 0 ? 1.0 : -1.0);
-        const double dn = std::min(1.0, std::max(-1.0, n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2]));
-        const double w = sg * std::acos(dn) / (4.0 * M_PI);
+        const double dn = n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2];
+        const double w = sg * std::atan2(std::sqrt(cx[0] * cx[0] + cx[1] * cx[1] + cx[2] * cx[2]), dn) / (4.0 * M_PI);
         for (int d = 0; d < 3; d++) {
             C[9 * a + 4 * d] += w;
             C[9 * b + 4 * d] += w;

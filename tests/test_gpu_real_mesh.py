@@ -1,0 +1,61 @@
+"""GPU parity on the reference's own scene meshes (tests/golden: the 770-vertex cube of
+data/cube_drop.json and its 870-vertex traction-discontinuous split, with the scene's material,
+BDF1 frequencies and 7-point x 4 (order 5, subdivision 2) quadrature) against the stored FP64
+oracle rows.  The cube's 90-degree edges and corners stress the singular rules; the split mesh
+exercises the vertex map (split vertices share their canonical vertex's singular handling).
+
+Tolerances (relative Frobenius over the sampled rows): full rows <= 1e-5, singular part <= 1e-10."""
+import os
+
+import numpy as np
+import pytest
+
+from surfaceonlydeformables_gb300.meshes import SurfaceMesh
+
+from .conftest import rel_fro
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+KINDS = ["G", "H", "B_trans", "B_angular"]
+
+
+@pytest.fixture(scope="module")
+def cube(gpu_ctx):
+    import importlib.util
+
+    from surfaceonlydeformables_gb300 import api
+
+    spec = importlib.util.spec_from_file_location("make_fixtures", os.path.join(GOLDEN, "make_fixtures.py"))
+    mf = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mf)
+    m = np.load(os.path.join(GOLDEN, "cube_meshes.npz"))
+    r = np.load(os.path.join(GOLDEN, "cube_oracle_rows.npz"))
+    dev = {}
+    for tag in ("cont", "disc"):
+        mesh = SurfaceMesh.from_arrays(m[f"V_{tag}"], m[f"F_{tag}"])
+        dev[tag] = api.Mesh(gpu_ctx, mesh, vmap=m["vmap_disc"] if tag == "disc" else None)
+    return mf, dev, r
+
+
+def _rows(full, verts, kind):
+    """Rows 3v..3v+2 of the sampled vertices (B_angular as [3nV][9])."""
+    full = full.reshape(full.shape[0], -1)
+    return np.concatenate([full[3 * v:3 * v + 3] for v in verts])
+
+
+@pytest.mark.parametrize("tag", ["cont", "disc"])
+@pytest.mark.parametrize("kind", KINDS)
+def test_cube_rows_match_oracle(gpu_ctx, cube, tag, kind):
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    mf, dev, r = cube
+    mat = mf.material()
+    verts = r[f"verts_{tag}"]
+    for fi, s in enumerate(r["s"]):
+        sing = api.assemble(gpu_ctx, dev[tag], kind, mat, s, order=mf.ORDER, subdiv=mf.SUBDIV,
+                            parts=L.PART_SINGULAR)
+        assert rel_fro(_rows(sing, verts, kind), r[f"{tag}_{kind}_sing"][fi]) <= 1e-10, (tag, kind, s)
+    full = api.assemble(gpu_ctx, dev[tag], kind, mat, r["s"][-1], order=mf.ORDER, subdiv=mf.SUBDIV)
+    assert rel_fro(_rows(full, verts, kind), r[f"{tag}_{kind}_all"]) <= 1e-5, (tag, kind)
