@@ -257,6 +257,42 @@ __global__ void __launch_bounds__(scatter_max_threads<KIND, BM>(), 1) coll_scatt
     scatter_body<KIND, BM>(a, pt, ft.kf[blockIdx.y], a.i0 + blockIdx.x, blockIdx.y, acc);
 }
 
+// Row accumulator in global memory, for meshes whose row block does not fit in shared memory (for
+// example H of a 3485-vertex mesh: 9 x 3485 complex FP32 = 251 KB).  A persistent grid walks the
+// (vertex, frequency) items in order and each CTA reuses its own slice of the scratch, which stays
+// in L2 (grid x slice is a few tens of MB).  The body is the same: colour-ordered adds separated by
+// CTA barriers (which also order the CTA's global-memory accesses), so the sums and their order are
+// those of the shared-memory variant.
+constexpr int SCATTER_GLOBAL_THREADS = 256;
+template <int KIND, int BM>
+__global__ void __launch_bounds__(SCATTER_GLOBAL_THREADS) coll_scatter_global_kernel(CollArgs a, PointTable pt,
+                                                                                   const __grid_constant__ FreqTable ft,
+                                                                                   float2 *scratch, long long per_cta,
+                                                                                   int nvert) {
+    float2 *acc = scratch + (size_t)blockIdx.x * per_cta;
+    const int items = nvert * ft.n;
+    for (int it = blockIdx.x; it < items; it += gridDim.x) {
+        const int fq = it / nvert, i = a.i0 + it % nvert;
+        scatter_body<KIND, BM>(a, pt, ft.kf[fq], i, fq, acc);
+        __syncthreads();  // the next item clears the accumulator
+    }
+}
+
+template <int KIND, int BM>
+static int launch_scatter_global(sod_context *ctx, const CollArgs &a, const PointTable &pt, const FreqTable &ft,
+                                 int nvert, cudaStream_t stream) {
+    const auto fn = coll_scatter_global_kernel<KIND, BM>;
+    int per_sm = 0;
+    SOD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SCATTER_GLOBAL_THREADS, 0));
+    const int grid = std::max(1, std::min(ctx->num_sms * std::max(per_sm, 1), nvert * ft.n));
+    const long long per_cta = (long long)scatter_smem_bytes(KIND, BM, a.nV, SCATTER_GLOBAL_THREADS) / sizeof(float2);
+    SOD_TRY(ctx->gacc.ensure(sizeof(float2) * (size_t)grid * per_cta));
+    fn<<<grid, SCATTER_GLOBAL_THREADS, 0, stream>>>(a, pt, ft, ctx->gacc.as<float2>(), per_cta, nvert);
+    SOD_CHECK_CUDA(cudaGetLastError());
+    ctx->count();
+    return SOD_OK;
+}
+
 // -------------------------------------------------------------------------------------------
 // B_trans / B_angular regular reduction kernel (MASK subset of KM_BT | KM_BA), used when G is not
 // assembled in the same call: per-thread sums over faces in FP32, fixed-order warp/CTA reduction in
@@ -766,23 +802,30 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
     int threads[2] = {0, 0};
     const sod_mesh::Coloured *col[2] = {nullptr, nullptr};
     size_t smem[2] = {0, 0};
+    bool global[2] = {false, false};  // row accumulator in global memory (row block too large for shared memory)
     for (int kd = 0; kd < 2; kd++) {
         if (!(mask & (1 << kd))) continue;
         const int bm = kd == SOD_G ? bmG : 0;
         int T = ctx->coll_threads;
-        if (T <= 0) SOD_TRY(autotune_scatter_threads(ctx, const_cast<sod_mesh *>(m), kd, bm, &T));
-        cudaFuncAttributes attr;
-        SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, scatter_fn(kd, bm, false)));
-        T = std::max(32, std::min(std::min(SCATTER_MAX_THREADS, attr.maxThreadsPerBlock), (T / 32) * 32));
+        int rc = SOD_OK;
+        if (T <= 0) rc = autotune_scatter_threads(ctx, const_cast<sod_mesh *>(m), kd, bm, &T);
+        int per_sm = 0;
+        if (rc == SOD_OK) {
+            cudaFuncAttributes attr;
+            SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, scatter_fn(kd, bm, false)));
+            T = std::max(32, std::min(std::min(SCATTER_MAX_THREADS, attr.maxThreadsPerBlock), (T / 32) * 32));
+            smem[kd] = scatter_smem_bytes(kd, bm, m->nV, T);
+            SOD_TRY(scatter_occupancy(ctx, kd, bm, false, T, smem[kd], &per_sm));
+        } else if (rc != SOD_ERR_UNSUPPORTED) {
+            return rc;
+        }
+        if (per_sm <= 0) {
+            global[kd] = true;
+            T = SCATTER_GLOBAL_THREADS;
+            smem[kd] = 0;
+        }
         threads[kd] = T;
         SOD_TRY(const_cast<sod_mesh *>(m)->coloured_for(T, &col[kd]));
-        smem[kd] = scatter_smem_bytes(kd, bm, m->nV, T);
-        int per_sm = 0;
-        SOD_TRY(scatter_occupancy(ctx, kd, bm, false, T, smem[kd], &per_sm));
-        if (per_sm <= 0) {
-            set_error("mesh too large for the shared-memory row accumulator (" + std::to_string(m->nV) + " vertices)");
-            return SOD_ERR_UNSUPPORTED;
-        }
     }
     const size_t esz = L.out_dtype == SOD_C64 ? 8 : 16;
     // host destinations: row chunks of whole waves of the scatter grid, each chunk's rows copied on
@@ -857,6 +900,15 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
                 a.canonF = m->has_vmap ? col[kd]->dCanonF.as<int4>() : nullptr;
                 a.color_off = col[kd]->dOff.as<int>();
                 a.ncolors = col[kd]->ncolors;
+                if (global[kd]) {
+                    const int nv = v1 - v0;
+                    if (kd == SOD_H) SOD_TRY((launch_scatter_global<SOD_H, 0>(ctx, a, pt, ft, nv, L.stream)));
+                    else if (bmG == KM_BT) SOD_TRY((launch_scatter_global<SOD_G, KM_BT>(ctx, a, pt, ft, nv, L.stream)));
+                    else if (bmG == KM_BA) SOD_TRY((launch_scatter_global<SOD_G, KM_BA>(ctx, a, pt, ft, nv, L.stream)));
+                    else if (bmG) SOD_TRY((launch_scatter_global<SOD_G, KM_BT | KM_BA>(ctx, a, pt, ft, nv, L.stream)));
+                    else SOD_TRY((launch_scatter_global<SOD_G, 0>(ctx, a, pt, ft, nv, L.stream)));
+                    continue;
+                }
                 if (kd == SOD_H)
                     coll_scatter_kernel<SOD_H, 0><<<grid, threads[kd], smem[kd], L.stream>>>(a, pt, ft);
                 else if (bmG == KM_BT)

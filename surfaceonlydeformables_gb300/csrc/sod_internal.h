@@ -116,6 +116,7 @@ struct sod_context {
     cudaStream_t copy_stream = nullptr;    // device-to-host copies overlapped with compute
     std::vector<cudaEvent_t> chunk_events;  // row-chunk completion markers (reused)
     sod::DevBuf gal_bsum;  // Galerkin: B_trans / B_angular sums of every test point
+    sod::DevBuf gacc;      // collocation row accumulators in global memory (meshes too large for shared memory)
     void count(int n = 1) { launches += n; }
 };
 

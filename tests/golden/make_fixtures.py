@@ -6,6 +6,9 @@ Reads data/cube_reordered.obj and data/cube_reordered_discontinuous.obj of the r
                        PhysicsBaseMatrixCollection::init does (src/physics_base_matrix_collection.cpp:
                        41-45); vmap of the discontinuous mesh: each split vertex maps to the first
                        vertex with the same coordinates (the reference's vertex_map_inverse)
+  bunny_mesh.npz       V, F of data/bunny_reordered.obj (3485 vertices, the bunny scene of
+                       data/bunny_friction.json), centred; its H row block (9 x 3485 complex FP32)
+                       is larger than shared memory, so it exercises the global-memory accumulator
   cube_oracle_rows.npz FP64 oracle rows (G, H, B_trans, B_angular) of a few vertices, with the scene's
                        material and quadrature: the singular part at two CQ frequencies (FP64,
                        for the 1e-10 check) and the full rows at the second one (G and H stored
@@ -74,6 +77,8 @@ def main():
     key = {tuple(V[i]): i for i in sorted(first)}
     out["vmap_disc"] = np.array([key[tuple(v)] for v in V], dtype=np.int32)
     np.savez_compressed(os.path.join(HERE, "cube_meshes.npz"), **out)
+    V, F = read_obj(os.path.join(ref, "data", "bunny_reordered.obj"))
+    np.savez_compressed(os.path.join(HERE, "bunny_mesh.npz"), V=meshes.center_mesh(V, F), F=F)
 
     s, R, L = oracle.cq_frequencies(BDF, DT, NSTEPS)
     s = np.asarray(s)[FREQ_INDEX]
