@@ -38,7 +38,7 @@ def lib():
         _lib.oracle_galerkin.argtypes = [i, i, p, i, p, i, p, p, d, d, d, d, d, i, i, i, i, p, i, i, p]
         _lib.oracle_inverse_transform.argtypes = [i, i, d, p, l, p]
         _lib.oracle_cq_frequencies.argtypes = [i, d, i, p, p, p]
-        _lib.oracle_c_matrix_collocation.argtypes = [p, i, p, i, p, d, p]
+        _lib.oracle_c_matrix_collocation.argtypes = [p, i, p, i, p, d, p, p]
         _lib.oracle_c_matrix_galerkin.argtypes = [p, i, p, i, p]
         _lib.oracle_elastostatic.argtypes = [i, i, p, i, p, i, p, d, d, i, i, i, i, p]
         _lib.oracle_rigid_modes.argtypes = [p, i, p, i, p]
@@ -111,9 +111,11 @@ def inverse_transform(Xhat: np.ndarray, L: int, R: float) -> np.ndarray:
     return out
 
 
-def c_matrix_collocation(mesh, nu: float) -> np.ndarray:
+def c_matrix_collocation(mesh, nu: float, vmap=None) -> np.ndarray:
     out = np.zeros((3 * mesh.nV, 3))
-    lib().oracle_c_matrix_collocation(_ptr(mesh.V), mesh.nV, _ptr(mesh.F), mesh.nF, _ptr(mesh.N), nu, _ptr(out))
+    vm = None if vmap is None else np.ascontiguousarray(vmap, dtype=np.int32)
+    lib().oracle_c_matrix_collocation(_ptr(mesh.V), mesh.nV, _ptr(mesh.F), mesh.nF, _ptr(mesh.N), nu, _ptr(vm),
+                                      _ptr(out))
     return out
 
 

@@ -1129,10 +1129,16 @@ int oracle_inverse_transform(int nfreq, int L, double R, const double *Xhat, lon
     return 0;
 }
 
-// Collocation free-term (jump) blocks C, 3V x 3 (src/elastics_bem_matrix_collection.cpp:387-445),
-// for meshes without traction-discontinuity splitting.
-int oracle_c_matrix_collocation(const double *V, int nV, const int *F, int nF, const double *N, double nu,
-                                double *out) {
+// Collocation free-term (jump) blocks C, 3V x 3 (src/elastics_bem_matrix_collection.cpp:387-445).
+// With traction-discontinuity splitting (vmap = vertex_map_inverse, may be NULL) the reference computes
+// C on the original mesh, i.e. with every face corner mapped to its canonical vertex, and copies the
+// canonical vertex's block to each split vertex (:395-400, :434-441).
+int oracle_c_matrix_collocation(const double *V, int nV, const int *F_in, int nF, const double *N, double nu,
+                                const int *vmap, double *out) {
+    std::vector<int> Fc(F_in, F_in + 3 * (size_t)nF);
+    if (vmap)
+        for (auto &v : Fc) v = vmap[v];
+    const int *F = Fc.data();
     std::memset(out, 0, sizeof(double) * 9 * nV);
     for (int i = 0; i < nV; i++)
         for (int d = 0; d < 3; d++) out[9 * i + 4 * d] += 0.5;
@@ -1177,6 +1183,10 @@ int oracle_c_matrix_collocation(const double *V, int nV, const int *F, int nF, c
                 for (int q = 0; q < 3; q++) out[9 * vi + 3 * p + q] -= (1. / (8. * PI * (1. - nu))) * c[p] * n[q];
         }
     }
+    if (vmap)
+        for (int v = 0; v < nV; v++)
+            if (vmap[v] != v)
+                for (int t = 0; t < 9; t++) out[9 * v + t] = out[9 * vmap[v] + t];
     return 0;
 }
 

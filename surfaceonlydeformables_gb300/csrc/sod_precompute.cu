@@ -19,10 +19,15 @@
 
 namespace sod {
 
-// Collocation free term, 3x3 per vertex (src/elastics_bem_matrix_collection.cpp:387-445), for meshes
-// without traction-discontinuity splitting.  O(F) host work on the mesh's FP64 geometry.
+// Collocation free term, 3x3 per vertex (src/elastics_bem_matrix_collection.cpp:387-445).  O(F) host
+// work on the mesh's FP64 geometry.  With traction-discontinuity splitting the reference computes C
+// on the original mesh (every face corner at its canonical vertex, so the split edges pair up again)
+// and copies the canonical vertex's block to each split vertex (:395-400, :434-441).
 static void c_matrix_collocation(const sod_mesh *m, double nu, std::vector<double> &C) {
     const int nV = m->nV, nF = m->nF;
+    std::vector<int> Fc(m->F);
+    if (m->has_vmap)
+        for (auto &v : Fc) v = m->vmap[v];
     C.assign(9 * (size_t)nV, 0.0);
     for (int v = 0; v < nV; v++)
         for (int d = 0; d < 3; d++) C[9 * v + 4 * d] = 0.5;
@@ -41,7 +46,7 @@ static void c_matrix_collocation(const sod_mesh *m, double nu, std::vector<doubl
     es.reserve(3 * (size_t)nF);
     for (int f = 0; f < nF; f++)
         for (int k = 0; k < 3; k++) {
-            const int a = m->F[3 * f + (k + 1) % 3], b = m->F[3 * f + (k + 2) % 3];
+            const int a = Fc[3 * f + (k + 1) % 3], b = Fc[3 * f + (k + 2) % 3];
             es.push_back({std::min(a, b), std::max(a, b), f + (long long)k * nF});
         }
     std::sort(es.begin(), es.end(), [](const E &x, const E &y) {
@@ -51,7 +56,7 @@ static void c_matrix_collocation(const sod_mesh *m, double nu, std::vector<doubl
         if (es[t].a != es[t + 1].a || es[t].b != es[t + 1].b) continue;
         const long long e1 = es[t].de, e2 = es[t + 1].de;
         const int f1 = (int)(e1 % nF), f2 = (int)(e2 % nF), k1 = (int)(e1 / nF);
-        const int a = m->F[3 * f1 + (k1 + 1) % 3], b = m->F[3 * f1 + (k1 + 2) % 3];
+        const int a = Fc[3 * f1 + (k1 + 1) % 3], b = Fc[3 * f1 + (k1 + 2) % 3];
         const double *n1 = &m->N[3 * f1], *n2 = &m->N[3 * f2];
         double r[3] = {P(a, 0) - P(b, 0), P(a, 1) - P(b, 1), P(a, 2) - P(b, 2)};
         unit(r);
@@ -70,7 +75,7 @@ static void c_matrix_collocation(const sod_mesh *m, double nu, std::vector<doubl
     for (int f = 0; f < nF; f++) {
         const double *n = &m->N[3 * f];
         for (int i = 0; i < 3; i++) {
-            const int vi = m->F[3 * f + i], v1 = m->F[3 * f + (i + 1) % 3], v2 = m->F[3 * f + (i + 2) % 3];
+            const int vi = Fc[3 * f + i], v1 = Fc[3 * f + (i + 1) % 3], v2 = Fc[3 * f + (i + 2) % 3];
             double r1[3], r2[3];
             for (int d = 0; d < 3; d++) r1[d] = P(v1, d) - P(vi, d), r2[d] = P(v2, d) - P(vi, d);
             unit(r1);
@@ -81,6 +86,10 @@ static void c_matrix_collocation(const sod_mesh *m, double nu, std::vector<doubl
                 for (int q = 0; q < 3; q++) C[9 * vi + 3 * p + q] -= coef * c[p] * n[q];
         }
     }
+    if (m->has_vmap)
+        for (int v = 0; v < nV; v++)
+            if (m->vmap[v] != v)
+                for (int t = 0; t < 9; t++) C[9 * (size_t)v + t] = C[9 * (size_t)m->vmap[v] + t];
 }
 
 // H_0 diagonal blocks += C (collocation)
@@ -147,8 +156,6 @@ extern "C" int sod_cqbem_precompute(sod_context *ctx, const sod_mesh *mesh, int 
     SOD_REQUIRE(out_dtype == SOD_F64 || out_dtype == SOD_F32, "time-domain output must be float64 or float32");
     SOD_REQUIRE(nu > -1.0 && nu < 0.5, "Poisson ratio must be in (-1, 0.5)");
     SOD_REQUIRE(G_out || H_out || B_trans_out || B_angular_out || B_euler_out, "no output requested");
-    SOD_REQUIRE(!mesh->has_vmap || method == SOD_GALERKIN || !H_out,
-                "collocation free term with traction-discontinuity splitting is not supported");
     SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
     const int nV = mesh->nV;
     double R;

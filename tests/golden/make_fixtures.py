@@ -57,7 +57,7 @@ def sample_vertices(V, vmap=None):
     """A corner, an edge and a face-interior vertex of the cube (and, with vmap, a split vertex)."""
     a = np.abs(V)
     m = a.max()
-    on = (np.abs(a - m) < 1e-12).sum(axis=1)  # coordinates on the cube's boundary planes
+    on = (np.abs(a - m) < 1e-9 * m).sum(axis=1)  # coordinates on the cube's boundary planes
     picks = [int(np.flatnonzero(on == 3)[0]), int(np.flatnonzero(on == 2)[0]), int(np.flatnonzero(on == 1)[0])]
     if vmap is not None:
         split = np.flatnonzero(vmap != np.arange(len(vmap)))

@@ -89,3 +89,38 @@ def test_bunny_row_accumulator_in_global_memory(gpu_ctx, oracle):
         ref = oracle.collocation(kind, mesh, mat, s[1], order=5, subdiv=2, rows=verts)
         assert rel_fro(got, ref) <= 1e-5, (kind, rel_fro(got, ref))
     del out
+
+
+def test_cube_scene_precompute_on_split_mesh(gpu_ctx, cube, oracle, sodlib):
+    """The cube scene's precompute (data/cube_drop.json: traction discontinuity, BDF1, dt 0.005,
+    order 5 / subdivision 2; N = 6 history steps) on the 870-vertex split mesh.  The oracle pipeline
+    (inverse transform; free term computed on the original mesh and copied to the split vertices;
+    B_trans shift of B_angular; B_euler) applied to the GPU's own Laplace-domain matrices agrees with
+    sod_cqbem_precompute to <= 1e-10."""
+    from surfaceonlydeformables_gb300 import api
+
+    mf, dev, r = cube
+    dm = dev["disc"]
+    mesh = dm.host
+    vmap = np.load(os.path.join(GOLDEN, "cube_meshes.npz"))["vmap_disc"]
+    mat = mf.material()
+    N = 6
+    # the library's own frequency table, as sod_cqbem_precompute uses it: with R^-n up to 1e5 here, a
+    # last-ulp difference in s would be amplified past the tolerance (the table itself is checked
+    # against the oracle elsewhere)
+    s, R, Lq = sodlib.cq_frequencies(mf.BDF, mf.DT, N)
+    got = {k: v.cpu().numpy() for k, v in
+           api.precompute(gpu_ctx, dm, mat, mf.BDF, mf.DT, N, order=mf.ORDER, subdiv=mf.SUBDIV).items()}
+    X = api.assemble_all(gpu_ctx, dm, mat, s, order=mf.ORDER, subdiv=mf.SUBDIV)
+    nV = mesh.nV
+    ref = {k: oracle.inverse_transform(X[k].reshape((len(s), 3 * nV, 3, 3) if k == "B_angular" else X[k].shape), Lq, R)
+           for k in KINDS}
+    C = oracle.c_matrix_collocation(mesh, mat.nu, vmap=vmap).reshape(nV, 3, 3)
+    for v in range(nV):
+        ref["H"][0, 3 * v:3 * v + 3, 3 * v:3 * v + 3] += C[v]
+    cm = np.zeros(3)
+    ref["B_angular"] = np.stack([oracle.b_angular_shift(ref["B_angular"][n], ref["B_trans"][n], mesh.V, cm)
+                                 for n in range(Lq)])
+    ref["B_euler"] = np.stack([oracle.b_euler(ref["B_angular"][n]) for n in range(Lq)])
+    for k in ("G", "H", "B_trans", "B_angular", "B_euler"):
+        assert rel_fro(got[k].reshape(ref[k].shape), ref[k]) <= 1e-10, (k, rel_fro(got[k].reshape(ref[k].shape), ref[k]))

@@ -237,3 +237,28 @@ def test_stable_kernels_agree_with_literal_formulas(oracle):
     a = oracle.collocation("H", m, mat, 5.0, rows=[0], parts=2, mode=oracle.FP64)
     b = oracle.collocation("H", m, mat, 5.0, rows=[0], parts=2, mode=oracle.LITERAL64)
     assert np.linalg.norm(a - b) / np.linalg.norm(a) > 1e-9
+
+
+def test_c_matrix_cube_and_split_cube(oracle):
+    """Collocation free term on the reference's cube: trace(C)/3 is the interior solid-angle fraction
+    (1/2 on faces, 1/4 on edges, 1/8 at corners).  On the traction-discontinuous split of the same
+    cube, C computed on the original mesh and copied to the split vertices equals the continuous
+    cube's C at the same points exactly (without the vertex map the split edges are lost)."""
+    import os
+
+    from surfaceonlydeformables_gb300.meshes import SurfaceMesh
+
+    m = np.load(os.path.join(os.path.dirname(__file__), "golden", "cube_meshes.npz"))
+    mc = SurfaceMesh.from_arrays(m["V_cont"], m["F_cont"])
+    md = SurfaceMesh.from_arrays(m["V_disc"], m["F_disc"])
+    Cc = oracle.c_matrix_collocation(mc, 0.45).reshape(-1, 3, 3)
+    a = np.abs(mc.V)
+    on = (np.abs(a - a.max()) < 1e-9 * a.max()).sum(axis=1)
+    tr = np.trace(Cc, axis1=1, axis2=2) / 3
+    for k, frac in ((1, 0.5), (2, 0.25), (3, 0.125)):
+        assert np.abs(tr[on == k] - frac).max() < 1e-12, k
+    key = {tuple(np.round(v, 12)): i for i, v in enumerate(mc.V)}
+    to_c = np.array([key[tuple(np.round(v, 12))] for v in md.V])
+    Cd = oracle.c_matrix_collocation(md, 0.45, vmap=m["vmap_disc"]).reshape(-1, 3, 3)
+    assert np.array_equal(Cd, Cc[to_c])
+    assert np.abs(oracle.c_matrix_collocation(md, 0.45).reshape(-1, 3, 3) - Cc[to_c]).max() > 0.1
