@@ -294,6 +294,72 @@ def wavelet_case(torch, ctx, stream, nV: int, K: int, ratio: float, reps: int, h
             "bytes": wb, "setup_s": round(setup_s, 2)}
 
 
+def scenes_leg(torch, ctx, stream):
+    """The reference's own scenes (meshes from tests/golden): the time-domain precompute of the cube
+    scene (data/cube_drop.json: 870-vertex traction-discontinuous cube, mu 1e5, nu 0.45, rho 1000,
+    BDF1, dt 0.005, order 5 / subdivision 2, N = 6) and of the bunny scene (data/bunny_friction.json:
+    3485 vertices, mu 1e6, nu 0.3, rho 3000, BDF1, dt 0.003, N = 5), device-resident FP64 outputs,
+    and one step of their wavelet-compressed histories at the scenes' ratio 0.1 (cube_collide,
+    bunny_friction).  Event-timed second runs (the first builds the mesh schedules)."""
+    import os
+
+    from surfaceonlydeformables_gb300 import api
+    from surfaceonlydeformables_gb300.meshes import Material, SurfaceMesh
+
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden")
+    cube = np.load(os.path.join(golden, "cube_meshes.npz"))
+    bunny = np.load(os.path.join(golden, "bunny_mesh.npz"))
+    scenes = [("cube_drop", SurfaceMesh.from_arrays(cube["V_disc"], cube["F_disc"]), cube["vmap_disc"],
+               Material(2.0 * 1e5 * (1.0 + 0.44999998807907104), 0.44999998807907104, 1000.0), 0.004999999888241291, 6),
+              ("bunny_friction", SurfaceMesh.from_arrays(bunny["V"], bunny["F"]), None,
+               Material(2.0 * 1e6 * 1.3, 0.3, 3000.0), 0.003, 5)]
+    res = {}
+    for name, mesh, vmap, mat, dt, N in scenes:
+        dm = api.Mesh(ctx, mesh, vmap=vmap)
+
+        def run():
+            return api.precompute(ctx, dm, mat, 1, dt, N, order=5, subdiv=2)
+
+        w = run()
+        del w
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        w = run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        n3 = 3 * mesh.nV
+        lam = (N + 1) // 2 + 1
+        entries = lam * (2 * n3 * n3 + 12 * n3)
+        out = {"vertices": mesh.nV, "faces": mesh.nF, "N": N, "precompute_ms": round(ms, 2),
+               "laplace_entries_per_s": entries / (ms * 1e-3)}
+        bank = api.HistoryBank.compressed(ctx, mesh.nV, N, 0.1)
+        for k in range(1, N + 1):
+            bank.set_weights(k, w["G"][k], w["H"][k])
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(1)
+        for _ in range(N):
+            bank.push(torch.randn(n3, dtype=torch.float64, device="cuda", generator=gen),
+                      torch.randn(n3, dtype=torch.float64, device="cuda", generator=gen))
+        b = torch.empty(n3, dtype=torch.float64, device="cuda")
+        for _ in range(3):
+            bank.convolve(b)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        bank.convolve(b)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out["compressed_history_step_ms"] = round(e0.elapsed_time(e1), 4)
+        out["compressed_history_bytes"] = bank.weight_bytes
+        bank.close()
+        del w, b
+        dm.close()
+        torch.cuda.empty_cache()
+        res[name] = out
+    return res
+
+
 def elastostatic_leg(torch, ctx, stream):
     """Elastostatic Kelvin G and H (H with the rigid-mode diagonal correction) of the 2562-vertex
     object, device-resident FP64 output."""
@@ -772,6 +838,7 @@ def run_gpu(args):
         extra["elastostatic"] = elastostatic_leg(torch, ctx, stream)
         extra["galerkin"] = galerkin_leg(torch, ctx, stream)
         extra["dense_solve"] = solve_leg(torch, ctx, stream)
+        extra["reference_scenes"] = scenes_leg(torch, ctx, stream)
         if not args.no_serve:
             extra["serving"] = serving_leg(torch, ctx)
 
@@ -831,6 +898,8 @@ def run_leg(args):
         out = galerkin_leg(torch, ctx, stream, level=args.galerkin_level)
     elif args.leg == "solve":
         out = solve_leg(torch, ctx, stream)
+    elif args.leg == "scenes":
+        out = scenes_leg(torch, ctx, stream)
     elif args.leg == "wavelet":
         out = wavelet_case(torch, ctx, stream, args.wavelet_nv, args.history_k, 0.1, args.steps, measured_hbm_gbs())
     else:
@@ -848,7 +917,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop leg")
-    ap.add_argument("--leg", default="all", choices=["all", "history", "elastostatic", "galerkin", "serving", "solve", "wavelet"],
+    ap.add_argument("--leg", default="all", choices=["all", "history", "elastostatic", "galerkin", "serving", "solve", "wavelet", "scenes"],
                     help="run one hot-path leg alone (profiling captures) and print its JSON")
     ap.add_argument("--history-k", type=int, default=64, help="history length of the --leg history bank")
     ap.add_argument("--wavelet-nv", type=int, default=2562,
