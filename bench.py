@@ -12,9 +12,10 @@ object.  Metric: complex matrix entries per second, counted as sum over objects 
 
   value : device-resident path -- one multi-frequency launch per (object, kind), outputs complex64
           kept in HBM; CUDA-event time summed over K steps, L2 flushed between steps.
-  e2e   : the plain drop-in through the C ABI with host buffers -- one call per (object, kind,
-          frequency) into a pinned host buffer in the reference layout (complex128), i.e. the
-          frequency loop of compute_G_matrices with its device-to-host copy, timed end to end.
+  e2e   : the drop-in through the C ABI with host buffers -- one sod_cqbem_assemble_frequencies call
+          per (object, kind), the replacement of the frequency loop of compute_{G,H,B_trans,
+          B_angular}_matrices, into a pinned host array of every frequency in the reference layout
+          (complex128), timed end to end (row chunks copied to the host while later rows compute).
   --impl reference : the reference's CPU algorithm (the oracle's reference-mixed restatement,
           OpenMP on all host cores) on a bounded sample of the same workload.
 """
@@ -774,21 +775,22 @@ def run_gpu(args):
         t_per_object = timed(step_per_object, max(1, args.steps // 2))
         t_plain = timed(step_plain, max(1, args.steps // 2))
 
-    # ---- end to end: plain per-frequency drop-in with pinned host buffers (reference layout) ----
-    big = max(m.nV for m in meshes)
-    host = torch.empty((3 * big, 3 * big), dtype=torch.complex128, pin_memory=True)
+    # ---- end to end: the per-(object, kind) frequency-loop drop-in with pinned host buffers ----
+    # one pinned array of the largest (frequencies x rows x columns) complex128 output, reused by
+    # every call as the reference's loop reuses its host matrix
+    host_elems = max(len(o["s"]) * 9 * m.nV * m.nV for o, m in zip(objs, meshes))
+    host = torch.empty(host_elems, dtype=torch.complex128, pin_memory=True)
     e2e_steps = max(1, args.steps // 2)
 
     def e2e_step():
         d2h = 0
         for o, m in zip(objs, meshes):
             for kind in KINDS:
-                shape = api.out_shape(L.KINDS[kind], m.nV)
-                buf = host.view(-1)[: shape[0] * shape[1]].view(shape).numpy()
-                for sl in o["s"]:
-                    api.assemble(ctx, m, kind, o["mat"], sl, order=o["order"], subdiv=o["subdiv"], out=buf,
-                                 dtype=L.C128)
-                    d2h += buf.nbytes
+                shape = (len(o["s"]),) + tuple(api.out_shape(L.KINDS[kind], m.nV))
+                buf = host[: int(np.prod(shape))].view(shape).numpy()
+                api.assemble_frequencies(ctx, m, kind, o["mat"], o["s"], order=o["order"], subdiv=o["subdiv"],
+                                         out=buf, dtype=L.C128)
+                d2h += buf.nbytes
         return d2h
 
     e2e_value, d2h_bytes = None, 0
@@ -869,8 +871,9 @@ def run_gpu(args):
                 "roofline": roofline, "cpu_baseline": cpu,
                 "paths": paths,
                 "e2e": {"value": e2e_value, "unit": "entries/s", "h2d_bytes_per_step": h2d_bytes,
-                        "d2h_bytes_per_step": d2h_bytes, "path": "sod_cqbem_assemble per (object, kind, "
-                        "frequency) into pinned host memory, complex128 reference layout", "steps": e2e_steps},
+                        "d2h_bytes_per_step": d2h_bytes, "path": "sod_cqbem_assemble_frequencies per (object, kind) "
+                        "(the frequency-loop drop-in) into pinned host memory, complex128 reference layout",
+                        "steps": e2e_steps},
                 "gpu_launches": int(launches), "clocks": clk.summary(), **extra}
         print(json.dumps(line))
     if dist:
