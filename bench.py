@@ -12,10 +12,10 @@ object.  Metric: complex matrix entries per second, counted as sum over objects 
 
   value : device-resident path -- one multi-frequency launch per (object, kind), outputs complex64
           kept in HBM; CUDA-event time summed over K steps, L2 flushed between steps.
-  e2e   : the drop-in through the C ABI with host buffers -- one sod_cqbem_assemble_frequencies call
-          per (object, kind), the replacement of the frequency loop of compute_{G,H,B_trans,
-          B_angular}_matrices, into a pinned host array of every frequency in the reference layout
-          (complex128), timed end to end (row chunks copied to the host while later rows compute).
+  e2e   : the drop-in through the C ABI with host buffers -- one sod_cqbem_assemble_all call per
+          object, the replacement of the frequency loops of compute_{G,H,B_trans,B_angular}_matrices,
+          into pinned host arrays of every frequency in the reference layout (complex128), timed end
+          to end (row chunks copied to the host while later rows compute).
   --impl reference : the reference's CPU algorithm (the oracle's reference-mixed restatement,
           OpenMP on all host cores) on a bounded sample of the same workload.
 """
@@ -778,22 +778,25 @@ def run_gpu(args):
         t_per_object = timed(step_per_object, max(1, args.steps // 2))
         t_plain = timed(step_plain, max(1, args.steps // 2))
 
-    # ---- end to end: the per-(object, kind) frequency-loop drop-in with pinned host buffers ----
-    # one pinned array of the largest (frequencies x rows x columns) complex128 output, reused by
-    # every call as the reference's loop reuses its host matrix
-    host_elems = max(len(o["s"]) * 9 * m.nV * m.nV for o, m in zip(objs, meshes))
-    host = torch.empty(host_elems, dtype=torch.complex128, pin_memory=True)
+    # ---- end to end: the per-object frequency-loop drop-in with pinned host buffers ----
+    # per kind one pinned array of the largest (frequencies x rows x columns) complex128 output,
+    # reused by every call as the reference's loops reuse their host matrices
+    host = {}
+    for kind in KINDS:
+        elems = max(len(o["s"]) * int(np.prod(api.out_shape(L.KINDS[kind], m.nV))) for o, m in zip(objs, meshes))
+        host[kind] = torch.empty(elems, dtype=torch.complex128, pin_memory=True)
     e2e_steps = max(1, args.steps // 2)
 
     def e2e_step():
         d2h = 0
         for o, m in zip(objs, meshes):
+            outs = {}
             for kind in KINDS:
                 shape = (len(o["s"]),) + tuple(api.out_shape(L.KINDS[kind], m.nV))
-                buf = host[: int(np.prod(shape))].view(shape).numpy()
-                api.assemble_frequencies(ctx, m, kind, o["mat"], o["s"], order=o["order"], subdiv=o["subdiv"],
-                                         out=buf, dtype=L.C128)
-                d2h += buf.nbytes
+                outs[kind] = host[kind][: int(np.prod(shape))].view(shape).numpy()
+                d2h += outs[kind].nbytes
+            api.assemble_all(ctx, m, o["mat"], o["s"], order=o["order"], subdiv=o["subdiv"], outs=outs,
+                             dtype=L.C128)
         return d2h
 
     e2e_value, d2h_bytes = None, 0
@@ -806,7 +809,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         e2e_t = time.perf_counter() - t0
         e2e_value = world * total_entries * e2e_steps / e2e_t
-    h2d_bytes = sum(16 * len(o["s"]) + 64 for o in objs) * 4  # per-call frequency constants
+    h2d_bytes = sum(16 * len(o["s"]) + 64 for o in objs)  # per-call frequency constants
 
     # ---- roofline of the dominant kernel of the batched step: per-launch CUDA-event times ----
     peak_fp32 = measure_fp32_peak(torch, dev)
@@ -874,8 +877,8 @@ def run_gpu(args):
                 "roofline": roofline, "cpu_baseline": cpu,
                 "paths": paths,
                 "e2e": {"value": e2e_value, "unit": "entries/s", "h2d_bytes_per_step": h2d_bytes,
-                        "d2h_bytes_per_step": d2h_bytes, "path": "sod_cqbem_assemble_frequencies per (object, kind) "
-                        "(the frequency-loop drop-in) into pinned host memory, complex128 reference layout",
+                        "d2h_bytes_per_step": d2h_bytes, "path": "sod_cqbem_assemble_all per object (the frequency-loop "
+                        "drop-in of all four kinds) into pinned host memory, complex128 reference layout",
                         "steps": e2e_steps},
                 "gpu_launches": int(launches), "clocks": clk.summary(), **extra}
         print(json.dumps(line))
