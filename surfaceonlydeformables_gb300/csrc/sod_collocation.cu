@@ -146,23 +146,20 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
 #pragma unroll
                         for (int p = 0; p < 3; p++)
 #pragma unroll
-                            for (int qq = p; qq < 3; qq++) {
-                                cf v = al * (rh[p] * rh[qq]);
-                                if (p == qq) v = v + be;
-                                u[sym_index(p, qq)] = v;
-                            }
+                            for (int qq = p; qq < 3; qq++)
+                                u[sym_index(p, qq)] = p == qq ? cfmar(al, rh[p] * rh[qq], be) : cmulr(al, rh[p] * rh[qq]);
                     } else {
                         cf ha, hb, hd;
                         h_coeffs(t, k, rinv * rinv, ha, hb, hd);
                         const float rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
-                        const cf hdr = hd * rn, hbr = hb * rn;
+                        const cf hdr = cmulr(hd, rn), hbr = cmulr(hb, rn);
 #pragma unroll
                         for (int p = 0; p < 3; p++)
 #pragma unroll
                             for (int qq = 0; qq < 3; qq++) {
-                                cf v = ha * (rh[p] * nn[qq]) + hb * (nn[p] * rh[qq]) + hdr * (rh[p] * rh[qq]);
-                                if (p == qq) v = v + hbr;
-                                u[3 * p + qq] = v;
+                                cf v = cfmar(hdr, rh[p] * rh[qq], p == qq ? hbr : mk(0.f, 0.f));
+                                v = cfmar(hb, nn[p] * rh[qq], v);
+                                u[3 * p + qq] = cfmar(ha, rh[p] * nn[qq], v);
                             }
                     }
                     const float w = P.w * fr.area;

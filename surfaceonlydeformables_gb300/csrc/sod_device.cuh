@@ -46,6 +46,21 @@ template <class C, class R> __device__ __forceinline__ void cfma(C &acc, C a, R 
     acc.x = fma(a.x, s, acc.x);
     acc.y = fma(a.y, s, acc.y);
 }
+// FP32 complex times real, accumulated: one packed two-lane FMA (sm_100+), each lane an ordinary
+// round-to-nearest fma, so the results are those of the two scalar fmas above
+__device__ __forceinline__ void cfma(cf &acc, cf a, float s) {
+    const float2 r = __ffma2_rn(make_float2(a.x, a.y), make_float2(s, s), make_float2(acc.x, acc.y));
+    acc = {r.x, r.y};
+}
+// a * s and a * s + b for FP32 complex a, b and real s, as single packed instructions
+__device__ __forceinline__ cf cmulr(cf a, float s) {
+    const float2 r = __fmul2_rn(make_float2(a.x, a.y), make_float2(s, s));
+    return {r.x, r.y};
+}
+__device__ __forceinline__ cf cfmar(cf a, float s, cf b) {
+    const float2 r = __ffma2_rn(make_float2(a.x, a.y), make_float2(s, s), make_float2(b.x, b.y));
+    return {r.x, r.y};
+}
 __device__ __forceinline__ cf crecip(cf a) {
     const float d = __frcp_rn(fmaf(a.x, a.x, a.y * a.y));
     return {a.x * d, -a.y * d};
