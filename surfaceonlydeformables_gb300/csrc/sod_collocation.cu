@@ -22,6 +22,7 @@
 #include <cstdio>
 
 #include "sod_bmom.cuh"
+#include "sod_dd.cuh"
 #include "sod_faces.cuh"
 #include "sod_geom.cuh"
 #include "sod_internal.h"
@@ -216,24 +217,25 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
         }
     }
     if (NCB) {
-        // column sums in FP64: 32 lanes per component, strided partial sums, fixed xor-tree
+        // column sums in double-float on the FP32 pipes (FP64 sums here kept GB300's small FP64
+        // pipe busy for ~8% of the pass): 32 lanes per component, strided partial sums, fixed xor tree
         __shared__ cd bsum[24];
         __syncthreads();
         const int T = blockDim.x;
         for (int p = threadIdx.x; p < NCB * 32; p += T) {
             const int cc = p >> 5, l = p & 31;
-            double sx = 0.0, sy = 0.0;
+            dd sx = dd{0.f, 0.f}, sy = dd{0.f, 0.f};
             for (int j = l; j < T; j += 32) {
                 const float2 v = accB[cc * T + j];
-                sx += v.x;
-                sy += v.y;
+                sx = sx + v.x;
+                sy = sy + v.y;
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                sx += __shfl_xor_sync(0xffffffffu, sx, o);
-                sy += __shfl_xor_sync(0xffffffffu, sy, o);
+                sx = sx + dd{__shfl_xor_sync(0xffffffffu, sx.hi, o), __shfl_xor_sync(0xffffffffu, sx.lo, o)};
+                sy = sy + dd{__shfl_xor_sync(0xffffffffu, sy.hi, o), __shfl_xor_sync(0xffffffffu, sy.lo, o)};
             }
-            if (l == 0) bsum[cc] = mk(sx, sy);
+            if (l == 0) bsum[cc] = mk(dd_to(sx), dd_to(sy));
         }
         __syncthreads();
         store_b<BM>(a, bsum, i, fq);
