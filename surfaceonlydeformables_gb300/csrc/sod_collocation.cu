@@ -139,7 +139,7 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
                     const float rinv = rsqrtf(r2);
                     const float r = r2 * rinv;
                     const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                    const RadialTerms<float, cf> t = radial<float, cf>(r, k);
+                    const RadialTerms<float, cf> t = radial(r, k);
                     cf u[NC];
                     if (KIND == SOD_G) {
                         cf al, be;
@@ -322,7 +322,7 @@ __device__ __forceinline__ void reduce_body(const CollArgs &a, const PointTable 
                 const float rinv = rsqrtf(r2);
                 const float r = r2 * rinv;
                 const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                const RadialTerms<float, cf> t = radial<float, cf>(r, k);
+                const RadialTerms<float, cf> t = radial(r, k);
                 bm.add(t, k, r, rh, nn, P.w);
             }
             bm.emit(nn, fr.area, [&](int c, cf v) { accl[c] = accl[c] + v; });

@@ -189,6 +189,41 @@ __device__ __forceinline__ void h_coeffs(const RadialTerms<R, C> &t, const KCons
     d = d * p;
 }
 
+// FP32 overloads of the above with packed two-lane FMA / multiply chains (same algebra; each
+// complex-times-real multiply-add is one instruction)
+__device__ __forceinline__ RadialTerms<float, cf> radial(float r, const KConst<float> &k) {
+    RadialTerms<float, cf> t;
+    t.z1 = mk(r * k.sc1r, r * k.sc1i);
+    t.z2 = mk(r * k.sc2r, r * k.sc2i);
+    t.e1 = cexp_neg(t.z1);
+    t.e2 = cexp_neg(t.z2);
+    t.psi1 = psi(t.z1, t.e1);
+    t.psi2 = psi(t.z2, t.e2);
+    t.Y = cfmar(t.psi2, -k.ic2s, cmulr(t.psi1, k.ic1s));
+    return t;
+}
+__device__ __forceinline__ void g_coeffs(const RadialTerms<float, cf> &t, const KConst<float> &k, float scale,
+                                         cf &alpha, cf &beta) {
+    const cf Cc = cmulr(t.e2, k.ic2s);
+    const cf B = cfmar(t.e1, k.ic1s, cmulr(Cc, -1.0f));
+    const float p = k.inv4pirho * scale;
+    alpha = cmulr(cfmar(t.Y, 3.0f, B), p);
+    beta = cmulr(cfmar(t.Y, -1.0f, Cc), p);
+}
+__device__ __forceinline__ void h_coeffs(const RadialTerms<float, cf> &t, const KConst<float> &k, float scale,
+                                         cf &a, cf &b, cf &d) {
+    const cf Yc = cmulr(t.Y, k.six_c2s);
+    const cf z1e1 = t.z1 * t.e1, z2e2 = t.z2 * t.e2;
+    const float kp = k.kappa;
+    a = cfmar(z1e1, -(1.0f - 2.0f * kp), cfmar(t.e2, -2.0f, cfmar(t.e1, 4.0f * kp - 1.0f, Yc)));
+    b = cfmar(z2e2, -1.0f, cfmar(t.e2, -3.0f, cfmar(t.e1, 2.0f * kp, Yc)));
+    d = cfmar(z2e2, 2.0f, cfmar(z1e1, -2.0f * kp, cfmar(t.e2, 12.0f, cfmar(t.e1, -12.0f * kp, cmulr(Yc, -5.0f)))));
+    const float p = k.inv4pi * scale;
+    a = cmulr(a, p);
+    b = cmulr(b, p);
+    d = cmulr(d, p);
+}
+
 // B_trans: b = [(Y/2)(rh n^T + n rh^T) + psi2/c2^2 rn I] * scale/(4 pi)
 template <class R, class C>
 __device__ __forceinline__ void bt_coeffs(const RadialTerms<R, C> &t, const KConst<R> &k, R scale, C &sym, C &dia) {

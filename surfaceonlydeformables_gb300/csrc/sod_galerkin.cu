@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_tp_kernel(
                 const float rinv = rsqrtf(r2);
                 const float r = r2 * rinv;
                 const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                const RadialTerms<float, cf> rt = radial<float, cf>(r, k);
+                const RadialTerms<float, cf> rt = radial(r, k);
                 cf u[NC];
                 if (KIND == SOD_G) {
                     cf al, be;
