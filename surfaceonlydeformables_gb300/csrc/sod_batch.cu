@@ -114,7 +114,10 @@ static int finalize_batch(sod_batch *b) {
             if (!(b->mask & (1 << kd))) continue;
             const int bm = kd == SOD_G ? bmask : 0;
             int T = ctx->coll_threads;
-            if (T <= 0) SOD_TRY(autotune_scatter_threads(ctx, const_cast<sod_mesh *>(ob.mesh), kd, bm, &T));
+            int rc = SOD_OK;
+            if (T <= 0) rc = autotune_scatter_threads(ctx, const_cast<sod_mesh *>(ob.mesh), kd, bm, &T);
+            if (rc == SOD_ERR_UNSUPPORTED) T = SCATTER_GLOBAL_THREADS;  // row block too large: global accumulator
+            else if (rc != SOD_OK) return rc;
             ob.T[kd] = T;
         }
     }
@@ -219,6 +222,9 @@ static int finalize_batch(sod_batch *b) {
     auto add_regular = [&](int which, int chain) -> int {
         const int kind = which == 3 ? SOD_H : SOD_G;
         const int bm = which == 3 ? 0 : bmask;
+        // class key (-CTAs per SM, T, point table); per_sm = 1 << 20 marks objects whose row block
+        // does not fit in shared memory (accumulators in global memory, a class of their own)
+        constexpr int GLOBAL_CLASS = 1 << 20;
         std::map<std::tuple<int, int, int>, std::vector<int>> classes;
         for (int o : order) {
             const auto &ob = b->objs[o];
@@ -227,21 +233,35 @@ static int finalize_batch(sod_batch *b) {
                 T = ob.T[kind];
                 SOD_TRY(scatter_occupancy(ctx, kind, bm, true, T, scatter_smem_bytes(kind, bm, ob.mesh->nV, T), &per_sm));
                 if (per_sm <= 0) {
-                    set_error("mesh too large for the shared-memory row accumulator");
-                    return SOD_ERR_UNSUPPORTED;
+                    T = SCATTER_GLOBAL_THREADS;
+                    per_sm = GLOBAL_CLASS;
                 }
             }
             classes[std::make_tuple(-per_sm, T, pt_idx[o])].push_back(o);
         }
         for (auto &c : classes) {
             const int T = std::get<1>(c.first), pi = std::get<2>(c.first);
+            const bool global = -std::get<0>(c.first) == GLOBAL_CLASS;
             const auto &members = c.second;
             for (size_t g0 = 0; g0 < members.size(); g0 += BATCH_OBJS) {
                 const size_t g1 = std::min(members.size(), g0 + (size_t)BATCH_OBJS);
                 size_t sm = 0;
-                for (size_t g = g0; g < g1; g++)
-                    if (which != 4) sm = std::max(sm, scatter_smem_bytes(kind, bm, b->objs[members[g]].mesh->nV, T));
-                std::shared_ptr<BatchRegular> reg(batch_regular_new(which, b->mask, T, sm, pts[pi]), RegularDeleter());
+                long long nit = 0;
+                for (size_t g = g0; g < g1; g++) {
+                    const auto &ob = b->objs[members[g]];
+                    if (which != 4) sm = std::max(sm, scatter_smem_bytes(kind, bm, ob.mesh->nV, T));
+                    nit += (long long)ob.mesh->nV * (long long)(ob.s.size() / 2);
+                }
+                std::shared_ptr<BatchRegular> reg;
+                if (global) {
+                    int grc = SOD_OK;
+                    reg.reset(batch_regular_new_global(ctx, which, b->mask, sm, (int)std::min<long long>(nit, 1 << 30),
+                                                       pts[pi], &grc),
+                              RegularDeleter());
+                    SOD_TRY(grc);
+                } else {
+                    reg.reset(batch_regular_new(which, b->mask, T, sm, pts[pi]), RegularDeleter());
+                }
                 const int off = (int)items.size();
                 double evals = 0;
                 for (size_t g = g0; g < g1; g++) {

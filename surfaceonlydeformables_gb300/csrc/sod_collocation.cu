@@ -262,7 +262,6 @@ __global__ void __launch_bounds__(scatter_max_threads<KIND, BM>(), 1) coll_scatt
 // in L2 (grid x slice is a few tens of MB).  The body is the same: colour-ordered adds separated by
 // CTA barriers (which also order the CTA's global-memory accesses), so the sums and their order are
 // those of the shared-memory variant.
-constexpr int SCATTER_GLOBAL_THREADS = 256;
 template <int KIND, int BM>
 __global__ void __launch_bounds__(SCATTER_GLOBAL_THREADS) coll_scatter_global_kernel(CollArgs a, PointTable pt,
                                                                                    const __grid_constant__ FreqTable ft,
@@ -638,6 +637,23 @@ __global__ void __launch_bounds__(scatter_max_threads<KIND, BM>(), 1) batch_scat
                                                                const int4 *__restrict__ items, int nitems,
                                                                int *counter, const KConst<float> *__restrict__ kcf) {
     extern __shared__ float2 acc[];
+    __shared__ int s_item;
+    for (;;) {
+        const int it = next_item(counter, &s_item);
+        if (it >= nitems) break;
+        const int4 w = items[it];
+        scatter_body<KIND, BM>(p.a[w.x], p.pt, kcf[p.kc_off[w.x] + w.z], w.y, w.z, acc);
+    }
+}
+
+// The batched scatter with each CTA's row accumulator in a slice of global memory (objects whose row
+// block exceeds shared memory; see coll_scatter_global_kernel).
+template <int KIND, int BM>
+__global__ void __launch_bounds__(256) batch_scatter_global_kernel(const __grid_constant__ BatchLaunchArgs p,
+                                                                   const int4 *__restrict__ items, int nitems,
+                                                                   int *counter, const KConst<float> *__restrict__ kcf,
+                                                                   float2 *scratch, long long per_cta) {
+    float2 *acc = scratch + (size_t)blockIdx.x * per_cta;
     __shared__ int s_item;
     for (;;) {
         const int it = next_item(counter, &s_item);
@@ -1118,7 +1134,10 @@ int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, d
 // which may be capturing into a CUDA graph.
 struct BatchRegular {
     int which, mask, threads;
-    size_t smem;
+    size_t smem;  // dynamic shared memory; for a global-memory launch, the accumulator slice per CTA
+    bool global = false;
+    int grid = 0;
+    DevBuf scratch;  // global-memory accumulators, grid x slice (allocated before graph capture)
     BatchLaunchArgs args;
 };
 
@@ -1130,6 +1149,37 @@ BatchRegular *batch_regular_new(int which, int mask, int threads, size_t smem, c
     r->smem = smem;
     r->args.pt = pt;
     r->args.nobj = 0;
+    return r;
+}
+
+template <int KIND, int BM> static const void *batch_global_fn() { return (const void *)batch_scatter_global_kernel<KIND, BM>; }
+static const void *batch_global_fn(int kind, int bm) {
+    if (kind == SOD_H) return batch_global_fn<SOD_H, 0>();
+    switch (bm) {
+    case KM_BT: return batch_global_fn<SOD_G, KM_BT>();
+    case KM_BA: return batch_global_fn<SOD_G, KM_BA>();
+    case KM_BT | KM_BA: return batch_global_fn<SOD_G, KM_BT | KM_BA>();
+    default: return batch_global_fn<SOD_G, 0>();
+    }
+}
+
+// A scatter launch whose row accumulators live in global memory: `slice` bytes per CTA (the largest
+// member's row block); the persistent grid and the scratch are sized here, before graph capture.
+BatchRegular *batch_regular_new_global(sod_context *ctx, int which, int mask, size_t slice, int nitems_hint,
+                                       const PointTable &pt, int *rc) {
+    *rc = SOD_OK;
+    auto *r = batch_regular_new(which, mask, SCATTER_GLOBAL_THREADS, slice, pt);
+    r->global = true;
+    const void *fn = batch_global_fn(which == 3 ? SOD_H : SOD_G, which == 3 ? 0 : (mask & (KM_BT | KM_BA)));
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SCATTER_GLOBAL_THREADS, 0) != cudaSuccess ||
+        per_sm <= 0) {
+        set_error("batched global-memory scatter does not fit on an SM");
+        *rc = SOD_ERR_CUDA;
+        return r;
+    }
+    r->grid = std::max(1, std::min(per_sm * ctx->num_sms, std::max(nitems_hint, 1)));
+    *rc = r->scratch.ensure(slice * (size_t)r->grid);
     return r;
 }
 void batch_regular_free(BatchRegular *r) { delete r; }
@@ -1179,6 +1229,25 @@ int batch_regular_issue(sod_context *ctx, const BatchRegular *r, const int4 *ite
     if (nitems <= 0) return SOD_OK;
     const int bm = r->mask & (KM_BT | KM_BA);
     const int T = r->threads;
+    if (r->global) {
+        SOD_CHECK_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), stream));
+        const BatchLaunchArgs &p = r->args;
+        float2 *sc = r->scratch.as<float2>();
+        const long long per_cta = (long long)(r->smem / sizeof(float2));
+        if (r->which == 3)
+            batch_scatter_global_kernel<SOD_H, 0><<<r->grid, T, 0, stream>>>(p, items, nitems, counter, kcf, sc, per_cta);
+        else if (bm == (KM_BT | KM_BA))
+            batch_scatter_global_kernel<SOD_G, KM_BT | KM_BA><<<r->grid, T, 0, stream>>>(p, items, nitems, counter, kcf, sc, per_cta);
+        else if (bm == KM_BT)
+            batch_scatter_global_kernel<SOD_G, KM_BT><<<r->grid, T, 0, stream>>>(p, items, nitems, counter, kcf, sc, per_cta);
+        else if (bm == KM_BA)
+            batch_scatter_global_kernel<SOD_G, KM_BA><<<r->grid, T, 0, stream>>>(p, items, nitems, counter, kcf, sc, per_cta);
+        else
+            batch_scatter_global_kernel<SOD_G, 0><<<r->grid, T, 0, stream>>>(p, items, nitems, counter, kcf, sc, per_cta);
+        SOD_CHECK_CUDA(cudaGetLastError());
+        ctx->count();
+        return SOD_OK;
+    }
     const void *fn = r->which == 2   ? scatter_fn(SOD_G, bm, true)
                      : r->which == 3 ? scatter_fn(SOD_H, 0, true)
                      : bm == (KM_BT | KM_BA) ? (const void *)batch_reduce_kernel<KM_BT | KM_BA>

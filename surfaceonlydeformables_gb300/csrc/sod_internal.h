@@ -227,6 +227,11 @@ bool is_device_pointer(const void *p);
 constexpr int BATCH_OBJS = 112;
 struct BatchRegular;
 BatchRegular *batch_regular_new(int which, int mask, int threads, size_t smem, const PointTable &pt);
+// scatter launch with the row accumulators in global memory (`slice` bytes per CTA); *rc reports
+// allocation failures (the object is returned either way and must be freed)
+constexpr int SCATTER_GLOBAL_THREADS = 256;
+BatchRegular *batch_regular_new_global(sod_context *ctx, int which, int mask, size_t slice, int nitems_hint,
+                                       const PointTable &pt, int *rc);
 void batch_regular_free(BatchRegular *r);
 int batch_regular_add(BatchRegular *r, const sod_mesh *m, int out_dtype, void *const out[4], cd *const S[4],
                       const sod_mesh::Coloured *col, int kc_off, int *slot);

@@ -133,3 +133,32 @@ def test_batch_kind_subsets(gpu_ctx, objects, oracle, kinds):
             r = out[k].cpu().numpy()
             assert rel_fro(r, single[k]) <= 1e-6, k
             assert rel_fro(r[l], oracle.collocation(k, o["host"], o["mat"], o["s"][l])) <= 1e-5, k
+
+
+def test_batch_with_row_block_beyond_shared_memory(gpu_ctx, sodlib, oracle):
+    """The reference's 3485-vertex bunny in a batch with a small sphere: its H row block exceeds
+    shared memory, so the batch gives it a launch with the accumulators in global memory.  Results
+    match the per-object path and sampled FP64 oracle rows."""
+    import os
+
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+    from surfaceonlydeformables_gb300.meshes import SurfaceMesh
+
+    b = np.load(os.path.join(os.path.dirname(__file__), "golden", "bunny_mesh.npz"))
+    bunny = SurfaceMesh.from_arrays(b["V"], b["F"])
+    s, R, Lq = sodlib.cq_frequencies(1, 0.003, 5)
+    mat = Material(2.0 * 1e6 * 1.3, 0.3, 3000.0)
+    small = make_icosphere_mesh(2, 0.1)
+    objs = [dict(host=bunny, dev=api.Mesh(gpu_ctx, bunny), mat=mat, s=s[:2]),
+            dict(host=small, dev=api.Mesh(gpu_ctx, small), mat=mat, s=s[:2])]
+    bt, res = run_batch(gpu_ctx, objs)
+    for o, r in zip(objs, res):
+        single = api.assemble_all(gpu_ctx, o["dev"], o["mat"], o["s"], dtype=L.C64)
+        for k in KINDS:
+            assert rel_fro(r[k], single[k]) <= 1e-6, k
+    verts = np.array([7, 2000], dtype=np.int32)
+    for k in ("G", "H"):
+        got = np.concatenate([res[0][k][1][3 * v:3 * v + 3] for v in verts])
+        ref = oracle.collocation(k, bunny, mat, s[1], rows=verts)
+        assert rel_fro(got, ref) <= 1e-5, k
