@@ -104,14 +104,19 @@ struct GalTpArgs {
 
 template <int KIND, int BM> constexpr int gal_max_threads() { return 512; }
 
-template <int KIND, int BM>
+// GLOBAL: the row block does not fit in shared memory, so the CTA accumulates directly in its
+// output row (global memory, exclusive to the CTA; the colour barriers order its accesses) and
+// keeps only the B columns in shared memory.
+template <int KIND, int BM, bool GLOBAL = false>
 __global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_tp_kernel(GalTpArgs a, PointTable pt,
                                                                                 const __grid_constant__ FreqTable ft) {
     constexpr int NC = KIND == SOD_G ? 6 : 9;
     using BMo = BMom<KIND == SOD_G ? BM : 0>;
     constexpr int NCB = BMo::NC;
-    extern __shared__ float2 acc[];  // [NC][nV], then [NCB][blockDim]
+    extern __shared__ float2 smem_tp[];  // [NC][nV] (unless GLOBAL), then [NCB][blockDim]
     const int tl = blockIdx.x, t = a.t0 + tl, fq = blockIdx.y, nV = a.nV;
+    float2 *dst = a.rows + (long long)fq * a.rows_fstride + (long long)tl * NC * nV;
+    float2 *acc = GLOBAL ? dst : smem_tp;
     const KConst<float> k = ft.kf[fq];
     const int f1 = t / a.nq, ix = t - f1 * a.nq;
     const FaceRec tf = load_face(a.faces_nat, f1);
@@ -120,7 +125,7 @@ __global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_tp_kernel(
                                  PX.x * tf.y1.y + PX.y * tf.y2.y + PX.z * tf.y3.y,
                                  PX.x * tf.y1.z + PX.y * tf.y2.z + PX.z * tf.y3.z);
     for (int e = threadIdx.x; e < NC * nV; e += blockDim.x) acc[e] = make_float2(0.f, 0.f);
-    float2 *accB = acc + NC * nV;
+    float2 *accB = GLOBAL ? smem_tp : acc + NC * nV;
 #pragma unroll
     for (int c = 0; c < NCB; c++) accB[c * blockDim.x + threadIdx.x] = make_float2(0.f, 0.f);
     __syncthreads();
@@ -156,23 +161,20 @@ __global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_tp_kernel(
 #pragma unroll
                     for (int p = 0; p < 3; p++)
 #pragma unroll
-                        for (int qq = p; qq < 3; qq++) {
-                            cf v = al * (rh[p] * rh[qq]);
-                            if (p == qq) v = v + be;
-                            u[sym_index(p, qq)] = v;
-                        }
+                        for (int qq = p; qq < 3; qq++)
+                            u[sym_index(p, qq)] = p == qq ? cfmar(al, rh[p] * rh[qq], be) : cmulr(al, rh[p] * rh[qq]);
                 } else {
                     cf ha, hb, hd;
                     h_coeffs(rt, k, rinv * rinv, ha, hb, hd);
                     const float rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
-                    const cf hdr = hd * rn, hbr = hb * rn;
+                    const cf hdr = cmulr(hd, rn), hbr = cmulr(hb, rn);
 #pragma unroll
                     for (int p = 0; p < 3; p++)
 #pragma unroll
                         for (int qq = 0; qq < 3; qq++) {
-                            cf v = ha * (rh[p] * nn[qq]) + hb * (nn[p] * rh[qq]) + hdr * (rh[p] * rh[qq]);
-                            if (p == qq) v = v + hbr;
-                            u[3 * p + qq] = v;
+                            cf v = cfmar(hdr, rh[p] * rh[qq], p == qq ? hbr : mk(0.f, 0.f));
+                            v = cfmar(hb, nn[p] * rh[qq], v);
+                            u[3 * p + qq] = cfmar(ha, rh[p] * nn[qq], v);
                         }
                 }
                 const float w = P.w * fr.area;
@@ -203,26 +205,27 @@ __global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_tp_kernel(
         }
         __syncthreads();
     }
-    // the row, unweighted, to scratch (coalesced)
-    float2 *dst = a.rows + (long long)fq * a.rows_fstride + (long long)tl * NC * nV;
-    for (int e = threadIdx.x; e < NC * nV; e += blockDim.x) dst[e] = acc[e];
+    // the row, unweighted, to scratch (coalesced; a GLOBAL CTA accumulated in place)
+    if (!GLOBAL)
+        for (int e = threadIdx.x; e < NC * nV; e += blockDim.x) dst[e] = acc[e];
     if (NCB) {
-        // per-thread B columns -> FP64 sums, 32 lanes per component in a fixed xor tree
+        // per-thread B columns -> double-float sums on the FP32 pipes (FP64 is ~1/64 of the FP32 rate
+        // on GB300), 32 lanes per component in a fixed xor tree
         const int T = blockDim.x;
         for (int p = threadIdx.x; p < NCB * 32; p += T) {
             const int cc = p >> 5, l = p & 31;
-            double sx = 0.0, sy = 0.0;
+            dd sx = dd{0.f, 0.f}, sy = dd{0.f, 0.f};
             for (int j = l; j < T; j += 32) {
                 const float2 v = accB[cc * T + j];
-                sx += v.x;
-                sy += v.y;
+                sx = sx + v.x;
+                sy = sy + v.y;
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                sx += __shfl_xor_sync(0xffffffffu, sx, o);
-                sy += __shfl_xor_sync(0xffffffffu, sy, o);
+                sx = sx + dd{__shfl_xor_sync(0xffffffffu, sx.hi, o), __shfl_xor_sync(0xffffffffu, sx.lo, o)};
+                sy = sy + dd{__shfl_xor_sync(0xffffffffu, sy.hi, o), __shfl_xor_sync(0xffffffffu, sy.lo, o)};
             }
-            if (l == 0) a.bsum[(long long)fq * a.b_fstride + (long long)tl * NCB + cc] = mk(sx, sy);
+            if (l == 0) a.bsum[(long long)fq * a.b_fstride + (long long)tl * NCB + cc] = mk(dd_to(sx), dd_to(sy));
         }
     }
 }
@@ -774,13 +777,16 @@ static int build_gal(const sod_mesh *m, sod_mesh::GalData *g) {
 
 namespace sod {
 
-static const void *gal_tp_fn(int kind, int bm) {
+template <bool GLOBAL> static const void *gal_tp_fn_t(int kind, int bm) {
     constexpr int BT = 1 << SOD_B_TRANS, BA = 1 << SOD_B_ANGULAR;
-    if (kind == SOD_H) return (const void *)gal_tp_kernel<SOD_H, 0>;
-    return bm == (BT | BA) ? (const void *)gal_tp_kernel<SOD_G, BT | BA>
-         : bm == BT        ? (const void *)gal_tp_kernel<SOD_G, BT>
-         : bm == BA        ? (const void *)gal_tp_kernel<SOD_G, BA>
-                           : (const void *)gal_tp_kernel<SOD_G, 0>;
+    if (kind == SOD_H) return (const void *)gal_tp_kernel<SOD_H, 0, GLOBAL>;
+    return bm == (BT | BA) ? (const void *)gal_tp_kernel<SOD_G, BT | BA, GLOBAL>
+         : bm == BT        ? (const void *)gal_tp_kernel<SOD_G, BT, GLOBAL>
+         : bm == BA        ? (const void *)gal_tp_kernel<SOD_G, BA, GLOBAL>
+                           : (const void *)gal_tp_kernel<SOD_G, 0, GLOBAL>;
+}
+static const void *gal_tp_fn(int kind, int bm, bool global = false) {
+    return global ? gal_tp_fn_t<true>(kind, bm) : gal_tp_fn_t<false>(kind, bm);
 }
 
 // CTA size of the test-point kernel: the collocation scatter's cost model (colours x T / occupancy,
@@ -873,23 +879,36 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
         const int ncb = (pbm & BT ? 6 : 0) + (pbm & BA ? 18 : 0);
         const void *fn = gal_tp_fn(kd, pbm);
         int T = 0;
+        bool tp_global = false;  // row block beyond shared memory: accumulate in the output row
         if (ctx->gal_threads > 0) {
             cudaFuncAttributes attr;
             SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
             T = std::max(32, std::min(attr.maxThreadsPerBlock, (ctx->gal_threads / 32) * 32));
         } else if (reg) {
-            SOD_TRY(gal_tp_threads(ctx, mm, kd, pbm, fn, &T));
+            const int rc = gal_tp_threads(ctx, mm, kd, pbm, fn, &T);
+            if (rc == SOD_ERR_UNSUPPORTED) {
+                tp_global = true;
+                T = 256;
+            } else if (rc != SOD_OK) {
+                return rc;
+            }
         }
         const sod_mesh::Coloured *col = nullptr;
         size_t smem = 0;
         if (reg) {
             SOD_TRY(mm->coloured_for(T, &col));
             cudaFuncAttributes attr;
-            SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
             smem = sizeof(float2) * ((size_t)NCS * m->nV + (size_t)ncb * T);
-            if (smem + attr.sharedSizeBytes > ctx->smem_optin) {
-                set_error("mesh too large for the shared-memory row accumulator");
-                return SOD_ERR_UNSUPPORTED;
+            SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
+            if (!tp_global && smem + attr.sharedSizeBytes > ctx->smem_optin) tp_global = true;
+            if (tp_global) {
+                fn = gal_tp_fn(kd, pbm, true);
+                SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
+                smem = sizeof(float2) * (size_t)ncb * T;  // only the B columns stay in shared memory
+                if (smem + attr.sharedSizeBytes > ctx->smem_optin) {
+                    set_error("Galerkin B columns exceed shared memory");
+                    return SOD_ERR_UNSUPPORTED;
+                }
             }
             SOD_CHECK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)(ctx->smem_optin - attr.sharedSizeBytes)));
@@ -1018,7 +1037,18 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
                 ta.bsum = ncb ? ctx->gal_bsum.as<cd>() : nullptr;
                 ta.b_fstride = ga.b_fstride;
                 const dim3 grid((unsigned)ntp, nf);
-                if (kd == SOD_H)
+                if (tp_global) {
+                    if (kd == SOD_H)
+                        gal_tp_kernel<SOD_H, 0, true><<<grid, T, smem, L.stream>>>(ta, pt, ft);
+                    else if (pbm == (BT | BA))
+                        gal_tp_kernel<SOD_G, BT | BA, true><<<grid, T, smem, L.stream>>>(ta, pt, ft);
+                    else if (pbm == BT)
+                        gal_tp_kernel<SOD_G, BT, true><<<grid, T, smem, L.stream>>>(ta, pt, ft);
+                    else if (pbm == BA)
+                        gal_tp_kernel<SOD_G, BA, true><<<grid, T, smem, L.stream>>>(ta, pt, ft);
+                    else
+                        gal_tp_kernel<SOD_G, 0, true><<<grid, T, smem, L.stream>>>(ta, pt, ft);
+                } else if (kd == SOD_H)
                     gal_tp_kernel<SOD_H, 0><<<grid, T, smem, L.stream>>>(ta, pt, ft);
                 else if (pbm == (BT | BA))
                     gal_tp_kernel<SOD_G, BT | BA><<<grid, T, smem, L.stream>>>(ta, pt, ft);

@@ -84,3 +84,32 @@ def test_galerkin_all_kinds_in_one_call(gpu_ctx, oracle, sodlib, small):
         assert rel_fro(allk[kind], one) <= 1e-6, kind
         ref = oracle.galerkin(kind, m, MAT, s[2], order=5, sorder=5, ssub=1)
         assert rel_fro(allk[kind][2], ref) <= 1e-5, kind
+
+
+def test_galerkin_row_block_beyond_shared_memory(gpu_ctx, oracle, sodlib):
+    """The reference's 3485-vertex bunny: the test-point rows of H (9 x 3485 complex FP32) exceed
+    shared memory, so each CTA accumulates directly in its global-memory output row.  Sampled rows
+    of G (with the B kinds) and H against the row-sampled FP64 oracle, <= 1e-5."""
+    import os
+
+    import torch
+
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+    from surfaceonlydeformables_gb300.meshes import SurfaceMesh
+
+    b = np.load(os.path.join(os.path.dirname(__file__), "golden", "bunny_mesh.npz"))
+    m = SurfaceMesh.from_arrays(b["V"], b["F"])
+    dm = api.Mesh(gpu_ctx, m)
+    s, R, Lq = sodlib.cq_frequencies(1, 0.003, 5)
+    rows = np.array([11, 1800], dtype=np.int32)
+    n3 = 3 * m.nV
+    for kind in ("H", "G"):
+        out = torch.empty((1, n3, n3), dtype=torch.complex128, device="cuda")
+        api.assemble_frequencies(gpu_ctx, dm, kind, MAT, s[1:2], order=5, sorder=5, ssub=1, method=L.GALERKIN,
+                                 out=out)
+        torch.cuda.synchronize()
+        got = np.concatenate([out[0, 3 * v:3 * v + 3].cpu().numpy() for v in rows])
+        ref = oracle.galerkin(kind, m, MAT, s[1], order=5, sorder=5, ssub=1, rows=rows)
+        assert rel_fro(got, ref) <= 1e-5, (kind, rel_fro(got, ref))
+        del out
