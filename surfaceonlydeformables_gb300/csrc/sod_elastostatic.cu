@@ -269,12 +269,12 @@ static int elastostatic_galerkin(sod_context *ctx, const sod_mesh *m, int kind, 
     const int blocks = (int)((n3 * 32 + 255) / 256);
     if (kind == SOD_G)
         static_gal_finish_kernel<SOD_G><<<blocks, 256, 0, ctx->stream>>>(
-            ctx->freqbuf.as<double2>(), nV, m->dV.as<double>(), m->dF.as<int>(), m->dStarOff.as<int>(),
-            m->dStarFace.as<int>(), dst, out_dtype == SOD_F32);
+            ctx->freqbuf.as<double2>(), nV, m->dV.as<double>(), m->dF.as<int>(), m->gal->astar_off.as<int>(),
+            m->gal->astar_face.as<int>(), dst, out_dtype == SOD_F32);
     else
         static_gal_finish_kernel<SOD_H><<<blocks, 256, 0, ctx->stream>>>(
-            ctx->freqbuf.as<double2>(), nV, m->dV.as<double>(), m->dF.as<int>(), m->dStarOff.as<int>(),
-            m->dStarFace.as<int>(), dst, out_dtype == SOD_F32);
+            ctx->freqbuf.as<double2>(), nV, m->dV.as<double>(), m->dF.as<int>(), m->gal->astar_off.as<int>(),
+            m->gal->astar_face.as<int>(), dst, out_dtype == SOD_F32);
     SOD_CHECK_CUDA(cudaGetLastError());
     ctx->count();
     return SOD_OK;

@@ -96,6 +96,8 @@ struct GalTpArgs {
     const int *color_off;
     int ncolors;
     const float4 *faces_nat;   // test faces, natural order
+    const int4 *canon_faces;   // canonical corner ids of the trial faces (colour order), NULL without splitting
+    const int4 *canon_nat;     // canonical corner ids of the test faces (natural order)
     float2 *rows;              // [fq][t - t0][NC][nV]
     long long rows_fstride;
     cd *bsum;                  // [fq][t - t0][NCB] (BM != 0)
@@ -133,8 +135,13 @@ __global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_tp_kernel(
         const int fend = a.color_off[c + 1];
         for (int f = a.color_off[c] + threadIdx.x; f < fend; f += blockDim.x) {
             const FaceRec fr = load_face(a.faces, f);
-            const bool touch = fr.j0 == tf.j0 || fr.j0 == tf.j1 || fr.j0 == tf.j2 || fr.j1 == tf.j0 || fr.j1 == tf.j1 ||
-                               fr.j1 == tf.j2 || fr.j2 == tf.j0 || fr.j2 == tf.j1 || fr.j2 == tf.j2;
+            int p0 = fr.j0, p1 = fr.j1, p2 = fr.j2, q0 = tf.j0, q1 = tf.j1, q2 = tf.j2;
+            if (a.canon_faces) {  // traction-discontinuity splitting: pairs touch through canonical ids
+                const int4 cp = __ldg(a.canon_faces + f), cq = __ldg(a.canon_nat + f1);
+                p0 = cp.x, p1 = cp.y, p2 = cp.z, q0 = cq.x, q1 = cq.y, q2 = cq.z;
+            }
+            const bool touch = p0 == q0 || p0 == q1 || p0 == q2 || p1 == q0 || p1 == q1 || p1 == q2 || p2 == q0 ||
+                               p2 == q1 || p2 == q2;
             if (touch) continue;  // singular pair (coincident, edge- or vertex-adjacent)
             const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
             cf part[3][NC];
@@ -670,22 +677,25 @@ __global__ void __launch_bounds__(128) gal_combine_kernel(int nV, int nent, cons
 
 // pair classification (the singular-pair structure of include/integrator_galerkin.hpp:262-334):
 // 1 coincident, 2 edge adjacent, 3 vertex adjacent, 0 regular; permuted vertex lists j1, j2
-int classify(const int *F, int f1, int f2, int j1[3], int j2[3]) {
+// With traction-discontinuity splitting (vmap, may be NULL) vertices match when their canonical ids do
+// (:290-291, :314); j1, j2 keep the faces' own vertex ids.
+int classify(const int *F, const int *vmap, int f1, int f2, int j1[3], int j2[3]) {
     auto fv = [&](int f, int k) { return F[3 * f + k]; };
+    auto cv = [&](int f, int k) { return vmap ? vmap[F[3 * f + k]] : F[3 * f + k]; };
     if (f1 == f2) {
         for (int k = 0; k < 3; k++) j1[k] = j2[k] = fv(f1, k);
         return 1;
     }
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++)
-            if (fv(f1, i) == fv(f2, j) && fv(f1, (i + 1) % 3) == fv(f2, (j + 2) % 3)) {
+            if (cv(f1, i) == cv(f2, j) && cv(f1, (i + 1) % 3) == cv(f2, (j + 2) % 3)) {
                 j1[0] = fv(f1, i), j1[1] = fv(f1, (i + 1) % 3), j1[2] = fv(f1, (i + 2) % 3);
                 j2[0] = fv(f2, j), j2[1] = fv(f2, (j + 2) % 3), j2[2] = fv(f2, (j + 1) % 3);
                 return 2;
             }
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++)
-            if (fv(f1, i) == fv(f2, j)) {
+            if (cv(f1, i) == cv(f2, j)) {
                 j1[0] = fv(f1, i), j1[1] = fv(f1, (i + 1) % 3), j1[2] = fv(f1, (i + 2) % 3);
                 j2[0] = fv(f2, j), j2[1] = fv(f2, (j + 1) % 3), j2[2] = fv(f2, (j + 2) % 3);
                 return 3;
@@ -698,9 +708,39 @@ int classify(const int *F, int f1, int f2, int j1[3], int j2[3]) {
 // ---- per-mesh Galerkin structures (built once, kept on the mesh) ----------------------------------
 static int build_gal(const sod_mesh *m, sod_mesh::GalData *g) {
     const int nV = m->nV, nF = m->nF;
-    std::vector<std::vector<int>> vf(nV);
+    const int *vm = m->has_vmap ? m->vmap.data() : nullptr;
+    auto canon = [&](int v) { return vm ? vm[v] : v; };
+    std::vector<std::vector<int>> vf(nV), vfc(nV);  // faces of each vertex; of each canonical vertex
     for (int f = 0; f < nF; f++)
-        for (int c = 0; c < 3; c++) vf[m->F[3 * f + c]].push_back(f);
+        for (int c = 0; c < 3; c++) {
+            vf[m->F[3 * f + c]].push_back(f);
+            auto &l = vfc[canon(m->F[3 * f + c])];
+            if (l.empty() || l.back() != f) l.push_back(f);
+        }
+    // actual-vertex stars (face order; corner = first corner holding the vertex)
+    {
+        std::vector<int> so(nV + 1, 0), sf, sc;
+        g->max_astar = 0;
+        for (int v = 0; v < nV; v++) {
+            for (int f : vf[v]) {
+                if (!sf.empty() && so[v] < (int)sf.size() && sf.back() == f) continue;  // v twice in f
+                int c = 0;
+                while (m->F[3 * f + c] != v) c++;
+                sf.push_back(f);
+                sc.push_back(c);
+            }
+            so[v + 1] = (int)sf.size();
+            g->max_astar = std::max(g->max_astar, so[v + 1] - so[v]);
+        }
+        auto up = [](DevBuf &b, const std::vector<int> &v) -> int {
+            SOD_TRY(b.ensure(std::max<size_t>(sizeof(int) * v.size(), 16)));
+            if (!v.empty()) SOD_CHECK_CUDA(cudaMemcpy(b.p, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice));
+            return SOD_OK;
+        };
+        SOD_TRY(up(g->astar_off, so));
+        SOD_TRY(up(g->astar_face, sf));
+        SOD_TRY(up(g->astar_corner, sc));
+    }
     std::vector<int4> ent;
     std::vector<int> ent_off(nV + 1, 0), slot_off(nV + 1, 0), slot_vert;
     // distinct pairs (f1, f2): the three entries of a pair (one per test corner of f1) share every
@@ -713,10 +753,10 @@ static int build_gal(const sod_mesh *m, sod_mesh::GalData *g) {
         for (int f1 : vf[a]) {
             std::set<int> partners;
             for (int c = 0; c < 3; c++)
-                for (int f2 : vf[m->F[3 * f1 + c]]) partners.insert(f2);
+                for (int f2 : vfc[canon(m->F[3 * f1 + c])]) partners.insert(f2);
             for (int f2 : partners) {
                 int j1[3], j2[3];
-                const int cls = classify(m->F.data(), f1, f2, j1, j2);
+                const int cls = classify(m->F.data(), vm, f1, f2, j1, j2);
                 int ac = 0;
                 while (ac < 3 && j1[ac] != a) ac++;
                 rows.push_back({f2, cls, ac, j1[0], j1[1], j1[2], j2[0], j2[1], j2[2]});
@@ -836,9 +876,6 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
     const int mask = L.kind_mask;
     constexpr int BT = 1 << SOD_B_TRANS, BA = 1 << SOD_B_ANGULAR;
     const int bm = mask & (BT | BA);
-    SOD_REQUIRE(!m->has_vmap, "Galerkin assembly with traction-discontinuity splitting is not supported");
-    for (int v = 0; v < m->nV; v++)
-        SOD_REQUIRE(m->star_off[v + 1] - m->star_off[v] <= GAL_MAXS, "vertex with more than 32 faces");
     PointTable pt;
     SOD_TRY(make_point_table(L.order, L.subdiv, pt));
     SOD_REQUIRE(pt.n <= GAL_MAXQ, "Galerkin test rule: at most 13 points (order <= 7, subdivision 1)");
@@ -850,6 +887,7 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
         mm->gal = std::move(gd);
     }
     sod_mesh::GalData *g = m->gal.get();
+    SOD_REQUIRE(g->max_astar <= GAL_MAXS, "vertex with more than 32 faces");
     const bool sing = (L.parts & SOD_PART_SINGULAR) != 0;
     const bool reg = (L.parts & SOD_PART_REGULAR) != 0;
     const long long nslots = g->nslots;
@@ -947,9 +985,9 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
             a.color_off = reg ? col->dOff.as<int>() : nullptr;
             a.ncolors = reg ? col->ncolors : 0;
             a.faces_nat = m->dFacesNat.as<float4>();
-            a.star_off = m->dStarOff.as<int>();
-            a.star_face = m->dStarFace.as<int>();
-            a.star_corner = m->dStarCorner.as<int>();
+            a.star_off = g->astar_off.as<int>();
+            a.star_face = g->astar_face.as<int>();
+            a.star_corner = g->astar_corner.as<int>();
             a.out = L.out[kd] ? static_cast<char *>(L.out[kd]) + (size_t)f0 * (size_t)L.freq_stride[kd] * esz : nullptr;
             a.fstride = L.freq_stride[kd];
             a.out_c64 = L.out_dtype == SOD_C64;
@@ -1032,6 +1070,8 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
                 ta.color_off = col->dOff.as<int>();
                 ta.ncolors = col->ncolors;
                 ta.faces_nat = m->dFacesNat.as<float4>();
+                ta.canon_faces = m->has_vmap ? col->dCanonF.as<int4>() : nullptr;
+                ta.canon_nat = m->has_vmap ? m->dCanonNat.as<int4>() : nullptr;
                 ta.rows = ctx->gal_rows.as<float2>();
                 ta.rows_fstride = ga.rows_fstride;
                 ta.bsum = ncb ? ctx->gal_bsum.as<cd>() : nullptr;

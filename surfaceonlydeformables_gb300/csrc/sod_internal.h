@@ -157,6 +157,10 @@ struct sod_mesh {
         int nent = 0, nslots = 0, npairs = 0;
         sod::DevBuf ent, ent_off, slot_off, slot_vert;
         sod::DevBuf pairs;  // per distinct singular face pair: {f2, class}, j1, j2, {entry of test corner 0..2}
+        // stars of the actual vertices (the support of each test function; with traction-discontinuity
+        // splitting a split vertex owns only its own corners): faces in order, corner of the vertex
+        sod::DevBuf astar_off, astar_face, astar_corner;
+        int max_astar = 0;
     };
     std::unique_ptr<GalData> gal;
     int sing_geom_for(int sorder, int ssub, cudaStream_t stream, const SingGeom **out);

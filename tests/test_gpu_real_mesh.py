@@ -124,3 +124,26 @@ def test_cube_scene_precompute_on_split_mesh(gpu_ctx, cube, oracle, sodlib):
     ref["B_euler"] = np.stack([oracle.b_euler(ref["B_angular"][n]) for n in range(Lq)])
     for k in ("G", "H", "B_trans", "B_angular", "B_euler"):
         assert rel_fro(got[k].reshape(ref[k].shape), ref[k]) <= 1e-10, (k, rel_fro(got[k].reshape(ref[k].shape), ref[k]))
+
+
+@pytest.mark.parametrize("kind", ["G", "H", "B_trans", "B_angular"])
+def test_galerkin_on_split_cube(gpu_ctx, cube, oracle, kind):
+    """Galerkin on the traction-discontinuous cube: face pairs touching through canonical vertices are
+    singular (include/integrator_galerkin.hpp:290-291, 314), each split vertex's test function lives
+    on its own faces.  Sampled rows (a split vertex, its canonical sibling, a corner) against the
+    row-sampled FP64 oracle: full rows <= 1e-5, singular part <= 1e-10."""
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    mf, dev, r = cube
+    dm = dev["disc"]
+    vmap = np.load(os.path.join(GOLDEN, "cube_meshes.npz"))["vmap_disc"]
+    mat = mf.material()
+    s = r["s"][-1]
+    verts = r["verts_disc"]
+    for parts, tol in ((L.PART_SINGULAR, 1e-10), (L.PART_ALL, 1e-5)):
+        got = api.assemble(gpu_ctx, dm, kind, mat, s, order=5, subdiv=1, sorder=5, ssub=1, method=L.GALERKIN,
+                           parts=parts)
+        ref = oracle.galerkin(kind, dm.host, mat, s, order=5, subdiv=1, sorder=5, ssub=1, rows=verts,
+                              parts=2 if parts == L.PART_SINGULAR else 3, vmap=vmap)
+        assert rel_fro(_rows(got, verts, kind), ref) <= tol, (kind, parts, rel_fro(_rows(got, verts, kind), ref))
