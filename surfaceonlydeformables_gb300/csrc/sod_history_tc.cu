@@ -24,10 +24,13 @@
 // kernel adds a row tile's k partials in FP64 in fixed order (deterministic).  Banks with more row
 // tiles than 2 CTAs per SM (nrow > 2 SMs x 128) run with k = 1 in several waves.
 // FP32 banks (16 right-hand sides) run the same pipeline with 3xTF32 arithmetic and FP32 accuracy:
-// 128 x 32 FP32 weight tiles arrive by TMA; four transform warps split each into w_hi (top 19 bits,
-// exact in TF32) in place and w_lo = w - w_hi into a second tile; the history comes as x_hi + x_lo
-// (x_hi TF32-exact); tcgen05.mma.kind::tf32 accumulates w_hi [x_hi | x_lo] (N = 32) and w_lo x_hi
-// (N = 16, same accumulator columns), dropping only w_lo x_lo (~2^-22 relative).
+// 128 x 32 FP32 weight tiles arrive by TMA.  The TF32 MMA reads the top 19 bits of each FP32
+// operand (w_hi), so the tile serves as w_hi as it lies; four transform warps form w_lo = w - w_hi,
+// one weight row per thread, and store it to tensor memory with tcgen05.st.  The history comes as
+// x_hi + x_lo (x_hi TF32-exact); tcgen05.mma.kind::tf32 accumulates w_hi [x_hi | x_lo] (N = 32,
+// A from shared memory) and w_lo x_hi (N = 16, A from tensor memory, same accumulator columns),
+// dropping only w_lo x_lo (~2^-22 relative).  Shared memory then carries each weight byte three
+// times (TMA write, the transform's read, the MMA's read), which keeps it below the HBM rate.
 // Every mbarrier wait is bounded (about one second of clock); a timeout sets an error flag that the
 // host reports, and the kernel lets its copies and MMAs in flight finish (again bounded) and
 // releases its tensor memory before returning.
@@ -49,16 +52,20 @@ constexpr int TC_A_BYTES = TC_BM * 128;  // 128 weight rows of 128 bytes: 16 KB
 template <bool F32> constexpr int tc_bk() { return F32 ? 32 : 64; }
 // MMA N (history rows of the B operand: 16 hi + 16 lo, or hi, lo and 14 zero rows)
 template <int R> constexpr int tc_n() { return R == 16 ? 32 : 16; }
-// stage: weight tile (+ its lo part for FP32) and history tile; 20 / 18 KB BF16, 36 / 34 KB FP32
-template <int R, bool F32> constexpr int tc_stage_bytes() { return TC_A_BYTES * (F32 ? 2 : 1) + tc_n<R>() * 128; }
-template <bool F32> constexpr int tc_stages() { return F32 ? 3 : 4; }  // 2 CTAs per SM either way
+// stage: weight tile and history tile, 20 / 18 KB (FP32 banks keep the weights' lo parts in tensor memory)
+template <int R, bool F32> constexpr int tc_stage_bytes() { return TC_A_BYTES + tc_n<R>() * 128; }
+template <bool F32> constexpr int tc_stages() { return 4; }  // 2 CTAs per SM
 // producer, MMA, 4 epilogue warps (+ 4 warps that split FP32 weight tiles)
 template <bool F32> constexpr int tc_threads() { return F32 ? 320 : 192; }
 template <int R, bool F32> constexpr int tc_smem() { return tc_stages<F32>() * tc_stage_bytes<R, F32>() + 1024; }
 // accumulators per unit: FP32 banks spread the K tiles round-robin over 4 accumulators (shorter
-// accumulation chains inside the tensor core), summed in the epilogue; two units in flight
+// accumulation chains inside the tensor core), summed in the epilogue.  BF16 banks keep two units in
+// flight; FP32 banks one, and 4 x 32 columns behind the accumulators hold the stages' w_lo tiles.
 template <bool F32> constexpr int tc_ngroups() { return F32 ? 4 : 1; }
-template <bool F32> constexpr int tc_tmem_cols() { return 2 * tc_ngroups<F32>() * 32; }  // 256 / 64
+template <bool F32> constexpr int tc_nbuf() { return F32 ? 1 : 2; }
+template <bool F32> constexpr int tc_acc_cols() { return tc_nbuf<F32>() * tc_ngroups<F32>() * 32; }
+template <bool F32> constexpr int tc_tmem_cols() { return tc_acc_cols<F32>() + (F32 ? tc_stages<F32>() * 32 : 0); }  // 256 / 64
+static_assert(tc_tmem_cols<true>() == 256 && tc_tmem_cols<false>() == 64, "tensor memory columns (power of two)");
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -143,6 +150,23 @@ __device__ __forceinline__ void mma_tc(uint32_t d_tmem, uint64_t a, uint64_t b, 
                 d_tmem),
             "l"(a), "l"(b), "r"(tc_idesc<N, false>()), "r"(accumulate));
 }
+// W_lo x_hi for FP32 banks: M 128 x N 16 x K 8 TF32 MMA with A in tensor memory (row i in lane i, one
+// 32-bit element per column), accumulating into d
+__device__ __forceinline__ void mma_tc_ts16(uint32_t d_tmem, uint32_t a_tmem, uint64_t b) {
+    asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, 1;" ::"r"(d_tmem), "r"(a_tmem), "l"(b),
+                 "r"(tc_idesc<16, true>()));
+}
+// 32 consecutive 32-bit columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t *v) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
+        "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]), "r"(v[16]), "r"(v[17]), "r"(v[18]),
+        "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]), "r"(v[24]), "r"(v[25]), "r"(v[26]), "r"(v[27]),
+        "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31])
+        : "memory");
+}
 // 16 consecutive FP32 columns of this thread's TMEM lane
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *v) {
     asm volatile(
@@ -168,7 +192,7 @@ __global__ void __launch_bounds__(tc_threads<F32>(), 2) hist_tc_kernel(const __g
                                                                        const __grid_constant__ CUtensorMap xmap,
                                                                        TcArgs a) {
     constexpr int STAGES = tc_stages<F32>(), BK = tc_bk<F32>(), SB = tc_stage_bytes<R, F32>();
-    constexpr int B_OFF = TC_A_BYTES * (F32 ? 2 : 1);  // history tile offset in a stage (after A and A_lo)
+    constexpr int B_OFF = TC_A_BYTES;  // history tile offset in a stage
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full[TC_MAX_STAGES], empty[TC_MAX_STAGES], ready[TC_MAX_STAGES], acc_full[2],
         acc_empty[2], drain;
@@ -239,8 +263,8 @@ __global__ void __launch_bounds__(tc_threads<F32>(), 2) hist_tc_kernel(const __g
             bool ok = true;
             int ul = 0;
             for (int seg = seg0; seg < a.nseg && ok; seg += a.k, ul++) {
-                const int buf = ul & 1;
-                const uint32_t aphase = (ul >> 1) & 1;
+                const int buf = ul % tc_nbuf<F32>();
+                const uint32_t aphase = (ul / tc_nbuf<F32>()) & 1;
                 ok = mbar_wait(smem_u32(&acc_empty[buf]), aphase ^ 1u, ab, a.err, 2);
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
@@ -258,8 +282,10 @@ __global__ void __launch_bounds__(tc_threads<F32>(), 2) hist_tc_kernel(const __g
                         const uint32_t d = tmem + (buf * NG + kt % NG) * 32;
                         mma_tc<tc_n<R>(), F32>(d, smem_desc(sA + k * 32), smem_desc(sA + B_OFF + k * 32),
                                                (kt >= NG) || (k > 0));
-                        // FP32: W_lo x (x_hi rows; for R = 1 the whole hi/lo tile)
-                        if (F32) mma_tc<16, F32>(d, smem_desc(sA + TC_A_BYTES + k * 32), smem_desc(sA + B_OFF + k * 32), 1u);
+                        // FP32: W_lo (tensor memory, 8 columns per K step) x (x_hi rows; for R = 1 the
+                        // whole hi/lo tile)
+                        if (F32)
+                            mma_tc_ts16(d, tmem + tc_acc_cols<F32>() + stage * 32 + k * 8, smem_desc(sA + B_OFF + k * 32));
                     }
                     mma_commit(smem_u32(&empty[stage]));  // frees the stage when these MMAs finish
                     if (++stage == STAGES) stage = 0, phase ^= 1u;
@@ -271,9 +297,12 @@ __global__ void __launch_bounds__(tc_threads<F32>(), 2) hist_tc_kernel(const __g
             if (!mbar_drain(smem_u32(&drain), 0)) atomicExch(a.err, 5);
         }
     } else if (F32 && warp >= 6) {
-        // ---- FP32 weights: split each tile into w_hi (top 19 bits, exact in TF32) and w_lo = w - w_hi,
-        // in place and into the stage's second weight tile (elementwise, so the swizzle is irrelevant)
-        const int tt = threadIdx.x - 192;
+        // ---- FP32 weights: w_lo = w - w_hi (w_hi = the top 19 bits, the part of w the TF32 MMA reads)
+        // of one weight row per thread, into the stage's tensor-memory tile.  Row r of the 128-byte
+        // swizzled TMA tile holds its 16-byte chunk j at chunk position j ^ (r & 7).
+        const int q = warp & 3;  // TMEM lane quadrant this warp may access
+        const int r = q * 32 + lane;
+        const uint32_t lo_cols = tmem + ((uint32_t)(q * 32) << 16) + tc_acc_cols<F32>();
         int stage = 0;
         uint32_t phase = 0;
         bool ok = true;
@@ -281,21 +310,23 @@ __global__ void __launch_bounds__(tc_threads<F32>(), 2) hist_tc_kernel(const __g
             for (int kt = 0; kt < KT && ok; kt++) {
                 ok = mbar_wait(smem_u32(&full[stage]), phase, ab, a.err, 6);
                 if (!ok) break;
-                float4 *hi = reinterpret_cast<float4 *>(smem_raw + (ring - smem_u32(smem_raw)) + stage * SB);
-                float4 *lo = hi + TC_A_BYTES / 16;
+                const float4 *w =
+                    reinterpret_cast<const float4 *>(smem_raw + (ring - smem_u32(smem_raw)) + stage * SB + r * 128);
+                uint32_t l[32];
 #pragma unroll
-                for (int e = tt; e < TC_A_BYTES / 16; e += 128) {
-                    const float4 v = hi[e];
-                    float4 h, l;
-                    h.x = __uint_as_float(__float_as_uint(v.x) & 0xffffe000u), l.x = v.x - h.x;
-                    h.y = __uint_as_float(__float_as_uint(v.y) & 0xffffe000u), l.y = v.y - h.y;
-                    h.z = __uint_as_float(__float_as_uint(v.z) & 0xffffe000u), l.z = v.z - h.z;
-                    h.w = __uint_as_float(__float_as_uint(v.w) & 0xffffe000u), l.w = v.w - h.w;
-                    hi[e] = h;
-                    lo[e] = l;
+                for (int j = 0; j < 8; j++) {
+                    const float4 v = w[j ^ (r & 7)];
+                    l[4 * j + 0] = __float_as_uint(v.x - __uint_as_float(__float_as_uint(v.x) & 0xffffe000u));
+                    l[4 * j + 1] = __float_as_uint(v.y - __uint_as_float(__float_as_uint(v.y) & 0xffffe000u));
+                    l[4 * j + 2] = __float_as_uint(v.z - __uint_as_float(__float_as_uint(v.z) & 0xffffe000u));
+                    l[4 * j + 3] = __float_as_uint(v.w - __uint_as_float(__float_as_uint(v.w) & 0xffffe000u));
                 }
-                // make the generic-proxy writes visible to the tensor core (async proxy), then signal
+                tmem_st32(lo_cols + stage * 32, l);
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                // order the shared-memory reads before the stage is refilled, and the tensor-memory
+                // writes before the MMA thread's reads, then signal
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;");
                 mbar_arrive(smem_u32(&ready[stage]));
                 if (++stage == STAGES) stage = 0, phase ^= 1u;
             }
@@ -308,8 +339,8 @@ __global__ void __launch_bounds__(tc_threads<F32>(), 2) hist_tc_kernel(const __g
         for (int j = 0; j < R; j++) acc[j] = 0.f;
         int ul = 0;
         for (int seg = seg0; seg < a.nseg; seg += a.k, ul++) {
-            const int buf = ul & 1;
-            const uint32_t aphase = (ul >> 1) & 1;
+            const int buf = ul % tc_nbuf<F32>();
+            const uint32_t aphase = (ul / tc_nbuf<F32>()) & 1;
             if (!mbar_wait(smem_u32(&acc_full[buf]), aphase, ab, a.err, 4)) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
             constexpr int NG = tc_ngroups<F32>();

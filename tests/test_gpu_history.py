@@ -109,6 +109,30 @@ def test_history_fp32_tensor_cores(gpu_ctx, oracle, n, m, K, nsteps, R):
     assert np.array_equal(tc.view(np.uint8), again.view(np.uint8))  # bitwise reproducible
 
 
+@pytest.mark.parametrize("R", [1, 16])
+def test_history_fp32_tensor_cores_truncated_operands(gpu_ctx, R):
+    """The FP32 tensor-core path takes w_hi as the top 19 bits the TF32 MMA reads.  Weights in [1, 2)
+    whose low 13 bits are at least half a TF32 unit would be off by about 2^-11 if the tensor core
+    rounded its operands.  With x = 1 (x_lo = 0) the result is w_hi + TF32(w_lo), which misses w only by
+    the bits of w_lo below TF32's 11: less than 2^-21 relative."""
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    n = 200
+    rng = np.random.default_rng(11)
+    bits = rng.integers(0x3F800000, 0x40000000, n).astype(np.uint32)
+    bits = (bits & np.uint32(0xFFFFE000)) | np.uint32(0x1000) | (rng.integers(0, 0x1000, n).astype(np.uint32))
+    w = bits.view(np.float32).astype(np.float64) * np.where(rng.random(n) < 0.5, -1.0, 1.0)
+    bank = api.HistoryBank(gpu_ctx, n, n, 1, R, L.F32)
+    bank.set_engine(L.HISTORY_ENGINE_TENSOR_CORES)
+    bank.set_weights(1, np.diag(w), np.zeros((n, n)))
+    bank.push(np.ones((n, R)) if R > 1 else np.ones(n), np.zeros((n, R)) if R > 1 else np.zeros(n))
+    got = bank.convolve()
+    want = np.repeat(w[:, None], R, axis=1) if R > 1 else w
+    err = np.max(np.abs(got - want) / np.abs(want))
+    assert err < 2.0**-21, err
+
+
 def test_history_engine_selection(gpu_ctx):
     from surfaceonlydeformables_gb300 import _lib as L
     from surfaceonlydeformables_gb300 import api
