@@ -10,12 +10,14 @@ One step = every Laplace-domain matrix (G, H, B_trans, B_angular at every freque
 object.  Metric: complex matrix entries per second, counted as sum over objects of
 (L/2+1) * (2 (3V)^2 + 12 * 3V).
 
-  value : device-resident path -- one multi-frequency launch per (object, kind), outputs complex64
-          kept in HBM; CUDA-event time summed over K steps, L2 flushed between steps.
+  value : device-resident path -- the batched persistent kernels of all objects and frequencies
+          under one CUDA graph, outputs complex64 kept in HBM; CUDA-event time over K steps, L2
+          flushed between steps.
   e2e   : the drop-in through the C ABI with host buffers -- one sod_cqbem_assemble_all call per
           object, the replacement of the frequency loops of compute_{G,H,B_trans,B_angular}_matrices,
           into pinned host arrays of every frequency in the reference layout (complex128), timed end
-          to end (row chunks copied to the host while later rows compute).
+          to end (row chunks copied to the host while later rows compute).  The CPU-GPU link bounds
+          it: ~193 GB/s device to host on GB300, by copy engine or by mapped stores alike.
   --impl reference : the reference's CPU algorithm (the oracle's reference-mixed restatement,
           OpenMP on all host cores) on a bounded sample of the same workload.
 """
