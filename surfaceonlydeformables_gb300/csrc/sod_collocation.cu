@@ -678,7 +678,7 @@ __global__ void __launch_bounds__(256) batch_reduce_kernel(const __grid_constant
 
 // -------------------------------------------------------------------------------------------
 // host side
-static bool g_const_ready[64] = {};
+static std::atomic<bool> g_const_ready[64];  // per device; the set-up is idempotent
 
 static int ensure_gl_constants(int device) {
     if (device >= 0 && device < 64 && g_const_ready[device]) return SOD_OK;
@@ -714,7 +714,7 @@ size_t scatter_smem_bytes(int kind, int bm, int nV, int threads) {
 }
 
 // Raise every scatter variant's dynamic shared-memory limit to the device maximum (once per device).
-static bool g_scatter_ready[64] = {};
+static std::atomic<bool> g_scatter_ready[64];  // per device; the set-up is idempotent
 static int prepare_scatter(sod_context *ctx) {
     if (ctx->device >= 0 && ctx->device < 64 && g_scatter_ready[ctx->device]) return SOD_OK;
     const int bms[4] = {0, KM_BT, KM_BA, KM_BT | KM_BA};

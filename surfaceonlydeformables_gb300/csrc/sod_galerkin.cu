@@ -1007,7 +1007,7 @@ int launch_galerkin(sod_context *ctx, const CollLaunch &L) {
             }
             // singular pairs and their combination into slot blocks
             if (sing && g->nent > 0) {
-                static bool attr_done[64] = {};  // per device: the G + B variants need more than 48 KB
+                static std::atomic<bool> attr_done[64];  // per device: the G + B variants need more than 48 KB
                 if (ctx->device < 0 || ctx->device >= 64 || !attr_done[ctx->device]) {
                     const void *fns[3] = {(const void *)gal_sing_kernel<SOD_G, BT | BA>,
                                           (const void *)gal_sing_kernel<SOD_G, BT>, (const void *)gal_sing_kernel<SOD_G, BA>};
