@@ -367,9 +367,16 @@ int sod_context_create(int device, sod_context **out) {
         return SOD_ERR_CUDA;
     }
     ctx->stream = ctx->own_stream;
+    if (ctx->dev_err.ensure(sizeof(int)) != SOD_OK || cudaMemset(ctx->dev_err.p, 0, sizeof(int)) != cudaSuccess) {
+        cudaStreamDestroy(ctx->own_stream);
+        delete ctx;
+        set_error("could not allocate the context's device error word");
+        return SOD_ERR_CUDA;
+    }
     *out = ctx;
     return SOD_OK;
 }
+
 
 int sod_context_destroy(sod_context *ctx) {
     if (!ctx) return SOD_OK;
@@ -397,7 +404,7 @@ int sod_context_synchronize(sod_context *ctx) {
     SOD_TRY(check_context(ctx));
     SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
     SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
-    return SOD_OK;
+    return take_device_error(ctx);
 }
 
 int sod_context_set_tuning(sod_context *ctx, int coll_threads, int galerkin_threads) {
@@ -595,6 +602,7 @@ static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int 
                 SOD_CHECK_CUDA(cudaMemcpyAsync(outs[kd2], L.out[kd2], kind_elems(kd2, mesh->nV) * nfreq * esz,
                                                cudaMemcpyDeviceToHost, ctx->stream));
         SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+        SOD_TRY(take_device_error(ctx));
     }
     return SOD_OK;
 }

@@ -52,6 +52,7 @@ struct CollArgs {
     long long S_fstride[4];
     const int *nbr_off;    // G/H: per vertex slot ranges
     const int *nbr_vert;
+    int *err;              // device error word of the bounded colour-phase waits (null: not recorded)
 };
 
 __device__ __forceinline__ bool is_singular(const CollArgs &a, int i, int ci, int f, const FaceRec &fr) {
@@ -97,13 +98,61 @@ __device__ __forceinline__ void store_b(const CollArgs &a, const cd *bsum, int i
 }
 
 // -------------------------------------------------------------------------------------------
+// Colour phases of the scatter: split arrive / wait on one mbarrier per CTA.  A warp arrives (one
+// lane, after __syncwarp) once its adds of a colour are done; a thread waits for the previous
+// colour's phase only just before its own row-accumulator adds, so the quadrature of its next face
+// overlaps the stragglers of the previous colour.  Phases run on across a CTA's work items: the
+// caller's `phase` counts the completed ones.  Every wait is bounded (about a second of clock); on
+// expiry the CTA stops waiting (its results are then wrong) and the error word tells the host,
+// which reports SOD_ERR_TIMEOUT from its next synchronising call.
+constexpr long long COLOUR_WAIT_CYCLES = 2000000000LL;
+struct ColourBar {
+    unsigned long long bar;
+    int abort;
+};
+__device__ __forceinline__ unsigned colour_bar_addr(ColourBar *cb) {
+    return (unsigned)__cvta_generic_to_shared(&cb->bar);
+}
+// thread 0 initialises; the callers' first CTA barrier orders it before any use
+__device__ __forceinline__ void colour_bar_init(ColourBar *cb) {
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(colour_bar_addr(cb)), "r"((blockDim.x + 31) >> 5)
+                     : "memory");
+        cb->abort = 0;
+    }
+}
+__device__ __forceinline__ void colour_arrive(ColourBar *cb) {
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(colour_bar_addr(cb)) : "memory");
+}
+__device__ __forceinline__ void colour_wait(ColourBar *cb, unsigned parity, int *err) {
+    volatile int *ab = &cb->abort;
+    if (*ab) return;
+    const long long t0 = clock64();
+    for (;;) {
+        unsigned ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(colour_bar_addr(cb)), "r"(parity)
+            : "memory");
+        if (ok || *ab) return;
+        if (clock64() - t0 > COLOUR_WAIT_CYCLES) {
+            *ab = 1;
+            if (err) atomicExch(err, 1);
+            return;
+        }
+    }
+}
+
+// -------------------------------------------------------------------------------------------
 // G / H regular scatter kernel.  With BM != 0 (G only) the same pass also integrates B_trans /
 // B_angular: the radial terms are shared, each thread adds its faces' B tensors into its own column
 // of a shared [NC_B][blockDim] accumulator, and the CTA sums the columns in FP64 in fixed order.
 // Dynamic shared memory: NC * nV float2 (row accumulator) + NC_B * blockDim float2.
 template <int KIND, int BM>
 __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable &pt, const KConst<float> k, int i,
-                                             int fq, float2 *acc) {
+                                             int fq, float2 *acc, ColourBar *cb, unsigned &phase) {
     constexpr int NC = KIND == SOD_G ? 6 : 9;  // acc: [NC][nV]
     using BMo = BMom<KIND == SOD_G ? BM : 0>;
     constexpr int NCB = BMo::NC;
@@ -118,6 +167,7 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
     if (a.do_regular) {
         for (int c = 0; c < a.ncolors; c++) {
             const int fend = a.color_off[c + 1];
+            bool ready = c == 0;  // the previous colour's adds are complete
             for (int f = a.color_off[c] + threadIdx.x; f < fend; f += blockDim.x) {
                 const FaceRec fr = load_face(a.faces, f);
                 if (is_singular(a, i, ci, f, fr)) continue;
@@ -171,6 +221,18 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
                         for (int cc = 0; cc < NC; cc++) cfma(part[kk][cc], u[cc], wl[kk]);
                     if (NCB) bm.add(t, k, r, rh, nn, P.w);
                 }
+                if (NCB) {  // this thread's own column: no other thread touches it
+                    float2 *col = accB + threadIdx.x;
+                    bm.emit(nn, fr.area, [&](int cc, cf v) {
+                        float2 &s = col[cc * blockDim.x];
+                        s.x += v.x;
+                        s.y += v.y;
+                    });
+                }
+                if (!ready) {
+                    colour_wait(cb, (phase + c - 1) & 1u, a.err);
+                    ready = true;
+                }
                 const int jj[3] = {fr.j0, fr.j1, fr.j2};
 #pragma unroll
                 for (int kk = 0; kk < 3; kk++)
@@ -180,17 +242,14 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
                         s.x += part[kk][cc].x;
                         s.y += part[kk][cc].y;
                     }
-                if (NCB) {
-                    float2 *col = accB + threadIdx.x;
-                    bm.emit(nn, fr.area, [&](int cc, cf v) {
-                        float2 &s = col[cc * blockDim.x];
-                        s.x += v.x;
-                        s.y += v.y;
-                    });
-                }
             }
-            __syncthreads();
+            if (c + 1 < a.ncolors) {
+                if (!ready) colour_wait(cb, (phase + c - 1) & 1u, a.err);
+                colour_arrive(cb);
+            }
         }
+        if (a.ncolors > 0) phase += (unsigned)(a.ncolors - 1);
+        __syncthreads();
     }
     // epilogue: row block 3 x 3nV
     const long long ld = 3LL * nV;
@@ -253,25 +312,31 @@ template <int KIND, int BM>
 __global__ void __launch_bounds__(scatter_max_threads<KIND, BM>(), 1) coll_scatter_kernel(CollArgs a, PointTable pt,
                                                                const __grid_constant__ FreqTable ft) {
     extern __shared__ float2 acc[];
-    scatter_body<KIND, BM>(a, pt, ft.kf[blockIdx.y], a.i0 + blockIdx.x, blockIdx.y, acc);
+    __shared__ ColourBar cb;
+    colour_bar_init(&cb);
+    unsigned phase = 0;
+    scatter_body<KIND, BM>(a, pt, ft.kf[blockIdx.y], a.i0 + blockIdx.x, blockIdx.y, acc, &cb, phase);
 }
 
 // Row accumulator in global memory, for meshes whose row block does not fit in shared memory (for
 // example H of a 3485-vertex mesh: 9 x 3485 complex FP32 = 251 KB).  A persistent grid walks the
 // (vertex, frequency) items in order and each CTA reuses its own slice of the scratch, which stays
 // in L2 (grid x slice is a few tens of MB).  The body is the same: colour-ordered adds separated by
-// CTA barriers (which also order the CTA's global-memory accesses), so the sums and their order are
-// those of the shared-memory variant.
+// the colour phases (mbarrier release / acquire at CTA scope, which also orders the CTA's
+// global-memory accesses), so the sums and their order are those of the shared-memory variant.
 template <int KIND, int BM>
 __global__ void __launch_bounds__(SCATTER_GLOBAL_THREADS) coll_scatter_global_kernel(CollArgs a, PointTable pt,
                                                                                    const __grid_constant__ FreqTable ft,
                                                                                    float2 *scratch, long long per_cta,
                                                                                    int nvert) {
     float2 *acc = scratch + (size_t)blockIdx.x * per_cta;
+    __shared__ ColourBar cb;
+    colour_bar_init(&cb);
+    unsigned phase = 0;
     const int items = nvert * ft.n;
     for (int it = blockIdx.x; it < items; it += gridDim.x) {
         const int fq = it / nvert, i = a.i0 + it % nvert;
-        scatter_body<KIND, BM>(a, pt, ft.kf[fq], i, fq, acc);
+        scatter_body<KIND, BM>(a, pt, ft.kf[fq], i, fq, acc, &cb, phase);
         __syncthreads();  // the next item clears the accumulator
     }
 }
@@ -638,11 +703,14 @@ __global__ void __launch_bounds__(scatter_max_threads<KIND, BM>(), 1) batch_scat
                                                                int *counter, const KConst<float> *__restrict__ kcf) {
     extern __shared__ float2 acc[];
     __shared__ int s_item;
+    __shared__ ColourBar cb;
+    colour_bar_init(&cb);
+    unsigned phase = 0;
     for (;;) {
         const int it = next_item(counter, &s_item);
         if (it >= nitems) break;
         const int4 w = items[it];
-        scatter_body<KIND, BM>(p.a[w.x], p.pt, kcf[p.kc_off[w.x] + w.z], w.y, w.z, acc);
+        scatter_body<KIND, BM>(p.a[w.x], p.pt, kcf[p.kc_off[w.x] + w.z], w.y, w.z, acc, &cb, phase);
     }
 }
 
@@ -655,11 +723,14 @@ __global__ void __launch_bounds__(256) batch_scatter_global_kernel(const __grid_
                                                                    float2 *scratch, long long per_cta) {
     float2 *acc = scratch + (size_t)blockIdx.x * per_cta;
     __shared__ int s_item;
+    __shared__ ColourBar cb;
+    colour_bar_init(&cb);
+    unsigned phase = 0;
     for (;;) {
         const int it = next_item(counter, &s_item);
         if (it >= nitems) break;
         const int4 w = items[it];
-        scatter_body<KIND, BM>(p.a[w.x], p.pt, kcf[p.kc_off[w.x] + w.z], w.y, w.z, acc);
+        scatter_body<KIND, BM>(p.a[w.x], p.pt, kcf[p.kc_off[w.x] + w.z], w.y, w.z, acc, &cb, phase);
     }
 }
 
@@ -678,6 +749,19 @@ __global__ void __launch_bounds__(256) batch_reduce_kernel(const __grid_constant
 
 // -------------------------------------------------------------------------------------------
 // host side
+
+}  // namespace sod
+
+int take_device_error(sod_context *ctx) {
+    int word = 0;
+    SOD_CHECK_CUDA(cudaMemcpy(&word, ctx->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (word == 0) return SOD_OK;
+    SOD_CHECK_CUDA(cudaMemset(ctx->dev_err.p, 0, sizeof(int)));
+    sod::set_error("a scatter kernel's bounded colour-phase wait expired; its results are not valid");
+    return SOD_ERR_TIMEOUT;
+}
+
+namespace sod {
 static std::atomic<bool> g_const_ready[64];  // per device; the set-up is idempotent
 
 static int ensure_gl_constants(int device) {
@@ -891,6 +975,7 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
         }
         if (sing) SOD_TRY(launch_singular(ctx, m, mask, L.sorder, L.ssub, ft.kd, nf, sa.S, sa.S_fstride, L.stream));
         CollArgs a{};
+        a.err = ctx->dev_err.as<int>();
         a.nV = m->nV;
         a.nF = m->nF;
         a.Vf = m->dVf.as<float>();
@@ -1093,6 +1178,7 @@ int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, d
         SOD_CHECK_CUDA(cudaGetLastError());
         ctx->count();
         CollArgs a{};
+        a.err = ctx->dev_err.as<int>();
         a.nV = m->nV;
         a.nF = m->nF;
         a.Vf = m->dVf.as<float>();
@@ -1191,6 +1277,7 @@ int batch_regular_add(BatchRegular *r, const sod_mesh *m, int out_dtype, void *c
     const long long sfs[4] = {nslots * 9, nslots * 9, (long long)m->nV * 9, (long long)m->nV * 27};
     const long long per[4] = {9LL * m->nV * m->nV, 9LL * m->nV * m->nV, 9LL * m->nV, 27LL * m->nV};
     CollArgs a{};
+    a.err = m->ctx ? m->ctx->dev_err.as<int>() : nullptr;
     a.nV = m->nV;
     a.nF = m->nF;
     a.Vf = m->dVf.as<float>();

@@ -117,8 +117,13 @@ struct sod_context {
     std::vector<cudaEvent_t> chunk_events;  // row-chunk completion markers (reused)
     sod::DevBuf gal_bsum;  // Galerkin: B_trans / B_angular sums of every test point
     sod::DevBuf gacc;      // collocation row accumulators in global memory (meshes too large for shared memory)
+    sod::DevBuf dev_err;   // error word of the scatter kernels' bounded colour-phase waits (0 = none)
     void count(int n = 1) { launches += n; }
 };
+
+// After the context's stream is synchronised: SOD_ERR_TIMEOUT (and the word cleared) if a scatter
+// kernel's bounded wait expired since the last check.
+int take_device_error(sod_context *ctx);
 
 struct sod_mesh {
     sod_context *ctx = nullptr;

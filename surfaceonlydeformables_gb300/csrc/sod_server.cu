@@ -180,6 +180,7 @@ void slot_main(sod_server *s, sod_server::Slot *sl) {
                                       r->order, r->subdiv, std::min(r->order, 5), r->subdiv, cm, tmp, tmp + L * nn,
                                       nullptr, nullptr, nullptr, SOD_F32);
         if (rc == SOD_OK && cudaStreamSynchronize(sl->ctx->stream) != cudaSuccess) rc = SOD_ERR_CUDA;
+        if (rc == SOD_OK) rc = take_device_error(sl->ctx);
         if (rc == SOD_OK) rc = sod_history_create(s->step_ctx, n, n, r->N, 1, SOD_F32, &d.bank);
         for (int k = 1; rc == SOD_OK && k <= r->N; k++)
             rc = sod_history_set_weights(d.bank, k, tmp + k * nn, tmp + (L + k) * nn, SOD_F32);
