@@ -36,6 +36,7 @@ _SIGS = {
     "sod_context_set_stream": ([_P, _P], _c.c_int),
     "sod_context_synchronize": ([_P], _c.c_int),
     "sod_context_set_tuning": ([_P, _c.c_int, _c.c_int], _c.c_int),
+    "sod_context_set_wait_test": ([_P, _c.c_int], _c.c_int),
     "sod_context_launch_count": ([_P], _c.c_int64),
     "sod_mesh_create": ([_P, _P, _c.c_int, _P, _c.c_int, _P, _P, _P], _c.c_int),
     "sod_mesh_destroy": ([_P], _c.c_int),

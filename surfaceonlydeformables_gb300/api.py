@@ -37,6 +37,10 @@ class Context:
     def set_tuning(self, coll_threads: int = 0, galerkin_threads: int = 0) -> None:
         L.check(L.load().sod_context_set_tuning(self._h, coll_threads, galerkin_threads))
 
+    def set_wait_test(self, stall: bool) -> None:
+        """Test hook: make the collocation scatter kernels' bounded colour-phase waits run out."""
+        L.check(L.load().sod_context_set_wait_test(self._h, 1 if stall else 0))
+
     @property
     def launches(self) -> int:
         return int(L.load().sod_context_launch_count(self._h))

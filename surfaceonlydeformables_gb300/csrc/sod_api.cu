@@ -407,6 +407,12 @@ int sod_context_synchronize(sod_context *ctx) {
     return take_device_error(ctx);
 }
 
+int sod_context_set_wait_test(sod_context *ctx, int stall) {
+    SOD_TRY(check_context(ctx));
+    ctx->wait_test = stall != 0;
+    return SOD_OK;
+}
+
 int sod_context_set_tuning(sod_context *ctx, int coll_threads, int galerkin_threads) {
     SOD_TRY(check_context(ctx));
     SOD_REQUIRE(coll_threads == 0 || (coll_threads >= 32 && coll_threads <= 512 && coll_threads % 32 == 0),

@@ -53,6 +53,7 @@ struct CollArgs {
     const int *nbr_off;    // G/H: per vertex slot ranges
     const int *nbr_vert;
     int *err;              // device error word of the bounded colour-phase waits (null: not recorded)
+    int bar_extra;         // test hook: extra arrivals the colour-phase barrier expects (0 normally)
 };
 
 __device__ __forceinline__ bool is_singular(const CollArgs &a, int i, int ci, int f, const FaceRec &fr) {
@@ -113,10 +114,12 @@ struct ColourBar {
 __device__ __forceinline__ unsigned colour_bar_addr(ColourBar *cb) {
     return (unsigned)__cvta_generic_to_shared(&cb->bar);
 }
-// thread 0 initialises; the callers' first CTA barrier orders it before any use
-__device__ __forceinline__ void colour_bar_init(ColourBar *cb) {
+// thread 0 initialises (one arrival per warp, plus `extra` for the timeout test); the callers' first
+// CTA barrier orders it before any use
+__device__ __forceinline__ void colour_bar_init(ColourBar *cb, int extra = 0) {
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(colour_bar_addr(cb)), "r"((blockDim.x + 31) >> 5)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(colour_bar_addr(cb)),
+                     "r"(((blockDim.x + 31) >> 5) + (unsigned)extra)
                      : "memory");
         cb->abort = 0;
     }
@@ -313,7 +316,7 @@ __global__ void __launch_bounds__(scatter_max_threads<KIND, BM>(), 1) coll_scatt
                                                                const __grid_constant__ FreqTable ft) {
     extern __shared__ float2 acc[];
     __shared__ ColourBar cb;
-    colour_bar_init(&cb);
+    colour_bar_init(&cb, a.bar_extra);
     unsigned phase = 0;
     scatter_body<KIND, BM>(a, pt, ft.kf[blockIdx.y], a.i0 + blockIdx.x, blockIdx.y, acc, &cb, phase);
 }
@@ -976,6 +979,7 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
         if (sing) SOD_TRY(launch_singular(ctx, m, mask, L.sorder, L.ssub, ft.kd, nf, sa.S, sa.S_fstride, L.stream));
         CollArgs a{};
         a.err = ctx->dev_err.as<int>();
+        a.bar_extra = ctx->wait_test ? 1 : 0;
         a.nV = m->nV;
         a.nF = m->nF;
         a.Vf = m->dVf.as<float>();
@@ -1179,6 +1183,7 @@ int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, d
         ctx->count();
         CollArgs a{};
         a.err = ctx->dev_err.as<int>();
+        a.bar_extra = ctx->wait_test ? 1 : 0;
         a.nV = m->nV;
         a.nF = m->nF;
         a.Vf = m->dVf.as<float>();

@@ -118,6 +118,7 @@ struct sod_context {
     sod::DevBuf gal_bsum;  // Galerkin: B_trans / B_angular sums of every test point
     sod::DevBuf gacc;      // collocation row accumulators in global memory (meshes too large for shared memory)
     sod::DevBuf dev_err;   // error word of the scatter kernels' bounded colour-phase waits (0 = none)
+    bool wait_test = false;  // test hook: colour-phase barriers expect one arrival more than comes
     void count(int n = 1) { launches += n; }
 };
 

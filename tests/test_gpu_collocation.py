@@ -281,3 +281,27 @@ def test_large_host_output_pipelined(gpu_ctx, freqs):
     torch.cuda.synchronize()
     for k in KINDS:
         assert np.array_equal(host[k].view(np.uint8), devs[k].cpu().numpy().view(np.uint8)), k
+
+
+def test_colour_phase_wait_timeout_is_reported(gpu_ctx, sodlib):
+    """The scatter kernels' colour-phase waits are bounded.  With the context's test hook the barrier
+    expects one arrival more than ever comes, so every wait runs out (about a second): the call returns
+    SOD_ERR_TIMEOUT instead of hanging, and the context stays usable -- the next call reproduces the
+    result bit for bit."""
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    dm = api.Mesh(gpu_ctx, make_icosphere_mesh(1, 0.1))
+    mat = Material(1e5, 0.3, 1000.0)
+    s = complex(sodlib.cq_frequencies(2, 0.01, 4)[0][1])
+    want = api.assemble(gpu_ctx, dm, "G", mat, s)
+    gpu_ctx.set_wait_test(True)
+    try:
+        with pytest.raises(L.SodError) as e:
+            api.assemble(gpu_ctx, dm, "G", mat, s)
+        assert e.value.code == L.SOD_ERR_TIMEOUT
+    finally:
+        gpu_ctx.set_wait_test(False)
+    got = api.assemble(gpu_ctx, dm, "G", mat, s)
+    assert np.array_equal(got, want)
+    gpu_ctx.synchronize()  # no error left behind
