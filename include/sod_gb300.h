@@ -85,10 +85,11 @@ int sod_context_set_stream(sod_context *ctx, void *stream);
 /* Also reports SOD_ERR_TIMEOUT if a bounded device-side wait of a scatter kernel expired since the
  * last synchronising call (the results of that work are then not valid; the context stays usable). */
 int sod_context_synchronize(sod_context *ctx);
-/* Test hook for the timeout path: with stall != 0 the collocation scatter kernels this context
- * launches initialise their colour-phase barrier for one more arrival than ever comes, so every
- * bounded wait runs out (about a second per CTA wave) and the next synchronising call returns
- * SOD_ERR_TIMEOUT.  0 (the default) restores normal operation. */
+/* Test hook for the timeout path: with stall != 0 the collocation scatter kernels of the per-call
+ * assembly functions (sod_cqbem_assemble*) launched by this context initialise their colour-phase
+ * barrier for one more arrival than ever comes, so every bounded wait runs out (about a second per
+ * CTA wave) and the next synchronising call returns SOD_ERR_TIMEOUT.  Batched launches are not
+ * affected.  0 (the default) restores normal operation. */
 int sod_context_set_wait_test(sod_context *ctx, int stall);
 /* Threads per CTA of the collocation scatter kernels (0 = automatic); for the autotuner. */
 int sod_context_set_tuning(sod_context *ctx, int coll_threads, int galerkin_threads);

@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(SCATTER_GLOBAL_THREADS) coll_scatter_global_ke
                                                                                    int nvert) {
     float2 *acc = scratch + (size_t)blockIdx.x * per_cta;
     __shared__ ColourBar cb;
-    colour_bar_init(&cb);
+    colour_bar_init(&cb, a.bar_extra);
     unsigned phase = 0;
     const int items = nvert * ft.n;
     for (int it = blockIdx.x; it < items; it += gridDim.x) {
