@@ -771,16 +771,9 @@ def run_gpu(args):
     t_max = float(t.item())
     value = world * total_entries * args.steps / t_max
 
-    # ---- the same workload through the per-object and the plain per-(kind, frequency) drop-in ----
-    t_per_object = t_plain = None
-    if not args.value_only:
-        step_per_object()
-        step_plain()
-        torch.cuda.synchronize()
-        t_per_object = timed(step_per_object, max(1, args.steps // 2))
-        t_plain = timed(step_plain, max(1, args.steps // 2))
-
     # ---- end to end: the per-object frequency-loop drop-in with pinned host buffers ----
+    # (measured before the per-object and plain legs: after them the same step measured 0.5-0.75 s
+    # instead of 0.36 s in full runs on shared boxes, for reasons not found)
     # per kind one pinned array of the largest (frequencies x rows x columns) complex128 output,
     # reused by every call as the reference's loops reuse their host matrices
     host = {}
@@ -811,6 +804,15 @@ def run_gpu(args):
         torch.cuda.synchronize()
         e2e_t = time.perf_counter() - t0
         e2e_value = world * total_entries * e2e_steps / e2e_t
+    # ---- the same workload through the per-object and the plain per-(kind, frequency) drop-in ----
+    t_per_object = t_plain = None
+    if not args.value_only:
+        step_per_object()
+        step_plain()
+        torch.cuda.synchronize()
+        t_per_object = timed(step_per_object, max(1, args.steps // 2))
+        t_plain = timed(step_plain, max(1, args.steps // 2))
+
     h2d_bytes = sum(16 * len(o["s"]) + 64 for o in objs)  # per-call frequency constants
 
     # ---- roofline of the dominant kernel of the batched step: per-launch CUDA-event times ----
