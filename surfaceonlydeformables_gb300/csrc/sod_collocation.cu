@@ -942,7 +942,7 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
                 SOD_TRY(scatter_occupancy(ctx, kd, kd == SOD_G ? bmG : 0, false, threads[kd], smem[kd], &per_sm));
                 wave = std::max(wave, ctx->num_sms * std::max(per_sm, 1));
             }
-        const int target = (m->nV + 5) / 6;  // about six chunks
+        const int target = (m->nV + 11) / 12;  // about twelve chunks: the first compute and the last copy are not overlapped
         vchunk = std::min(m->nV, std::max(wave, (target + wave - 1) / wave * wave));
         if (!ctx->copy_stream) SOD_CHECK_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
         const size_t need = (size_t)((m->nV + vchunk - 1) / vchunk) + 1;
