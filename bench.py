@@ -869,7 +869,7 @@ def run_gpu(args):
         line = {"metric": "CQBEM Laplace-domain entries/s (mixed-size 24-object set)", "value": value,
                 "unit": "entries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic",
+                "vs_baseline": None, "dtype": "fp32+double-float", "data": "synthetic",
                 "config": {"workload": "mixed-size 24-object collocation assembly (G,H,B_trans,B_angular, all "
                                        "Laplace frequencies); batched persistent kernels under one CUDA graph",
                            "objects": len(objs),

@@ -71,7 +71,7 @@ const char *sod_last_error(void);
 int sod_triangle_rule(int order, double *out, int *npts);
 /* CQ frequencies s_l = gamma(R zeta^l)/dt for l = 0..L/2, R = (1e-10)^(1/(2N)), L = N+1,
  * gamma_BDF1(z) = 1-z, gamma_BDF2(z) = 3/2 - 2z + z^2/2.  Replaces the prologue of
- * compute_G_matrices (src/elastodynamics_cqbem_G.cu:177-182,223).  s_out: (L/2+1) complex.
+ * compute_G_matrices (src/elastodynamics_cqbem_G.cu:19-24,65).  s_out: (L/2+1) complex.
  * Needs no GPU. */
 int sod_cq_frequencies(int bdf, double dt, int N, double *s_out, double *R_out, int *L_out);
 
@@ -108,13 +108,13 @@ int sod_mesh_destroy(sod_mesh *mesh);
 /* Whole-matrix replacement of the reference's per-row / per-pair kernels for one Laplace
  * frequency s = (s_re, s_im):
  *   kind G, collocation : compute_elastodynamic_G_kernel_collocation over all rows
- *                         (src/elastodynamics_cqbem_G_collocation.cu:18-142; driver G.cu:280-305)
- *   kind H, collocation : src/elastodynamics_cqbem_H_collocation.cu:18-158 (H.cu:300-327)
+ *                         (src/elastodynamics_cqbem_G_collocation.cu:18-142; driver src/elastodynamics_cqbem_G.cu:122-146)
+ *   kind H, collocation : src/elastodynamics_cqbem_H_collocation.cu:18-158 (src/elastodynamics_cqbem_H.cu:125-151)
  *   kind B_trans, coll. : src/elastodynamics_cqbem_B_trans_collocation.cu:17-124
  *   kind B_angular,coll.: src/elastodynamics_cqbem_B_angular_collocation.cu:17-143
  *   Galerkin (any kind) : non-singular pairs (..._galerkin_non_singular.cu) plus singular pairs
  *                         (src/elastodynamics_cqbem_galerkin_singular.cpp), i.e. the sum formed at
- *                         src/elastodynamics_cqbem_G.cu:225-260.
+ *                         src/elastodynamics_cqbem_G.cu:67-120.
  * Regular integrals run in FP32, singular ones in FP64.  order: triangle rule (1..5, 7);
  * subdiv: uniform subdivision (1..4); sorder/ssub: 1-D Gauss order (1..5) and subdivision of the
  * singular rules (the reference uses order/subdiv for both).
@@ -125,7 +125,7 @@ int sod_cqbem_assemble(sod_context *ctx, const sod_mesh *mesh, int kind, int met
 
 /* Same for nfreq frequencies s[2*l], s[2*l+1] in one launch; out holds nfreq consecutive matrices.
  * Replaces the frequency loop of compute_{G,H,B_trans,B_angular}_matrices
- * (src/elastodynamics_cqbem_G.cu:221-309 and its H / B_trans / B_angular twins). */
+ * (src/elastodynamics_cqbem_G.cu:63-151 and its H / B_trans / B_angular twins). */
 int sod_cqbem_assemble_frequencies(sod_context *ctx, const sod_mesh *mesh, int kind, int method, double c1,
                                    double c2, double rho, const double *s, int nfreq, int order, int subdiv,
                                    int sorder, int ssub, int parts, void *out, int out_dtype);
@@ -149,8 +149,11 @@ int sod_cqbem_assemble_all(sod_context *ctx, const sod_mesh *mesh, int method, d
  *   - `out` must be device memory; `mesh` must have been assembled once through
  *     sod_cqbem_assemble* during set-up (that builds the scatter schedule, with allocation);
  *   - one frequency's side buffer (9 complex doubles per neighbour slot for G/H, 9 or 27 per vertex
- *     for B_trans/B_angular) must fit in 4 MiB, else SOD_ERR_CAPACITY (G/H: up to about 3600
- *     vertices); frequencies are processed in chunks that fit;
+ *     for B_trans/B_angular) must fit in 4 MiB, else SOD_ERR_CAPACITY; frequencies are processed
+ *     in chunks that fit;
+ *   - the G/H row block must also fit in shared memory (48 bytes per vertex for G, 72 for H; there
+ *     is no global-memory accumulator here), else SOD_ERR_CAPACITY.  Together: G up to about 4100
+ *     vertices (the scratch), H up to about 3200 (shared memory);
  *   - the first call on a device looks up the array's device address (cudaGetSymbolAddress); make
  *     that first call before any stream capture;
  *   - all calls share the array: calls whose kernels overlap on the GPU (other streams, other host
@@ -349,7 +352,7 @@ int sod_cqbem_precompute(sod_context *ctx, const sod_mesh *mesh, int method, dou
 
 /* ---- inverse transform to CQ time weights (FP64-accurate) --------------------------------- */
 /* X_n = R^-n / L * sum_{l=0}^{L/2} c_l Re(Xhat_l zeta^-nl),  c_0 = 1, c_l = 2 otherwise except
- * c_{L/2} = 1 for even L;  n = 0..L-1 (src/elastodynamics_cqbem_G.cu:324-337).
+ * c_{L/2} = 1 for even L;  n = 0..L-1 (src/elastodynamics_cqbem_G.cu:166-179).
  * Xhat: nfreq = L/2+1 blocks of M complex (dtype SOD_C128 or SOD_C64), out: L blocks of M reals
  * (SOD_F64 or SOD_F32).  SOD_F64 output accumulates in FP64 (agrees with an FP64 CPU transform to
  * <= 1e-10 of the stacked Frobenius norm); SOD_F32 output uses double-float arithmetic on the FP32

@@ -152,7 +152,7 @@ def b_euler(B_angular_n: np.ndarray) -> np.ndarray:
 
 
 def b_angular_shift(B_ang_n: np.ndarray, B_trans_n: np.ndarray, V: np.ndarray, cm: np.ndarray) -> np.ndarray:
-    """B_ang(3v+i, j, k) += B_trans(3v+i, j) * (x_v - cm)_k  (src/elastodynamics_cqbem_B_angular.cu:326-334)."""
+    """B_ang(3v+i, j, k) += B_trans(3v+i, j) * (x_v - cm)_k  (src/elastodynamics_cqbem_B_angular.cu:167-175)."""
     d = np.repeat(V - cm[None, :], 3, axis=0)
     return B_ang_n + B_trans_n[:, :, None] * d[:, None, :]
 

@@ -976,7 +976,7 @@ int oracle_tri_rule(int order, double *out) {
     return r.n;
 }
 
-// CQ frequencies s_l = gamma(R zeta^l)/dt, l = 0..L/2 (src/elastodynamics_cqbem_G.cu:177-182, 223)
+// CQ frequencies s_l = gamma(R zeta^l)/dt, l = 0..L/2 (src/elastodynamics_cqbem_G.cu:19-24, 65)
 // bdf: 1 or 2.  Writes Lambda complex values; returns Lambda.  R and L are written to R_out, L_out.
 int oracle_cq_frequencies(int bdf, double dt, int N, double *s_out, double *R_out, int *L_out) {
     const double R = std::pow(1e-10, 1. / (2. * N));
@@ -1101,7 +1101,7 @@ int oracle_galerkin(int kind, int mode, const double *V, int nV, const int *F, i
 }
 
 // Inverse transform X_n = R^-n / L * sum_l Re(c_l Xhat_l zeta^-nl), n = 0..L-1
-// (src/elastodynamics_cqbem_G.cu:324-337).  Xhat: nfreq x M complex, out: L x M real.
+// (src/elastodynamics_cqbem_G.cu:166-179).  Xhat: nfreq x M complex, out: L x M real.
 int oracle_inverse_transform(int nfreq, int L, double R, const double *Xhat, long M, double *out) {
     if (nfreq != L / 2 + 1) return 1;
     const std::complex<double> z = std::exp(std::complex<double>(0.0, 1.0) * (2. * PI) / (double)L);

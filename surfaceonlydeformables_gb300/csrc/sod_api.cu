@@ -231,6 +231,7 @@ using namespace sod;
 // Balanced greedy colouring of faces such that faces of one colour share no vertex and no colour
 // holds more than `threads` faces (one scatter round per colour).
 int sod_mesh::coloured_for(int threads, const Coloured **out) {
+    std::lock_guard<std::recursive_mutex> lock(sched_mu);
     auto it = coloured.find(threads);
     if (it != coloured.end()) {
         *out = it->second.get();

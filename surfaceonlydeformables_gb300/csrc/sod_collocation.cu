@@ -840,6 +840,7 @@ int scatter_occupancy(sod_context *ctx, int kind, int bm, bool batch, int thread
 // The choice depends only on the mesh and the device, so results stay bitwise reproducible.
 int autotune_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int bm, int *threads) {
     const int key = kind * 16 + bm;
+    std::lock_guard<std::recursive_mutex> lock(m->sched_mu);
     auto it = m->tuned.find(key);
     if (it != m->tuned.end()) {
         *threads = it->second;
@@ -1123,6 +1124,15 @@ int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, d
     const sod_mesh::Coloured *col = nullptr;
     size_t smem = 0;
     if (kind <= SOD_H) {
+        // the row block must fit in shared memory (this entry point has no global-memory accumulator):
+        // H needs 72 bytes and G 48 bytes of shared memory per vertex
+        if (scatter_smem_bytes(kind, 0, m->nV, 32) > ctx->smem_optin) {
+            set_error("mesh too large for the allocation-free entry point: the " + std::string(kind == SOD_G ? "G" : "H") +
+                      " row block of " + std::to_string(m->nV) + " vertices exceeds the " +
+                      std::to_string(ctx->smem_optin) + " bytes of shared memory per CTA");
+            return SOD_ERR_CAPACITY;
+        }
+        std::lock_guard<std::recursive_mutex> lock(m->sched_mu);
         threads = ctx->coll_threads;
         if (threads <= 0) {  // the CTA size the autotuner chose for this kind (any fused variant)
             auto tt = m->tuned.find(kind * 16);

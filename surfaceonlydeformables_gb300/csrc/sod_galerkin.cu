@@ -833,6 +833,7 @@ static const void *gal_tp_fn(int kind, int bm, bool global = false) {
 // occupancy from the CUDA occupancy calculator), cached on the mesh.
 static int gal_tp_threads(sod_context *ctx, sod_mesh *m, int kind, int bm, const void *fn, int *threads) {
     const int key = 4096 + kind * 16 + bm;
+    std::lock_guard<std::recursive_mutex> lock(m->sched_mu);
     auto it = m->tuned.find(key);
     if (it != m->tuned.end()) {
         *threads = it->second;

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -150,6 +151,10 @@ struct sod_mesh {
     };
     std::map<int, std::unique_ptr<Coloured>> coloured;
     std::map<int, int> tuned;  // scatter CTA size chosen by the autotuner, key kind * 16 + fused B kinds
+    // guards `coloured` and `tuned`: host threads sharing a mesh (a request loop's workers, or the
+    // allocation-free entry point while another thread autotunes) may look up and insert at once;
+    // recursive because the autotuners call coloured_for while they hold it
+    mutable std::recursive_mutex sched_mu;
     // frequency-independent singular-quadrature geometry per (order, subdivision), double-float
     struct SingGeom {
         int nq2 = 0;          // points per star entry

@@ -7,7 +7,7 @@
 //   2. inverse transform to the L time weights (FP64 accumulation for FP64 outputs);
 //   3. H_0 += C, the free term (collocation: 3x3 blocks on the diagonal from solid angles,
 //      src/elastics_bem_matrix_collection.cpp:387-445; Galerkin: mass matrix A/24, A/48, :447-467);
-//   4. B_angular_n(3v+i, j, k) += B_trans_n(3v+i, j) (x_v - cm)_k (src/elastodynamics_cqbem_B_angular.cu:326-334);
+//   4. B_angular_n(3v+i, j, k) += B_trans_n(3v+i, j) (x_v - cm)_k (src/elastodynamics_cqbem_B_angular.cu:167-175);
 //   5. B_euler_n(i, j) = B_angular_n(i, (j+2)%3, (j+1)%3) - B_angular_n(i, (j+1)%3, (j+2)%3).
 // Everything after the host-side free-term geometry runs on the device; the reference writes every
 // U_l to disk and re-reads all of them for every n.

@@ -1,8 +1,8 @@
 // sod_transform.cu -- inverse transform from Laplace frequencies to CQ time weights.
 //
 // X_n = R^-n / L * sum_{l=0}^{L/2} c_l Re(Xhat_l zeta^-nl)  for every matrix entry, n = 0..L-1
-// (reference: src/elastodynamics_cqbem_G.cu:324-337, H.cu:347-371, B_trans.cu:289-304,
-// B_angular.cu:310-325).  The reference re-reads every U_l.mat from disk for each n; here each
+// (reference: src/elastodynamics_cqbem_G.cu:166-179, H.cu:172-195, B_trans.cu:148-163,
+// B_angular.cu:151-175).  The reference re-reads every U_l.mat from disk for each n; here each
 // CTA stages a tile of entries x all frequencies in shared memory once and produces all L outputs.
 //
 // Two kernels:

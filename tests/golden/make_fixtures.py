@@ -1,7 +1,7 @@
 """Builds the real-mesh fixtures of tests/golden from the reference's scene meshes.
 
-Reads data/cube_reordered.obj and data/cube_reordered_discontinuous.obj of the reference checkout
-(default /root/reference, or the path given as the first argument) and writes:
+Reads data/cube_reordered.obj and data/cube_reordered_discontinuous.obj of a reference checkout
+(its directory is the required first argument) and writes:
   cube_meshes.npz      V, F of both meshes, centred at the volume centroid as the reference's
                        PhysicsBaseMatrixCollection::init does (src/physics_base_matrix_collection.cpp:
                        41-45); vmap of the discontinuous mesh: each split vertex maps to the first
@@ -15,7 +15,7 @@ Reads data/cube_reordered.obj and data/cube_reordered_discontinuous.obj of the r
                        as complex64, enough for the 1e-5 check)
                        (data/cube_drop.json: mu 1e5, nu 0.45, rho 1000, BDF1, dt 0.005, order 5,
                        subdivision 2)
-Run from the repository root: python tests/golden/make_fixtures.py [reference_dir]
+Run from the repository root: python tests/golden/make_fixtures.py <reference_checkout_dir>
 """
 import os
 import sys
@@ -66,7 +66,9 @@ def sample_vertices(V, vmap=None):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_fixtures.py <reference_checkout_dir>")
+    ref = sys.argv[1]
     out = {}
     for tag, name in (("cont", "cube_reordered.obj"), ("disc", "cube_reordered_discontinuous.obj")):
         V, F = read_obj(os.path.join(ref, "data", name))

@@ -1,7 +1,7 @@
 """Known-answer tests that pin the CPU oracle (the reference ships no golden vectors).
 
 Quadrature exactness, closed-form convolution-quadrature weights (which exercise the R, L,
-zeta and R^-n pipeline of src/elastodynamics_cqbem_G.cu:177-182,324-337), the static limit of
+zeta and R^-n pipeline of src/elastodynamics_cqbem_G.cu:19-24,166-179), the static limit of
 the elastodynamic single layer, Galerkin symmetry and the rigid-mode null space of H.
 """
 import math
