@@ -190,6 +190,35 @@ def cpu_sample(objs, threads: int, budget_s: float = 12.0):
     return done / dt, dt, cores, sample
 
 
+def check_batched_rows(objs, outs, rows_per_object: int = 2, seed: int = 17) -> dict:
+    """Relative Frobenius error of the batched step's device outputs on sampled rows (seeded field
+    vertices of every object) at the first, middle and last frequency, against the FP64 oracle's
+    row-sampled assembly (those rows are exact: every face is integrated for the listed vertices)."""
+    from oracle import oracle as O
+
+    O.build()
+    rng = np.random.default_rng(seed)
+    num = {k: 0.0 for k in KINDS}
+    den = {k: 0.0 for k in KINDS}
+    worst = {k: 0.0 for k in KINDS}
+    for o, per in zip(objs, outs):
+        m = o["mesh"]
+        rows = np.sort(rng.choice(m.nV, size=min(rows_per_object, m.nV), replace=False)).astype(np.int32)
+        idx = np.concatenate([np.arange(3 * v, 3 * v + 3) for v in rows])
+        nf = len(o["s"])
+        for l in sorted({0, nf // 2, nf - 1}):
+            for kind in KINDS:
+                got = per[kind][l].cpu().numpy()[idx].astype(np.complex128)
+                ref = O.collocation(kind, m, o["mat"], o["s"][l], order=o["order"], subdiv=o["subdiv"], rows=rows)
+                d, r = float(np.linalg.norm(got - ref)), float(np.linalg.norm(ref))
+                num[kind] += d * d
+                den[kind] += r * r
+                worst[kind] = max(worst[kind], d / r)
+    return {"check": f"{rows_per_object} seeded rows per object, first / middle / last frequency, vs FP64 oracle rows",
+            "rel_err_stacked": {k: (num[k] / den[k]) ** 0.5 for k in KINDS}, "rel_err_worst": worst,
+            "tolerance": 1e-5}
+
+
 def measured_hbm_gbs() -> float:
     """HBM copy bandwidth measured on the GB300s (MEASURED_PEAKS.json), else the fallback."""
     try:
@@ -770,6 +799,8 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     t_max = float(t.item())
     value = world * total_entries * args.steps / t_max
+    # check of the timed step's own outputs (after the timed region): sampled rows against the FP64 oracle
+    accuracy = None if args.value_only else check_batched_rows(objs, outs)
 
     # ---- end to end: the per-object frequency-loop drop-in with pinned host buffers ----
     # (measured before the per-object and plain legs: after them the same step measured 0.5-0.75 s
@@ -878,7 +909,7 @@ def run_gpu(args):
                            "l2": "L2 flushed (256 MB write) between timed steps; outputs (~"
                                  f"{total_entries * 8 / 1e9:.0f} GB complex64) exceed L2",
                            "parallelism": f"replicas x{world}"},
-                "roofline": roofline, "cpu_baseline": cpu,
+                "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
                 "paths": paths,
                 "e2e": {"value": e2e_value, "unit": "entries/s", "h2d_bytes_per_step": h2d_bytes,
                         "d2h_bytes_per_step": d2h_bytes, "path": "sod_cqbem_assemble_all per object (the frequency-loop "

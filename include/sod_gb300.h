@@ -93,6 +93,19 @@ int sod_context_synchronize(sod_context *ctx);
 int sod_context_set_wait_test(sod_context *ctx, int stall);
 /* Threads per CTA of the collocation scatter kernels (0 = automatic); for the autotuner. */
 int sod_context_set_tuning(sod_context *ctx, int coll_threads, int galerkin_threads);
+/* Precision of the regular (non-singular) collocation quadrature.  The geometry (distances,
+ * directions, weights) is FP32 either way; FP32 evaluates the frequency-dependent terms (complex
+ * exponentials, psi, kernel coefficients) and the sums in FP32 (~3e-7 relative error per
+ * Laplace-domain matrix), COMPENSATED in double-float arithmetic on the FP32 pipes with
+ * compensated sums (~3e-8, the FP32 geometry alone).  The inverse transform multiplies the late time
+ * weights by up to R^-N = 1e5, so FP32 noise becomes ~1e-3 of the stacked time-domain weights, and
+ * compensated evaluation brings them back to ~1e-7.  AUTO (the default): FP32 for the Laplace-domain
+ * entry points (sod_cqbem_assemble*), COMPENSATED for time-domain outputs (sod_cqbem_precompute and
+ * the request loop's assemblies).  FP32 / COMPENSATED force one for both.  The Galerkin regular pairs
+ * and the batched kernels are FP32 in every mode.  No counterpart in the reference, whose regular
+ * collocation G and B are FP32 and H FP64 (src/elastodynamics_cqbem_*_collocation.cu:15). */
+enum sod_precision { SOD_PRECISION_AUTO = 0, SOD_PRECISION_FP32 = 1, SOD_PRECISION_COMPENSATED = 2 };
+int sod_context_set_precision(sod_context *ctx, int precision);
 /* Count of kernel launches issued by this context since creation (for launch accounting). */
 int64_t sod_context_launch_count(const sod_context *ctx);
 

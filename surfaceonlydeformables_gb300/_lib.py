@@ -22,6 +22,7 @@ COLLOCATION, GALERKIN = 0, 1
 C128, C64, F64, F32, BF16 = 0, 1, 2, 3, 4
 PART_REGULAR, PART_SINGULAR, PART_ALL = 1, 2, 3
 HISTORY_ENGINE_AUTO, HISTORY_ENGINE_CUDA_CORES, HISTORY_ENGINE_TENSOR_CORES = 0, 1, 2
+PRECISION_AUTO, PRECISION_FP32, PRECISION_COMPENSATED = 0, 1, 2
 
 # every function the header declares, with its ctypes signature
 _c = ctypes
@@ -37,6 +38,7 @@ _SIGS = {
     "sod_context_synchronize": ([_P], _c.c_int),
     "sod_context_set_tuning": ([_P, _c.c_int, _c.c_int], _c.c_int),
     "sod_context_set_wait_test": ([_P, _c.c_int], _c.c_int),
+    "sod_context_set_precision": ([_P, _c.c_int], _c.c_int),
     "sod_context_launch_count": ([_P], _c.c_int64),
     "sod_mesh_create": ([_P, _P, _c.c_int, _P, _c.c_int, _P, _P, _P], _c.c_int),
     "sod_mesh_destroy": ([_P], _c.c_int),

@@ -37,6 +37,11 @@ class Context:
     def set_tuning(self, coll_threads: int = 0, galerkin_threads: int = 0) -> None:
         L.check(L.load().sod_context_set_tuning(self._h, coll_threads, galerkin_threads))
 
+    def set_precision(self, precision: int) -> None:
+        """Regular-pass precision: L.PRECISION_AUTO (FP32 for Laplace-domain outputs, compensated for
+        time-domain outputs), L.PRECISION_FP32 or L.PRECISION_COMPENSATED."""
+        L.check(L.load().sod_context_set_precision(self._h, precision))
+
     def set_wait_test(self, stall: bool) -> None:
         """Test hook: make the collocation scatter kernels' bounded colour-phase waits run out."""
         L.check(L.load().sod_context_set_wait_test(self._h, 1 if stall else 0))

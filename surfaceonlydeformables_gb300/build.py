@@ -11,7 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libsod_gb300.so")
-SOURCES = ["sod_api.cu", "sod_collocation.cu", "sod_singular.cu", "sod_transform.cu", "sod_noalloc.cu", "sod_precompute.cu",
+SOURCES = ["sod_api.cu", "sod_collocation.cu", "sod_coll_compensated.cu", "sod_singular.cu", "sod_transform.cu", "sod_noalloc.cu", "sod_precompute.cu",
            "sod_batch.cu", "sod_history.cu", "sod_elastostatic.cu",
            "sod_server.cu", "sod_galerkin.cu", "sod_history_tc.cu", "sod_cache.cu",
            "sod_solve.cu", "sod_lstsq.cu", "sod_static_solve.cu", "sod_wavelet.cu"]

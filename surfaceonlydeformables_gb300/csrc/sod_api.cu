@@ -425,6 +425,15 @@ int sod_context_set_tuning(sod_context *ctx, int coll_threads, int galerkin_thre
     return SOD_OK;
 }
 
+int sod_context_set_precision(sod_context *ctx, int precision) {
+    SOD_TRY(check_context(ctx));
+    SOD_REQUIRE(precision == SOD_PRECISION_AUTO || precision == SOD_PRECISION_FP32 ||
+                    precision == SOD_PRECISION_COMPENSATED,
+                "precision must be SOD_PRECISION_AUTO, _FP32 or _COMPENSATED");
+    ctx->precision = precision;
+    return SOD_OK;
+}
+
 int64_t sod_context_launch_count(const sod_context *ctx) { return ctx ? ctx->launches.load() : -1; }
 
 int sod_mesh_create(sod_context *ctx, const double *V, int nV, const int *F, int nF, const double *N, const int *vmap,
@@ -542,9 +551,12 @@ static size_t kind_elems(int kind, int nV) {
 // stream while later rows compute (the copy engine moves ~190 GB/s over the CPU-GPU link, about
 // twice what kernel stores into host memory reach); small page-locked ones are written in place by
 // the kernels through their device-mapped address (no copy launch at all).
-static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int method, double c1, double c2,
-                          double rho, const double *s, int nfreq, int order, int subdiv, int sorder, int ssub,
-                          int parts, void *const outs[4], int out_dtype) {
+}  // extern "C"
+
+namespace sod {
+int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int method, double c1, double c2, double rho,
+                   const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, int parts,
+                   void *const outs[4], int out_dtype, bool compensated) {
     SOD_TRY(check_context(ctx));
     SOD_REQUIRE(mesh && mesh->ctx == ctx, "mesh does not belong to this context");
     SOD_REQUIRE(out_dtype == SOD_C128 || out_dtype == SOD_C64, "output dtype must be complex128 or complex64");
@@ -600,6 +612,7 @@ static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int 
     L.parts = parts;
     L.out_dtype = out_dtype;
     L.stream = ctx->stream;
+    L.compensated = compensated && method == SOD_COLLOCATION;
     if (pipelined)
         for (int kd = 0; kd < 4; kd++) L.host[kd] = host_out[kd] ? outs[kd] : nullptr;
     SOD_TRY(method == SOD_GALERKIN ? launch_galerkin(ctx, L) : launch_collocation(ctx, L));
@@ -613,6 +626,9 @@ static int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int 
     }
     return SOD_OK;
 }
+}  // namespace sod
+
+extern "C" {
 
 int sod_cqbem_assemble_frequencies(sod_context *ctx, const sod_mesh *mesh, int kind, int method, double c1, double c2,
                                    double rho, const double *s, int nfreq, int order, int subdiv, int sorder, int ssub,
@@ -621,7 +637,7 @@ int sod_cqbem_assemble_frequencies(sod_context *ctx, const sod_mesh *mesh, int k
     void *outs[4] = {nullptr, nullptr, nullptr, nullptr};
     outs[kind] = out;
     return assemble_kinds(ctx, mesh, 1 << kind, method, c1, c2, rho, s, nfreq, order, subdiv, sorder, ssub, parts,
-                          outs, out_dtype);
+                          outs, out_dtype, ctx && ctx->precision == SOD_PRECISION_COMPENSATED);
 }
 
 int sod_cqbem_assemble_all(sod_context *ctx, const sod_mesh *mesh, int method, double c1, double c2, double rho,
@@ -633,7 +649,7 @@ int sod_cqbem_assemble_all(sod_context *ctx, const sod_mesh *mesh, int method, d
         if (outs[kd]) mask |= 1 << kd;
     SOD_REQUIRE(mask != 0, "no output requested");
     return assemble_kinds(ctx, mesh, mask, method, c1, c2, rho, s, nfreq, order, subdiv, sorder, ssub, parts, outs,
-                          out_dtype);
+                          out_dtype, ctx && ctx->precision == SOD_PRECISION_COMPENSATED);
 }
 
 int sod_cqbem_assemble(sod_context *ctx, const sod_mesh *mesh, int kind, int method, double c1, double c2, double rho,

@@ -73,21 +73,34 @@ __device__ __forceinline__ cd crecip(cd a) {
 // e^-z for complex z in FP32 on the SFU: Cody-Waite reduction of the phase to [-pi, pi] and of the
 // exponent to [-1/2, 1/2] (three-term splits of 2 pi and log2 e), then MUFU sin/cos/ex2.  Phase
 // error < 4e-7 rad, magnitude error < 3e-7 relative (checked against the FP64 oracle in the tests).
+// The reduction integers come from the 1.5 * 2^23 rounding constant (an add on the FMA pipe instead
+// of a round and a float-to-int conversion on the SFU pipe), and 2^n is added into the exponent
+// field of 2^f; results below 2^-125 flush to zero.
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+constexpr float kRound23 = 12582912.0f;  // 1.5 * 2^23: x + kRound23 - kRound23 = round(x), |x| < 2^22
 __device__ __forceinline__ cf cexp_neg(cf z) {
-    // phase: y - k 2pi with 2pi = P1 + P2 + P3
-    const float k = rintf(z.y * 0.15915494309189535f);
+    // phase: y - k 2pi with 2pi = P1 + P2
+    const float k = fmaf(z.y, 0.15915494309189535f, kRound23) - kRound23;
     float ph = fmaf(-k, 6.28318548202514648f, z.y);
     ph = fmaf(-k, -1.74845553e-7f, ph);
     float sn, cs;
     __sincosf(ph, &sn, &cs);
-    // magnitude: e^-x = 2^(-x log2 e) = 2^n 2^f
-    const float t = -z.x * 1.44269504088896341f;
-    const float n = rintf(t);
+    // magnitude: e^-x = 2^(-x log2 e) = 2^n 2^f (n <= 0 here: Re z >= 0)
+    const float nr = fmaf(-z.x, 1.44269504088896341f, kRound23);
+    const int ni = __float_as_int(nr) - __float_as_int(kRound23);
+    const float n = nr - kRound23;
     float f = fmaf(-z.x, 1.44269502162933350f, -n);
     f = fmaf(-z.x, 1.92596299e-8f, f);
-    // 2^n from the exponent bits (n <= 0 here: Re z >= 0); results below 2^-126 flush to zero
-    const float scale = __int_as_float(((int)n + 127) << 23);
-    const float m = (n < -126.f) ? 0.f : exp2f(f) * scale;
+    const float m = ni > -125 ? __int_as_float(__float_as_int(ex2_approx(f)) + ni * (1 << 23)) : 0.f;
     return {m * cs, -m * sn};
 }
 __device__ __forceinline__ cd cexp_neg(cd z) {
@@ -98,22 +111,31 @@ __device__ __forceinline__ cd cexp_neg(cd z) {
 }
 
 // psi(z) = ((1+z) e^-z - 1) / z^2 = -sum_{m>=0} (-1)^m (m+1) z^m / (m+2)!
-// FP32: Horner with 12 terms below |z| = 1 (truncation < 2e-9 relative).
+// FP32: below |z| = 1 the 11-term series (truncation < 4e-9 relative) in Estrin's scheme (dependency
+// depth 4 complex multiply-adds instead of Horner's 10); above, the closed form with an approximate
+// reciprocal.
+__device__ __forceinline__ cf cfmac(cf a, cf b, cf c) {  // a b + c
+    return {fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y))};
+}
 __device__ __forceinline__ cf psi(cf z, cf ez) {
     const float az2 = z.x * z.x + z.y * z.y;
     if (az2 < 1.0f) {
-        // coefficients -(-1)^m (m+1)/(m+2)!, m = 11..0
-        const float c[12] = {-1.0f / 2.0f,          1.0f / 3.0f,          -1.0f / 8.0f,        1.0f / 30.0f,
-                             -1.0f / 144.0f,        1.0f / 840.0f,        -1.0f / 5760.0f,     1.0f / 45360.0f,
-                             -9.0f / 3628800.0f,    10.0f / 39916800.0f,  -11.0f / 479001600.0f,
-                             12.0f / 6227020800.0f};
-        cf acc = {c[11], 0.0f};
-#pragma unroll
-        for (int m = 10; m >= 0; m--) acc = acc * z + mk(c[m], 0.0f);
-        return acc;
+        // c_m = -(-1)^m (m+1)/(m+2)!, m = 0..10, paired as c_2j + c_2j+1 z
+        const float c0 = -1.0f / 2.0f, c1 = 1.0f / 3.0f, c2 = -1.0f / 8.0f, c3 = 1.0f / 30.0f, c4 = -1.0f / 144.0f,
+                    c5 = 1.0f / 840.0f, c6 = -1.0f / 5760.0f, c7 = 1.0f / 45360.0f, c8 = -9.0f / 3628800.0f,
+                    c9 = 10.0f / 39916800.0f, c10 = -11.0f / 479001600.0f;
+        const cf z2 = z * z, z4 = z2 * z2, z8 = z4 * z4;
+        const cf p01 = {fmaf(c1, z.x, c0), c1 * z.y}, p23 = {fmaf(c3, z.x, c2), c3 * z.y};
+        const cf p45 = {fmaf(c5, z.x, c4), c5 * z.y}, p67 = {fmaf(c7, z.x, c6), c7 * z.y};
+        const cf p89 = {fmaf(c9, z.x, c8), c9 * z.y};
+        const cf q0 = cfmac(z2, p23, p01), q1 = cfmac(z2, p67, p45);
+        const cf q2 = {fmaf(c10, z2.x, p89.x), fmaf(c10, z2.y, p89.y)};
+        return cfmac(z8, q2, cfmac(z4, q1, q0));
     }
     const cf num = (mk(1.0f, 0.0f) + z) * ez - mk(1.0f, 0.0f);
-    return num * crecip(z * z);
+    const cf zz = z * z;
+    const float d = rcp_approx(fmaf(zz.x, zz.x, zz.y * zz.y));
+    return num * cf{zz.x * d, -zz.y * d};
 }
 // FP64: the closed form loses about 2 eps / |z|^2, i.e. <= 2e-12 relative for |z| >= 0.01; below
 // that a 7-term series (truncation < 1e-17 relative) is used.

@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_tp_kernel(
                 }
             if (NCB) {
                 float2 *col = accB + threadIdx.x;
-                bm.emit(nn, fr.area, [&](int cc, cf v) {
+                bm.emit(k, nn, fr.area, [&](int cc, cf v) {
                     float2 &sb = col[cc * blockDim.x];
                     sb.x += v.x;
                     sb.y += v.y;

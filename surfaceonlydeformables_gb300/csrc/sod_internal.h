@@ -120,6 +120,7 @@ struct sod_context {
     sod::DevBuf gacc;      // collocation row accumulators in global memory (meshes too large for shared memory)
     sod::DevBuf dev_err;   // error word of the scatter kernels' bounded colour-phase waits (0 = none)
     bool wait_test = false;  // test hook: colour-phase barriers expect one arrival more than comes
+    int precision = SOD_PRECISION_AUTO;  // regular-pass precision (sod_context_set_precision)
     void count(int n = 1) { launches += n; }
 };
 
@@ -199,6 +200,9 @@ struct CollLaunch {
     int out_dtype;
     long long freq_stride[4];  // elements between consecutive frequencies of out[kind]
     cudaStream_t stream;
+    // collocation only: regular pass in compensated double-float arithmetic (sod_coll_compensated.cu)
+    // instead of FP32; for time-domain outputs, whose late weights amplify FP32 noise by up to R^-N
+    int compensated;
     // collocation only: host destinations of out[kind] (device staging).  When set, the scatter runs
     // in row chunks and each chunk's rows are copied to the host on the context's copy stream while
     // the next chunk computes; `stream` waits for the copies at the end.
@@ -231,6 +235,18 @@ size_t sing_result_elems(int mask, int nstar, int nf, bool guiggiani);
 // of the kinds in `mask`; one CTA per item
 int sing_batch_launch(sod_context *ctx, int which, int mask, const SingBatchObj *objs, const int4 *items, int nitems,
                       const KConst<double> *kcd, cudaStream_t stream);
+// Compensated (double-float) regular collocation pass of one chunk of field vertices
+// (sod_coll_compensated.cu); the CollArgs carry everything but the face schedule.
+struct CollArgs;
+int comp_scatter_threads();
+int launch_regular_compensated(sod_context *ctx, const sod_mesh *m, CollArgs a, int mask,
+                               const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, const PointTable &pt,
+                               const FreqTable &ft, int nvert, cudaStream_t stream);
+// Assembly of the kinds in `mask` (sod_api.cu): the shared driver of the sod_cqbem_assemble* entry
+// points, with the regular-pass precision chosen by the caller (compensated: time-domain outputs).
+int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int method, double c1, double c2, double rho,
+                   const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, int parts,
+                   void *const outs[4], int out_dtype, bool compensated);
 // Allocation-free launcher over caller-provided scratch (see sod_collocation.cu).
 int launch_collocation_prealloc(sod_context *ctx, const sod_mesh *m, int kind, double c1, double c2, double rho,
                                 const double *s, int nfreq, int order, int subdiv, int sorder, int ssub, void *out,

@@ -195,8 +195,13 @@ extern "C" int sod_cqbem_precompute(sod_context *ctx, const sod_mesh *mesh, int 
         fdom[kd] = fb + foff[kd];
         tdom[kd] = outs[kd] ? outs[kd] : fb + ftot + toff[kd];
     }
-    SOD_TRY(sod_cqbem_assemble_all(ctx, mesh, method, c1, c2, rho, s.data(), nf, order, subdiv, sorder, ssub,
-                                   SOD_PART_ALL, fdom[0], fdom[1], fdom[2], fdom[3], fdt));
+    // time-domain outputs: the regular pass in compensated arithmetic unless the caller forced FP32 (the
+    // transform multiplies the late weights by up to R^-N = 1e5, FP32 noise included)
+    int mask = 0;
+    for (int kd = 0; kd < 4; kd++)
+        if (want[kd]) mask |= 1 << kd;
+    SOD_TRY(assemble_kinds(ctx, mesh, mask, method, c1, c2, rho, s.data(), nf, order, subdiv, sorder, ssub,
+                           SOD_PART_ALL, fdom, fdt, ctx->precision != SOD_PRECISION_FP32));
     for (int kd = 0; kd < 4; kd++)
         if (want[kd])
             SOD_TRY(launch_inverse_transform(ctx, fdom[kd], fdt, (int64_t)per[kd], nf, L, R, tdom[kd], out_dtype,

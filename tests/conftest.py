@@ -34,9 +34,16 @@ def sodlib():
 
 @pytest.fixture(scope="session")
 def gpu_ctx(sodlib):
+    """A library context whose work shares one CUDA stream with torch: library calls with device
+    outputs return before their kernels finish (stream-ordered, as for a C++ caller), so torch's
+    reads of those outputs (tensor.cpu()) must be ordered after them on the same stream."""
+    import torch
+
     from surfaceonlydeformables_gb300.api import Context
 
-    return Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    return Context(0, stream=stream)
 
 
 def rel_fro(a, b):

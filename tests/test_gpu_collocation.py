@@ -305,3 +305,22 @@ def test_colour_phase_wait_timeout_is_reported(gpu_ctx, sodlib):
     got = api.assemble(gpu_ctx, dm, "G", mat, s)
     assert np.array_equal(got, want)
     gpu_ctx.synchronize()  # no error left behind
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_compensated_regular_pass(gpu_ctx, dev_meshes, meshes, oracle, freqs, kind):
+    """SOD_PRECISION_COMPENSATED: the frequency-dependent terms and the sums in double-float, the
+    geometry in FP32.  The whole matrix is then limited by the FP32 geometry (~3e-8 for G and B,
+    ~1.5e-7 for H, whose 1/r^2 kernel is more sensitive to it), below the FP32 pass."""
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    gpu_ctx.set_precision(L.PRECISION_COMPENSATED)
+    try:
+        for s in freqs:
+            got = api.assemble(gpu_ctx, dev_meshes[2], kind, MAT, s)
+            ref = oracle.collocation(kind, meshes[2], MAT, s)
+            print(kind, s, f"{rel_fro(got, ref):.2e}")
+            assert rel_fro(got, ref) <= 3e-7, (kind, s, rel_fro(got, ref))
+    finally:
+        gpu_ctx.set_precision(L.PRECISION_AUTO)

@@ -172,3 +172,52 @@ def test_history_empty_and_reset(gpu_ctx):
     assert np.allclose(bank.convolve(), np.arange(10.0))
     bank.reset()
     assert np.all(bank.convolve() == 0.0)
+
+
+@pytest.mark.parametrize("wdt_name,R,tol", [("F32", 1, 2e-6), ("F32", 16, 2e-6), ("BF16", 1, 4e-3), ("BF16", 16, 4e-3)])
+def test_history_full_size_against_fp64(gpu_ctx, wdt_name, R, tol):
+    """The benchmarked bank: one 2562-vertex object (3V = 7686) with K = 64 steps of FP64 weights
+    (G_k ~ 1e-6 x 0.8^k, H_k ~ 0.8^k), the ring wrapped, default engine.  The FP64 reference
+    b = sum_k G_k p_{n-k} - H_k u_{n-k} is formed on the device in FP64 from the same FP64 weights
+    (regenerated from per-k seeds), so the bank's FP32 / BF16 storage is what is measured."""
+    import torch
+
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+
+    n, K, nsteps = 7686, 64, 67
+    ctx = api.Context(0, stream=torch.cuda.current_stream())  # torch's and the bank's work in one stream order
+    bank = api.HistoryBank(ctx, n, n, K, R, getattr(L, wdt_name))
+    gen = torch.Generator(device="cuda")
+
+    def weights(k):
+        gen.manual_seed(1000 + k)
+        G = torch.randn((n, n), dtype=torch.float64, device="cuda", generator=gen) * (1e-6 * 0.8 ** k)
+        H = torch.randn((n, n), dtype=torch.float64, device="cuda", generator=gen) * (0.8 ** k)
+        return G, H
+
+    for k in range(1, K + 1):
+        G, H = weights(k)
+        bank.set_weights(k, G, H)
+        del G, H
+    gen.manual_seed(7)
+    shape = (n, R) if R > 1 else (n,)
+    ps, us = [], []
+    for _ in range(nsteps):
+        p = torch.randn(shape, dtype=torch.float64, device="cuda", generator=gen) * 10.0
+        u = torch.randn(shape, dtype=torch.float64, device="cuda", generator=gen) * 1e-4
+        bank.push(p, u)
+        ps.append(p), us.append(u)
+    got = torch.empty(shape, dtype=torch.float64, device="cuda")
+    bank.convolve(got)
+    torch.cuda.synchronize()
+    ref = torch.zeros(shape, dtype=torch.float64, device="cuda")
+    for i in range(K):  # G_{i+1} p_{n-1-i} - H_{i+1} u_{n-1-i}
+        G, H = weights(i + 1)
+        ref += G @ ps[nsteps - 1 - i] - H @ us[nsteps - 1 - i]
+        del G, H
+    err = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+    bank.close()
+    ctx.close()
+    torch.cuda.empty_cache()
+    assert err <= tol, (wdt_name, R, err)

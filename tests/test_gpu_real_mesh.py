@@ -109,9 +109,16 @@ def test_cube_scene_precompute_on_split_mesh(gpu_ctx, cube, oracle, sodlib):
     # last-ulp difference in s would be amplified past the tolerance (the table itself is checked
     # against the oracle elsewhere)
     s, R, Lq = sodlib.cq_frequencies(mf.BDF, mf.DT, N)
-    got = {k: v.cpu().numpy() for k, v in
-           api.precompute(gpu_ctx, dm, mat, mf.BDF, mf.DT, N, order=mf.ORDER, subdiv=mf.SUBDIV).items()}
-    X = api.assemble_all(gpu_ctx, dm, mat, s, order=mf.ORDER, subdiv=mf.SUBDIV)
+    from surfaceonlydeformables_gb300 import _lib as L
+
+    pre = api.precompute(gpu_ctx, dm, mat, mf.BDF, mf.DT, N, order=mf.ORDER, subdiv=mf.SUBDIV)
+    gpu_ctx.synchronize()
+    got = {k: v.cpu().numpy() for k, v in pre.items()}
+    gpu_ctx.set_precision(L.PRECISION_COMPENSATED)  # the precompute's own (compensated) Laplace-domain pass
+    try:
+        X = api.assemble_all(gpu_ctx, dm, mat, s, order=mf.ORDER, subdiv=mf.SUBDIV)
+    finally:
+        gpu_ctx.set_precision(L.PRECISION_AUTO)
     nV = mesh.nV
     ref = {k: oracle.inverse_transform(X[k].reshape((len(s), 3 * nV, 3, 3) if k == "B_angular" else X[k].shape), Lq, R)
            for k in KINDS}
