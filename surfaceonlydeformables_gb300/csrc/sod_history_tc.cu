@@ -58,11 +58,17 @@ template <bool F32> constexpr int tc_stages() { return 4; }  // 2 CTAs per SM
 // producer, MMA, 4 epilogue warps (+ 4 warps that split FP32 weight tiles)
 template <bool F32> constexpr int tc_threads() { return F32 ? 320 : 192; }
 template <int R, bool F32> constexpr int tc_smem() { return tc_stages<F32>() * tc_stage_bytes<R, F32>() + 1024; }
-// accumulators per unit: FP32 banks spread the K tiles round-robin over 4 accumulators (shorter
-// accumulation chains inside the tensor core), summed in the epilogue.  BF16 banks keep two units in
-// flight; FP32 banks one, and 4 x 32 columns behind the accumulators hold the stages' w_lo tiles.
-template <bool F32> constexpr int tc_ngroups() { return F32 ? 4 : 1; }
-template <bool F32> constexpr int tc_nbuf() { return F32 ? 1 : 2; }
+// Units and accumulators.  A BF16 unit is one segment (its row scale applies to the whole sum).  The
+// tensor core's FP32 accumulation does not round to nearest at every step, and its error grows with
+// the number of MMAs that feed one accumulator: over a whole 7686-column segment (961 TF32 MMAs
+// spread over 4 accumulators) it reached 1e-5 relative.  So an FP32 unit is a run of TC_SUB K tiles
+// of a segment, spread round-robin over 2 accumulators (16 MMAs each), and the epilogue adds every
+// unit into its FP32 registers, rounding to nearest; two accumulator sets alternate so that the MMAs
+// of the next unit overlap the epilogue's reads.  Behind the accumulators, 4 x 32 columns hold the
+// stages' w_lo tiles.
+constexpr int TC_SUB = 8;
+template <bool F32> constexpr int tc_ngroups() { return F32 ? 2 : 1; }
+template <bool F32> constexpr int tc_nbuf() { return 2; }
 template <bool F32> constexpr int tc_acc_cols() { return tc_nbuf<F32>() * tc_ngroups<F32>() * 32; }
 template <bool F32> constexpr int tc_tmem_cols() { return tc_acc_cols<F32>() + (F32 ? tc_stages<F32>() * 32 : 0); }  // 256 / 64
 static_assert(tc_tmem_cols<true>() == 256 && tc_tmem_cols<false>() == 64, "tensor memory columns (power of two)");
@@ -262,14 +268,17 @@ __global__ void __launch_bounds__(tc_threads<F32>(), 2) hist_tc_kernel(const __g
             uint32_t phase = 0;
             bool ok = true;
             int ul = 0;
-            for (int seg = seg0; seg < a.nseg && ok; seg += a.k, ul++) {
+            const int SUBT = F32 ? TC_SUB : KT;  // K tiles per unit
+            for (int seg = seg0; seg < a.nseg && ok; seg += a.k)
+            for (int u0 = 0; u0 < KT && ok; u0 += SUBT, ul++) {
+                const int u1 = min(KT, u0 + SUBT);
                 const int buf = ul % tc_nbuf<F32>();
                 const uint32_t aphase = (ul / tc_nbuf<F32>()) & 1;
                 ok = mbar_wait(smem_u32(&acc_empty[buf]), aphase ^ 1u, ab, a.err, 2);
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 constexpr int NG = tc_ngroups<F32>();
-                for (int kt = 0; kt < KT && ok; kt++) {
+                for (int kt = u0; kt < u1 && ok; kt++) {
                     // BF16: the TMA tiles; FP32: the tiles after the transform warps split the weights
                     ok = mbar_wait(smem_u32(F32 ? &ready[stage] : &full[stage]), phase, ab, a.err, 3);
                     if (!ok) break;
@@ -279,9 +288,9 @@ __global__ void __launch_bounds__(tc_threads<F32>(), 2) hist_tc_kernel(const __g
 #pragma unroll
                     for (int k = 0; k < 4; k++) {
                         // accumulator of this K tile; the first MMA into it overwrites
-                        const uint32_t d = tmem + (buf * NG + kt % NG) * 32;
+                        const uint32_t d = tmem + (buf * NG + (kt - u0) % NG) * 32;
                         mma_tc<tc_n<R>(), F32>(d, smem_desc(sA + k * 32), smem_desc(sA + B_OFF + k * 32),
-                                               (kt >= NG) || (k > 0));
+                                               (kt - u0 >= NG) || (k > 0));
                         // FP32: W_lo (tensor memory, 8 columns per K step) x (x_hi rows; for R = 1 the
                         // whole hi/lo tile)
                         if (F32)
@@ -334,17 +343,25 @@ __global__ void __launch_bounds__(tc_threads<F32>(), 2) hist_tc_kernel(const __g
         // ---- epilogue: TMEM -> registers -> scaled sum over the CTA's segments ----
         const int q = warp & 3;  // TMEM lane quadrant this warp may access
         const int row = m * TC_BM + q * 32 + lane;
-        float acc[R];
+        // running sum over the CTA's units; FP32 banks add a thousand units or so per row, so the sum is
+        // compensated (TwoSum into a correction term) to stay at FP32 accuracy
+        float acc[R], cmp[R];
 #pragma unroll
-        for (int j = 0; j < R; j++) acc[j] = 0.f;
+        for (int j = 0; j < R; j++) acc[j] = 0.f, cmp[j] = 0.f;
         int ul = 0;
-        for (int seg = seg0; seg < a.nseg; seg += a.k, ul++) {
+        const int SUBT = F32 ? TC_SUB : KT;  // K tiles per unit
+        bool ok = true;
+        for (int seg = seg0; seg < a.nseg && ok; seg += a.k)
+        for (int u0 = 0; u0 < KT; u0 += SUBT, ul++) {
             const int buf = ul % tc_nbuf<F32>();
             const uint32_t aphase = (ul / tc_nbuf<F32>()) & 1;
-            if (!mbar_wait(smem_u32(&acc_full[buf]), aphase, ab, a.err, 4)) break;
+            if (!mbar_wait(smem_u32(&acc_full[buf]), aphase, ab, a.err, 4)) {
+                ok = false;
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;");
             constexpr int NG = tc_ngroups<F32>();
-            const int ng = min(NG, KT);  // accumulators this unit wrote
+            const int ng = min(NG, min(KT, u0 + SUBT) - u0);  // accumulators this unit wrote
             float vs[32];
 #pragma unroll
             for (int j = 0; j < 32; j++) vs[j] = 0.f;
@@ -362,13 +379,20 @@ __global__ void __launch_bounds__(tc_threads<F32>(), 2) hist_tc_kernel(const __g
             if (lane == 0) mbar_arrive(smem_u32(&acc_empty[buf]));
             // BF16: the row's power-of-two scale; FP32: unscaled
             const float sc = row < a.nrow ? (a.scale ? a.scale[(size_t)seg * a.nrow + row] : 1.f) : 0.f;
-            if (R == 1) {
-                acc[0] = fmaf(vs[0] + vs[1], sc, acc[0]);
-            } else {
 #pragma unroll
-                for (int j = 0; j < R; j++) acc[j] = fmaf(vs[j] + vs[16 + j], sc, acc[j]);
+            for (int j = 0; j < R; j++) {
+                const float v = R == 1 ? vs[0] + vs[1] : vs[j] + vs[16 + j];
+                if (F32) {  // unscaled: TwoSum of acc and v
+                    const float t = acc[j] + v, bp = t - acc[j];
+                    cmp[j] += (acc[j] - (t - bp)) + (v - bp);
+                    acc[j] = t;
+                } else {
+                    acc[j] = fmaf(v, sc, acc[j]);
+                }
             }
         }
+#pragma unroll
+        for (int j = 0; j < R; j++) acc[j] += cmp[j];
         float *dst = a.partial + ((size_t)blockIdx.x * TC_BM + q * 32 + lane) * R;
         if (R == 1) {
             dst[0] = acc[0];
