@@ -262,9 +262,9 @@ int sod_history_destroy(sod_history *bank);
 /* Replace the Eigen::PartialPivLU uses of ElastodynamicsCQBEMMatrixCollection::init
  * (src/elastodynamics_cqbem_matrix_collection.cpp:200-214: H_inv.compute(H_0), u_p = H_inv.solve(G'),
  * H_inv_B_trans / H_inv_B_euler, H_inv.inverse()) and the per-step H_inv.solve(b)
- * (src/elastodynamics_cqbem_object.cpp:63): LU with partial pivoting in FP64 on the device
- * (cuSOLVER, loaded at first use: SOD_ERR_UNSUPPORTED if it is not installed).  All matrices are
- * row-major FP64, host or device.  A singular matrix gives SOD_ERR_INVALID_ARG. */
+ * (src/elastodynamics_cqbem_object.cpp:63): LU with partial pivoting in FP64 on the device (this
+ * library's blocked right-looking factorisation, LAPACK's pivot choice).  All matrices are row-major
+ * FP64, host or device.  A singular matrix gives SOD_ERR_INVALID_ARG. */
 typedef struct sod_solver sod_solver;
 int sod_solver_create(sod_context *ctx, int n, const double *A, sod_solver **solver);
 /* X = A^-1 B, B and X n x nrhs (X may alias B). */
@@ -300,7 +300,7 @@ int sod_lstsq_destroy(sod_lstsq *lstsq);
  * rigid modes of the mesh,
  *   u_p = (H^T H + (tr H / 3nV)^2 T^T T)^-1 H^T G (I - T^T (T T^T)^-1 T).
  * The symmetric positive definite system is factored by Cholesky (the reference's LDL^T); FP64 on
- * the device (cuBLAS and cuSOLVER, loaded at first use).  u_p: 3nV x 3nV row-major, host or device.
+ * the device with this library's GEMM and Cholesky kernels.  u_p: 3nV x 3nV row-major, host or device.
  * SOD_ERR_INVALID_ARG if the regularised matrix is not positive definite. */
 int sod_elastostatic_u_p(sod_context *ctx, const sod_mesh *mesh, const double *H, const double *G, double *u_p);
 /* T (6 x 3nV row-major, host or device): rows 0-2 translations (A_e / 6 per face corner), rows 3-5

@@ -14,7 +14,7 @@ LIB = os.path.join(OUT, "libsod_gb300.so")
 SOURCES = ["sod_api.cu", "sod_collocation.cu", "sod_coll_compensated.cu", "sod_singular.cu", "sod_transform.cu", "sod_noalloc.cu", "sod_precompute.cu",
            "sod_batch.cu", "sod_history.cu", "sod_elastostatic.cu",
            "sod_server.cu", "sod_galerkin.cu", "sod_history_tc.cu", "sod_cache.cu",
-           "sod_solve.cu", "sod_lstsq.cu", "sod_static_solve.cu", "sod_wavelet.cu"]
+           "sod_solve.cu", "sod_dense_kernels.cu", "sod_lstsq.cu", "sod_static_solve.cu", "sod_wavelet.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
          "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

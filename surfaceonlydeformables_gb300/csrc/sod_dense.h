@@ -1,44 +1,24 @@
-// sod_dense.h -- cuSOLVER / cuBLAS entry points of the dense solves (LU, Cholesky, FP64 GEMM).
-//
-// Both libraries are loaded with dlopen at first use, so only the dense-solve entry points depend on
-// them; the assembly, transform and history paths never load them.
+// sod_dense.h -- FP64 dense linear algebra of the solves (sod_dense_kernels.cu): GEMM, LU with partial
+// pivoting, Cholesky and their triangular solves.  Row-major device buffers, work on the context's
+// stream.
 #pragma once
-#include <cublas_api.h>
-#include <cusolverDn.h>
-
-#include <string>
-
 #include "sod_internal.h"
 
 namespace sod {
 
-struct DenseApi {
-    // cuSOLVER (dense)
-    cusolverStatus_t (*dn_create)(cusolverDnHandle_t *) = nullptr;
-    cusolverStatus_t (*dn_destroy)(cusolverDnHandle_t) = nullptr;
-    cusolverStatus_t (*dn_set_stream)(cusolverDnHandle_t, cudaStream_t) = nullptr;
-    cusolverStatus_t (*getrf_buf)(cusolverDnHandle_t, int, int, double *, int, int *) = nullptr;
-    cusolverStatus_t (*getrf)(cusolverDnHandle_t, int, int, double *, int, double *, int *, int *) = nullptr;
-    cusolverStatus_t (*getrs)(cusolverDnHandle_t, cublasOperation_t, int, int, const double *, int, const int *,
-                              double *, int, int *) = nullptr;
-    cusolverStatus_t (*potrf_buf)(cusolverDnHandle_t, cublasFillMode_t, int, double *, int, int *) = nullptr;
-    cusolverStatus_t (*potrf)(cusolverDnHandle_t, cublasFillMode_t, int, double *, int, double *, int, int *) = nullptr;
-    cusolverStatus_t (*potrs)(cusolverDnHandle_t, cublasFillMode_t, int, int, const double *, int, double *, int,
-                              int *) = nullptr;
-    // cuBLAS
-    cublasStatus_t (*blas_create)(cublasHandle_t *) = nullptr;
-    cublasStatus_t (*blas_destroy)(cublasHandle_t) = nullptr;
-    cublasStatus_t (*blas_set_stream)(cublasHandle_t, cudaStream_t) = nullptr;
-    cublasStatus_t (*dgemm)(cublasHandle_t, cublasOperation_t, cublasOperation_t, int, int, int, const double *,
-                            const double *, int, const double *, int, const double *, double *, int) = nullptr;
-    cublasStatus_t (*dsyrk)(cublasHandle_t, cublasFillMode_t, cublasOperation_t, int, int, const double *,
-                            const double *, int, const double *, double *, int) = nullptr;
-    bool solver_ok = false, blas_ok = false;
-    std::string why_solver, why_blas;
-};
-const DenseApi &dense_api();
-
-// out[c][r] = in[r][c] for an R x C row-major FP64 matrix, on the context's stream
-int transpose_f64(sod_context *ctx, const double *in, int R, int C, double *out);
+// C[M x N] = alpha op(A) op(B) + beta C, op(X) = X^T when the flag is set (row-major storage, leading
+// dimensions in elements).  lower_only: only the lower triangle (and the diagonal tiles) of C.
+int dgemm(sod_context *ctx, bool ta, bool tb, int M, int N, int K, double alpha, const double *A, long long lda,
+          const double *B, long long ldb, double beta, double *C, long long ldc, bool lower_only);
+// P A = L U in place (unit lower L below the diagonal, U on and above); ipiv[i] = the row interchanged
+// with row i at step i; perm[i] = the original row now at position i; *info = 1-based index of the
+// first exactly zero pivot, 0 if none (device ints)
+int lu_factor(sod_context *ctx, double *A, int n, int *ipiv, int *perm, int *info);
+// X = A^-1 B (n x nrhs); X must not alias B
+int lu_solve(sod_context *ctx, const double *LU, int n, const int *perm, int nrhs, const double *B, double *X);
+// A = L L^T in place from A's lower triangle; *info = 1-based column of the first non-positive pivot
+int chol_factor(sod_context *ctx, double *A, int n, int *info);
+// X = A^-1 B for the factored A (n x nrhs); X may alias B
+int chol_solve(sod_context *ctx, const double *L, int n, int nrhs, const double *B, double *X);
 
 }  // namespace sod

@@ -6,85 +6,16 @@
 // ElastodynamicsCQBEMObject (src/elastodynamics_cqbem_object.cpp:63), fused after the history
 // convolution so the served time step stays on the device.
 //
-// The factorisation is LAPACK-style LU with partial pivoting in FP64 (cuSOLVER getrf / getrs: a plain
-// library factorisation; the library is loaded at first use, so the rest of this library does not
-// depend on it).  Matrices are row-major at the interface; a row-major A is the column-major A^T, so
-// the buffer is factored as it is (P A^T = L U) and solves use the transposed form, A X = B.
-// Right-hand sides are transposed to column-major and back by a tiled shared-memory kernel.
-#include <dlfcn.h>
-
-#include <mutex>
+// The factorisation is LU with partial pivoting in FP64 (P A = L U on the row-major matrix, with
+// LAPACK's pivot choice; sod_dense_kernels.cu).
+#include <memory>
 #include <string>
 
 #include "sod_dense.h"
 
 using namespace sod;
 
-namespace sod {
-
-const DenseApi &dense_api() {
-    static DenseApi api;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        auto open = [](const char *const *names, int n) -> void * {
-            for (int i = 0; i < n; i++)
-                if (void *h = dlopen(names[i], RTLD_NOW | RTLD_LOCAL)) return h;
-            return nullptr;
-        };
-        const char *sol[] = {"libcusolver.so.12", "libcusolver.so", "/usr/local/cuda/lib64/libcusolver.so.12"};
-        if (void *h = open(sol, 3)) {
-            auto sym = [&](const char *s) { return dlsym(h, s); };
-            api.dn_create = reinterpret_cast<decltype(api.dn_create)>(sym("cusolverDnCreate"));
-            api.dn_destroy = reinterpret_cast<decltype(api.dn_destroy)>(sym("cusolverDnDestroy"));
-            api.dn_set_stream = reinterpret_cast<decltype(api.dn_set_stream)>(sym("cusolverDnSetStream"));
-            api.getrf_buf = reinterpret_cast<decltype(api.getrf_buf)>(sym("cusolverDnDgetrf_bufferSize"));
-            api.getrf = reinterpret_cast<decltype(api.getrf)>(sym("cusolverDnDgetrf"));
-            api.getrs = reinterpret_cast<decltype(api.getrs)>(sym("cusolverDnDgetrs"));
-            api.potrf_buf = reinterpret_cast<decltype(api.potrf_buf)>(sym("cusolverDnDpotrf_bufferSize"));
-            api.potrf = reinterpret_cast<decltype(api.potrf)>(sym("cusolverDnDpotrf"));
-            api.potrs = reinterpret_cast<decltype(api.potrs)>(sym("cusolverDnDpotrs"));
-            api.solver_ok = api.dn_create && api.dn_destroy && api.dn_set_stream && api.getrf_buf && api.getrf &&
-                            api.getrs && api.potrf_buf && api.potrf && api.potrs;
-            if (!api.solver_ok) api.why_solver = "cuSOLVER is missing dense LU / Cholesky entry points";
-        } else {
-            api.why_solver = std::string("cuSOLVER not found (") + dlerror() + ")";
-        }
-        const char *blas[] = {"libcublas.so.13", "libcublas.so", "/usr/local/cuda/lib64/libcublas.so.13"};
-        if (void *h = open(blas, 3)) {
-            auto sym = [&](const char *s) { return dlsym(h, s); };
-            api.blas_create = reinterpret_cast<decltype(api.blas_create)>(sym("cublasCreate_v2"));
-            api.blas_destroy = reinterpret_cast<decltype(api.blas_destroy)>(sym("cublasDestroy_v2"));
-            api.blas_set_stream = reinterpret_cast<decltype(api.blas_set_stream)>(sym("cublasSetStream_v2"));
-            api.dgemm = reinterpret_cast<decltype(api.dgemm)>(sym("cublasDgemm_v2"));
-            api.dsyrk = reinterpret_cast<decltype(api.dsyrk)>(sym("cublasDsyrk_v2"));
-            api.blas_ok = api.blas_create && api.blas_destroy && api.blas_set_stream && api.dgemm && api.dsyrk;
-            if (!api.blas_ok) api.why_blas = "cuBLAS is missing FP64 GEMM entry points";
-        } else {
-            api.why_blas = std::string("cuBLAS not found (") + dlerror() + ")";
-        }
-    });
-    return api;
-}
-
-}  // namespace sod
-
 namespace {
-
-// out[c][r] = in[r][c] for an R x C row-major matrix (32 x 32 tiles through shared memory)
-__global__ void transpose_kernel(const double *__restrict__ in, int R, int C, double *__restrict__ out) {
-    __shared__ double tile[32][33];
-    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
-    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-        const int r = r0 + k, c = c0 + threadIdx.x;
-        if (r < R && c < C) tile[k][threadIdx.x] = in[(size_t)r * C + c];
-    }
-    __syncthreads();
-    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
-        const int c = c0 + k, r = r0 + threadIdx.x;
-        if (r < R && c < C) out[(size_t)c * R + r] = tile[threadIdx.x][k];
-    }
-}
-
 
 // X[r][j] = sum_c Ai[r][c] B[c][j] (FP64): one warp per row, lanes over the columns in a fixed
 // stride, FP64 xor tree over the lanes (deterministic).  B (n x R) stays in L2.
@@ -118,24 +49,12 @@ __global__ void identity_kernel(double *I, int n) {
 
 }  // namespace
 
-int sod::transpose_f64(sod_context *ctx, const double *in, int R, int C, double *out) {
-    const dim3 grid((C + 31) / 32, (R + 31) / 32), block(32, 8);
-    transpose_kernel<<<grid, block, 0, ctx->stream>>>(in, R, C, out);
-    SOD_CHECK_CUDA(cudaGetLastError());
-    ctx->count();
-    return SOD_OK;
-}
-
 struct sod_solver {
     sod_context *ctx = nullptr;
     int n = 0;
-    cusolverDnHandle_t h = nullptr;
-    DevBuf lu, ipiv, info, work, rhs, tmp;
+    DevBuf lu, ipiv, perm, info, rhs, tmp;
     DevBuf inv;         // A^-1 (row-major) once sod_solver_keep_inverse ran
     bool has_inv = false;
-    ~sod_solver() {
-        if (h) dense_api().dn_destroy(h);
-    }
 };
 
 namespace sod {
@@ -158,26 +77,11 @@ int solver_apply_device(sod_solver *s, int nrhs, const double *B, double *X) {
 int solver_solve_device(sod_solver *s, int nrhs, const double *B, double *X) {
     sod_context *ctx = s->ctx;
     const int n = s->n;
-    const DenseApi &api = dense_api();
     const size_t bytes = sizeof(double) * (size_t)n * nrhs;
+    if (X != B) return lu_solve(ctx, s->lu.as<double>(), n, s->perm.as<int>(), nrhs, B, X);
     SOD_TRY(s->rhs.ensure(bytes));
-    double *cm = s->rhs.as<double>();
-    if (nrhs == 1) {
-        if (cm != B) SOD_CHECK_CUDA(cudaMemcpyAsync(cm, B, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    } else {
-        SOD_TRY(transpose_f64(ctx, B, n, nrhs, cm));  // -> column-major n x nrhs
-    }
-    if (api.getrs(s->h, CUBLAS_OP_T, n, nrhs, s->lu.as<double>(), n, s->ipiv.as<int>(), cm, n, s->info.as<int>()) !=
-        CUSOLVER_STATUS_SUCCESS) {
-        set_error("cusolverDnDgetrs failed");
-        return SOD_ERR_CUDA;
-    }
-    ctx->count();
-    if (nrhs == 1) {
-        if (X != cm) SOD_CHECK_CUDA(cudaMemcpyAsync(X, cm, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    } else {
-        SOD_TRY(transpose_f64(ctx, cm, nrhs, n, X));  // column-major n x nrhs is row-major nrhs x n
-    }
+    SOD_TRY(lu_solve(ctx, s->lu.as<double>(), n, s->perm.as<int>(), nrhs, B, s->rhs.as<double>()));
+    SOD_CHECK_CUDA(cudaMemcpyAsync(X, s->rhs.p, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     return SOD_OK;
 }
 }  // namespace sod
@@ -187,38 +91,17 @@ extern "C" {
 int sod_solver_create(sod_context *ctx, int n, const double *A, sod_solver **out) {
     SOD_REQUIRE(ctx && A && out, "null argument");
     SOD_REQUIRE(n >= 1, "matrix size must be >= 1");
-    const DenseApi &api = dense_api();
-    if (!api.solver_ok) {
-        set_error(api.why_solver);
-        return SOD_ERR_UNSUPPORTED;
-    }
     SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
     auto s = std::make_unique<sod_solver>();
     s->ctx = ctx;
     s->n = n;
-    if (api.dn_create(&s->h) != CUSOLVER_STATUS_SUCCESS || api.dn_set_stream(s->h, ctx->stream) != CUSOLVER_STATUS_SUCCESS) {
-        s->h = nullptr;
-        set_error("cusolverDnCreate failed");
-        return SOD_ERR_CUDA;
-    }
     const size_t bytes = sizeof(double) * (size_t)n * n;
     SOD_TRY(s->lu.ensure(bytes));
     SOD_CHECK_CUDA(cudaMemcpyAsync(s->lu.p, A, bytes, cudaMemcpyDefault, ctx->stream));
     SOD_TRY(s->ipiv.ensure(sizeof(int) * (size_t)n));
+    SOD_TRY(s->perm.ensure(sizeof(int) * (size_t)n));
     SOD_TRY(s->info.ensure(sizeof(int)));
-    int lwork = 0;
-    if (api.getrf_buf(s->h, n, n, s->lu.as<double>(), n, &lwork) != CUSOLVER_STATUS_SUCCESS) {
-        set_error("cusolverDnDgetrf_bufferSize failed");
-        return SOD_ERR_CUDA;
-    }
-    SOD_TRY(s->work.ensure(sizeof(double) * (size_t)std::max(lwork, 1)));
-    // the row-major buffer is the column-major A^T: P A^T = L U
-    if (api.getrf(s->h, n, n, s->lu.as<double>(), n, s->work.as<double>(), s->ipiv.as<int>(), s->info.as<int>()) !=
-        CUSOLVER_STATUS_SUCCESS) {
-        set_error("cusolverDnDgetrf failed");
-        return SOD_ERR_CUDA;
-    }
-    ctx->count();
+    SOD_TRY(lu_factor(ctx, s->lu.as<double>(), n, s->ipiv.as<int>(), s->perm.as<int>(), s->info.as<int>()));
     int info = 0;
     SOD_CHECK_CUDA(cudaMemcpyAsync(&info, s->info.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -264,10 +147,11 @@ int sod_solver_inverse(sod_solver *s, double *Ainv) {
         d = ctx->staging.as<double>();
     }
     const size_t nn = (size_t)n * n;
-    identity_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, ctx->stream>>>(d, n);
+    SOD_TRY(s->rhs.ensure(bytes));
+    identity_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, ctx->stream>>>(s->rhs.as<double>(), n);
     SOD_CHECK_CUDA(cudaGetLastError());
     ctx->count();
-    SOD_TRY(solver_solve_device(s, n, d, d));  // A X = I, row-major
+    SOD_TRY(lu_solve(ctx, s->lu.as<double>(), n, s->perm.as<int>(), n, s->rhs.as<double>(), d));  // A X = I
     if (host) {
         SOD_CHECK_CUDA(cudaMemcpyAsync(Ainv, d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
         SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));

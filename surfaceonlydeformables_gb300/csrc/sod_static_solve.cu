@@ -9,14 +9,10 @@
 //   G'  = H^T G (I - A^T (A A^T)^-1 A), A = T   (tractions projected to be globally force-free);
 //   u_p = H'^-1 G'                               (H' symmetric: Eigen's LDL^T in the reference).
 // H' is symmetric positive definite once T spans the null space of H, so the factorisation here is
-// Cholesky (cuSOLVER potrf / potrs), the LDL^T of an SPD matrix without pivoting.  The two large
-// products are cuBLAS FP64 GEMM / SYRK (plain library GEMMs); T, the 6 x 6 projection, the rank-6
-// updates and the trace are kernels of this file, every reduction in a fixed order.
-//
-// Layout: all matrices are row-major 3V x 3V at the interface.  A row-major buffer is the
-// column-major transpose, so SYRK of the H buffer gives H^T H directly, and GEMM(N, T) of the H and
-// G' buffers gives H^T G' in column-major order, which is the right-hand side potrs expects.  The
-// column-major solution is transposed back to row-major at the end.
+// Cholesky, the LDL^T of an SPD matrix without pivoting.  The two large products (H^T G' and the lower
+// triangle of H^T H) are this library's FP64 GEMM, the Cholesky factorisation and its solves those of
+// sod_dense_kernels.cu; T, the 6 x 6 projection, the rank-6 updates and the trace are kernels of this
+// file.  Every reduction runs in a fixed order.  All matrices are row-major 3V x 3V.
 #include <cmath>
 
 #include "sod_dense.h"
@@ -186,8 +182,8 @@ __global__ void add_ttt_kernel(double *__restrict__ Hr, const double *__restrict
                                const double *__restrict__ scal) {
     const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (size_t)n * n) return;
-    const size_t j = e / n, i = e % n;  // column-major: element (i, j) at j * n + i
-    if (i < j) return;
+    const size_t i = e / n, j = e % n;  // row-major lower triangle: element (i, j), j <= i
+    if (j > i) return;
     double v = 0.0;
 #pragma unroll
     for (int a = 0; a < 6; a++) v = fma(T[(size_t)a * n + i], T[(size_t)a * n + j], v);
@@ -201,15 +197,6 @@ int rigid_modes_device(sod_context *ctx, const sod_mesh *m, double *T) {
     ctx->count();
     return SOD_OK;
 }
-
-struct Handles {
-    cusolverDnHandle_t dn = nullptr;
-    cublasHandle_t blas = nullptr;
-    ~Handles() {
-        if (dn) dense_api().dn_destroy(dn);
-        if (blas) dense_api().blas_destroy(blas);
-    }
-};
 
 }  // namespace
 
@@ -235,32 +222,12 @@ int sod_elastostatic_rigid_modes(sod_context *ctx, const sod_mesh *m, double *T)
 int sod_elastostatic_u_p(sod_context *ctx, const sod_mesh *m, const double *H, const double *G, double *u_p) {
     SOD_REQUIRE(ctx && m && m->ctx == ctx, "bad context or mesh");
     SOD_REQUIRE(H && G && u_p, "null argument");
-    const DenseApi &api = dense_api();
-    if (!api.solver_ok || !api.blas_ok) {
-        set_error(!api.solver_ok ? api.why_solver : api.why_blas);
-        return SOD_ERR_UNSUPPORTED;
-    }
     SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
     const int n = 3 * m->nV;
     const size_t nn = (size_t)n * n, bytes = sizeof(double) * nn;
     cudaStream_t st = ctx->stream;
-    Handles hd;
-    if (api.dn_create(&hd.dn) != CUSOLVER_STATUS_SUCCESS) {
-        hd.dn = nullptr;
-        set_error("cusolverDnCreate failed");
-        return SOD_ERR_CUDA;
-    }
-    if (api.blas_create(&hd.blas) != CUBLAS_STATUS_SUCCESS) {
-        hd.blas = nullptr;
-        set_error("cublasCreate failed");
-        return SOD_ERR_CUDA;
-    }
-    if (api.dn_set_stream(hd.dn, st) != CUSOLVER_STATUS_SUCCESS || api.blas_set_stream(hd.blas, st) != CUBLAS_STATUS_SUCCESS) {
-        set_error("cannot set the stream of the dense-solve handles");
-        return SOD_ERR_CUDA;
-    }
     // device copies of host inputs; Gp, the right-hand side / solution and H' are scratch
-    DevBuf dh, dg, gp, y, hr, small, info, work;
+    DevBuf dh, dg, gp, y, hr, small, info;
     const double *Hd = H, *Gd = G;
     if (!is_device_pointer(H)) {
         SOD_TRY(dh.ensure(bytes));
@@ -293,33 +260,13 @@ int sod_elastostatic_u_p(sod_context *ctx, const sod_mesh *m, const double *H, c
     project_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(Gd, GA, M, n, gp.as<double>());
     SOD_CHECK_CUDA(cudaGetLastError());
     ctx->count(3);
-    const double one = 1.0, zero = 0.0;
-    // y (column-major) = H^T Gp: the H buffer is the column-major H^T, the Gp buffer the column-major Gp^T
-    if (api.dgemm(hd.blas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, n, &one, Hd, n, gp.as<double>(), n, &zero, y.as<double>(),
-                  n) != CUBLAS_STATUS_SUCCESS) {
-        set_error("cublasDgemm failed");
-        return SOD_ERR_CUDA;
-    }
-    // H' (lower, column-major) = H^T H + c2 T^T T
-    if (api.dsyrk(hd.blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, n, &one, Hd, n, &zero, hr.as<double>(), n) !=
-        CUBLAS_STATUS_SUCCESS) {
-        set_error("cublasDsyrk failed");
-        return SOD_ERR_CUDA;
-    }
+    // y = H^T Gp (row-major), H' (lower triangle) = H^T H + c2 T^T T
+    SOD_TRY(dgemm(ctx, true, false, n, n, n, 1.0, Hd, n, gp.as<double>(), n, 0.0, y.as<double>(), n, false));
+    SOD_TRY(dgemm(ctx, true, false, n, n, n, 1.0, Hd, n, Hd, n, 0.0, hr.as<double>(), n, true));
     add_ttt_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(hr.as<double>(), T, n, scal);
     SOD_CHECK_CUDA(cudaGetLastError());
-    ctx->count(3);
-    int lwork = 0;
-    if (api.potrf_buf(hd.dn, CUBLAS_FILL_MODE_LOWER, n, hr.as<double>(), n, &lwork) != CUSOLVER_STATUS_SUCCESS) {
-        set_error("cusolverDnDpotrf_bufferSize failed");
-        return SOD_ERR_CUDA;
-    }
-    SOD_TRY(work.ensure(sizeof(double) * (size_t)std::max(lwork, 1)));
-    if (api.potrf(hd.dn, CUBLAS_FILL_MODE_LOWER, n, hr.as<double>(), n, work.as<double>(), lwork, info.as<int>()) !=
-        CUSOLVER_STATUS_SUCCESS) {
-        set_error("cusolverDnDpotrf failed");
-        return SOD_ERR_CUDA;
-    }
+    ctx->count();
+    SOD_TRY(chol_factor(ctx, hr.as<double>(), n, info.as<int>()));
     int pinfo = 0;
     SOD_CHECK_CUDA(cudaMemcpyAsync(&pinfo, info.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     SOD_CHECK_CUDA(cudaStreamSynchronize(st));
@@ -327,16 +274,9 @@ int sod_elastostatic_u_p(sod_context *ctx, const sod_mesh *m, const double *H, c
         set_error("regularised H^T H + c T^T T is not positive definite (leading minor " + std::to_string(pinfo) + ")");
         return SOD_ERR_INVALID_ARG;
     }
-    if (api.potrs(hd.dn, CUBLAS_FILL_MODE_LOWER, n, n, hr.as<double>(), n, y.as<double>(), n, info.as<int>()) !=
-        CUSOLVER_STATUS_SUCCESS) {
-        set_error("cusolverDnDpotrs failed");
-        return SOD_ERR_CUDA;
-    }
-    ctx->count(2);
-    // column-major solution -> row-major u_p
     const bool host = !is_device_pointer(u_p);
     double *dst = host ? gp.as<double>() : u_p;
-    SOD_TRY(transpose_f64(ctx, y.as<double>(), n, n, dst));
+    SOD_TRY(chol_solve(ctx, hr.as<double>(), n, n, y.as<double>(), dst));
     if (host) SOD_CHECK_CUDA(cudaMemcpyAsync(u_p, dst, bytes, cudaMemcpyDeviceToHost, st));
     SOD_CHECK_CUDA(cudaStreamSynchronize(st));
     return SOD_OK;
