@@ -392,6 +392,45 @@ def scenes_leg(torch, ctx, stream):
     return res
 
 
+def precompute_leg(torch, ctx, stream, levels=(3, 4)):
+    """Time-domain precompute (sod_cqbem_precompute: every Laplace frequency of G, H, B_trans, B_angular
+    with the compensated regular pass, the inverse transform, the free term, B_euler) of one icosphere:
+    level 3 is the single-object case (642 vertices, E 1e5, nu 0.3, dt 0.01, BDF2, N 32), level 4 the
+    2562-vertex object at the same parameters.  Device-resident FP64 outputs.  Time-domain entries =
+    L (2 (3V)^2 + 6 3V) (G, H, and B = [B_trans | B_euler]); B_angular's 27 per row ride along.  The
+    same call with the regular pass in FP32 is timed beside it (its late weights are not accurate)."""
+    from surfaceonlydeformables_gb300 import _lib as L
+    from surfaceonlydeformables_gb300 import api
+    from surfaceonlydeformables_gb300.meshes import Material, make_icosphere_mesh
+
+    res = {}
+    for level in levels:
+        m = make_icosphere_mesh(level, 0.1)
+        dm = api.Mesh(ctx, m)
+        mat = Material(1e5, 0.3, 1000.0)
+        N = 32
+        n3 = 3 * m.nV
+        row = {"vertices": m.nV, "N": N}
+        for prec, tag in ((L.PRECISION_AUTO, "compensated"), (L.PRECISION_FP32, "fp32_regular_pass")):
+            ctx.set_precision(prec)
+            w = api.precompute(ctx, dm, mat, 2, 0.01, N)
+            del w
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            w = api.precompute(ctx, dm, mat, 2, 0.01, N)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            del w
+            torch.cuda.empty_cache()
+            row[tag] = {"ms": round(ms, 2), "time_domain_entries_per_s": (N + 1) * (2 * n3 * n3 + 6 * n3) / (ms * 1e-3)}
+        ctx.set_precision(L.PRECISION_AUTO)
+        dm.close()
+        res[f"ico{m.nV}"] = row
+    return res
+
+
 def elastostatic_leg(torch, ctx, stream):
     """Elastostatic Kelvin G and H (H with the rigid-mode diagonal correction) of the 2562-vertex
     object, device-resident FP64 output."""
@@ -878,6 +917,7 @@ def run_gpu(args):
         del outs, batch
         torch.cuda.empty_cache()
         extra["history_convolution"] = history_leg(torch, ctx, stream)
+        extra["precompute"] = precompute_leg(torch, ctx, stream)
         extra["elastostatic"] = elastostatic_leg(torch, ctx, stream)
         extra["galerkin"] = galerkin_leg(torch, ctx, stream)
         extra["dense_solve"] = solve_leg(torch, ctx, stream)
@@ -938,10 +978,12 @@ def run_leg(args):
         out = history_leg(torch, ctx, stream, K=args.history_k, reps=args.steps)
     elif args.leg == "elastostatic":
         out = elastostatic_leg(torch, ctx, stream)
+    elif args.leg == "precompute":
+        out = precompute_leg(torch, ctx, stream, levels=(args.precompute_level,))
     elif args.leg == "galerkin":
         out = galerkin_leg(torch, ctx, stream, level=args.galerkin_level)
     elif args.leg == "solve":
-        out = solve_leg(torch, ctx, stream)
+        out = solve_leg(torch, ctx, stream, n=args.solve_n)
     elif args.leg == "scenes":
         out = scenes_leg(torch, ctx, stream)
     elif args.leg == "wavelet":
@@ -961,11 +1003,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop leg")
-    ap.add_argument("--leg", default="all", choices=["all", "history", "elastostatic", "galerkin", "serving", "solve", "wavelet", "scenes"],
+    ap.add_argument("--leg", default="all", choices=["all", "history", "elastostatic", "galerkin", "serving", "solve", "wavelet", "scenes",
+                                                     "precompute"],
                     help="run one hot-path leg alone (profiling captures) and print its JSON")
     ap.add_argument("--history-k", type=int, default=64, help="history length of the --leg history bank")
     ap.add_argument("--wavelet-nv", type=int, default=2562,
                     help="vertices of the --leg wavelet compressed bank (642 = the small profiling case)")
+    ap.add_argument("--solve-n", type=int, default=7686,
+                    help="matrix size of the --leg solve systems (1926: the small profiling case)")
+    ap.add_argument("--precompute-level", type=int, default=3, choices=[2, 3, 4],
+                    help="icosphere level of the --leg precompute object (2: the small profiling case)")
     ap.add_argument("--galerkin-level", type=int, default=4, choices=[3, 4],
                     help="icosphere level of the --leg galerkin mesh (3: the small profiling case)")
     ap.add_argument("--value-only", action="store_true",

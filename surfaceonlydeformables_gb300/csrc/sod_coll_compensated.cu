@@ -11,8 +11,9 @@
 // answer for a perturbed mesh, and its effect on the time-domain weights stays at ~3e-8.
 //
 // So this pass keeps the FP32 geometry of the fast pass and evaluates everything that depends on the
-// frequency in double-float arithmetic on the FP32 pipes (sod_dd.cuh: TwoSum / TwoProd, Tang's exp,
-// Cody-Waite sin/cos), with compensated sums at every level: the quadrature points of a face, the
+// frequency in double-float arithmetic on the FP32 pipes (TwoSum / TwoProd without renormalisation,
+// Tang's table-driven exp, sin/cos by reduction with pi/32 and angle addition, with the tables in
+// shared memory), with compensated sums at every level: the quadrature points of a face, the
 // faces of the row block, and the per-thread B columns.  Measured on a 162-vertex sphere, N = 16:
 // per-evaluation relative noise eps in the kernel coefficients costs ~2000 eps of stacked
 // time-domain error, and noise eps in the per-face sums ~5500 eps, so the ~1e-14 of double-float
@@ -51,19 +52,140 @@ __device__ __forceinline__ KDD kdd_from(const KConst<double> &k) {
     return d;
 }
 
+// ---- double-float arithmetic without renormalisation ----------------------------------------------
+// The pass needs ~1e-10 relative per evaluation, not the 1e-14 of renormalised double-float, so the
+// radial terms use products and sums that keep the rounding error of the high words exactly (TwoProd
+// by FMA, TwoSum) and add the low words in plain float, without the renormalising steps: the low word
+// then carries a few ulps of the high word, which is harmless at this accuracy.  Sums that cancel
+// (the psi numerator, Y, the kernel coefficients) are followed by one FastTwoSum.
+__device__ __forceinline__ dd sd_mul(dd a, dd b) {
+    const float p = a.hi * b.hi;
+    return dd{p, fmaf(a.lo, b.hi, fmaf(a.hi, b.lo, fmaf(a.hi, b.hi, -p)))};
+}
+__device__ __forceinline__ dd sd_mulf(dd a, float b) {
+    const float p = a.hi * b;
+    return dd{p, fmaf(a.lo, b, fmaf(a.hi, b, -p))};
+}
+__device__ __forceinline__ dd sd_add(dd a, dd b) {
+    const float s = a.hi + b.hi, bb = s - a.hi;
+    return dd{s, ((a.hi - (s - bb)) + (b.hi - bb)) + (a.lo + b.lo)};
+}
+__device__ __forceinline__ dd sd_neg(dd a) { return dd{-a.hi, -a.lo}; }
+__device__ __forceinline__ dd sd_sub(dd a, dd b) { return sd_add(a, sd_neg(b)); }
+// renormalisation by TwoSum: after a cancelling sum the low word can exceed the high word
+__device__ __forceinline__ dd sd_norm(dd a) { return two_sum(a.hi, a.lo); }
+__device__ __forceinline__ cdd cs_mul(const cdd &a, const cdd &b) {
+    return cdd{sd_sub(sd_mul(a.x, b.x), sd_mul(a.y, b.y)), sd_add(sd_mul(a.x, b.y), sd_mul(a.y, b.x))};
+}
+__device__ __forceinline__ cdd cs_add(const cdd &a, const cdd &b) { return cdd{sd_add(a.x, b.x), sd_add(a.y, b.y)}; }
+__device__ __forceinline__ cdd cs_sub(const cdd &a, const cdd &b) { return cdd{sd_sub(a.x, b.x), sd_sub(a.y, b.y)}; }
+__device__ __forceinline__ cdd cs_scale(const cdd &a, dd s) { return cdd{sd_mul(a.x, s), sd_mul(a.y, s)}; }
+__device__ __forceinline__ cdd cs_scalef(const cdd &a, float s) { return cdd{sd_mulf(a.x, s), sd_mulf(a.y, s)}; }
+__device__ __forceinline__ cdd cs_norm(const cdd &a) { return cdd{sd_norm(a.x), sd_norm(a.y)}; }
+
+// Tables of the exponential and sine / cosine reductions (2^(j/64) and sin, cos (j pi / 32), double-float)
+// copied to shared memory at kernel start: their indices differ from lane to lane, which the constant
+// cache would serialise.
+struct DdTabs {
+    float2 e[64];
+    float4 sc[64];
+};
+__device__ __forceinline__ void dd_tabs_load(DdTabs *t) {
+    for (int j = threadIdx.x; j < 64; j += blockDim.x) {
+        t->e[j] = make_float2(c_dd_exp2_tab[j][0], c_dd_exp2_tab[j][1]);
+        t->sc[j] = make_float4(c_dd_sincos_tab[j][0], c_dd_sincos_tab[j][1], c_dd_sincos_tab[j][2], c_dd_sincos_tab[j][3]);
+    }
+}
+
+// e^-z for z = x + iy with x >= 0: Tang's reduction of the exponent (-x = (64k + j) ln2/64 + r,
+// |r| <= ln2/128) and a reduction of the phase by pi/32 (|u| <= pi/64), short Taylor series with only
+// the leading terms in double-float (the rest is below 1e-12 of the result in float), table values
+// combined by the angle addition.  About 1e-13 relative; results below 2^-124 flush to zero.  Phases
+// beyond |y| = 400 (outside the exact range of the reduction) take FP64 sin/cos.
+__device__ __forceinline__ cdd cs_exp_neg(const cdd &z, const DdTabs *tb) {
+    dd mag;
+    {
+        const float ah = -z.x.hi;
+        if (ah < -86.0f) return cdd{dd{0.f, 0.f}, dd{0.f, 0.f}};
+        const float m = fmaf(ah, kDd64oLn2, kRound23) - kRound23;
+        const float rh0 = fmaf(-m, kDdLn2o64_1, ah);  // exact: m kDdLn2o64_1 has few bits
+        const dd p2 = two_prod(m, kDdLn2o64_2);
+        const dd r0 = two_sum(rh0, -p2.hi);
+        // renormalised: the low word of x (up to half an ulp of x, ~4e-6 at x = 80) is far above an ulp
+        // of r, and the series below drops the cross terms of the low word beyond the first order
+        const dd r = two_sum(r0.hi, r0.lo + (-z.x.lo - p2.lo - m * kDdLn2o64_3));
+        const float rl = r.lo;
+        // e^r = 1 + r + r^2/2 + r^3/6 + r^4/24 (|r| <= 0.0055: the r^2 terms and beyond in float)
+        const float h = r.hi;
+        const float q = h * h * fmaf(h, fmaf(h, 1.0f / 24.0f, 1.0f / 6.0f), 0.5f);
+        const dd one_r = fast_two_sum(1.0f, h);
+        const dd em = dd{one_r.hi, one_r.lo + fmaf(h, rl, rl + q)};
+        const int mi = (int)m, j = mi & 63, k = (mi - j) / 64;
+        const float2 t = tb->e[j];
+        const dd v = sd_mul(dd{t.x, t.y}, em);
+        const float sc = __int_as_float((k + 127) * (1 << 23));  // 2^k, k >= -124 here
+        mag = dd{v.hi * sc, v.lo * sc};
+    }
+    dd sn, cs;
+    {
+        const float yh = z.y.hi;
+        if (!(fabsf(yh) < 400.0f)) {
+            double sv, cv;
+            sincos(dd_to(z.y), &sv, &cv);
+            sn = dd_from(sv), cs = dd_from(cv);
+        } else {
+            const float m = fmaf(yh, kDd32oPi, kRound23) - kRound23;
+            const float uh0 = fmaf(-m, kDdPio32_1, yh);  // exact
+            const dd p2 = two_prod(m, kDdPio32_2);
+            const dd u0 = two_sum(uh0, -p2.hi);
+            // renormalised for the same reason (the low word of y reaches ~8e-6 at |y| = 150)
+            const dd u = two_sum(u0.hi, u0.lo + (z.y.lo - p2.lo - m * kDdPio32_3));
+            const float ul = u.lo;
+            const float h = u.hi, h2 = h * h;
+            // sin u = u - u^3/6 + u^5/120; cos u = 1 - u^2/2 + u^4/24 - u^6/720
+            const dd su = dd{h, fmaf(h * h2, fmaf(h2, 1.0f / 120.0f, -1.0f / 6.0f), ul)};
+            const dd sq = two_prod(h, h);  // u^2 high part, exactly
+            const dd c1 = fast_two_sum(1.0f, -0.5f * sq.hi);
+            const dd cu = dd{c1.hi, c1.lo + (fmaf(-h, ul, -0.5f * sq.lo) + h2 * h2 * fmaf(h2, -1.0f / 720.0f, 1.0f / 24.0f))};
+            const float4 t = tb->sc[((int)m) & 63];
+            const dd S = dd{t.x, t.y}, C = dd{t.z, t.w};
+            sn = sd_norm(sd_add(sd_mul(S, cu), sd_mul(C, su)));  // cancel near the zeros of sin / cos
+            cs = sd_norm(sd_sub(sd_mul(C, cu), sd_mul(S, su)));
+        }
+    }
+    return cdd{sd_mul(mag, cs), sd_neg(sd_mul(mag, sn))};
+}
+
+// psi(z) = ((1 + z) e^-z - 1) / z^2: the renormalised series below |z| = 0.1 (sod_dd.cuh), above it the
+// closed form, which loses ~1e-11 there
+__device__ __forceinline__ cdd cs_psi(const cdd &z, const cdd &ez) {
+    const float az2 = z.x.hi * z.x.hi + z.y.hi * z.y.hi;
+    if (az2 < 0.01f) return cdd_psi(z, ez);
+    cdd num = cs_mul(cdd{sd_add(z.x, dd{1.0f, 0.0f}), z.y}, ez);
+    num.x = sd_norm(sd_add(num.x, dd{-1.0f, 0.0f}));
+    num.y = sd_norm(num.y);
+    const cdd zz = cs_norm(cs_mul(z, z));
+    const dd n2 = sd_norm(sd_add(sd_mul(zz.x, zz.x), sd_mul(zz.y, zz.y)));
+    // 1 / n2: float reciprocal and one Newton step
+    const float y = 1.0f / n2.hi;
+    const dd e = sd_norm(sd_sub(dd{1.0f, 0.0f}, sd_mulf(n2, y)));
+    const dd inv = dd{y, e.hi * y};
+    return cs_mul(num, cdd{sd_mul(zz.x, inv), sd_neg(sd_mul(zz.y, inv))});
+}
+
 struct RadDD {
     cdd z1, z2, e1, e2, psi2, Y;
 };
 // the frequency-dependent radial terms at distance r (an exact float)
-__device__ __forceinline__ RadDD radial_dd(float r, const KDD &k) {
+__device__ __forceinline__ RadDD radial_dd(float r, const KDD &k, const DdTabs *tb) {
     RadDD t;
-    t.z1 = cdd{k.sc1.x * r, k.sc1.y * r};
-    t.z2 = cdd{k.sc2.x * r, k.sc2.y * r};
-    t.e1 = cdd_exp_neg(t.z1);
-    t.e2 = cdd_exp_neg(t.z2);
-    const cdd psi1 = cdd_psi(t.z1, t.e1);
-    t.psi2 = cdd_psi(t.z2, t.e2);
-    t.Y = psi1 * k.ic1s - t.psi2 * k.ic2s;
+    t.z1 = cs_scalef(k.sc1, r);
+    t.z2 = cs_scalef(k.sc2, r);
+    t.e1 = cs_exp_neg(t.z1, tb);
+    t.e2 = cs_exp_neg(t.z2, tb);
+    const cdd psi1 = cs_psi(t.z1, t.e1);
+    t.psi2 = cs_psi(t.z2, t.e2);
+    t.Y = cs_norm(cs_sub(cs_scale(psi1, k.ic1s), cs_scale(t.psi2, k.ic2s)));
     return t;
 }
 
@@ -94,7 +216,8 @@ __device__ __forceinline__ cdd cdd_scale(const cdd &a, float s) { return cdd{a.x
 // slice; layout [NC][nV] float4.
 template <int KIND>
 __device__ __forceinline__ void comp_scatter_body(const CollArgs &a, const PointTable &pt, const KConst<double> &kd,
-                                                  int i, int fq, float4 *acc, ColourBar *cb, unsigned &phase) {
+                                                  int i, int fq, float4 *acc, ColourBar *cb, unsigned &phase,
+                                                  const DdTabs *tb) {
     constexpr int NC = KIND == SOD_G ? 6 : 9;
     const int nV = a.nV;
     const KDD k = kdd_from(kd);
@@ -125,41 +248,45 @@ __device__ __forceinline__ void comp_scatter_body(const CollArgs &a, const Point
                     const float rinv = rsqrtf(r2);
                     const float r = r2 * rinv;
                     const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                    const RadDD t = radial_dd(r, k);
+                    const RadDD t = radial_dd(r, k, tb);
                     cdd u[NC];
                     if (KIND == SOD_G) {
                         // alpha = (3Y + e1/c1^2 - e2/c2^2) / (4 pi rho r), beta = (e2/c2^2 - Y) / (4 pi rho r)
-                        const dd p = k.inv4pirho * rinv;
-                        const cdd C2 = cdd_scale(t.e2, k.ic2s);
-                        const cdd al = cdd_scale(cdd_scale(t.Y, 3.0f) + cdd_scale(t.e1, k.ic1s) - C2, p);
-                        const cdd be = cdd_scale(C2 - t.Y, p);
+                        const dd p = sd_mulf(k.inv4pirho, rinv);
+                        const cdd C2 = cs_scale(t.e2, k.ic2s);
+                        const cdd al = cs_scale(cs_norm(cs_sub(cs_add(cs_scalef(t.Y, 3.0f), cs_scale(t.e1, k.ic1s)), C2)), p);
+                        const cdd be = cs_scale(cs_norm(cs_sub(C2, t.Y)), p);
 #pragma unroll
                         for (int pp = 0; pp < 3; pp++)
 #pragma unroll
                             for (int qq = pp; qq < 3; qq++) {
-                                cdd v = cdd_scale(al, rh[pp] * rh[qq]);
-                                if (pp == qq) v = v + be;
+                                cdd v = cs_scalef(al, rh[pp] * rh[qq]);
+                                if (pp == qq) v = cs_add(v, be);
                                 u[sym_index(pp, qq)] = v;
                             }
                     } else {
                         // a, b, d of the traction kernel, scaled by 1 / (4 pi r^2)
-                        const cdd Yc = cdd_scale(t.Y, k.six_c2s);
-                        const cdd z1e1 = t.z1 * t.e1, z2e2 = t.z2 * t.e2;
-                        const dd p = k.inv4pi * (rinv * rinv);
-                        const cdd ha = cdd_scale(Yc + cdd_scale(t.e1, k.k4m1) - cdd_scale(t.e2, 2.0f) - cdd_scale(z1e1, k.k1m2), p);
-                        const cdd hb = cdd_scale(Yc + cdd_scale(t.e1, k.k2) - cdd_scale(t.e2, 3.0f) - z2e2, p);
-                        const cdd hd = cdd_scale(cdd_scale(z2e2, 2.0f) - cdd_scale(z1e1, k.k2) + cdd_scale(t.e2, 12.0f) -
-                                                     cdd_scale(t.e1, k.k12) - cdd_scale(Yc, 5.0f),
-                                                 p);
+                        const cdd Yc = cs_scale(t.Y, k.six_c2s);
+                        const cdd z1e1 = cs_mul(t.z1, t.e1), z2e2 = cs_mul(t.z2, t.e2);
+                        const dd p = sd_mulf(k.inv4pi, rinv * rinv);
+                        const cdd ha = cs_scale(cs_norm(cs_sub(cs_sub(cs_add(Yc, cs_scale(t.e1, k.k4m1)), cs_scalef(t.e2, 2.0f)),
+                                                               cs_scale(z1e1, k.k1m2))),
+                                                p);
+                        const cdd hb = cs_scale(cs_norm(cs_sub(cs_sub(cs_add(Yc, cs_scale(t.e1, k.k2)), cs_scalef(t.e2, 3.0f)), z2e2)), p);
+                        const cdd hd = cs_scale(
+                            cs_norm(cs_sub(cs_sub(cs_add(cs_sub(cs_scalef(z2e2, 2.0f), cs_scale(z1e1, k.k2)), cs_scalef(t.e2, 12.0f)),
+                                                  cs_scale(t.e1, k.k12)),
+                                           cs_scalef(Yc, 5.0f))),
+                            p);
                         const float rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
-                        const cdd hdr = cdd_scale(hd, rn), hbr = cdd_scale(hb, rn);
+                        const cdd hdr = cs_scalef(hd, rn), hbr = cs_scalef(hb, rn);
 #pragma unroll
                         for (int pp = 0; pp < 3; pp++)
 #pragma unroll
                             for (int qq = 0; qq < 3; qq++) {
-                                cdd v = cdd_scale(hdr, rh[pp] * rh[qq]) + cdd_scale(hb, nn[pp] * rh[qq]) +
-                                        cdd_scale(ha, rh[pp] * nn[qq]);
-                                if (pp == qq) v = v + hbr;
+                                cdd v = cs_add(cs_add(cs_scalef(hdr, rh[pp] * rh[qq]), cs_scalef(hb, nn[pp] * rh[qq])),
+                                               cs_scalef(ha, rh[pp] * nn[qq]));
+                                if (pp == qq) v = cs_add(v, hbr);
                                 u[3 * pp + qq] = v;
                             }
                     }
@@ -224,9 +351,11 @@ __global__ void __launch_bounds__(COMP_SCATTER_THREADS) comp_scatter_kernel(Coll
                                                                           const __grid_constant__ FreqTable ft) {
     extern __shared__ float4 acc4[];
     __shared__ ColourBar cb;
+    __shared__ DdTabs tb;
+    dd_tabs_load(&tb);
     colour_bar_init(&cb, a.bar_extra);
     unsigned phase = 0;
-    comp_scatter_body<KIND>(a, pt, ft.kd[blockIdx.y], a.i0 + blockIdx.x, blockIdx.y, acc4, &cb, phase);
+    comp_scatter_body<KIND>(a, pt, ft.kd[blockIdx.y], a.i0 + blockIdx.x, blockIdx.y, acc4, &cb, phase, &tb);
 }
 
 // persistent grid, each CTA's row block in its own slice of global memory (L2-resident)
@@ -237,12 +366,14 @@ __global__ void __launch_bounds__(COMP_SCATTER_THREADS) comp_scatter_global_kern
                                                                                  int nvert) {
     float4 *acc = scratch + (size_t)blockIdx.x * per_cta;
     __shared__ ColourBar cb;
+    __shared__ DdTabs tb;
+    dd_tabs_load(&tb);
     colour_bar_init(&cb, a.bar_extra);
     unsigned phase = 0;
     const int items = nvert * ft.n;
     for (int it = blockIdx.x; it < items; it += gridDim.x) {
         const int fq = it / nvert, i = a.i0 + it % nvert;
-        comp_scatter_body<KIND>(a, pt, ft.kd[fq], i, fq, acc, &cb, phase);
+        comp_scatter_body<KIND>(a, pt, ft.kd[fq], i, fq, acc, &cb, phase, &tb);
         __syncthreads();
     }
 }
@@ -259,6 +390,8 @@ __global__ void __launch_bounds__(COMP_REDUCE_THREADS) comp_reduce_kernel(CollAr
     constexpr int NT = BT ? 6 : 0, NA = BA ? 18 : 0, NCB = NT + NA;
     extern __shared__ float4 colB[];  // [NCB][T]
     __shared__ cd bsum[24];
+    __shared__ DdTabs tb;
+    dd_tabs_load(&tb);
     const int i = a.i0 + blockIdx.x, fq = blockIdx.y;
     const KDD k = kdd_from(ft.kd[fq]);
     const int T = blockDim.x;
@@ -266,6 +399,7 @@ __global__ void __launch_bounds__(COMP_REDUCE_THREADS) comp_reduce_kernel(CollAr
     for (int cc = 0; cc < NCB; cc++) colB[cc * T + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
     const float3 x = make_float3(a.Vf[3 * i], a.Vf[3 * i + 1], a.Vf[3 * i + 2]);
     const int ci = a.canonV ? a.canonV[i] : i;
+    __syncthreads();  // the tables
     // B_trans / B_angular scalar factors (with 1/(4 pi))
     const dd hp = k.inv4pi * 0.5f;
     const dd dia_f = k.ic2s * k.inv4pi;
@@ -291,7 +425,7 @@ __global__ void __launch_bounds__(COMP_REDUCE_THREADS) comp_reduce_kernel(CollAr
                 const float rinv = rsqrtf(r2);
                 const float r = r2 * rinv;
                 const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                const RadDD t = radial_dd(r, k);
+                const RadDD t = radial_dd(r, k, &tb);
                 const float w = P.w;
                 if (BT) {
                     const cdd ws = cdd_scale(t.Y, hp * w);

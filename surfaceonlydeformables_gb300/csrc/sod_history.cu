@@ -94,17 +94,16 @@ __device__ __forceinline__ void load_w(const __nv_bfloat16 *w, float v[8]) {
 // per SM, BF16 (whose weights unpack into twice the registers) with 4 rows per warp at 4 CTAs per SM
 template <int R, int RW, class WT> constexpr int hist_min_ctas() { return R == 1 ? (RW == 8 ? 2 : 4) : 1; }
 
+// one (column chunk bx, row block by) tile of a bank; shared by the per-bank and the grouped kernels
 template <int R, int RW, class WT>
-__global__ void __launch_bounds__(HIST_THREADS, hist_min_ctas<R, RW, WT>()) hist_conv_kernel(const WT *__restrict__ W,
-                                                                 const float *__restrict__ scale,
-                                                                 const float *__restrict__ X, int used, int head,
-                                                                 int K, int nrow, int ldw, int cchunk,
-                                                                 double *__restrict__ partial) {
+__device__ __forceinline__ void hist_conv_tile(const WT *__restrict__ W, const float *__restrict__ scale,
+                                               const float *__restrict__ X, int used, int head, int K, int nrow,
+                                               int ldw, int cchunk, double *__restrict__ partial, int bx, int by) {
     constexpr int VEC = WVec<WT>::VEC;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row0 = (blockIdx.y * (HIST_THREADS / 32) + warp) * RW;
+    const int row0 = (by * (HIST_THREADS / 32) + warp) * RW;
     if (row0 >= nrow) return;
-    const int c0 = blockIdx.x * cchunk, c1 = min(ldw, c0 + cchunk);
+    const int c0 = bx * cchunk, c1 = min(ldw, c0 + cchunk);
     float acc[RW][R];
 #pragma unroll
     for (int r = 0; r < RW; r++)
@@ -179,16 +178,23 @@ __global__ void __launch_bounds__(HIST_THREADS, hist_min_ctas<R, RW, WT>()) hist
             double v = acc[r][j];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0 && row0 + r < nrow) partial[((size_t)blockIdx.x * nrow + row0 + r) * R + j] = v;
+            if (lane == 0 && row0 + r < nrow) partial[((size_t)bx * nrow + row0 + r) * R + j] = v;
         }
 }
 
+template <int R, int RW, class WT>
+__global__ void __launch_bounds__(HIST_THREADS, hist_min_ctas<R, RW, WT>()) hist_conv_kernel(const WT *__restrict__ W,
+                                                                 const float *__restrict__ scale,
+                                                                 const float *__restrict__ X, int used, int head,
+                                                                 int K, int nrow, int ldw, int cchunk,
+                                                                 double *__restrict__ partial) {
+    hist_conv_tile<R, RW, WT>(W, scale, X, used, head, K, nrow, ldw, cchunk, partial, blockIdx.x, blockIdx.y);
+}
+
 // b[row][j] = sum_chunks partial + sum_i B_{i+1}[row][:] a_slot[:][j]   (FP64, fixed order)
-__global__ void hist_finish_kernel(const double *__restrict__ partial, int nchunk, const double *__restrict__ Bw,
-                                   const double *__restrict__ A, int used, int head, int K, int nrow, int R,
-                                   double *__restrict__ out) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= nrow * R) return;
+__device__ __forceinline__ void hist_finish_elem(const double *__restrict__ partial, int nchunk,
+                                                 const double *__restrict__ Bw, const double *__restrict__ A, int used,
+                                                 int head, int K, int nrow, int R, double *__restrict__ out, int e) {
     const int row = e / R, j = e % R;
     double s = 0.0;
     for (int c = 0; c < nchunk; c++) s += partial[(size_t)c * nrow * R + e];
@@ -201,6 +207,13 @@ __global__ void hist_finish_kernel(const double *__restrict__ partial, int nchun
         }
     }
     out[e] = s;
+}
+__global__ void hist_finish_kernel(const double *__restrict__ partial, int nchunk, const double *__restrict__ Bw,
+                                   const double *__restrict__ A, int used, int head, int K, int nrow, int R,
+                                   double *__restrict__ out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nrow * R) return;
+    hist_finish_elem(partial, nchunk, Bw, A, used, head, K, nrow, R, out, e);
 }
 
 // One matrix (nrow x ncol, FP64 or FP32, row-major) -> bank layout, with `sign` and per-row scale.
@@ -273,6 +286,57 @@ __global__ void hist_push_kernel(const double *__restrict__ p, const double *__r
         }
     }
     if (e < 6 * R) A[(size_t)slot * 6 * R + e] = a ? a[e] : 0.0;
+}
+
+// ---- one step of several banks in three launches (the request loop's grouped steps) -----------------
+// FP32 banks with one right-hand side on the CUDA-core engine.  Each bank's push, convolution tiles
+// and finish run the same device code with the same tiling as sod_history_push + sod_history_convolve,
+// so a bank's result is bitwise the same in a group and alone.
+struct GroupBank {
+    const float *W;
+    float *X;
+    double *partial, *A, *out;
+    const double *Bw, *p, *u;
+    int used, head, slot, K, nrow, ncol, ldw, cchunk, nchunk, gy;
+};
+struct GroupArgs {
+    int n;
+    int push_off[HIST_GROUP_MAX + 1], conv_off[HIST_GROUP_MAX + 1], fin_off[HIST_GROUP_MAX + 1];
+    GroupBank b[HIST_GROUP_MAX];
+};
+static_assert(sizeof(GroupArgs) <= 16000, "grouped-step arguments exceed the kernel parameter space");
+__device__ __forceinline__ int group_of(const int *off, int n, int e) {
+    int g = 0;
+    while (g + 1 < n && off[g + 1] <= e) g++;
+    return g;
+}
+__global__ void hist_group_push_kernel(const __grid_constant__ GroupArgs ga) {
+    const int e0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e0 >= ga.push_off[ga.n]) return;
+    const int g = group_of(ga.push_off, ga.n, e0);
+    const GroupBank &b = ga.b[g];
+    const int e = e0 - ga.push_off[g];
+    if (e < b.ldw) {
+        float *x = b.X + (size_t)b.slot * 2 * b.ldw;
+        x[e] = e < b.ncol ? (float)b.p[e] : 0.0f;
+        x[(size_t)b.ldw + e] = e < b.ncol ? (float)b.u[e] : 0.0f;
+    }
+    if (e < 6) b.A[(size_t)b.slot * 6 + e] = 0.0;
+}
+__global__ void __launch_bounds__(HIST_THREADS, hist_min_ctas<1, 8, float>()) hist_group_conv_kernel(
+    const __grid_constant__ GroupArgs ga) {
+    const int g = group_of(ga.conv_off, ga.n, blockIdx.x);
+    const GroupBank &b = ga.b[g];
+    const int t = blockIdx.x - ga.conv_off[g];
+    hist_conv_tile<1, 8, float>(b.W, nullptr, b.X, b.used, b.head, b.K, b.nrow, b.ldw, b.cchunk, b.partial,
+                                t % b.nchunk, t / b.nchunk);
+}
+__global__ void hist_group_finish_kernel(const __grid_constant__ GroupArgs ga) {
+    const int e0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e0 >= ga.fin_off[ga.n]) return;
+    const int g = group_of(ga.fin_off, ga.n, e0);
+    const GroupBank &b = ga.b[g];
+    hist_finish_elem(b.partial, b.nchunk, b.Bw, b.A, b.used, b.head, b.K, b.nrow, 1, b.out, e0 - ga.fin_off[g]);
 }
 
 template <int R, int RW, class WT>
@@ -619,3 +683,54 @@ int sod_history_destroy(sod_history *h) {
 }
 
 }  // extern "C"
+
+namespace sod {
+bool history_groupable(const sod_history *h) {
+    return h && !h->wav && h->wdtype == SOD_F32 && h->R == 1 && !h->use_tensor() && h->ctx;
+}
+// One step of each of n banks (all groupable, distinct, on contexts sharing ctx's stream): push p[g], u[g]
+// (device, ncol doubles) and b[g] (device, nrow doubles) = the convolution, in three launches.
+int history_step_group(sod_context *ctx, sod_history *const *banks, int n, const double *const *p,
+                       const double *const *u, double *const *b) {
+    SOD_REQUIRE(n >= 1 && n <= HIST_GROUP_MAX, "group of 1..HIST_GROUP_MAX banks");
+    GroupArgs ga{};
+    ga.n = n;
+    int push = 0, conv = 0, fin = 0;
+    for (int g = 0; g < n; g++) {
+        sod_history *h = banks[g];
+        SOD_REQUIRE(history_groupable(h), "grouped steps need FP32 banks with one right-hand side");
+        for (int q = 0; q < g; q++) SOD_REQUIRE(banks[q] != h, "a bank appears twice in one group");
+        const int rows_per_cta = (HIST_THREADS / 32) * 8;
+        GroupBank &gb = ga.b[g];
+        gb.W = h->W.as<float>();
+        gb.X = h->X.as<float>();
+        gb.partial = h->partial.as<double>();
+        gb.A = h->A.as<double>();
+        gb.out = b[g];
+        gb.Bw = h->has_b ? h->Bw.as<double>() : nullptr;
+        gb.p = p[g];
+        gb.u = u[g];
+        gb.slot = h->head;
+        gb.head = (h->head + 1) % h->K;
+        gb.used = std::min(h->count + 1, h->K);
+        gb.K = h->K, gb.nrow = h->nrow, gb.ncol = h->ncol, gb.ldw = h->ldw, gb.cchunk = h->cchunk, gb.nchunk = h->nchunk;
+        gb.gy = (h->nrow + rows_per_cta - 1) / rows_per_cta;
+        ga.push_off[g] = push, ga.conv_off[g] = conv, ga.fin_off[g] = fin;
+        push += std::max(h->ldw, 6);
+        conv += h->nchunk * gb.gy;
+        fin += h->nrow;
+    }
+    ga.push_off[n] = push, ga.conv_off[n] = conv, ga.fin_off[n] = fin;
+    cudaStream_t st = ctx->stream;
+    hist_group_push_kernel<<<(push + 255) / 256, 256, 0, st>>>(ga);
+    hist_group_conv_kernel<<<conv, HIST_THREADS, 0, st>>>(ga);
+    hist_group_finish_kernel<<<(fin + 255) / 256, 256, 0, st>>>(ga);
+    SOD_CHECK_CUDA(cudaGetLastError());
+    ctx->count(3);
+    for (int g = 0; g < n; g++) {
+        banks[g]->head = ga.b[g].head;
+        banks[g]->count = ga.b[g].used;
+    }
+    return SOD_OK;
+}
+}  // namespace sod

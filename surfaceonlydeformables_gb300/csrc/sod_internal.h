@@ -310,6 +310,14 @@ int64_t wavelet_bytes(const WaveletBank *w);
 int wavelet_block(const WaveletBank *w, int b, int64_t *nnz, int *row_ptr, int *col, double *val, cudaStream_t st);
 int wavelet_dims(const WaveletBank *w, int *N, int *L);
 
+// One time step of several history banks in three launches (sod_history.cu), for the request loop:
+// FP32 banks with one right-hand side on the CUDA-core engine, each bank at most once; p, u, b device
+// vectors per bank.  A bank's b is bitwise the same as from sod_history_push + sod_history_convolve.
+constexpr int HIST_GROUP_MAX = 48;
+bool history_groupable(const sod_history *h);
+int history_step_group(sod_context *ctx, sod_history *const *banks, int n, const double *const *p,
+                       const double *const *u, double *const *b);
+
 // dense LU solves (sod_solve.cu); X = A^-1 B, row-major device buffers, X may alias B
 int solver_size(const sod_solver *s);
 int solver_solve_device(sod_solver *s, int nrhs, const double *B, double *X);

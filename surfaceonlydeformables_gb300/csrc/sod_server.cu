@@ -12,7 +12,9 @@
 //   * `slots` assembly threads, each with its own context and stream, run admitted assemblies
 //     concurrently with each other and with the steps;
 //   * one step stream (the scheduler's context) runs the steps of all objects in arrival order per
-//     object, through a ring of pinned host / device staging slots;
+//     object: each dispatch groups one pending step of every ready object (up to HIST_GROUP_MAX) into
+//     one host-to-device copy, three launches (push, convolution tiles of every bank, finish) and one
+//     device-to-host copy, through a ring of pinned host / device staging slots;
 //   * a janitor thread frees evicted objects (cudaFree may wait for the device).
 // Admission: an assembly is admitted while a slot is free and the bytes of resident banks plus
 // in-flight assembly buffers stay under the HBM cap; least recently used idle objects are evicted
@@ -64,12 +66,15 @@ struct Object {
     std::deque<Request *> steps;
 };
 
+// One group of time steps in flight: at most one step per object, all run by three launches
+// (history_step_group).  Pinned and device buffers hold the members' [p | u] back to back, then their b.
 struct StepSlot {
-    double *hbuf = nullptr;  // pinned: p, u, b
-    double *dbuf = nullptr;  // device: p, u, b
+    double *hbuf = nullptr;  // pinned
+    double *dbuf = nullptr;  // device
     cudaEvent_t ev = nullptr;
-    Request *req = nullptr;
-    Object *obj = nullptr;
+    std::vector<Request *> reqs;
+    std::vector<Object *> objs;
+    std::vector<size_t> boff;  // offset of each member's b
 };
 
 struct AsmDone {
@@ -347,13 +352,16 @@ void scheduler_main(sod_server *s) {
         // finished steps
         for (size_t k = 0; k < s->ring.size(); k++) {
             StepSlot &st = s->ring[k];
-            if (!st.req || cudaEventQuery(st.ev) != cudaSuccess) continue;
-            st.req->b.assign(st.hbuf + 2 * st.obj->n, st.hbuf + 3 * st.obj->n);
-            st.obj->pending--;
-            st.obj->last_use = Clock::now();
-            complete(s, st.req, SOD_OK);
-            st.req = nullptr;
-            st.obj = nullptr;
+            if (st.reqs.empty() || cudaEventQuery(st.ev) != cudaSuccess) continue;
+            for (size_t g = 0; g < st.reqs.size(); g++) {
+                Object *o = st.objs[g];
+                st.reqs[g]->b.assign(st.hbuf + st.boff[g], st.hbuf + st.boff[g] + o->n);
+                o->pending--;
+                o->last_use = Clock::now();
+                complete(s, st.reqs[g], SOD_OK);
+            }
+            st.reqs.clear();
+            st.objs.clear();
             s->free_ring.push_back((int)k);
             progress = true;
         }
@@ -399,38 +407,62 @@ void scheduler_main(sod_server *s) {
             free_slot->cv.notify_one();
             progress = true;
         }
-        // dispatch steps of ready objects (per object in arrival order, one staging slot each)
-        for (auto &kv : s->objects) {
-            Object *o = kv.second.get();
-            while (o->ready && !o->steps.empty() && !s->free_ring.empty()) {
+        // dispatch steps of ready objects in groups: one step of each object with work per group (an
+        // object's steps stay in arrival order: later groups run after earlier ones on the step stream)
+        while (!s->free_ring.empty()) {
+            std::vector<Object *> members;
+            for (auto &kv : s->objects) {
+                Object *o = kv.second.get();
+                if (o->ready && !o->steps.empty()) members.push_back(o);
+                if ((int)members.size() == HIST_GROUP_MAX) break;
+            }
+            if (members.empty()) break;
+            const int k = s->free_ring.front();
+            s->free_ring.pop_front();
+            StepSlot &st = s->ring[k];
+            size_t in = 0;
+            for (Object *o : members) in += 2 * (size_t)o->n;
+            std::vector<const double *> dp, du;
+            std::vector<double *> db;
+            std::vector<sod_history *> banks;
+            size_t off = 0, bo = in;
+            for (Object *o : members) {
                 Request *r = o->steps.front();
                 o->steps.pop_front();
-                const int k = s->free_ring.front();
-                s->free_ring.pop_front();
-                StepSlot &st = s->ring[k];
-                const int n = o->n;
-                std::memcpy(st.hbuf, r->p.data(), sizeof(double) * n);
-                std::memcpy(st.hbuf + n, r->u.data(), sizeof(double) * n);
-                cudaStream_t ss = s->step_ctx->stream;
-                int rc = cudaMemcpyAsync(st.dbuf, st.hbuf, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, ss) == cudaSuccess
-                             ? SOD_OK
-                             : SOD_ERR_CUDA;
-                if (rc == SOD_OK) rc = sod_history_push(o->bank, st.dbuf, st.dbuf + n, nullptr);
-                if (rc == SOD_OK) rc = sod_history_convolve(o->bank, st.dbuf + 2 * n);
-                if (rc == SOD_OK && cudaMemcpyAsync(st.hbuf + 2 * n, st.dbuf + 2 * n, sizeof(double) * n,
-                                                    cudaMemcpyDeviceToHost, ss) != cudaSuccess)
-                    rc = SOD_ERR_CUDA;
-                if (rc == SOD_OK && cudaEventRecord(st.ev, ss) != cudaSuccess) rc = SOD_ERR_CUDA;
-                if (rc != SOD_OK) {
-                    o->pending--;
-                    s->free_ring.push_back(k);
-                    complete(s, r, rc);
-                    continue;
-                }
-                st.req = r;
-                st.obj = o;
-                progress = true;
+                std::memcpy(st.hbuf + off, r->p.data(), sizeof(double) * o->n);
+                std::memcpy(st.hbuf + off + o->n, r->u.data(), sizeof(double) * o->n);
+                dp.push_back(st.dbuf + off);
+                du.push_back(st.dbuf + off + o->n);
+                db.push_back(st.dbuf + bo);
+                banks.push_back(o->bank);
+                st.reqs.push_back(r);
+                st.objs.push_back(o);
+                st.boff.resize(st.reqs.size());
+                st.boff.back() = bo;
+                off += 2 * (size_t)o->n;
+                bo += o->n;
             }
+            cudaStream_t ss = s->step_ctx->stream;
+            int rc = cudaMemcpyAsync(st.dbuf, st.hbuf, sizeof(double) * in, cudaMemcpyHostToDevice, ss) == cudaSuccess
+                         ? SOD_OK
+                         : SOD_ERR_CUDA;
+            if (rc == SOD_OK)
+                rc = history_step_group(s->step_ctx, banks.data(), (int)banks.size(), dp.data(), du.data(), db.data());
+            if (rc == SOD_OK && cudaMemcpyAsync(st.hbuf + in, st.dbuf + in, sizeof(double) * (bo - in),
+                                                cudaMemcpyDeviceToHost, ss) != cudaSuccess)
+                rc = SOD_ERR_CUDA;
+            if (rc == SOD_OK && cudaEventRecord(st.ev, ss) != cudaSuccess) rc = SOD_ERR_CUDA;
+            if (rc != SOD_OK) {
+                for (size_t g = 0; g < st.reqs.size(); g++) {
+                    st.objs[g]->pending--;
+                    complete(s, st.reqs[g], rc);
+                }
+                st.reqs.clear();
+                st.objs.clear();
+                s->free_ring.push_back(k);
+                continue;
+            }
+            progress = true;
         }
         if (!progress) std::this_thread::yield();
     }
@@ -460,13 +492,13 @@ int sod_server_create(int device, int64_t hbm_cap_bytes, int slots, int max_vert
         SOD_CHECK_CUDA(cudaStreamDestroy(s->step_ctx->own_stream));
         s->step_ctx->own_stream = s->step_ctx->stream = hs;
     }
-    constexpr int RING = 32;
+    constexpr int RING = 6;  // groups in flight
     s->ring.resize(RING);
+    const size_t gbytes = sizeof(double) * 3 * (size_t)s->vmax_n * HIST_GROUP_MAX;
     for (int k = 0; k < RING; k++) {
         StepSlot &st = s->ring[k];
-        SOD_CHECK_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&st.hbuf), sizeof(double) * 3 * s->vmax_n,
-                                     cudaHostAllocDefault));
-        SOD_CHECK_CUDA(cudaMalloc(reinterpret_cast<void **>(&st.dbuf), sizeof(double) * 3 * s->vmax_n));
+        SOD_CHECK_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&st.hbuf), gbytes, cudaHostAllocDefault));
+        SOD_CHECK_CUDA(cudaMalloc(reinterpret_cast<void **>(&st.dbuf), gbytes));
         SOD_CHECK_CUDA(cudaEventCreateWithFlags(&st.ev, cudaEventDisableTiming));
         s->free_ring.push_back(k);
     }
