@@ -923,7 +923,7 @@ def run_gpu(args):
         extra["dense_solve"] = solve_leg(torch, ctx, stream)
         extra["reference_scenes"] = scenes_leg(torch, ctx, stream)
         if not args.no_serve:
-            extra["serving"] = serving_leg(torch, ctx)
+            extra["serving"] = serving_leg(torch, ctx, n_requests=args.serve_requests, rate_hz=args.serve_rate)
 
     # ---- CPU baseline (rank 0, N = 1 only) ----
     cpu = None
@@ -989,7 +989,7 @@ def run_leg(args):
     elif args.leg == "wavelet":
         out = wavelet_case(torch, ctx, stream, args.wavelet_nv, args.history_k, 0.1, args.steps, measured_hbm_gbs())
     else:
-        out = serving_leg(torch, ctx)
+        out = serving_leg(torch, ctx, n_requests=args.serve_requests, rate_hz=args.serve_rate)
     print(json.dumps({"leg": args.leg, **out}))
     return 0
 
@@ -1009,6 +1009,8 @@ def main():
     ap.add_argument("--history-k", type=int, default=64, help="history length of the --leg history bank")
     ap.add_argument("--wavelet-nv", type=int, default=2562,
                     help="vertices of the --leg wavelet compressed bank (642 = the small profiling case)")
+    ap.add_argument("--serve-requests", type=int, default=240, help="requests of the serving leg")
+    ap.add_argument("--serve-rate", type=float, default=150.0, help="Poisson arrival rate of the serving leg (req/s)")
     ap.add_argument("--solve-n", type=int, default=7686,
                     help="matrix size of the --leg solve systems (1926: the small profiling case)")
     ap.add_argument("--precompute-level", type=int, default=3, choices=[2, 3, 4],
