@@ -516,14 +516,51 @@ template <class F> static int raise_smem(sod_context *ctx, F fn) {
     return SOD_OK;
 }
 
-int comp_scatter_threads() { return COMP_SCATTER_THREADS; }
+// CTA size of the compensated scatter for a mesh and kind.  A colour holds at most T faces and the
+// CTA waits for each colour's adds, so on small meshes (a few hundred faces in ~10 colours) a 256-thread
+// CTA leaves most lanes idle at every colour; smaller CTAs, several per SM, keep them busy.  Cost model
+// as for the fast pass: colours x T / occupancy, occupancy = resident warps per SM / 8 (the registers
+// of these kernels allow 8 warps of 256 threads), capped at 1.  Row blocks beyond shared memory run in
+// the global-memory variant with 256 threads.  Cached on the mesh.
+int comp_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int *threads) {
+    const int key = 8192 + kind;
+    std::lock_guard<std::recursive_mutex> lock(m->sched_mu);
+    auto it = m->tuned.find(key);
+    if (it != m->tuned.end()) {
+        *threads = it->second;
+        return SOD_OK;
+    }
+    const size_t smem = comp_row_bytes(kind, m->nV);
+    const void *fn = kind == SOD_G ? (const void *)comp_scatter_kernel<SOD_G> : (const void *)comp_scatter_kernel<SOD_H>;
+    cudaFuncAttributes attr;
+    SOD_CHECK_CUDA(cudaFuncGetAttributes(&attr, fn));
+    int best_t = COMP_SCATTER_THREADS;
+    if (smem + attr.sharedSizeBytes <= ctx->smem_optin) {
+        if (kind == SOD_G) SOD_TRY(raise_smem(ctx, comp_scatter_kernel<SOD_G>));
+        else SOD_TRY(raise_smem(ctx, comp_scatter_kernel<SOD_H>));
+        double best = 1e300;
+        for (int T = 32; T <= COMP_SCATTER_THREADS; T *= 2) {
+            int per_sm = 0;
+            SOD_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, T, smem));
+            if (per_sm <= 0) continue;
+            const sod_mesh::Coloured *col = nullptr;
+            SOD_TRY(m->coloured_for(T, &col));
+            const double occ = std::min(1.0, (double)per_sm * T / 32.0 / 8.0);
+            const double cost = (double)col->ncolors * T / occ;
+            if (cost < best * 0.999) best = cost, best_t = T;
+        }
+    }
+    m->tuned[key] = best_t;
+    *threads = best_t;
+    return SOD_OK;
+}
 
 // The regular pass of one chunk of field vertices [a.i0, a.i0 + nvert) for the kinds in `mask`:
-// G / H through the compensated scatter (faces/colours of `colG` / `colH`, coloured for
-// COMP_SCATTER_THREADS), B kinds through the compensated reduction (natural face order).
+// G / H through the compensated scatter (faces/colours of `colG` / `colH`, coloured for threads[kind]
+// from comp_scatter_threads), B kinds through the compensated reduction (natural face order).
 int launch_regular_compensated(sod_context *ctx, const sod_mesh *m, CollArgs a, int mask,
-                               const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, const PointTable &pt,
-                               const FreqTable &ft, int nvert, cudaStream_t stream) {
+                               const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, const int threads[2],
+                               const PointTable &pt, const FreqTable &ft, int nvert, cudaStream_t stream) {
     const dim3 grid(nvert, ft.n);
     for (int kd = 0; kd < 2; kd++) {
         if (!(mask & (1 << kd))) continue;
@@ -539,10 +576,10 @@ int launch_regular_compensated(sod_context *ctx, const sod_mesh *m, CollArgs a, 
         if (smem + attr.sharedSizeBytes <= ctx->smem_optin) {
             if (kd == SOD_G) {
                 SOD_TRY(raise_smem(ctx, comp_scatter_kernel<SOD_G>));
-                comp_scatter_kernel<SOD_G><<<grid, COMP_SCATTER_THREADS, smem, stream>>>(a, pt, ft);
+                comp_scatter_kernel<SOD_G><<<grid, threads[SOD_G], smem, stream>>>(a, pt, ft);
             } else {
                 SOD_TRY(raise_smem(ctx, comp_scatter_kernel<SOD_H>));
-                comp_scatter_kernel<SOD_H><<<grid, COMP_SCATTER_THREADS, smem, stream>>>(a, pt, ft);
+                comp_scatter_kernel<SOD_H><<<grid, threads[SOD_H], smem, stream>>>(a, pt, ft);
             }
         } else {
             const void *gfn = kd == SOD_G ? (const void *)comp_scatter_global_kernel<SOD_G>

@@ -795,7 +795,7 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
     for (int kd = 0; kd < 2; kd++) {
         if (!(mask & (1 << kd))) continue;
         if (L.compensated) {  // the compensated pass has its own CTA size and launcher
-            threads[kd] = comp_scatter_threads();
+            SOD_TRY(comp_scatter_threads(ctx, const_cast<sod_mesh *>(m), kd, &threads[kd]));
             SOD_TRY(const_cast<sod_mesh *>(m)->coloured_for(threads[kd], &col[kd]));
             continue;
         }
@@ -891,7 +891,8 @@ int launch_collocation(sod_context *ctx, const CollLaunch &L) {
             const dim3 grid(v1 - v0, nf);
             a.i0 = v0;
             if (L.compensated)
-                SOD_TRY(launch_regular_compensated(ctx, m, a, mask, col[SOD_G], col[SOD_H], pt, ft, v1 - v0, L.stream));
+                SOD_TRY(launch_regular_compensated(ctx, m, a, mask, col[SOD_G], col[SOD_H], threads, pt, ft, v1 - v0,
+                                                   L.stream));
             for (int kd = 0; kd < 2 && !L.compensated; kd++) {
                 if (!(mask & (1 << kd))) continue;
                 a.faces = col[kd]->dFaces.as<float4>();

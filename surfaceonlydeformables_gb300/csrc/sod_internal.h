@@ -238,10 +238,10 @@ int sing_batch_launch(sod_context *ctx, int which, int mask, const SingBatchObj 
 // Compensated (double-float) regular collocation pass of one chunk of field vertices
 // (sod_coll_compensated.cu); the CollArgs carry everything but the face schedule.
 struct CollArgs;
-int comp_scatter_threads();
+int comp_scatter_threads(sod_context *ctx, sod_mesh *m, int kind, int *threads);
 int launch_regular_compensated(sod_context *ctx, const sod_mesh *m, CollArgs a, int mask,
-                               const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, const PointTable &pt,
-                               const FreqTable &ft, int nvert, cudaStream_t stream);
+                               const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, const int threads[2],
+                               const PointTable &pt, const FreqTable &ft, int nvert, cudaStream_t stream);
 // Assembly of the kinds in `mask` (sod_api.cu): the shared driver of the sod_cqbem_assemble* entry
 // points, with the regular-pass precision chosen by the caller (compensated: time-domain outputs).
 int assemble_kinds(sod_context *ctx, const sod_mesh *mesh, int mask, int method, double c1, double c2, double rho,
