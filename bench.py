@@ -43,8 +43,9 @@ FLOPS_PER_EVAL = {"G": 130, "H": 240, "B_trans": 60, "B_angular": 150}
 # (130 + 60 + 150); the stand-alone B reduction (batches without G) does 60 + 150
 PASS_FLOPS = {"scatter_G": 340, "scatter_H": 240, "reduce_B": 210}
 # DRAM bytes per evaluation of each pass from an ncu capture (dram__bytes_read.sum +
-# dram__bytes_write.sum over the launch's evaluations); filled from the committed profile summaries
-TRAFFIC_BYTES_PER_EVAL: dict = {}
+# dram__bytes_write.sum over the launch's evaluations): the capture of the 2562-vertex scatter pair at two
+# frequencies (183.4 M evaluations per launch: 897 MB and 892 MB, almost all of it the complex64 output rows)
+TRAFFIC_BYTES_PER_EVAL = {"scatter_G": 4.89, "scatter_H": 4.87}
 KINDS = ("G", "H", "B_trans", "B_angular")
 
 
@@ -842,31 +843,56 @@ def run_gpu(args):
     accuracy = None if args.value_only else check_batched_rows(objs, outs)
 
     # ---- end to end: the per-object frequency-loop drop-in with pinned host buffers ----
-    # (measured before the per-object and plain legs: after them the same step measured 0.5-0.75 s
-    # instead of 0.36 s in full runs on shared boxes, for reasons not found)
-    # per kind one pinned array of the largest (frequencies x rows x columns) complex128 output,
-    # reused by every call as the reference's loops reuse their host matrices
-    host = {}
-    for kind in KINDS:
-        elems = max(len(o["s"]) * int(np.prod(api.out_shape(L.KINDS[kind], m.nV))) for o, m in zip(objs, meshes))
-        host[kind] = torch.empty(elems, dtype=torch.complex128, pin_memory=True)
+    # Two host threads, each with its own context (stream) and meshes, call sod_cqbem_assemble_all for
+    # their share of the objects (largest first, balanced by output bytes), so that one object's compute
+    # overlaps the other thread's device-to-host copies; every call returns with its outputs complete in
+    # host memory.  Per thread and kind one pinned array of its largest (frequencies x rows x columns)
+    # complex128 output, reused by every call as the reference's loops reuse their host matrices.
+    e2e_threads = 2
+    def out_bytes(o, m):
+        return sum(len(o["s"]) * int(np.prod(api.out_shape(L.KINDS[k], m.nV))) * 16 for k in KINDS)
+    order_ = sorted(range(len(objs)), key=lambda i: -out_bytes(objs[i], meshes[i]))
+    shares, load = [[] for _ in range(e2e_threads)], [0] * e2e_threads
+    for i in order_:
+        t_ = load.index(min(load))
+        shares[t_].append(i)
+        load[t_] += out_bytes(objs[i], meshes[i])
+    workers = []
+    for t_ in range(e2e_threads):
+        wstream = torch.cuda.Stream(dev)
+        wctx = ctx if t_ == 0 else api.Context(local, stream=wstream)
+        wmeshes = {i: (meshes[i] if t_ == 0 else api.Mesh(wctx, objs[i]["mesh"])) for i in shares[t_]}
+        whost = {}
+        for kind in KINDS:
+            elems = max(len(objs[i]["s"]) * int(np.prod(api.out_shape(L.KINDS[kind], objs[i]["mesh"].nV)))
+                        for i in shares[t_])
+            whost[kind] = torch.empty(elems, dtype=torch.complex128, pin_memory=True)
+        workers.append((wctx, wmeshes, whost, shares[t_]))
     e2e_steps = max(1, args.steps // 2)
 
-    def e2e_step():
+    def e2e_worker(w):
+        wctx, wmeshes, whost, share = w
         d2h = 0
-        for o, m in zip(objs, meshes):
-            outs = {}
+        for i in share:
+            o, m = objs[i], wmeshes[i]
+            outs_h = {}
             for kind in KINDS:
                 shape = (len(o["s"]),) + tuple(api.out_shape(L.KINDS[kind], m.nV))
-                outs[kind] = host[kind][: int(np.prod(shape))].view(shape).numpy()
-                d2h += outs[kind].nbytes
-            api.assemble_all(ctx, m, o["mat"], o["s"], order=o["order"], subdiv=o["subdiv"], outs=outs,
+                outs_h[kind] = whost[kind][: int(np.prod(shape))].view(shape).numpy()
+                d2h += outs_h[kind].nbytes
+            api.assemble_all(wctx, m, o["mat"], o["s"], order=o["order"], subdiv=o["subdiv"], outs=outs_h,
                              dtype=L.C128)
         return d2h
 
+    import concurrent.futures as _cf
+    e2e_pool = _cf.ThreadPoolExecutor(e2e_threads)
+
+    def e2e_step():
+        return sum(e2e_pool.map(e2e_worker, workers))
+
     e2e_value, d2h_bytes = None, 0
     if not (args.no_e2e or args.value_only):
-        e2e_step()  # warm the staging buffers
+        e2e_step()  # warm the staging buffers and the second context's mesh schedules
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
@@ -874,6 +900,12 @@ def run_gpu(args):
         torch.cuda.synchronize()
         e2e_t = time.perf_counter() - t0
         e2e_value = world * total_entries * e2e_steps / e2e_t
+    e2e_pool.shutdown()
+    for wctx, wmeshes, whost, share in workers[1:]:
+        for m_ in wmeshes.values():
+            m_.close()
+        wctx.close()
+    del workers
     # ---- the same workload through the per-object and the plain per-(kind, frequency) drop-in ----
     t_per_object = t_plain = None
     if not args.value_only:
@@ -953,7 +985,8 @@ def run_gpu(args):
                 "paths": paths,
                 "e2e": {"value": e2e_value, "unit": "entries/s", "h2d_bytes_per_step": h2d_bytes,
                         "d2h_bytes_per_step": d2h_bytes, "path": "sod_cqbem_assemble_all per object (the frequency-loop "
-                        "drop-in of all four kinds) into pinned host memory, complex128 reference layout",
+                        "drop-in of all four kinds) into pinned host memory, complex128 reference layout, "
+                        "from two host threads with a context each",
                         "steps": e2e_steps},
                 "gpu_launches": int(launches), "clocks": clk.summary(), **extra}
         print(json.dumps(line))

@@ -158,6 +158,8 @@ KConst<double> make_kconst(double c1, double c2, double rho, double sr, double s
     k.isi = -si / d;
     k.sc1r = sr / c1, k.sc1i = si / c1;
     k.sc2r = sr / c2, k.sc2i = si / c2;
+    k.is2r = k.isr * k.isr - k.isi * k.isi, k.is2i = 2.0 * k.isr * k.isi;
+    k.c2sq = c2 * c2;
     return k;
 }
 KConst<float> to_float(const KConst<double> &k) {
@@ -166,6 +168,7 @@ KConst<float> to_float(const KConst<double> &k) {
     f.kappa = (float)k.kappa, f.six_c2s = (float)k.six_c2s, f.inv4pirho = (float)k.inv4pirho;
     f.inv4pi = (float)k.inv4pi, f.sr = (float)k.sr, f.si = (float)k.si, f.isr = (float)k.isr, f.isi = (float)k.isi;
     f.sc1r = (float)k.sc1r, f.sc1i = (float)k.sc1i, f.sc2r = (float)k.sc2r, f.sc2i = (float)k.sc2i;
+    f.is2r = (float)k.is2r, f.is2i = (float)k.is2i, f.c2sq = (float)k.c2sq;
     return f;
 }
 

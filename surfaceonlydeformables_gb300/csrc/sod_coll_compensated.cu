@@ -36,21 +36,36 @@ namespace sod {
 
 // per-frequency constants in double-float
 struct KDD {
-    cdd sc1, sc2, is;  // s/c1, s/c2, 1/s
+    cdd sc1, sc2, is, is2;  // s/c1, s/c2, 1/s, 1/s^2
+    dd c2sq;                // c2^2
     dd ic1, ic2, ic1s, ic2s, six_c2s, inv4pirho, inv4pi;
     dd k4m1, k1m2, k2, k12;  // 4 kappa - 1, 1 - 2 kappa, 2 kappa, 12 kappa
 };
-__device__ __forceinline__ KDD kdd_from(const KConst<double> &k) {
+__host__ __device__ inline dd kdd_split(double x) {
+    const float h = (float)x;
+    return dd{h, (float)(x - (double)h)};
+}
+__host__ __device__ inline KDD kdd_from(const KConst<double> &k) {
     KDD d;
-    d.sc1 = cdd{dd_from(k.sc1r), dd_from(k.sc1i)};
-    d.sc2 = cdd{dd_from(k.sc2r), dd_from(k.sc2i)};
-    d.is = cdd{dd_from(k.isr), dd_from(k.isi)};
-    d.ic1 = dd_from(k.ic1), d.ic2 = dd_from(k.ic2), d.ic1s = dd_from(k.ic1s), d.ic2s = dd_from(k.ic2s);
-    d.six_c2s = dd_from(k.six_c2s), d.inv4pirho = dd_from(k.inv4pirho), d.inv4pi = dd_from(k.inv4pi);
-    d.k4m1 = dd_from(4.0 * k.kappa - 1.0), d.k1m2 = dd_from(1.0 - 2.0 * k.kappa);
-    d.k2 = dd_from(2.0 * k.kappa), d.k12 = dd_from(12.0 * k.kappa);
+    d.sc1 = cdd{kdd_split(k.sc1r), kdd_split(k.sc1i)};
+    d.sc2 = cdd{kdd_split(k.sc2r), kdd_split(k.sc2i)};
+    d.is = cdd{kdd_split(k.isr), kdd_split(k.isi)};
+    d.is2 = cdd{kdd_split(k.is2r), kdd_split(k.is2i)};
+    d.c2sq = kdd_split(k.c2sq);
+    d.ic1 = kdd_split(k.ic1), d.ic2 = kdd_split(k.ic2), d.ic1s = kdd_split(k.ic1s), d.ic2s = kdd_split(k.ic2s);
+    d.six_c2s = kdd_split(k.six_c2s), d.inv4pirho = kdd_split(k.inv4pirho), d.inv4pi = kdd_split(k.inv4pi);
+    d.k4m1 = kdd_split(4.0 * k.kappa - 1.0), d.k1m2 = kdd_split(1.0 - 2.0 * k.kappa);
+    d.k2 = kdd_split(2.0 * k.kappa), d.k12 = kdd_split(12.0 * k.kappa);
     return d;
 }
+// The kernels take the constants as float pairs built on the host: members read straight from the
+// parameter space (one constant-cache load when the compiler re-reads one) instead of a per-thread
+// conversion from double, which the compiler re-materialises inside the loops under register pressure
+// (two conversions and an FP64 add on the slow FP64 pipe for every re-read).
+struct KddTable {
+    int n;
+    KDD k[MAX_FREQ_PER_LAUNCH];
+};
 
 // ---- double-float arithmetic without renormalisation ----------------------------------------------
 // The pass needs ~1e-10 relative per evaluation, not the 1e-14 of renormalised double-float, so the
@@ -58,17 +73,18 @@ __device__ __forceinline__ KDD kdd_from(const KConst<double> &k) {
 // by FMA, TwoSum) and add the low words in plain float, without the renormalising steps: the low word
 // then carries a few ulps of the high word, which is harmless at this accuracy.  Sums that cancel
 // (the psi numerator, Y, the kernel coefficients) are followed by one FastTwoSum.
+// (high words through the non-contractible _rn operations, see sod_dd.cuh)
 __device__ __forceinline__ dd sd_mul(dd a, dd b) {
-    const float p = a.hi * b.hi;
+    const float p = SOD_MUL_RN(a.hi, b.hi);
     return dd{p, fmaf(a.lo, b.hi, fmaf(a.hi, b.lo, fmaf(a.hi, b.hi, -p)))};
 }
 __device__ __forceinline__ dd sd_mulf(dd a, float b) {
-    const float p = a.hi * b;
+    const float p = SOD_MUL_RN(a.hi, b);
     return dd{p, fmaf(a.lo, b, fmaf(a.hi, b, -p))};
 }
 __device__ __forceinline__ dd sd_add(dd a, dd b) {
-    const float s = a.hi + b.hi, bb = s - a.hi;
-    return dd{s, ((a.hi - (s - bb)) + (b.hi - bb)) + (a.lo + b.lo)};
+    const float s = SOD_ADD_RN(a.hi, b.hi), bb = SOD_SUB_RN(s, a.hi);
+    return dd{s, SOD_ADD_RN(SOD_SUB_RN(a.hi, SOD_SUB_RN(s, bb)), SOD_SUB_RN(b.hi, bb)) + (a.lo + b.lo)};
 }
 __device__ __forceinline__ dd sd_neg(dd a) { return dd{-a.hi, -a.lo}; }
 __device__ __forceinline__ dd sd_sub(dd a, dd b) { return sd_add(a, sd_neg(b)); }
@@ -156,36 +172,52 @@ __device__ __forceinline__ cdd cs_exp_neg(const cdd &z, const DdTabs *tb) {
     return cdd{sd_mul(mag, cs), sd_neg(sd_mul(mag, sn))};
 }
 
-// psi(z) = ((1 + z) e^-z - 1) / z^2: the renormalised series below |z| = 0.1 (sod_dd.cuh), above it the
-// closed form, which loses ~1e-11 there
-__device__ __forceinline__ cdd cs_psi(const cdd &z, const cdd &ez) {
-    const float az2 = z.x.hi * z.x.hi + z.y.hi * z.y.hi;
-    if (az2 < 0.01f) return cdd_psi(z, ez);
-    cdd num = cs_mul(cdd{sd_add(z.x, dd{1.0f, 0.0f}), z.y}, ez);
-    num.x = sd_norm(sd_add(num.x, dd{-1.0f, 0.0f}));
-    num.y = sd_norm(num.y);
-    const cdd zz = cs_norm(cs_mul(z, z));
-    const dd n2 = sd_norm(sd_add(sd_mul(zz.x, zz.x), sd_mul(zz.y, zz.y)));
-    // 1 / n2: float reciprocal and one Newton step
-    const float y = 1.0f / n2.hi;
-    const dd e = sd_norm(sd_sub(dd{1.0f, 0.0f}, sd_mulf(n2, y)));
-    const dd inv = dd{y, e.hi * y};
-    return cs_mul(num, cdd{sd_mul(zz.x, inv), sd_neg(sd_mul(zz.y, inv))});
-}
-
 struct RadDD {
     cdd z1, z2, e1, e2, psi2, Y;
 };
-// the frequency-dependent radial terms at distance r (an exact float)
-__device__ __forceinline__ RadDD radial_dd(float r, const KDD &k, const DdTabs *tb) {
+// the frequency-dependent radial terms at distance r (an exact float; rinv ~ 1/r in float).  Since
+// c1^2 z1^2 = c2^2 z2^2 = s^2 r^2,  Y = psi(z1)/c1^2 - psi(z2)/c2^2 = ((1 + z1) e1 - (1 + z2) e2) / (s^2 r^2)
+// with the -1 of both psi cancelled exactly: above |z1| = 0.1 no reciprocal of a complex number is
+// taken, 1 / r^2 comes from one Newton correction of rinv (consistent with r to ~1e-14, so that Y's
+// terms stay consistent with each other).  Below |z| = 0.1 the series of psi (sod_dd.cuh).  psi2
+// (B_trans) only when PSI2.
+template <bool PSI2>
+__device__ __forceinline__ RadDD radial_dd(float r, float rinv, const KDD &k, const DdTabs *tb) {
     RadDD t;
     t.z1 = cs_scalef(k.sc1, r);
     t.z2 = cs_scalef(k.sc2, r);
     t.e1 = cs_exp_neg(t.z1, tb);
     t.e2 = cs_exp_neg(t.z2, tb);
-    const cdd psi1 = cs_psi(t.z1, t.e1);
-    t.psi2 = cs_psi(t.z2, t.e2);
-    t.Y = cs_norm(cs_sub(cs_scale(psi1, k.ic1s), cs_scale(t.psi2, k.ic2s)));
+    const float az1 = t.z1.x.hi * t.z1.x.hi + t.z1.y.hi * t.z1.y.hi;
+    const float az2 = t.z2.x.hi * t.z2.x.hi + t.z2.y.hi * t.z2.y.hi;
+    if (az2 < 0.01f) {  // both series
+        const cdd psi1 = cdd_psi(t.z1, t.e1);
+        t.psi2 = cdd_psi(t.z2, t.e2);
+        t.Y = cs_norm(cs_sub(cs_scale(psi1, k.ic1s), cs_scale(t.psi2, k.ic2s)));
+        return t;
+    }
+    const dd ir = dd{rinv, rinv * fmaf(-r, rinv, 1.0f)};  // 1/r: rinv (1 + (1 - r rinv))
+    const dd ir2 = sd_mul(ir, ir);
+    const cdd W = cdd{sd_mul(k.is2.x, ir2), sd_mul(k.is2.y, ir2)};  // 1 / (s^2 r^2)
+    const cdd a2 = cs_add(t.e2, cs_mul(t.z2, t.e2));                 // (1 + z2) e2
+    if (az1 < 0.01f) {  // z1 on the series, z2 closed
+        const cdd psi1 = cdd_psi(t.z1, t.e1);
+        cdd n2 = a2;
+        n2.x = sd_norm(sd_add(n2.x, dd{-1.0f, 0.0f}));
+        n2.y = sd_norm(n2.y);
+        const cdd p2s = cs_mul(n2, W);  // psi2 / c2^2
+        if (PSI2) t.psi2 = cs_scale(p2s, k.c2sq);
+        t.Y = cs_norm(cs_sub(cs_scale(psi1, k.ic1s), p2s));
+        return t;
+    }
+    const cdd a1 = cs_add(t.e1, cs_mul(t.z1, t.e1));  // (1 + z1) e1
+    t.Y = cs_mul(cs_norm(cs_sub(a1, a2)), W);
+    if (PSI2) {
+        cdd n2 = a2;
+        n2.x = sd_norm(sd_add(n2.x, dd{-1.0f, 0.0f}));
+        n2.y = sd_norm(n2.y);
+        t.psi2 = cs_scale(cs_mul(n2, W), k.c2sq);
+    }
     return t;
 }
 
@@ -193,7 +225,7 @@ __device__ __forceinline__ RadDD radial_dd(float r, const KDD &k, const DdTabs *
 // words are summed in float.  acc.lo is left unnormalised (a face adds at most a few dozen terms);
 // dd_norm() renormalises it.
 __device__ __forceinline__ void dd_fma_acc(dd &acc, dd x, float w) {
-    const float p = x.hi * w;
+    const float p = SOD_MUL_RN(x.hi, w);
     const float e = fmaf(x.hi, w, -p);
     const dd s = two_sum(acc.hi, p);
     acc.hi = s.hi;
@@ -215,12 +247,11 @@ __device__ __forceinline__ cdd cdd_scale(const cdd &a, float s) { return cdd{a.x
 // G / H scatter.  ROW: double-float row block, shared (per-CTA dynamic shared memory) or a global
 // slice; layout [NC][nV] float4.
 template <int KIND>
-__device__ __forceinline__ void comp_scatter_body(const CollArgs &a, const PointTable &pt, const KConst<double> &kd,
+__device__ __forceinline__ void comp_scatter_body(const CollArgs &a, const PointTable &pt, const KDD &k,
                                                   int i, int fq, float4 *acc, ColourBar *cb, unsigned &phase,
                                                   const DdTabs *tb) {
     constexpr int NC = KIND == SOD_G ? 6 : 9;
     const int nV = a.nV;
-    const KDD k = kdd_from(kd);
     for (int t = threadIdx.x; t < NC * nV; t += blockDim.x) acc[t] = make_float4(0.f, 0.f, 0.f, 0.f);
     const float3 x = make_float3(a.Vf[3 * i], a.Vf[3 * i + 1], a.Vf[3 * i + 2]);
     const int ci = a.canonV ? a.canonV[i] : i;
@@ -248,7 +279,7 @@ __device__ __forceinline__ void comp_scatter_body(const CollArgs &a, const Point
                     const float rinv = rsqrtf(r2);
                     const float r = r2 * rinv;
                     const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                    const RadDD t = radial_dd(r, k, tb);
+                    const RadDD t = radial_dd<false>(r, rinv, k, tb);
                     cdd u[NC];
                     if (KIND == SOD_G) {
                         // alpha = (3Y + e1/c1^2 - e2/c2^2) / (4 pi rho r), beta = (e2/c2^2 - Y) / (4 pi rho r)
@@ -348,20 +379,20 @@ constexpr int COMP_SCATTER_THREADS = 256;
 
 template <int KIND>
 __global__ void __launch_bounds__(COMP_SCATTER_THREADS) comp_scatter_kernel(CollArgs a, PointTable pt,
-                                                                          const __grid_constant__ FreqTable ft) {
+                                                                          const __grid_constant__ KddTable kt) {
     extern __shared__ float4 acc4[];
     __shared__ ColourBar cb;
     __shared__ DdTabs tb;
     dd_tabs_load(&tb);
     colour_bar_init(&cb, a.bar_extra);
     unsigned phase = 0;
-    comp_scatter_body<KIND>(a, pt, ft.kd[blockIdx.y], a.i0 + blockIdx.x, blockIdx.y, acc4, &cb, phase, &tb);
+    comp_scatter_body<KIND>(a, pt, kt.k[blockIdx.y], a.i0 + blockIdx.x, blockIdx.y, acc4, &cb, phase, &tb);
 }
 
 // persistent grid, each CTA's row block in its own slice of global memory (L2-resident)
 template <int KIND>
 __global__ void __launch_bounds__(COMP_SCATTER_THREADS) comp_scatter_global_kernel(CollArgs a, PointTable pt,
-                                                                                 const __grid_constant__ FreqTable ft,
+                                                                                 const __grid_constant__ KddTable kt,
                                                                                  float4 *scratch, long long per_cta,
                                                                                  int nvert) {
     float4 *acc = scratch + (size_t)blockIdx.x * per_cta;
@@ -370,10 +401,10 @@ __global__ void __launch_bounds__(COMP_SCATTER_THREADS) comp_scatter_global_kern
     dd_tabs_load(&tb);
     colour_bar_init(&cb, a.bar_extra);
     unsigned phase = 0;
-    const int items = nvert * ft.n;
+    const int items = nvert * kt.n;
     for (int it = blockIdx.x; it < items; it += gridDim.x) {
         const int fq = it / nvert, i = a.i0 + it % nvert;
-        comp_scatter_body<KIND>(a, pt, ft.kd[fq], i, fq, acc, &cb, phase, &tb);
+        comp_scatter_body<KIND>(a, pt, kt.k[fq], i, fq, acc, &cb, phase, &tb);
         __syncthreads();
     }
 }
@@ -385,7 +416,7 @@ constexpr int COMP_REDUCE_THREADS = 128;
 
 template <int MASK>
 __global__ void __launch_bounds__(COMP_REDUCE_THREADS) comp_reduce_kernel(CollArgs a, PointTable pt,
-                                                                        const __grid_constant__ FreqTable ft) {
+                                                                        const __grid_constant__ KddTable kt) {
     constexpr bool BT = (MASK & KM_BT) != 0, BA = (MASK & KM_BA) != 0;
     constexpr int NT = BT ? 6 : 0, NA = BA ? 18 : 0, NCB = NT + NA;
     extern __shared__ float4 colB[];  // [NCB][T]
@@ -393,7 +424,7 @@ __global__ void __launch_bounds__(COMP_REDUCE_THREADS) comp_reduce_kernel(CollAr
     __shared__ DdTabs tb;
     dd_tabs_load(&tb);
     const int i = a.i0 + blockIdx.x, fq = blockIdx.y;
-    const KDD k = kdd_from(ft.kd[fq]);
+    const KDD &k = kt.k[fq];
     const int T = blockDim.x;
 #pragma unroll
     for (int cc = 0; cc < NCB; cc++) colB[cc * T + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -425,7 +456,7 @@ __global__ void __launch_bounds__(COMP_REDUCE_THREADS) comp_reduce_kernel(CollAr
                 const float rinv = rsqrtf(r2);
                 const float r = r2 * rinv;
                 const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                const RadDD t = radial_dd(r, k, &tb);
+                const RadDD t = radial_dd<true>(r, rinv, k, &tb);
                 const float w = P.w;
                 if (BT) {
                     const cdd ws = cdd_scale(t.Y, hp * w);
@@ -562,6 +593,9 @@ int launch_regular_compensated(sod_context *ctx, const sod_mesh *m, CollArgs a, 
                                const sod_mesh::Coloured *colG, const sod_mesh::Coloured *colH, const int threads[2],
                                const PointTable &pt, const FreqTable &ft, int nvert, cudaStream_t stream) {
     const dim3 grid(nvert, ft.n);
+    KddTable kt;
+    kt.n = ft.n;
+    for (int l = 0; l < ft.n; l++) kt.k[l] = kdd_from(ft.kd[l]);
     for (int kd = 0; kd < 2; kd++) {
         if (!(mask & (1 << kd))) continue;
         const sod_mesh::Coloured *col = kd == SOD_G ? colG : colH;
@@ -576,10 +610,10 @@ int launch_regular_compensated(sod_context *ctx, const sod_mesh *m, CollArgs a, 
         if (smem + attr.sharedSizeBytes <= ctx->smem_optin) {
             if (kd == SOD_G) {
                 SOD_TRY(raise_smem(ctx, comp_scatter_kernel<SOD_G>));
-                comp_scatter_kernel<SOD_G><<<grid, threads[SOD_G], smem, stream>>>(a, pt, ft);
+                comp_scatter_kernel<SOD_G><<<grid, threads[SOD_G], smem, stream>>>(a, pt, kt);
             } else {
                 SOD_TRY(raise_smem(ctx, comp_scatter_kernel<SOD_H>));
-                comp_scatter_kernel<SOD_H><<<grid, threads[SOD_H], smem, stream>>>(a, pt, ft);
+                comp_scatter_kernel<SOD_H><<<grid, threads[SOD_H], smem, stream>>>(a, pt, kt);
             }
         } else {
             const void *gfn = kd == SOD_G ? (const void *)comp_scatter_global_kernel<SOD_G>
@@ -590,10 +624,10 @@ int launch_regular_compensated(sod_context *ctx, const sod_mesh *m, CollArgs a, 
             const long long per_cta = (long long)(smem / sizeof(float4));
             SOD_TRY(ctx->gacc.ensure(sizeof(float4) * (size_t)g * per_cta));
             if (kd == SOD_G)
-                comp_scatter_global_kernel<SOD_G><<<g, COMP_SCATTER_THREADS, 0, stream>>>(a, pt, ft, ctx->gacc.as<float4>(),
+                comp_scatter_global_kernel<SOD_G><<<g, COMP_SCATTER_THREADS, 0, stream>>>(a, pt, kt, ctx->gacc.as<float4>(),
                                                                                          per_cta, nvert);
             else
-                comp_scatter_global_kernel<SOD_H><<<g, COMP_SCATTER_THREADS, 0, stream>>>(a, pt, ft, ctx->gacc.as<float4>(),
+                comp_scatter_global_kernel<SOD_H><<<g, COMP_SCATTER_THREADS, 0, stream>>>(a, pt, kt, ctx->gacc.as<float4>(),
                                                                                          per_cta, nvert);
         }
         SOD_CHECK_CUDA(cudaGetLastError());
@@ -606,13 +640,13 @@ int launch_regular_compensated(sod_context *ctx, const sod_mesh *m, CollArgs a, 
         const size_t smem = comp_colb_bytes(bm);
         if (bm == KM_BT) {
             SOD_TRY(raise_smem(ctx, comp_reduce_kernel<KM_BT>));
-            comp_reduce_kernel<KM_BT><<<grid, COMP_REDUCE_THREADS, smem, stream>>>(a, pt, ft);
+            comp_reduce_kernel<KM_BT><<<grid, COMP_REDUCE_THREADS, smem, stream>>>(a, pt, kt);
         } else if (bm == KM_BA) {
             SOD_TRY(raise_smem(ctx, comp_reduce_kernel<KM_BA>));
-            comp_reduce_kernel<KM_BA><<<grid, COMP_REDUCE_THREADS, smem, stream>>>(a, pt, ft);
+            comp_reduce_kernel<KM_BA><<<grid, COMP_REDUCE_THREADS, smem, stream>>>(a, pt, kt);
         } else {
             SOD_TRY(raise_smem(ctx, comp_reduce_kernel<KM_BT | KM_BA>));
-            comp_reduce_kernel<KM_BT | KM_BA><<<grid, COMP_REDUCE_THREADS, smem, stream>>>(a, pt, ft);
+            comp_reduce_kernel<KM_BT | KM_BA><<<grid, COMP_REDUCE_THREADS, smem, stream>>>(a, pt, kt);
         }
         SOD_CHECK_CUDA(cudaGetLastError());
         ctx->count();

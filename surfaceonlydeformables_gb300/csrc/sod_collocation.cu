@@ -78,7 +78,7 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
                     const float rinv = rsqrtf(r2);
                     const float r = r2 * rinv;
                     const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                    const RadialTerms<float, cf> t = radial(r, k);
+                    const RadialTerms<float, cf> t = radial<(NCB > 0)>(r, rinv, k);
                     cf u[NC];
                     if (KIND == SOD_G) {
                         cf al, be;
@@ -275,7 +275,7 @@ __device__ __forceinline__ void reduce_body(const CollArgs &a, const PointTable 
                 const float rinv = rsqrtf(r2);
                 const float r = r2 * rinv;
                 const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                const RadialTerms<float, cf> t = radial(r, k);
+                const RadialTerms<float, cf> t = radial<true>(r, rinv, k);
                 bm.add(t, k, r, rh, nn, P.w);
             }
             bm.emit(k, nn, fr.area, [&](int c, cf v) { accl[c] = accl[c] + v; });

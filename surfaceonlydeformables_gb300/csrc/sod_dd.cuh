@@ -21,6 +21,21 @@
 #pragma once
 #include <cmath>
 
+// The error-free transformations below need every operation rounded on its own.  nvcc contracts a
+// multiply into a later add or subtract (-fmad=true, also across statements and when the product
+// has other uses), which would make TwoSum / TwoProduct compute their error term from an unrounded
+// product, i.e. return the rounding error of a different sum: the pair then loses the low word's
+// accuracy (~1e-7 relative instead of ~1e-14).  The _rn intrinsics are never contracted.
+#if defined(__CUDA_ARCH__)
+#define SOD_ADD_RN(a, b) __fadd_rn((a), (b))
+#define SOD_SUB_RN(a, b) __fsub_rn((a), (b))
+#define SOD_MUL_RN(a, b) __fmul_rn((a), (b))
+#else
+#define SOD_ADD_RN(a, b) ((a) + (b))
+#define SOD_SUB_RN(a, b) ((a) - (b))
+#define SOD_MUL_RN(a, b) ((a) * (b))
+#endif
+
 #ifdef __CUDACC__
 #define SOD_HD __device__ __forceinline__
 #define SOD_DD_TABLE static __device__ __constant__ const
@@ -46,17 +61,17 @@ SOD_HD double dd_to(dd a) { return (double)a.hi + (double)a.lo; }
 
 // ---- error-free transformations ----
 SOD_HD dd two_sum(float a, float b) {
-    const float s = a + b;
-    const float bb = s - a;
-    const float e = (a - (s - bb)) + (b - bb);
+    const float s = SOD_ADD_RN(a, b);
+    const float bb = SOD_SUB_RN(s, a);
+    const float e = SOD_ADD_RN(SOD_SUB_RN(a, SOD_SUB_RN(s, bb)), SOD_SUB_RN(b, bb));
     return dd{s, e};
 }
 SOD_HD dd fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
-    const float s = a + b;
-    return dd{s, b - (s - a)};
+    const float s = SOD_ADD_RN(a, b);
+    return dd{s, SOD_SUB_RN(b, SOD_SUB_RN(s, a))};
 }
 SOD_HD dd two_prod(float a, float b) {
-    const float p = a * b;
+    const float p = SOD_MUL_RN(a, b);
     return dd{p, fmaf(a, b, -p)};
 }
 

@@ -112,30 +112,23 @@ __device__ __forceinline__ cd cexp_neg(cd z) {
 
 // psi(z) = ((1+z) e^-z - 1) / z^2 = -sum_{m>=0} (-1)^m (m+1) z^m / (m+2)!
 // FP32: below |z| = 1 the 11-term series (truncation < 4e-9 relative) in Estrin's scheme (dependency
-// depth 4 complex multiply-adds instead of Horner's 10); above, the closed form with an approximate
-// reciprocal.
+// depth 4 complex multiply-adds instead of Horner's 10); above it the FP32 radial terms below need no
+// psi of their own.
 __device__ __forceinline__ cf cfmac(cf a, cf b, cf c) {  // a b + c
     return {fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y))};
 }
-__device__ __forceinline__ cf psi(cf z, cf ez) {
-    const float az2 = z.x * z.x + z.y * z.y;
-    if (az2 < 1.0f) {
-        // c_m = -(-1)^m (m+1)/(m+2)!, m = 0..10, paired as c_2j + c_2j+1 z
-        const float c0 = -1.0f / 2.0f, c1 = 1.0f / 3.0f, c2 = -1.0f / 8.0f, c3 = 1.0f / 30.0f, c4 = -1.0f / 144.0f,
-                    c5 = 1.0f / 840.0f, c6 = -1.0f / 5760.0f, c7 = 1.0f / 45360.0f, c8 = -9.0f / 3628800.0f,
-                    c9 = 10.0f / 39916800.0f, c10 = -11.0f / 479001600.0f;
-        const cf z2 = z * z, z4 = z2 * z2, z8 = z4 * z4;
-        const cf p01 = {fmaf(c1, z.x, c0), c1 * z.y}, p23 = {fmaf(c3, z.x, c2), c3 * z.y};
-        const cf p45 = {fmaf(c5, z.x, c4), c5 * z.y}, p67 = {fmaf(c7, z.x, c6), c7 * z.y};
-        const cf p89 = {fmaf(c9, z.x, c8), c9 * z.y};
-        const cf q0 = cfmac(z2, p23, p01), q1 = cfmac(z2, p67, p45);
-        const cf q2 = {fmaf(c10, z2.x, p89.x), fmaf(c10, z2.y, p89.y)};
-        return cfmac(z8, q2, cfmac(z4, q1, q0));
-    }
-    const cf num = (mk(1.0f, 0.0f) + z) * ez - mk(1.0f, 0.0f);
-    const cf zz = z * z;
-    const float d = rcp_approx(fmaf(zz.x, zz.x, zz.y * zz.y));
-    return num * cf{zz.x * d, -zz.y * d};
+__device__ __forceinline__ cf psi_series(cf z) {
+    // c_m = -(-1)^m (m+1)/(m+2)!, m = 0..10, paired as c_2j + c_2j+1 z
+    const float c0 = -1.0f / 2.0f, c1 = 1.0f / 3.0f, c2 = -1.0f / 8.0f, c3 = 1.0f / 30.0f, c4 = -1.0f / 144.0f,
+                c5 = 1.0f / 840.0f, c6 = -1.0f / 5760.0f, c7 = 1.0f / 45360.0f, c8 = -9.0f / 3628800.0f,
+                c9 = 10.0f / 39916800.0f, c10 = -11.0f / 479001600.0f;
+    const cf z2 = z * z, z4 = z2 * z2, z8 = z4 * z4;
+    const cf p01 = {fmaf(c1, z.x, c0), c1 * z.y}, p23 = {fmaf(c3, z.x, c2), c3 * z.y};
+    const cf p45 = {fmaf(c5, z.x, c4), c5 * z.y}, p67 = {fmaf(c7, z.x, c6), c7 * z.y};
+    const cf p89 = {fmaf(c9, z.x, c8), c9 * z.y};
+    const cf q0 = cfmac(z2, p23, p01), q1 = cfmac(z2, p67, p45);
+    const cf q2 = {fmaf(c10, z2.x, p89.x), fmaf(c10, z2.y, p89.y)};
+    return cfmac(z8, q2, cfmac(z4, q1, q0));
 }
 // FP64: the closed form loses about 2 eps / |z|^2, i.e. <= 2e-12 relative for |z| >= 0.01; below
 // that a 7-term series (truncation < 1e-17 relative) is used.
@@ -165,6 +158,8 @@ template <class R> struct KConst {
     R isr, isi;          // 1/s
     R sc1r, sc1i;        // s/c1
     R sc2r, sc2i;        // s/c2
+    R is2r, is2i;        // 1/s^2
+    R c2sq;              // c2^2
 };
 
 template <class R, class C> struct RadialTerms {
@@ -212,16 +207,30 @@ __device__ __forceinline__ void h_coeffs(const RadialTerms<R, C> &t, const KCons
 }
 
 // FP32 overloads of the above with packed two-lane FMA / multiply chains (same algebra; each
-// complex-times-real multiply-add is one instruction)
-__device__ __forceinline__ RadialTerms<float, cf> radial(float r, const KConst<float> &k) {
+// complex-times-real multiply-add is one instruction).  Since c1^2 z1^2 = c2^2 z2^2 = s^2 r^2,
+//     Y = psi(z1)/c1^2 - psi(z2)/c2^2 = ((1 + z1) e1 - (1 + z2) e2) / (s^2 r^2)
+// (the -1 of both psi cancel exactly), so above |z2| = 1 (|z1| >= |z2| c2/c1) Y takes no reciprocal
+// and no psi at all; below, both psi come from the series.  psi2 itself (the B kinds, PSI2) is
+// ((1 + z2) e2 - 1) c2^2 / (s^2 r^2) there.  rinv is the caller's 1/r: a relative error of it scales
+// Y uniformly over the frequencies.
+template <bool PSI2>
+__device__ __forceinline__ RadialTerms<float, cf> radial(float r, float rinv, const KConst<float> &k) {
     RadialTerms<float, cf> t;
     t.z1 = mk(r * k.sc1r, r * k.sc1i);
     t.z2 = mk(r * k.sc2r, r * k.sc2i);
     t.e1 = cexp_neg(t.z1);
     t.e2 = cexp_neg(t.z2);
-    t.psi1 = psi(t.z1, t.e1);
-    t.psi2 = psi(t.z2, t.e2);
-    t.Y = cfmar(t.psi2, -k.ic2s, cmulr(t.psi1, k.ic1s));
+    if (t.z2.x * t.z2.x + t.z2.y * t.z2.y < 1.0f) {
+        const cf psi1 = psi_series(t.z1);
+        t.psi2 = psi_series(t.z2);
+        t.Y = cfmar(t.psi2, -k.ic2s, cmulr(psi1, k.ic1s));
+    } else {
+        const float ri2 = rinv * rinv;
+        const cf W = mk(k.is2r * ri2, k.is2i * ri2);
+        const cf a1 = cfmac(t.z1, t.e1, t.e1), a2 = cfmac(t.z2, t.e2, t.e2);  // (1 + z) e
+        t.Y = (a1 - a2) * W;
+        if (PSI2) t.psi2 = cmulr((a2 - mk(1.0f, 0.0f)) * W, k.c2sq);
+    }
     return t;
 }
 __device__ __forceinline__ void g_coeffs(const RadialTerms<float, cf> &t, const KConst<float> &k, float scale,

@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_tp_kernel(
                 const float rinv = rsqrtf(r2);
                 const float r = r2 * rinv;
                 const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
-                const RadialTerms<float, cf> rt = radial(r, k);
+                const RadialTerms<float, cf> rt = radial<(NCB > 0)>(r, rinv, k);
                 cf u[NC];
                 if (KIND == SOD_G) {
                     cf al, be;
@@ -245,8 +245,9 @@ __global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_tp_kernel(
 struct Comp2 {  // compensated FP32 complex sum
     float sx = 0.f, cx = 0.f, sy = 0.f, cy = 0.f;
     __device__ __forceinline__ static void add1(float &s, float &c, float p) {
-        const float t = s + p, bp = t - s;
-        c += (s - (t - bp)) + (p - bp);
+        // _rn operations: the product w v must not be contracted into the TwoSum's adds
+        const float t = __fadd_rn(s, p), bp = __fsub_rn(t, s);
+        c += __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
         s = t;
     }
     __device__ __forceinline__ void add(float w, float2 v) {

@@ -21,17 +21,18 @@
 namespace sod {
 
 // error-free transformations on FP32
+// (each operation rounded on its own: _rn intrinsics, which nvcc never contracts into an FMA)
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 struct df {
     float hi, lo;
 };
 // acc += a * x  where a = (ahi + alo) is a double-float constant and x an FP32 value
 __device__ __forceinline__ void df_mac(df &acc, float ahi, float alo, float x) {
-    const float p = ahi * x;
+    const float p = __fmul_rn(ahi, x);
     const float pe = fmaf(ahi, x, -p);  // exact: p + pe = ahi * x
     float s, e;
     two_sum(acc.hi, p, s, e);
