@@ -13,6 +13,7 @@
 //    twiddles split hi+lo, every product hi*x formed exactly with an FMA (TwoProduct), the sum
 //    carried as an unevaluated pair with TwoSum -- about 2^-48 of the term magnitude, far below
 //    the rounding of the FP32 result.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -91,14 +92,23 @@ __global__ void __launch_bounds__(TILE) inv_transform_df_kernel(const void *__re
     }
 }
 
+// FP64 output.  With theta = 2 pi n l / L, Re(Xhat_l zeta^-nl) = xr cos(theta) + xi sin(theta), and
+// n -> L - n keeps the cosine and flips the sine, so for n <= L/2
+//     A_n = sum_l c_l xr_l cos,  B_n = sum_l c_l xi_l sin,
+//     X_n = R^-n / L (A_n + B_n),  X_{L-n} = R^-(L-n) / L (A_n - B_n):
+// (L/2 + 1) nfreq multiply-add pairs per entry instead of L nfreq (the same terms, summed as two
+// partial sums).
 template <int TILE>
 __global__ void __launch_bounds__(TILE) inv_transform_f64_kernel(const void *__restrict__ Xhat, int in_c128, long long M,
                                                                 int nfreq, int L, const double2 *__restrict__ tw,
-                                                                double *__restrict__ out) {
+                                                                const double *__restrict__ gsc, double *__restrict__ out) {
     extern __shared__ double2 smd[];
-    double2 *stw = smd;                    // [L][nfreq] twiddles
-    double2 *sx = stw + (size_t)L * nfreq;  // [nfreq][TILE] inputs
-    for (int t = threadIdx.x; t < L * nfreq; t += TILE) stw[t] = tw[t];
+    const int nh = L / 2;
+    double2 *stw = smd;                                                  // [nh + 1][nfreq] (c_l cos, c_l sin)
+    double2 *sx = stw + (size_t)(nh + 1) * nfreq;                        // [nfreq][TILE] inputs
+    double *sg = reinterpret_cast<double *>(sx + (size_t)nfreq * TILE);  // [L] R^-n / L
+    for (int t = threadIdx.x; t < (nh + 1) * nfreq; t += TILE) stw[t] = tw[t];
+    for (int t = threadIdx.x; t < L; t += TILE) sg[t] = gsc[t];
     const long long e = (long long)blockIdx.x * TILE + threadIdx.x;
     const bool live = e < M;
     for (int l = 0; l < nfreq; l++) {
@@ -115,16 +125,31 @@ __global__ void __launch_bounds__(TILE) inv_transform_f64_kernel(const void *__r
     }
     __syncthreads();
     if (!live) return;
-    for (int n = 0; n < L; n++) {
-        double acc = 0.0;
+    for (int n = 0; n <= nh; n++) {
+        double A = 0.0, B = 0.0;
         for (int l = 0; l < nfreq; l++) {
             const double2 w = stw[n * nfreq + l];
             const double2 x = sx[l * TILE + threadIdx.x];
-            acc = fma(x.x, w.x, acc);
-            acc = fma(-x.y, w.y, acc);
+            A = fma(x.x, w.x, A);
+            B = fma(x.y, w.y, B);
         }
-        out[(long long)n * M + e] = acc;
+        out[(long long)n * M + e] = sg[n] * (A + B);
+        const int m = L - n;
+        if (n >= 1 && m != n) out[(long long)m * M + e] = sg[m] * (A - B);
     }
+}
+
+// c_l cos(2 pi n l / L), c_l sin(2 pi n l / L) for n <= L/2, l < nfreq, and R^-n / L for n < L
+__global__ void twiddle_half_kernel(int L, int nfreq, double R, double2 *tw, double *gsc) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nh = L / 2;
+    if (t < L) gsc[t] = pow(R, -(double)t) / (double)L;
+    if (t >= (nh + 1) * nfreq) return;
+    const int n = t / nfreq, l = t % nfreq;
+    const double c = (l != 0 && (l != L / 2 || L % 2 == 1)) ? 2.0 : 1.0;
+    double sn, cs;
+    sincospi(2.0 * (double)(((long long)n * l) % L) / (double)L, &sn, &cs);
+    tw[t] = make_double2(c * cs, c * sn);
 }
 
 // twiddles c_l R^-n / L zeta^-nl for n < L, l < nfreq, generated on the device (no host copy)
@@ -153,13 +178,16 @@ int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, i
     if (M == 0) return SOD_OK;
     const int in_c128 = in_dtype == SOD_C128;
     if (out_dtype == SOD_F64) {
-        const size_t ntw = (size_t)L * nfreq;
-        SOD_TRY(ctx->twiddle.ensure(sizeof(double2) * ntw));
-        twiddle_kernel<<<(unsigned)((ntw + 255) / 256), 256, 0, stream>>>(L, nfreq, R, ctx->twiddle.as<double2>(), nullptr);
+        const size_t ntw = (size_t)(L / 2 + 1) * nfreq;
+        SOD_TRY(ctx->twiddle.ensure(sizeof(double2) * ntw + sizeof(double) * (size_t)L));
+        double2 *dtw = ctx->twiddle.as<double2>();
+        double *dg = reinterpret_cast<double *>(dtw + ntw);
+        const size_t nt = std::max(ntw, (size_t)L);
+        twiddle_half_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, stream>>>(L, nfreq, R, dtw, dg);
         SOD_CHECK_CUDA(cudaGetLastError());
         ctx->count();
         constexpr int TILE = 128;
-        const size_t smem = sizeof(double2) * (ntw + (size_t)nfreq * TILE);
+        const size_t smem = sizeof(double2) * (ntw + (size_t)nfreq * TILE) + sizeof(double) * (size_t)L;
         if (smem > ctx->smem_optin) {
             set_error("inverse transform: too many frequencies for the shared-memory tile");
             return SOD_ERR_UNSUPPORTED;
@@ -167,8 +195,8 @@ int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, i
         SOD_CHECK_CUDA(cudaFuncSetAttribute(inv_transform_f64_kernel<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem));
         const long long blocks = (M + TILE - 1) / TILE;
-        inv_transform_f64_kernel<TILE><<<(unsigned)blocks, TILE, smem, stream>>>(
-            Xhat, in_c128, M, nfreq, L, ctx->twiddle.as<double2>(), reinterpret_cast<double *>(out));
+        inv_transform_f64_kernel<TILE><<<(unsigned)blocks, TILE, smem, stream>>>(Xhat, in_c128, M, nfreq, L, dtw, dg,
+                                                                                 reinterpret_cast<double *>(out));
         SOD_CHECK_CUDA(cudaGetLastError());
         ctx->count();
         return SOD_OK;

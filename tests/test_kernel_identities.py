@@ -79,3 +79,25 @@ def test_stable_forms_equal_literal_formulas():
             num = mp.sqrt(sum(abs(x - y) ** 2 for x, y in zip(fa, fb)))
             den = mp.sqrt(sum(abs(x) ** 2 for x in fa))
             assert num / den < mp.mpf(10) ** -30
+
+
+def test_radial_y_without_psi():
+    """Y = psi(z1)/c1^2 - psi(z2)/c2^2 equals ((1 + z1) e1 - (1 + z2) e2) / (s^2 r^2) (c_a^2 z_a^2 =
+    s^2 r^2: the -1 of both psi cancel), and psi(z2)/c2^2 = ((1 + z2) e2 - 1) / (s^2 r^2) -- the forms
+    the FP32 and compensated radial terms evaluate above the series thresholds."""
+    mp.mp.dps = 40
+    rng = np.random.default_rng(11)
+    psi = lambda z: ((1 + z) * mp.exp(-z) - 1) / (z * z)
+    for _ in range(40):
+        nu = mp.mpf(rng.uniform(0.2, 0.45))
+        c2 = mp.mpf(rng.uniform(2, 20))
+        c1 = c2 * mp.sqrt(2 * (1 - nu) / (1 - 2 * nu))
+        r = mp.mpf(10 ** rng.uniform(-3, -0.5))
+        s = mp.mpc(rng.uniform(10, 400), rng.uniform(-400, 400))
+        z1, z2 = r * s / c1, r * s / c2
+        e1, e2 = mp.exp(-z1), mp.exp(-z2)
+        Y = psi(z1) / c1 ** 2 - psi(z2) / c2 ** 2
+        Yc = ((1 + z1) * e1 - (1 + z2) * e2) / (s * s * r * r)
+        assert abs(Y - Yc) / abs(Y) < mp.mpf(10) ** -30
+        p2 = ((1 + z2) * e2 - 1) / (s * s * r * r)
+        assert abs(psi(z2) / c2 ** 2 - p2) / abs(p2) < mp.mpf(10) ** -30
