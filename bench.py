@@ -612,8 +612,9 @@ def galerkin_leg(torch, ctx, stream, nfreq: int = 2, level: int = 4):
 def serving_requests(seed: int, n_requests: int, rate_hz: float):
     """Poisson arrivals; 30% assembly requests (objects from the mixed-size distribution), 70% time
     steps of device-resident objects with seeded Gaussian tractions (10 Pa) and displacements.  A step
-    targets one of the 8 most recently submitted objects: at most 8 banks of the largest class (15.6 GB
-    each) stay under the 150 GB cap, so the targets are resident and not evicted."""
+    targets one of the 4 most recently submitted objects: 4 banks of the largest class (15.6 GB each)
+    plus the two assemblies in flight (31 GB each with their transform buffers) stay under the 150 GB
+    cap, so the targets stay resident under least-recently-used eviction."""
     from surfaceonlydeformables_gb300.meshes import Material, make_icosphere_mesh
 
     rng = np.random.default_rng(seed)
@@ -632,7 +633,7 @@ def serving_requests(seed: int, n_requests: int, rate_hz: float):
             objs.append(len(reqs))
             reqs.append(dict(t=t, type="assembly", mesh=mesh, mat=Material(E, nu, 1000.0), N=N))
         else:
-            recent = objs[-8:]
+            recent = objs[-4:]
             j = recent[int(rng.integers(len(recent)))]
             n = 3 * reqs[j]["mesh"].nV
             reqs.append(dict(t=t, type="step", target=j, p=rng.normal(size=n) * 10.0, u=rng.normal(size=n) * 1e-4))

@@ -40,19 +40,35 @@ __device__ __forceinline__ void df_mac(df &acc, float ahi, float alo, float x) {
     acc.lo += e + fmaf(alo, x, pe);
     acc.hi = s;
 }
+// (A + sign B) g rounded to float, g = (g.x + g.y) a float pair
+__device__ __forceinline__ float df_scaled(df A, df B, float sign, float2 g) {
+    float s, e;
+    two_sum(A.hi, sign * B.hi, s, e);
+    const float lo = e + (A.lo + sign * B.lo);
+    const float p = __fmul_rn(s, g.x);
+    const float pe = fmaf(s, g.x, -p);
+    return p + fmaf(s, g.y, fmaf(lo, g.x, pe));
+}
 
+// FP32 output, double-float accumulation, on the same n <-> L - n symmetry as the FP64 kernel below:
+// A_n = sum_l c_l cos xr_l and B_n = sum_l c_l sin xi_l for n <= L/2, then X_n = g_n (A + B) and
+// X_{L-n} = g_{L-n} (A - B), g_n = R^-n / L as a float pair; the combination and the scaling stay in
+// float arithmetic (TwoSum / TwoProduct), the output is their rounded sum.
 template <int TILE>
 __global__ void __launch_bounds__(TILE) inv_transform_df_kernel(const void *__restrict__ Xhat, int in_c128, long long M,
                                                                int nfreq, int L, const float4 *__restrict__ tw,
-                                                               void *__restrict__ out, int out_f64) {
-    // shared: twiddles [L][nfreq] as float4 (re_hi, re_lo, im_hi, im_lo), entries [nfreq][TILE] hi (+lo)
+                                                               const float2 *__restrict__ gsc, float *__restrict__ out) {
+    // shared: twiddles [L/2 + 1][nfreq] as float4 (c cos hi, lo, c sin hi, lo), scales [L] (hi, lo),
+    // entries [nfreq][TILE] hi (+ lo)
     extern __shared__ float4 sm[];
+    const int nh = L / 2;
     float4 *stw = sm;
-    float2 *sx_hi = reinterpret_cast<float2 *>(stw + L * nfreq);
+    float2 *sg = reinterpret_cast<float2 *>(stw + (nh + 1) * nfreq);
+    float2 *sx_hi = sg + ((L + 1) & ~1);
     float2 *sx_lo = sx_hi + (size_t)nfreq * TILE;
-    for (int t = threadIdx.x; t < L * nfreq; t += TILE) stw[t] = tw[t];
-    const long long e0 = (long long)blockIdx.x * TILE;
-    const long long e = e0 + threadIdx.x;
+    for (int t = threadIdx.x; t < (nh + 1) * nfreq; t += TILE) stw[t] = tw[t];
+    for (int t = threadIdx.x; t < L; t += TILE) sg[t] = gsc[t];
+    const long long e = (long long)blockIdx.x * TILE + threadIdx.x;
     const bool live = e < M;
     for (int l = 0; l < nfreq; l++) {
         float2 hi = make_float2(0.f, 0.f), lo = make_float2(0.f, 0.f);
@@ -70,25 +86,22 @@ __global__ void __launch_bounds__(TILE) inv_transform_df_kernel(const void *__re
     }
     __syncthreads();
     if (!live) return;
-    for (int n = 0; n < L; n++) {
-        df acc = {0.f, 0.f};
+    for (int n = 0; n <= nh; n++) {
+        df A = {0.f, 0.f}, B = {0.f, 0.f};
         for (int l = 0; l < nfreq; l++) {
             const float4 w = stw[n * nfreq + l];
             const float2 x = sx_hi[l * TILE + threadIdx.x];
-            // Re(x * w) = x.re * w.re - x.im * w.im
-            df_mac(acc, w.x, w.y, x.x);
-            df_mac(acc, -w.z, -w.w, x.y);
+            df_mac(A, w.x, w.y, x.x);
+            df_mac(B, w.z, w.w, x.y);
             if (in_c128) {
                 const float2 xl = sx_lo[l * TILE + threadIdx.x];
-                df_mac(acc, w.x, w.y, xl.x);
-                df_mac(acc, -w.z, -w.w, xl.y);
+                df_mac(A, w.x, w.y, xl.x);
+                df_mac(B, w.z, w.w, xl.y);
             }
         }
-        const double v = (double)acc.hi + (double)acc.lo;
-        if (out_f64)
-            reinterpret_cast<double *>(out)[(long long)n * M + e] = v;
-        else
-            reinterpret_cast<float *>(out)[(long long)n * M + e] = (float)v;
+        out[(long long)n * M + e] = df_scaled(A, B, 1.0f, sg[n]);
+        const int m = L - n;
+        if (n >= 1 && m != n) out[(long long)m * M + e] = df_scaled(A, B, -1.0f, sg[m]);
     }
 }
 
@@ -139,34 +152,24 @@ __global__ void __launch_bounds__(TILE) inv_transform_f64_kernel(const void *__r
     }
 }
 
-// c_l cos(2 pi n l / L), c_l sin(2 pi n l / L) for n <= L/2, l < nfreq, and R^-n / L for n < L
-__global__ void twiddle_half_kernel(int L, int nfreq, double R, double2 *tw, double *gsc) {
+// c_l cos(2 pi n l / L), c_l sin(2 pi n l / L) for n <= L/2, l < nfreq, and R^-n / L for n < L: in FP64
+// (tw, gsc) or as float pairs (tw32 = (cos hi, lo, sin hi, lo), g32 = (hi, lo))
+__global__ void twiddle_half_kernel(int L, int nfreq, double R, double2 *tw, double *gsc, float4 *tw32, float2 *g32) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int nh = L / 2;
-    if (t < L) gsc[t] = pow(R, -(double)t) / (double)L;
+    if (t < L) {
+        const double g = pow(R, -(double)t) / (double)L;
+        if (gsc) gsc[t] = g;
+        if (g32) g32[t] = make_float2((float)g, (float)(g - (double)(float)g));
+    }
     if (t >= (nh + 1) * nfreq) return;
     const int n = t / nfreq, l = t % nfreq;
     const double c = (l != 0 && (l != L / 2 || L % 2 == 1)) ? 2.0 : 1.0;
     double sn, cs;
     sincospi(2.0 * (double)(((long long)n * l) % L) / (double)L, &sn, &cs);
-    tw[t] = make_double2(c * cs, c * sn);
-}
-
-// twiddles c_l R^-n / L zeta^-nl for n < L, l < nfreq, generated on the device (no host copy)
-__global__ void twiddle_kernel(int L, int nfreq, double R, double2 *tw64, float4 *tw32) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= L * nfreq) return;
-    const int n = t / nfreq, l = t % nfreq;
-    const bool twice = l != 0 && (l != L / 2 || L % 2 == 1);
-    const double sc = (twice ? 2.0 : 1.0) * pow(R, -(double)n) / (double)L;
-    double sn, cs;
-    sincospi(-2.0 * (double)(((long long)n * l) % L) / (double)L, &sn, &cs);
-    const double re = sc * cs, im = sc * sn;
-    if (tw64) tw64[t] = make_double2(re, im);
-    if (tw32) {
-        const float rh = (float)re, ih = (float)im;
-        tw32[t] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
-    }
+    const double re = c * cs, im = c * sn;
+    if (tw) tw[t] = make_double2(re, im);
+    if (tw32) tw32[t] = make_float4((float)re, (float)(re - (double)(float)re), (float)im, (float)(im - (double)(float)im));
 }
 
 int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, int64_t M, int nfreq, int L, double R,
@@ -183,7 +186,7 @@ int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, i
         double2 *dtw = ctx->twiddle.as<double2>();
         double *dg = reinterpret_cast<double *>(dtw + ntw);
         const size_t nt = std::max(ntw, (size_t)L);
-        twiddle_half_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, stream>>>(L, nfreq, R, dtw, dg);
+        twiddle_half_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, stream>>>(L, nfreq, R, dtw, dg, nullptr, nullptr);
         SOD_CHECK_CUDA(cudaGetLastError());
         ctx->count();
         constexpr int TILE = 128;
@@ -201,21 +204,25 @@ int launch_inverse_transform(sod_context *ctx, const void *Xhat, int in_dtype, i
         ctx->count();
         return SOD_OK;
     }
-    const size_t ntw = (size_t)L * nfreq;
-    SOD_TRY(ctx->twiddle.ensure(sizeof(float4) * ntw));
+    const size_t ntw = (size_t)(L / 2 + 1) * nfreq;
+    SOD_TRY(ctx->twiddle.ensure(sizeof(float4) * ntw + sizeof(float2) * (size_t)L));
     float4 *dtw = ctx->twiddle.as<float4>();
-    twiddle_kernel<<<(unsigned)((ntw + 255) / 256), 256, 0, stream>>>(L, nfreq, R, nullptr, dtw);
+    float2 *dg = reinterpret_cast<float2 *>(dtw + ntw);
+    const size_t nt = std::max(ntw, (size_t)L);
+    twiddle_half_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, stream>>>(L, nfreq, R, nullptr, nullptr, dtw, dg);
     SOD_CHECK_CUDA(cudaGetLastError());
     ctx->count();
     constexpr int TILE = 128;
-    const size_t smem = sizeof(float4) * ntw + sizeof(float2) * (size_t)nfreq * TILE * (in_c128 ? 2 : 1);
+    const size_t smem = sizeof(float4) * ntw + sizeof(float2) * (size_t)((L + 1) & ~1) +
+                        sizeof(float2) * (size_t)nfreq * TILE * (in_c128 ? 2 : 1);
     if (smem > ctx->smem_optin) {
         set_error("inverse transform: too many frequencies for the shared-memory tile");
         return SOD_ERR_UNSUPPORTED;
     }
     SOD_CHECK_CUDA(cudaFuncSetAttribute(inv_transform_df_kernel<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long blocks = (M + TILE - 1) / TILE;
-    inv_transform_df_kernel<TILE><<<(unsigned)blocks, TILE, smem, stream>>>(Xhat, in_c128, M, nfreq, L, dtw, out, 0);
+    inv_transform_df_kernel<TILE><<<(unsigned)blocks, TILE, smem, stream>>>(Xhat, in_c128, M, nfreq, L, dtw, dg,
+                                                                            reinterpret_cast<float *>(out));
     SOD_CHECK_CUDA(cudaGetLastError());
     ctx->count();
     return SOD_OK;

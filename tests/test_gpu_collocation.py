@@ -150,7 +150,10 @@ def test_inverse_transform_matches_fp64(gpu_ctx, oracle, sodlib):
         got32 = api.inverse_transform(gpu_ctx, X32, Lq, R)
         assert rel_fro(got32, ref32) <= 1e-10
         got32f = api.inverse_transform(gpu_ctx, X32, Lq, R, out_dtype=L.F32)
-        assert rel_fro(got32f, ref32) <= 1e-6
+        assert rel_fro(got32f, ref32) <= 2e-7  # the FP32 rounding of the outputs
+        # complex128 input, FP32 output (the request loop's banks): double-float accumulation
+        got64f = api.inverse_transform(gpu_ctx, X, Lq, R, out_dtype=L.F32)
+        assert rel_fro(got64f, ref) <= 2e-7, (N, rel_fro(got64f, ref))
 
 
 def test_inverse_transform_closed_form_weights(gpu_ctx, sodlib):
