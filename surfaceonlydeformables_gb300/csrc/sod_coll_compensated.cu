@@ -338,7 +338,9 @@ __device__ __forceinline__ void comp_scatter_body(const CollArgs &a, const Point
 #pragma unroll
                     for (int cc = 0; cc < NC; cc++) {
                         float4 &s = acc[cc * nV + jj[kk]];
-                        s = f4(cdd4(s) + cdd_norm(part[kk][cc]));
+                        // sloppy double-float add (TwoSum of the high words, low words summed): a row
+                        // entry takes the parts of its ~6 faces, and the epilogue adds hi + lo in FP64
+                        s = f4(cs_add(cdd4(s), part[kk][cc]));
                     }
             }
             if (c + 1 < a.ncolors) {
