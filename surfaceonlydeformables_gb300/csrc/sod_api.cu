@@ -233,9 +233,11 @@ static void face_record(const sod_mesh *m, int f, float4 *rec) {
 namespace {
 // Colouring of the face conflict graph (faces sharing a vertex) with k colours of at most `cap` faces
 // each, by min-conflicts local search with a tabu list: start from a random order, each face taking the
-// least-conflicting colour with room, then move conflicting faces to the colour with room that removes
-// the most conflicts (a move back to the colour it left is barred for 10-19 steps).  Deterministic for
-// a given seed.  Returns false if conflicts remain after the iteration budget.
+// least-conflicting colour with room, then take a conflicting face f and the best of: moving it to a
+// colour with room, or swapping it with one of 16 random faces of a full colour (which keeps every
+// colour's size, so k colours of exactly cap faces are reachable).  A move of f back to the colour it
+// left is barred for 10-19 steps.  Deterministic for a given seed.  Returns false if conflicts remain
+// after the iteration budget.
 bool colour_search(const std::vector<std::vector<int>> &nbr, int nF, int k, int cap, uint64_t seed,
                    std::vector<int> &col, std::vector<int> &size) {
     if ((long long)k * cap < nF) return false;
@@ -243,10 +245,28 @@ bool colour_search(const std::vector<std::vector<int>> &nbr, int nF, int k, int 
     col.assign(nF, -1);
     size.assign(k, 0);
     std::vector<int> C((size_t)nF * k, 0);  // C[f k + c]: neighbours of f in colour c
+    std::vector<std::vector<int>> members(k);
+    std::vector<int> pos(nF, 0);
     std::vector<int> order(nF);
     std::iota(order.begin(), order.end(), 0);
     std::shuffle(order.begin(), order.end(), rng);
     long long conflicts = 0;
+    auto place = [&](int f, int c) {
+        col[f] = c;
+        size[c]++;
+        pos[f] = (int)members[c].size();
+        members[c].push_back(f);
+        for (int g : nbr[f]) C[(size_t)g * k + c]++;
+    };
+    auto take = [&](int f) {
+        const int c = col[f];
+        size[c]--;
+        const int last = members[c].back();
+        members[c][pos[f]] = last;
+        pos[last] = pos[f];
+        members[c].pop_back();
+        for (int g : nbr[f]) C[(size_t)g * k + c]--;
+    };
     for (int f : order) {
         int best = -1;
         for (int c = 0; c < k; c++) {
@@ -255,11 +275,10 @@ bool colour_search(const std::vector<std::vector<int>> &nbr, int nF, int k, int 
                 (C[(size_t)f * k + c] == C[(size_t)f * k + best] && size[c] < size[best]))
                 best = c;
         }
-        col[f] = best;
-        size[best]++;
         conflicts += C[(size_t)f * k + best];
-        for (int g : nbr[f]) C[(size_t)g * k + best]++;
+        place(f, best);
     }
+    auto adjacent = [&](int f, int g) { return std::binary_search(nbr[f].begin(), nbr[f].end(), g); };
     std::vector<long long> tabu((size_t)nF * k, 0);
     std::vector<int> bad;
     const long long budget = 200LL * nF;
@@ -278,22 +297,32 @@ bool colour_search(const std::vector<std::vector<int>> &nbr, int nF, int k, int 
             bad.pop_back();
             continue;
         }
-        int best = -1, bestd = 0;
+        int best = -1, bestg = -1;
+        long long bestd = 0;
         for (int c = 0; c < k; c++) {
-            if (c == c0 || size[c] >= cap || tabu[(size_t)f * k + c] > it) continue;
-            const int d = C[(size_t)f * k + c] - C[(size_t)f * k + c0];
-            if (best < 0 || d < bestd) best = c, bestd = d;
+            if (c == c0 || tabu[(size_t)f * k + c] > it) continue;
+            if (size[c] < cap) {
+                const long long d = C[(size_t)f * k + c] - C[(size_t)f * k + c0];
+                if (best < 0 || d < bestd) best = c, bestg = -1, bestd = d;
+            } else {
+                for (int t = 0; t < 16 && !members[c].empty(); t++) {
+                    const int g = members[c][(size_t)(rng() % members[c].size())];
+                    const int adj = adjacent(f, g) ? 1 : 0;
+                    const long long d = (long long)C[(size_t)f * k + c] - C[(size_t)f * k + c0] +
+                                        C[(size_t)g * k + c0] - C[(size_t)g * k + c] - 2 * adj;
+                    if (best < 0 || d < bestd) best = c, bestg = g, bestd = d;
+                }
+            }
         }
         if (best < 0) continue;
-        col[f] = best;
-        size[c0]--;
-        size[best]++;
+        take(f);
+        if (bestg >= 0) {
+            take(bestg);
+            place(bestg, c0);
+        }
+        place(f, best);
         conflicts += bestd;
         tabu[(size_t)f * k + c0] = it + 10 + (long long)(rng() % 10);
-        for (int g : nbr[f]) {
-            C[(size_t)g * k + c0]--;
-            C[(size_t)g * k + best]++;
-        }
     }
     return conflicts == 0;
 }
