@@ -127,7 +127,9 @@ SOD_HD dd dd_sqrt(dd a) {
 // ---- exp ----
 // e^a for a.hi in [-87, 88]: 2^-47 relative accuracy down to a = -69; below that the low word
 // falls into FP32 subnormals and loses bits, and below -87 the result is flushed to zero.
-SOD_HD dd dd_exp(dd a) {
+// (the table of 2^(j/64) is read through `tab(j)`: the constant table here, a shared-memory copy in
+// kernels whose lanes index it differently)
+template <class Tab> SOD_HD dd dd_exp_t(dd a, const Tab &tab) {
     if (a.hi < -87.0f) return dd{0.0f, 0.0f};
     const float m = rintf(a.hi * kDd64oLn2);
     // r = a - m ln2/64 (m ln2/64 with a three-part constant; m * c1 is exact for |m| < 2^13)
@@ -145,13 +147,17 @@ SOD_HD dd dd_exp(dd a) {
     const int mi = (int)m;
     const int j = mi & 63;
     const int k = (mi - j) / 64;
-    const dd t = dd{c_dd_exp2_tab[j][0], c_dd_exp2_tab[j][1]};
+    const dd t = tab(j);
     return dd_ldexp(t + t * em1, k);
+}
+
+SOD_HD dd dd_exp(dd a) {
+    return dd_exp_t(a, [](int j) { return dd{c_dd_exp2_tab[j][0], c_dd_exp2_tab[j][1]}; });
 }
 
 // ---- sin / cos ----
 // |y.hi| < 400 (|m| < 2^12 keeps m * c1 exact); larger arguments fall back to FP64.
-SOD_HD void dd_sincos(dd y, dd &s, dd &c) {
+template <class Tab> SOD_HD void dd_sincos_t(dd y, dd &s, dd &c, const Tab &tab) {
     if (!(fabsf(y.hi) < 400.0f)) {
         const double v = dd_to(y);
         s = dd_from(sin(v));
@@ -173,10 +179,17 @@ SOD_HD void dd_sincos(dd y, dd &s, dd &c) {
     Q = Q + (u2 * u2) * dd{kDdTwentyFourth_hi, kDdTwentyFourth_lo};
     Q = Q + h * h * h * (-1.0f / 720.0f + h * (1.0f / 40320.0f));
     const int j = ((int)m) & 63;
-    const dd S = dd{c_dd_sincos_tab[j][0], c_dd_sincos_tab[j][1]};
-    const dd C = dd{c_dd_sincos_tab[j][2], c_dd_sincos_tab[j][3]};
+    dd S, C;
+    tab(j, S, C);
     s = S + (S * Q + C * su);
     c = C + (C * Q - S * su);
+}
+
+SOD_HD void dd_sincos(dd y, dd &s, dd &c) {
+    dd_sincos_t(y, s, c, [](int j, dd &S, dd &C) {
+        S = dd{c_dd_sincos_tab[j][0], c_dd_sincos_tab[j][1]};
+        C = dd{c_dd_sincos_tab[j][2], c_dd_sincos_tab[j][3]};
+    });
 }
 
 // ---- complex double-float ----

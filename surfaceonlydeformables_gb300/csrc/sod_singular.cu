@@ -18,6 +18,7 @@
 #include <algorithm>
 
 #include "sod_dd.cuh"
+#include "sod_dd_fast.cuh"
 #include "sod_geom.cuh"
 #include "sod_internal.h"
 
@@ -131,12 +132,14 @@ __device__ __forceinline__ KDD make_kdd(const KConst<double> &k) {
 struct RadialDD {
     cdd z1, z2, e1, e2, psi2, Y;
 };
-__device__ __forceinline__ RadialDD radial_dd(dd r, const KDD &k) {
+// e^-z with the exponential and sine / cosine tables in shared memory (sod_dd_fast.cuh): the
+// constant-memory tables are read with lane-varying indices, which the constant cache serialises
+__device__ __forceinline__ RadialDD radial_dd(dd r, const KDD &k, const DdTabs *tb) {
     RadialDD t;
     t.z1 = k.sc1 * r;
     t.z2 = k.sc2 * r;
-    t.e1 = cdd_exp_neg(t.z1);
-    t.e2 = cdd_exp_neg(t.z2);
+    t.e1 = cdd_exp_neg_tab(t.z1, tb);
+    t.e2 = cdd_exp_neg_tab(t.z2, tb);
     const cdd psi1 = cdd_psi(t.z1, t.e1);
     t.psi2 = cdd_psi(t.z2, t.e2);
     t.Y = psi1 * k.ic1s - t.psi2 * k.ic2s;
@@ -160,7 +163,7 @@ template <int MASK> struct PolarLayout {
 // polar weights, as in the reference's polar rule with the FP64 kernels of sod_device.cuh.
 template <int MASK>
 __device__ __forceinline__ void polar_dd_body(const float2 *__restrict__ tab, int nstar, int nq2, int e,
-                                              const KDD &k, double2 *__restrict__ R) {
+                                              const KDD &k, double2 *__restrict__ R, const DdTabs *tb) {
     using Ly = PolarLayout<MASK>;
     cdd acc[Ly::N];
 #pragma unroll
@@ -169,7 +172,7 @@ __device__ __forceinline__ void polar_dd_body(const float2 *__restrict__ tab, in
         const float2 *t = tab + (size_t)p * POLAR_FIELDS * nstar + e;
         const dd r = ldd(t), rh[3] = {ldd(t + nstar), ldd(t + 2 * nstar), ldd(t + 3 * nstar)};
         const dd rn = ldd(t + 4 * (size_t)nstar), w = ldd(t + 5 * (size_t)nstar);
-        const RadialDD T = radial_dd(r, k);
+        const RadialDD T = radial_dd(r, k, tb);
         if (Ly::DG) {
             const dd wl[3] = {ldd(t + 6 * (size_t)nstar), ldd(t + 7 * (size_t)nstar), ldd(t + 8 * (size_t)nstar)};
             const cdd B = T.e1 * k.ic1s - T.e2 * k.ic2s;
@@ -217,7 +220,7 @@ __device__ __forceinline__ void polar_dd_body(const float2 *__restrict__ tab, in
 // subtraction is frequency-independent and added by the combine kernel).  Scaled by 1/(4 pi) there.
 __device__ __forceinline__ void guig_dd_body(const float2 *__restrict__ tab, int nstar, int nq2, int e,
                                              const double *__restrict__ N, int f, const KDD &k,
-                                             double2 *__restrict__ R) {
+                                             double2 *__restrict__ R, const DdTabs *tb) {
     cdd acc[GUIG_COMPS];
 #pragma unroll
     for (int c = 0; c < GUIG_COMPS; c++) acc[c] = cdd_zero();
@@ -227,7 +230,7 @@ __device__ __forceinline__ void guig_dd_body(const float2 *__restrict__ tab, int
         const dd r = ldd(t), rh[3] = {ldd(t + nstar), ldd(t + 2 * nstar), ldd(t + 3 * nstar)};
         const dd rn = ldd(t + 4 * (size_t)nstar);
         const dd wc[3] = {ldd(t + 5 * (size_t)nstar), ldd(t + 6 * (size_t)nstar), ldd(t + 7 * (size_t)nstar)};
-        const RadialDD T = radial_dd(r, k);
+        const RadialDD T = radial_dd(r, k, tb);
         const cdd Yc = T.Y * k.six_c2s;
         const cdd z1e1 = T.z1 * T.e1, z2e2 = T.z2 * T.e2;
         const cdd ca = Yc + T.e1 * k.k4m1 - T.e2 * 2.0f - z1e1 * k.k1m2;
@@ -350,20 +353,26 @@ template <int MASK>
 __global__ void __launch_bounds__(SING_THREADS) polar_dd_kernel(const float2 *__restrict__ tab, int nstar, int nq2,
                                                                 double2 *__restrict__ R,
                                                                 const __grid_constant__ FreqD fd) {
+    __shared__ DdTabs tb;
+    dd_tabs_load(&tb);
+    __syncthreads();
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nstar) return;
     const KDD k = make_kdd(fd.k[blockIdx.y]);
-    polar_dd_body<MASK>(tab, nstar, nq2, e, k, R + (size_t)blockIdx.y * PolarLayout<MASK>::N * nstar);
+    polar_dd_body<MASK>(tab, nstar, nq2, e, k, R + (size_t)blockIdx.y * PolarLayout<MASK>::N * nstar, &tb);
 }
 
 __global__ void __launch_bounds__(SING_THREADS) guig_dd_kernel(const float2 *__restrict__ tab, int nstar, int nq2,
                                                                const int *__restrict__ star_face,
                                                                const double *__restrict__ N, double2 *__restrict__ R,
                                                                const __grid_constant__ FreqD fd) {
+    __shared__ DdTabs tb;
+    dd_tabs_load(&tb);
+    __syncthreads();
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nstar) return;
     const KDD k = make_kdd(fd.k[blockIdx.y]);
-    guig_dd_body(tab, nstar, nq2, e, N, star_face[e], k, R + (size_t)blockIdx.y * GUIG_COMPS * nstar);
+    guig_dd_body(tab, nstar, nq2, e, N, star_face[e], k, R + (size_t)blockIdx.y * GUIG_COMPS * nstar, &tb);
 }
 
 // one warp per (vertex, frequency); `a` holds frequency 0's pointers
@@ -386,23 +395,29 @@ template <int PM>
 __global__ void __launch_bounds__(SING_THREADS) batch_polar_dd_kernel(const SingBatchObj *__restrict__ objs,
                                                                       const int4 *__restrict__ items,
                                                                       const KConst<double> *__restrict__ kcd) {
+    __shared__ DdTabs tb;
+    dd_tabs_load(&tb);
+    __syncthreads();
     const int4 w = items[blockIdx.x];
     const SingBatchObj &o = objs[w.x];
     const int e = w.z + threadIdx.x;
     if (e >= o.nstar) return;
     const KDD k = make_kdd(kcd[o.kc_off + w.y]);
-    polar_dd_body<PM>(o.polar, o.nstar, o.nq2, e, k, o.Rp + (size_t)w.y * PolarLayout<PM>::N * o.nstar);
+    polar_dd_body<PM>(o.polar, o.nstar, o.nq2, e, k, o.Rp + (size_t)w.y * PolarLayout<PM>::N * o.nstar, &tb);
 }
 
 __global__ void __launch_bounds__(SING_THREADS) batch_guig_dd_kernel(const SingBatchObj *__restrict__ objs,
                                                                      const int4 *__restrict__ items,
                                                                      const KConst<double> *__restrict__ kcd) {
+    __shared__ DdTabs tb;
+    dd_tabs_load(&tb);
+    __syncthreads();
     const int4 w = items[blockIdx.x];
     const SingBatchObj &o = objs[w.x];
     const int e = w.z + threadIdx.x;
     if (e >= o.nstar) return;
     const KDD k = make_kdd(kcd[o.kc_off + w.y]);
-    guig_dd_body(o.guig, o.nstar, o.nq2, e, o.N, o.star_face[e], k, o.Rg + (size_t)w.y * GUIG_COMPS * o.nstar);
+    guig_dd_body(o.guig, o.nstar, o.nq2, e, o.N, o.star_face[e], k, o.Rg + (size_t)w.y * GUIG_COMPS * o.nstar, &tb);
 }
 
 template <int MASK>
