@@ -116,6 +116,11 @@ int64_t sod_context_launch_count(const sod_context *ctx);
 int sod_mesh_create(sod_context *ctx, const double *V, int nV, const int *F, int nF, const double *N,
                     const int *vmap, sod_mesh **mesh);
 int sod_mesh_destroy(sod_mesh *mesh);
+/* The face colouring behind the deterministic scatter, on the host (no device needed): colour[f] for
+ * every face such that no two faces of a colour share a vertex and no colour holds more than
+ * `capacity` faces (the scatter CTA size: one round per colour, one face per thread); *ncolours
+ * receives the colour count.  No reference counterpart (the reference adds with atomics). */
+int sod_face_colouring(const int *F, int nF, int nV, int capacity, int *colour, int *ncolours);
 
 /* ---- Laplace-domain assembly, one frequency (the drop-in kernels) ------------------------- */
 /* Whole-matrix replacement of the reference's per-row / per-pair kernels for one Laplace

@@ -42,6 +42,7 @@ _SIGS = {
     "sod_context_launch_count": ([_P], _c.c_int64),
     "sod_mesh_create": ([_P, _P, _c.c_int, _P, _c.c_int, _P, _P, _P], _c.c_int),
     "sod_mesh_destroy": ([_P], _c.c_int),
+    "sod_face_colouring": ([_P, _c.c_int, _c.c_int, _c.c_int, _P, _P], _c.c_int),
     "sod_cqbem_assemble": ([_P, _P, _c.c_int, _c.c_int, _c.c_double, _c.c_double, _c.c_double, _c.c_double,
                             _c.c_double, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _P, _c.c_int], _c.c_int),
     "sod_cqbem_assemble_frequencies": ([_P, _P, _c.c_int, _c.c_int, _c.c_double, _c.c_double, _c.c_double, _P,

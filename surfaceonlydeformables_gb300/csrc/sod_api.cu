@@ -328,24 +328,16 @@ bool colour_search(const std::vector<std::vector<int>> &nbr, int nF, int k, int 
 }
 }  // namespace
 
-using namespace sod;
-
-// Colouring of faces such that faces of one colour share no vertex and no colour holds more than
-// `threads` faces (one scatter round per colour, each thread one face).  A balanced greedy pass
-// gives about 13 colours on a 5120-face sphere whatever the capacity above ~400 (each face conflicts
-// with ~12 others); a min-conflicts search with k = ceil(nF / threads) colours (then k + 1, k + 2)
-// usually reaches the capacity, so larger CTAs get fewer, fuller colours.  The fewer colours win.
-int sod_mesh::coloured_for(int threads, const Coloured **out) {
-    std::lock_guard<std::recursive_mutex> lock(sched_mu);
-    auto it = coloured.find(threads);
-    if (it != coloured.end()) {
-        *out = it->second.get();
-        return SOD_OK;
-    }
+namespace sod {
+// Colouring of the faces (no two faces of a colour share a vertex, at most `threads` faces per
+// colour): the balanced greedy pass, then, where it is two or more colours above ceil(nF / threads),
+// the capacity search above.  Host-only; the mesh schedules and sod_face_colouring use it.
+void colour_faces(const int *F, int nF, int nV, int threads, std::vector<int> &color, std::vector<int> &size) {
     std::vector<std::vector<int>> vf(nV);
     for (int f = 0; f < nF; f++)
         for (int k = 0; k < 3; k++) vf[F[3 * f + k]].push_back(f);
-    std::vector<int> color(nF, -1), size;
+    color.assign(nF, -1);
+    size.clear();
     std::vector<char> forbidden;
     for (int f = 0; f < nF; f++) {
         forbidden.assign(size.size(), 0);
@@ -390,6 +382,25 @@ int sod_mesh::coloured_for(int threads, const Coloured **out) {
                 break;
             }
     }
+}
+}  // namespace sod
+
+using namespace sod;
+
+// Colouring of faces such that faces of one colour share no vertex and no colour holds more than
+// `threads` faces (one scatter round per colour, each thread one face).  A balanced greedy pass
+// gives about 13 colours on a 5120-face sphere whatever the capacity above ~400 (each face conflicts
+// with ~12 others); a min-conflicts search with k = ceil(nF / threads) colours (then k + 1, k + 2)
+// usually reaches the capacity, so larger CTAs get fewer, fuller colours.  The fewer colours win.
+int sod_mesh::coloured_for(int threads, const Coloured **out) {
+    std::lock_guard<std::recursive_mutex> lock(sched_mu);
+    auto it = coloured.find(threads);
+    if (it != coloured.end()) {
+        *out = it->second.get();
+        return SOD_OK;
+    }
+    std::vector<int> color, size;
+    colour_faces(F.data(), nF, nV, threads, color, size);
     auto C = std::make_unique<Coloured>();
     C->ncolors = (int)size.size();
     C->off.assign(C->ncolors + 1, 0);
@@ -663,6 +674,16 @@ int sod_mesh_create(sod_context *ctx, const double *V, int nV, const int *F, int
     SOD_TRY(upload(m->dFacesNat, rec));
     if (m->has_vmap) SOD_TRY(upload(m->dCanonNat, cn));
     *out = m.release();
+    return SOD_OK;
+}
+
+int sod_face_colouring(const int *F, int nF, int nV, int capacity, int *colour, int *ncolours) {
+    SOD_REQUIRE(F && colour && ncolours && nF >= 1 && nV >= 3 && capacity >= 1, "bad face colouring arguments");
+    for (int t = 0; t < 3 * nF; t++) SOD_REQUIRE(F[t] >= 0 && F[t] < nV, "face index out of range");
+    std::vector<int> color, size;
+    colour_faces(F, nF, nV, capacity, color, size);
+    std::copy(color.begin(), color.end(), colour);
+    *ncolours = (int)size.size();
     return SOD_OK;
 }
 

@@ -86,3 +86,36 @@ def test_mat_file_format_roundtrip(sodlib, tmp_path):
     assert np.array_equal(api.mat_read(None, p, 7, 5), M.astype(np.float32).astype(np.float64))
     with pytest.raises(sodlib.SodError):
         api.mat_read(None, p, 5, 7)  # wrong dimensions are rejected
+
+
+@pytest.mark.parametrize("level,axes", [(2, (1.0, 1.0, 1.0)), (3, (1.4, 0.8, 1.1)), (4, (1.0, 1.0, 1.0)),
+                                        (4, (0.7, 1.5, 1.0))])
+def test_face_colouring_is_a_proper_capacity_colouring(sodlib, level, axes):
+    """The scatter schedule (sod_face_colouring): no two faces of a colour share a vertex (the
+    colour-ordered adds need no atomics), no colour above the CTA size, every colour used, the same
+    result on every call; on the 2562-vertex spheres the capacity search reaches ceil(nF / T)."""
+    from surfaceonlydeformables_gb300.meshes import make_icosphere_mesh
+
+    m = make_icosphere_mesh(level, 0.1, axes=axes, seed=5)
+    F = np.ascontiguousarray(m.F, dtype=np.int32)
+    lib = sodlib.load()
+    for cap in (32, 128, 256, 480, 512):
+        col = np.empty(m.nF, dtype=np.int32)
+        n = ctypes.c_int()
+        assert lib.sod_face_colouring(sodlib.ptr(F), m.nF, m.nV, cap, sodlib.ptr(col), ctypes.byref(n)) == 0
+        k = n.value
+        assert col.min() == 0 and col.max() == k - 1
+        counts = np.bincount(col, minlength=k)
+        assert counts.min() >= 1 and counts.max() <= cap
+        # faces sharing a vertex: every pair of faces in one vertex star has distinct colours
+        for v in range(m.nV):
+            star = col[np.nonzero((F == v).any(axis=1))[0]]
+            assert len(np.unique(star)) == len(star), (cap, v)
+        col2 = np.empty_like(col)
+        lib.sod_face_colouring(sodlib.ptr(F), m.nF, m.nV, cap, sodlib.ptr(col2), ctypes.byref(n))
+        np.testing.assert_array_equal(col, col2)
+        if level == 4 and cap >= 480:
+            assert k == -(-m.nF // cap), (cap, k)
+    bad = np.array([[0, 1, 99]], dtype=np.int32)
+    col = np.empty(1, dtype=np.int32)
+    assert lib.sod_face_colouring(sodlib.ptr(bad), 1, 3, 32, sodlib.ptr(col), ctypes.byref(n)) == sodlib.SOD_ERR_INVALID_ARG
