@@ -113,6 +113,26 @@ __device__ __forceinline__ cdd cs_exp_neg(const cdd &z, const DdTabs *tb) {
     return cdd{sd_mul(mag, cs), sd_neg(sd_mul(mag, sn))};
 }
 
+// acc += x * w for double-float x and w: one TwoSum on the high words, the product's error and the
+// cross terms summed in float into an unnormalised low word (a few dozen terms per accumulator; the
+// caller reads hi + lo at the end).
+__device__ __forceinline__ void sd_fma_acc(dd &acc, dd x, dd w) {
+    const float p = SOD_MUL_RN(x.hi, w.hi);
+    const float e = fmaf(x.hi, w.hi, -p);
+    const dd s = two_sum(acc.hi, p);
+    acc.hi = s.hi;
+    acc.lo += s.lo + fmaf(x.lo, w.hi, fmaf(x.hi, w.lo, e));
+}
+__device__ __forceinline__ void cs_fma_acc(cdd &acc, const cdd &x, dd w) {
+    sd_fma_acc(acc.x, x.x, w);
+    sd_fma_acc(acc.y, x.y, w);
+}
+__device__ __forceinline__ void sd_acc(dd &acc, dd x) {
+    const dd s = two_sum(acc.hi, x.hi);
+    acc.hi = s.hi;
+    acc.lo += s.lo + x.lo;
+}
+
 // e^-z with the renormalised double-float arithmetic of sod_dd.cuh (2^-47 relative) and the tables in
 // shared memory: for the singular passes, whose cancelling traction kernel needs the full accuracy
 __device__ __forceinline__ cdd cdd_exp_neg_tab(const cdd &z, const DdTabs *tb) {

@@ -185,7 +185,7 @@ __device__ __forceinline__ void polar_dd_body(const float2 *__restrict__ tab, in
                     cdd v = al * (rh[p2] * rh[q2]);
                     if (p2 == q2) v = v + be;
 #pragma unroll
-                    for (int c = 0; c < 3; c++) cdd_acc(acc[c * 6 + sym_index(p2, q2)], v, wl[c]);
+                    for (int c = 0; c < 3; c++) cs_fma_acc(acc[c * 6 + sym_index(p2, q2)], v, wl[c]);
                 }
         }
         if (Ly::DT || Ly::DA) {
@@ -194,8 +194,8 @@ __device__ __forceinline__ void polar_dd_body(const float2 *__restrict__ tab, in
                 const cdd ws = T.Y * (pr * 0.5f) * w;
                 const cdd di = T.psi2 * (k.ic2s * pr);
 #pragma unroll
-                for (int p2 = 0; p2 < 3; p2++) cdd_acc(acc[Ly::OT + p2], ws, rh[p2]);
-                cdd_acc(acc[Ly::OT + 3], di, w * rn);
+                for (int p2 = 0; p2 < 3; p2++) cs_fma_acc(acc[Ly::OT + p2], ws, rh[p2]);
+                cs_fma_acc(acc[Ly::OT + 3], di, w * rn);
             }
             if (Ly::DA) {
                 const cdd wA = T.Y * (r * pr * 0.5f) * w;
@@ -204,11 +204,11 @@ __device__ __forceinline__ void polar_dd_body(const float2 *__restrict__ tab, in
 #pragma unroll
                 for (int p2 = 0; p2 < 3; p2++)
 #pragma unroll
-                    for (int q2 = p2; q2 < 3; q2++) cdd_acc(acc[Ly::OA + sym_index(p2, q2)], wA, rh[p2] * rh[q2]);
-                dd_acc(acc[Ly::OA + 6].x, wA.x);
-                dd_acc(acc[Ly::OA + 6].y, wA.y);
-                cdd_acc(acc[Ly::OA + 7], Bq, w);
-                cdd_acc(acc[Ly::OA + 8], Cq, w);
+                    for (int q2 = p2; q2 < 3; q2++) cs_fma_acc(acc[Ly::OA + sym_index(p2, q2)], wA, rh[p2] * rh[q2]);
+                sd_acc(acc[Ly::OA + 6].x, wA.x);
+                sd_acc(acc[Ly::OA + 6].y, wA.y);
+                cs_fma_acc(acc[Ly::OA + 7], Bq, w);
+                cs_fma_acc(acc[Ly::OA + 8], Cq, w);
             }
         }
     }
@@ -244,7 +244,7 @@ __device__ __forceinline__ void guig_dd_body(const float2 *__restrict__ tab, int
                 cdd v = ca * (rh[p2] * nn[q2]) + cb * (nn[p2] * rh[q2]) + cdr * (rh[p2] * rh[q2]);
                 if (p2 == q2) v = v + cbr;
 #pragma unroll
-                for (int c = 0; c < 3; c++) cdd_acc(acc[c * 9 + 3 * p2 + q2], v, wc[c]);
+                for (int c = 0; c < 3; c++) cs_fma_acc(acc[c * 9 + 3 * p2 + q2], v, wc[c]);
             }
     }
 #pragma unroll
