@@ -61,10 +61,6 @@ __device__ __forceinline__ cf cfmar(cf a, float s, cf b) {
     const float2 r = __ffma2_rn(make_float2(a.x, a.y), make_float2(s, s), make_float2(b.x, b.y));
     return {r.x, r.y};
 }
-__device__ __forceinline__ cf crecip(cf a) {
-    const float d = __frcp_rn(fmaf(a.x, a.x, a.y * a.y));
-    return {a.x * d, -a.y * d};
-}
 __device__ __forceinline__ cd crecip(cd a) {
     const double d = 1.0 / fma(a.x, a.x, a.y * a.y);
     return {a.x * d, -a.y * d};
@@ -79,11 +75,6 @@ __device__ __forceinline__ cd crecip(cd a) {
 __device__ __forceinline__ float ex2_approx(float x) {
     float y;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float rcp_approx(float x) {
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
 constexpr float kRound23 = 12582912.0f;  // 1.5 * 2^23: x + kRound23 - kRound23 = round(x), |x| < 2^22
