@@ -25,6 +25,7 @@
 
 #include "sod_bmom.cuh"
 #include "sod_dd.cuh"
+#include "sod_dd_fast.cuh"
 #include "sod_faces.cuh"
 #include "sod_internal.h"
 
@@ -401,6 +402,9 @@ __global__ void __launch_bounds__(128) gal_sing_kernel(GalSingArgs a, const __gr
     constexpr int NA = 9 * NCS + (DB ? 3 * GAL_BMOM : 0), PER = (NA + 31) / 32;
     constexpr int OFF_V = 32 * NCS * 4, OFF_L = OFF_V + (DB ? 32 * GAL_BMOM * 4 : 0);
     extern __shared__ float smem_sing[];
+    __shared__ DdTabs tb;  // exp / sin-cos tables: the lanes' points index them differently
+    dd_tabs_load(&tb);
+    __syncthreads();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= a.npairs) return;
     float *sw = smem_sing + (threadIdx.x >> 5) * sing_warp_floats<KIND, BM>();
@@ -499,7 +503,7 @@ __global__ void __launch_bounds__(128) gal_sing_kernel(GalSingArgs a, const __gr
             Ly[0] = one - yh0, Ly[1] = yh0 - yh1, Ly[2] = yh1;
             // radial terms
             const cdd z1 = k.sc1 * r, z2 = k.sc2 * r;
-            const cdd ez1 = cdd_exp_neg(z1), ez2 = cdd_exp_neg(z2);
+            const cdd ez1 = cdd_exp_neg_tab(z1, &tb), ez2 = cdd_exp_neg_tab(z2, &tb);
             const cdd psi1 = cdd_psi(z1, ez1), psi2 = cdd_psi(z2, ez2);
             const cdd Y = psi1 * k.ic1s - psi2 * k.ic2s;
             if (KIND == SOD_G) {
@@ -580,13 +584,13 @@ __global__ void __launch_bounds__(128) gal_sing_kernel(GalSingArgs a, const __gr
                 const int ac = q / (3 * NCS), b = (q / NCS) % 3, c = q % NCS;
                 for (int pt = 0; pt < 32; pt++) {
                     const float *L = sw + OFF_L + pt * 24 + 6 + 2 * (3 * ac + b);
-                    cdd_acc(acc[t], ld_cdd(sw + (pt * NCS + c) * 4), dd{L[0], L[1]});
+                    cs_fma_acc(acc[t], ld_cdd(sw + (pt * NCS + c) * 4), dd{L[0], L[1]});
                 }
             } else if (DB) {
                 const int qm = q - 9 * NCS, ac = qm / GAL_BMOM, c = qm % GAL_BMOM;
                 for (int pt = 0; pt < 32; pt++) {
                     const float *L = sw + OFF_L + pt * 24;
-                    cdd_acc(acc[t], ld_cdd(sw + OFF_V + (pt * GAL_BMOM + c) * 4), dd{L[2 * ac], L[2 * ac + 1]});
+                    cs_fma_acc(acc[t], ld_cdd(sw + OFF_V + (pt * GAL_BMOM + c) * 4), dd{L[2 * ac], L[2 * ac + 1]});
                 }
             }
         }
