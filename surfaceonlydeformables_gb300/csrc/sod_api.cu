@@ -3,6 +3,8 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <numeric>
 #include <random>
 #include <set>
@@ -281,7 +283,7 @@ bool colour_search(const std::vector<std::vector<int>> &nbr, int nF, int k, int 
     auto adjacent = [&](int f, int g) { return std::binary_search(nbr[f].begin(), nbr[f].end(), g); };
     std::vector<long long> tabu((size_t)nF * k, 0);
     std::vector<int> bad;
-    const long long budget = 200LL * nF;
+    const long long budget = 20LL * nF;  // feasible sizes converge in a few hundred steps
     for (long long it = 1; conflicts > 0 && it <= budget; it++) {
         if (bad.empty() || (it & 255) == 0) {
             bad.clear();
@@ -332,7 +334,8 @@ namespace sod {
 // Colouring of the faces (no two faces of a colour share a vertex, at most `threads` faces per
 // colour): the balanced greedy pass, then, where it is two or more colours above ceil(nF / threads),
 // the capacity search above.  Host-only; the mesh schedules and sod_face_colouring use it.
-void colour_faces(const int *F, int nF, int nV, int threads, std::vector<int> &color, std::vector<int> &size) {
+static void colour_faces_compute(const int *F, int nF, int nV, int threads, std::vector<int> &color,
+                                 std::vector<int> &size) {
     std::vector<std::vector<int>> vf(nV);
     for (int f = 0; f < nF; f++)
         for (int k = 0; k < 3; k++) vf[F[3 * f + k]].push_back(f);
@@ -354,7 +357,11 @@ void colour_faces(const int *F, int nF, int nV, int threads, std::vector<int> &c
         color[f] = best;
         size[best]++;
     }
-    if ((int)size.size() >= (nF + threads - 1) / threads + 2) {  // the greedy pass is 2+ colours above the bound
+    // lower bound: the faces around a vertex all conflict, so at least the largest valence
+    int valence = 0;
+    for (int v = 0; v < nV; v++) valence = std::max(valence, (int)vf[v].size());
+    const int kb = std::max((nF + threads - 1) / threads, valence);
+    if ((int)size.size() >= kb + 2) {  // the greedy pass is 2+ colours above the bound
         std::vector<std::vector<int>> nbr(nF);
         for (int f = 0; f < nF; f++) {
             for (int k = 0; k < 3; k++)
@@ -363,7 +370,7 @@ void colour_faces(const int *F, int nF, int nV, int threads, std::vector<int> &c
             std::sort(nbr[f].begin(), nbr[f].end());
             nbr[f].erase(std::unique(nbr[f].begin(), nbr[f].end()), nbr[f].end());
         }
-        const int k0 = (nF + threads - 1) / threads;
+        const int k0 = kb;
         std::vector<int> col2, size2;
         for (int k = k0; k < (int)size.size() && k <= k0 + 2; k++)
             if (colour_search(nbr, nF, k, threads, 0x5eedull + (uint64_t)k, col2, size2)) {
@@ -383,7 +390,49 @@ void colour_faces(const int *F, int nF, int nV, int threads, std::vector<int> &c
             }
     }
 }
-}  // namespace sod
+
+// The colouring depends only on the connectivity: objects of one topology (a request loop's spheres of
+// one level, say) share it, so results are kept per (F, nV, capacity), up to 64 of them.
+void colour_faces(const int *F, int nF, int nV, int threads, std::vector<int> &color, std::vector<int> &size) {
+    uint64_t h = 1469598103934665603ull;  // FNV-1a over the connectivity
+    auto mix = [&h](uint64_t x) {
+        for (int b = 0; b < 8; b++) {
+            h ^= (x >> (8 * b)) & 0xff;
+            h *= 1099511628211ull;
+        }
+    };
+    mix((uint64_t)nV);
+    mix((uint64_t)nF);
+    mix((uint64_t)threads);
+    for (int t = 0; t < 3 * nF; t++) mix((uint64_t)(uint32_t)F[t]);
+    struct Entry {
+        std::vector<int> F, color, size;
+        int nV, threads;
+    };
+    static std::mutex mu;
+    static std::map<uint64_t, Entry> cache;
+    static std::vector<uint64_t> order;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = cache.find(h);
+        if (it != cache.end() && it->second.nV == nV && it->second.threads == threads &&
+            it->second.F.size() == (size_t)3 * nF && std::equal(it->second.F.begin(), it->second.F.end(), F)) {
+            color = it->second.color;
+            size = it->second.size;
+            return;
+        }
+    }
+    colour_faces_compute(F, nF, nV, threads, color, size);
+    std::lock_guard<std::mutex> g(mu);
+    if (!cache.count(h)) {
+        if (order.size() >= 64) {
+            cache.erase(order.front());
+            order.erase(order.begin());
+        }
+        cache[h] = Entry{std::vector<int>(F, F + 3 * nF), color, size, nV, threads};
+        order.push_back(h);
+    }
+}}  // namespace sod
 
 using namespace sod;
 
