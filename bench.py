@@ -774,6 +774,16 @@ def serving_leg(torch, ctx, n_requests: int = 240, rate_hz: float = 30.0, cap_gb
     return out
 
 
+def max_over_ranks(torch, t_local: float, dist, device) -> float:
+    """The job's time: every rank's timed-region seconds, reduced by max after a barrier (replicas
+    run independently; the slowest sets the whole-job rate).  `dist` is torch.distributed or None."""
+    t = torch.tensor([t_local], dtype=torch.float64, device=device)
+    if dist:
+        dist.barrier()
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     objs = CASES[args.case]()
     threads = os.cpu_count() or 1
@@ -894,12 +904,7 @@ def run_gpu(args):
             times.append(e0.elapsed_time(e1) * 1e-3)
     launches = ctx.launches - launches0
     torch.cuda.synchronize()
-    t_local = float(sum(times))
-    t = torch.tensor([t_local], device=dev)
-    if dist:
-        dist.barrier()
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    t_max = float(t.item())
+    t_max = max_over_ranks(torch, float(sum(times)), dist, dev)
     value = world * total_entries * args.steps / t_max
     # check of the timed step's own outputs (after the timed region): sampled rows against the FP64 oracle
     accuracy = None if args.value_only else check_batched_rows(objs, outs)
