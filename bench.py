@@ -563,7 +563,7 @@ def solve_leg(torch, ctx, stream, n: int = 7686, K: int = 8):
 
 
 def galerkin_leg(torch, ctx, stream, nfreq: int | None = None, level: int = 4):
-    """Galerkin G and H of the jittered icosphere (level 4 = 2562 vertices, configs[1]: E 1e5, nu 0.45,
+    """Galerkin G and H of the jittered icosphere (level 4 = 2562 vertices, the Galerkin case: E 1e5, nu 0.45,
     dt 1/200, N = 64 -> 33 Laplace frequencies; 13-point rule for regular pairs, Sauter-Schwab order 5
     for the singular ones), timed over all 33 frequencies (or `nfreq` of them, from l = 1), with four
     rows of the first and the last timed frequency checked against the FP64 oracle (the rows of the
