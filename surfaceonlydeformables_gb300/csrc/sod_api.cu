@@ -243,10 +243,11 @@ namespace {
 bool colour_search(const std::vector<std::vector<int>> &nbr, int nF, int k, int cap, uint64_t seed,
                    std::vector<int> &col, std::vector<int> &size) {
     if ((long long)k * cap < nF) return false;
+    if ((size_t)nF * (size_t)k > ((size_t)1 << 24)) return false;  // host memory: 6 bytes per (face, colour)
     std::mt19937_64 rng(seed);
     col.assign(nF, -1);
     size.assign(k, 0);
-    std::vector<int> C((size_t)nF * k, 0);  // C[f k + c]: neighbours of f in colour c
+    std::vector<int16_t> C((size_t)nF * k, 0);  // C[f k + c]: neighbours of f in colour c
     std::vector<std::vector<int>> members(k);
     std::vector<int> pos(nF, 0);
     std::vector<int> order(nF);
@@ -281,7 +282,7 @@ bool colour_search(const std::vector<std::vector<int>> &nbr, int nF, int k, int 
         place(f, best);
     }
     auto adjacent = [&](int f, int g) { return std::binary_search(nbr[f].begin(), nbr[f].end(), g); };
-    std::vector<long long> tabu((size_t)nF * k, 0);
+    std::vector<int> tabu((size_t)nF * k, 0);  // iteration until which the move is barred
     std::vector<int> bad;
     const long long budget = 20LL * nF;  // feasible sizes converge in a few hundred steps
     for (long long it = 1; conflicts > 0 && it <= budget; it++) {
@@ -324,7 +325,7 @@ bool colour_search(const std::vector<std::vector<int>> &nbr, int nF, int k, int 
         }
         place(f, best);
         conflicts += bestd;
-        tabu[(size_t)f * k + c0] = it + 10 + (long long)(rng() % 10);
+        tabu[(size_t)f * k + c0] = (int)(it + 10 + (long long)(rng() % 10));
     }
     return conflicts == 0;
 }
