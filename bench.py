@@ -1056,6 +1056,7 @@ def run_gpu(args):
                            "parallelism": f"replicas x{world}"},
                 "roofline": roofline, "cpu_baseline": cpu, "accuracy": accuracy,
                 "paths": paths,
+                "batched_over_plain": paths.get("batched_over_plain"),
                 "e2e": {"value": e2e_value, "unit": "entries/s", "h2d_bytes_per_step": h2d_bytes,
                         "d2h_bytes_per_step": d2h_bytes, "path": "sod_cqbem_assemble_all per object (the frequency-loop "
                         "drop-in of all four kinds) into pinned host memory, complex128 reference layout, "
