@@ -67,3 +67,26 @@ def test_reference_arm_other_ranks_exit_without_work(monkeypatch):
         gpus = 2
 
     assert bench.run_reference(Args()) == 0
+
+
+def test_serving_requests_target_resident_objects():
+    """The request stream of the serving leg: Poisson arrivals, ~30% assemblies, and every step targets
+    one of the four most recently submitted objects (so that it stays resident under the HBM cap)."""
+    import numpy as np
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    reqs = bench.serving_requests(7, 400, 30.0)
+    t = np.array([r["t"] for r in reqs])
+    assert np.all(np.diff(t) > 0)
+    assert abs(len(reqs) / t[-1] - 30.0) < 6.0
+    n_asm = sum(r["type"] == "assembly" for r in reqs)
+    assert 0.2 < n_asm / len(reqs) < 0.4
+    submitted = []
+    for k, r in enumerate(reqs):
+        if r["type"] == "assembly":
+            submitted.append(k)
+        else:
+            assert r["target"] in submitted[-4:]
+            assert len(r["p"]) == 3 * reqs[r["target"]]["mesh"].nV
