@@ -79,30 +79,39 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
                     const float r = r2 * rinv;
                     const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
                     const RadialTerms<float, cf> t = radial<(NCB > 0)>(r, rinv, k);
+                    // u without its common factor (1/(4 pi rho r) for G, 1/(4 pi r^2) for H), which
+                    // goes into the weight; the tensors are built from per-row vectors, so that each
+                    // entry is two packed operations:
+                    //   G: u_pq = (al rh_p) rh_q + be d_pq
+                    //   H: u_pq = (hd rn rh_p + hb n_p) rh_q + (ha rh_p) n_q + hb rn d_pq
                     cf u[NC];
+                    float sc;
                     if (KIND == SOD_G) {
                         cf al, be;
-                        g_coeffs(t, k, rinv, al, be);
+                        g_coeffs_unit(t, k, al, be);
+                        sc = k.inv4pirho * rinv;
 #pragma unroll
-                        for (int p = 0; p < 3; p++)
+                        for (int p = 0; p < 3; p++) {
+                            const cf ar = cmulr(al, rh[p]);
 #pragma unroll
                             for (int qq = p; qq < 3; qq++)
-                                u[sym_index(p, qq)] = p == qq ? cfmar(al, rh[p] * rh[qq], be) : cmulr(al, rh[p] * rh[qq]);
+                                u[sym_index(p, qq)] = p == qq ? cfmar(ar, rh[qq], be) : cmulr(ar, rh[qq]);
+                        }
                     } else {
                         cf ha, hb, hd;
-                        h_coeffs(t, k, rinv * rinv, ha, hb, hd);
+                        h_coeffs_unit(t, k, ha, hb, hd);
+                        sc = k.inv4pi * (rinv * rinv);
                         const float rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
                         const cf hdr = cmulr(hd, rn), hbr = cmulr(hb, rn);
 #pragma unroll
-                        for (int p = 0; p < 3; p++)
+                        for (int p = 0; p < 3; p++) {
+                            const cf dp = cfmar(hdr, rh[p], cmulr(hb, nn[p])), bp = cmulr(ha, rh[p]);
 #pragma unroll
-                            for (int qq = 0; qq < 3; qq++) {
-                                cf v = cfmar(hdr, rh[p] * rh[qq], p == qq ? hbr : mk(0.f, 0.f));
-                                v = cfmar(hb, nn[p] * rh[qq], v);
-                                u[3 * p + qq] = cfmar(ha, rh[p] * nn[qq], v);
-                            }
+                            for (int qq = 0; qq < 3; qq++)
+                                u[3 * p + qq] = cfmar(dp, rh[qq], p == qq ? cfmar(bp, nn[qq], hbr) : cmulr(bp, nn[qq]));
+                        }
                     }
-                    const float w = P.w * fr.area;
+                    const float w = P.w * fr.area * sc;
                     const float wl[3] = {w * P.x, w * P.y, w * P.z};
 #pragma unroll
                     for (int kk = 0; kk < 3; kk++)

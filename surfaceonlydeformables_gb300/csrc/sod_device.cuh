@@ -224,22 +224,34 @@ __device__ __forceinline__ RadialTerms<float, cf> radial(float r, float rinv, co
     }
     return t;
 }
-__device__ __forceinline__ void g_coeffs(const RadialTerms<float, cf> &t, const KConst<float> &k, float scale,
-                                         cf &alpha, cf &beta) {
+// The _unit forms leave out the common factor (1/(4 pi rho) for G, 1/(4 pi) for H, times `scale`),
+// for callers that fold it into their quadrature weight.
+__device__ __forceinline__ void g_coeffs_unit(const RadialTerms<float, cf> &t, const KConst<float> &k, cf &alpha,
+                                              cf &beta) {
     const cf Cc = cmulr(t.e2, k.ic2s);
     const cf B = cfmar(t.e1, k.ic1s, cmulr(Cc, -1.0f));
-    const float p = k.inv4pirho * scale;
-    alpha = cmulr(cfmar(t.Y, 3.0f, B), p);
-    beta = cmulr(cfmar(t.Y, -1.0f, Cc), p);
+    alpha = cfmar(t.Y, 3.0f, B);
+    beta = cfmar(t.Y, -1.0f, Cc);
 }
-__device__ __forceinline__ void h_coeffs(const RadialTerms<float, cf> &t, const KConst<float> &k, float scale,
-                                         cf &a, cf &b, cf &d) {
+__device__ __forceinline__ void g_coeffs(const RadialTerms<float, cf> &t, const KConst<float> &k, float scale,
+                                         cf &alpha, cf &beta) {
+    g_coeffs_unit(t, k, alpha, beta);
+    const float p = k.inv4pirho * scale;
+    alpha = cmulr(alpha, p);
+    beta = cmulr(beta, p);
+}
+__device__ __forceinline__ void h_coeffs_unit(const RadialTerms<float, cf> &t, const KConst<float> &k, cf &a, cf &b,
+                                              cf &d) {
     const cf Yc = cmulr(t.Y, k.six_c2s);
     const cf z1e1 = t.z1 * t.e1, z2e2 = t.z2 * t.e2;
     const float kp = k.kappa;
     a = cfmar(z1e1, -(1.0f - 2.0f * kp), cfmar(t.e2, -2.0f, cfmar(t.e1, 4.0f * kp - 1.0f, Yc)));
     b = cfmar(z2e2, -1.0f, cfmar(t.e2, -3.0f, cfmar(t.e1, 2.0f * kp, Yc)));
     d = cfmar(z2e2, 2.0f, cfmar(z1e1, -2.0f * kp, cfmar(t.e2, 12.0f, cfmar(t.e1, -12.0f * kp, cmulr(Yc, -5.0f)))));
+}
+__device__ __forceinline__ void h_coeffs(const RadialTerms<float, cf> &t, const KConst<float> &k, float scale,
+                                         cf &a, cf &b, cf &d) {
+    h_coeffs_unit(t, k, a, b, d);
     const float p = k.inv4pi * scale;
     a = cmulr(a, p);
     b = cmulr(b, p);
