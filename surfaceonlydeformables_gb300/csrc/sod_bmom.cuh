@@ -17,16 +17,16 @@ namespace sod {
 template <int BM> struct BMom {
     static constexpr bool BT = (BM & (1 << SOD_B_TRANS)) != 0, BA = (BM & (1 << SOD_B_ANGULAR)) != 0;
     static constexpr int NT = BT ? 6 : 0, NA = BA ? 18 : 0, NC = NT + NA;
-    cf Ms[3], Md, M1[6], M0, SB, SC;
+    cf Ms[3], Md, M1[6], M0, SE, SC;
     __device__ __forceinline__ void zero() {
 #pragma unroll
         for (int c = 0; c < 3; c++) Ms[c] = mk(0.f, 0.f);
 #pragma unroll
         for (int c = 0; c < 6; c++) M1[c] = mk(0.f, 0.f);
-        Md = M0 = SB = SC = mk(0.f, 0.f);
+        Md = M0 = SE = SC = mk(0.f, 0.f);
     }
     // Ms_p += Y w rh_p, Md += psi2 w rn;  M1_pk += Y r w rh_p rh_k, M0 += Y r w,
-    // SB += (e2/c2 - e1/c1) w, SC += e2 w
+    // SE += e1 w, SC += e2 w (the sum of (e2/c2 - e1/c1) w is SC/c2 - SE/c1, formed at the emit)
     __device__ __forceinline__ void add(const RadialTerms<float, cf> &t, const KConst<float> &k, float r,
                                         const float rh[3], const float nn[3], float w) {
         if (BT) {
@@ -38,12 +38,13 @@ template <int BM> struct BMom {
         if (BA) {
             const cf wA = cmulr(t.Y, r * w);
 #pragma unroll
-            for (int p = 0; p < 3; p++)
+            for (int p = 0; p < 3; p++) {
+                const cf wp = cmulr(wA, rh[p]);
 #pragma unroll
-                for (int kk = p; kk < 3; kk++) cfma(M1[sym_index(p, kk)], wA, rh[p] * rh[kk]);
+                for (int kk = p; kk < 3; kk++) cfma(M1[sym_index(p, kk)], wp, rh[kk]);
+            }
             M0 = M0 + wA;
-            cfma(SB, t.e2, w * k.ic2);
-            cfma(SB, t.e1, -w * k.ic1);
+            cfma(SE, t.e1, w);
             cfma(SC, t.e2, w);
         }
     }
@@ -70,6 +71,7 @@ template <int BM> struct BMom {
             const cf is = mk(k.isr, k.isi);
 #pragma unroll
             for (int c = 0; c < 6; c++) M1[c] = cmulr(M1[c], half);
+            const cf SB = cfmar(SE, -k.ic1, cmulr(SC, k.ic2));
             const cf M0B = cmulr(M0, half) + cmulr(SB * is, half);
             const cf SCs = cmulr(SC * is, k.ic2 * k.inv4pi * ar);
 #pragma unroll

@@ -61,6 +61,10 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
                 const FaceRec fr = load_face(a.faces, f);
                 if (is_singular(a, i, ci, f, fr)) continue;
                 const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
+                // corners relative to the collocation point: y - x = sum_l P_l (y_l - x)
+                const float3 d1 = make_float3(fr.y1.x - x.x, fr.y1.y - x.y, fr.y1.z - x.z),
+                             d2 = make_float3(fr.y2.x - x.x, fr.y2.y - x.y, fr.y2.z - x.z),
+                             d3 = make_float3(fr.y3.x - x.x, fr.y3.y - x.y, fr.y3.z - x.z);
                 cf part[3][NC];
 #pragma unroll
                 for (int kk = 0; kk < 3; kk++)
@@ -70,10 +74,9 @@ __device__ __forceinline__ void scatter_body(const CollArgs &a, const PointTable
                 if (NCB) bm.zero();
                 for (int q = 0; q < pt.n; q++) {
                     const float4 P = pt.p[q];
-                    const float yx = P.x * fr.y1.x + P.y * fr.y2.x + P.z * fr.y3.x;
-                    const float yy = P.x * fr.y1.y + P.y * fr.y2.y + P.z * fr.y3.y;
-                    const float yz = P.x * fr.y1.z + P.y * fr.y2.z + P.z * fr.y3.z;
-                    const float dx = yx - x.x, dy = yy - x.y, dz = yz - x.z;
+                    const float dx = P.x * d1.x + P.y * d2.x + P.z * d3.x;
+                    const float dy = P.x * d1.y + P.y * d2.y + P.z * d3.y;
+                    const float dz = P.x * d1.z + P.y * d2.z + P.z * d3.z;
                     const float r2 = dx * dx + dy * dy + dz * dz;
                     const float rinv = rsqrtf(r2);
                     const float r = r2 * rinv;
