@@ -145,6 +145,10 @@ __global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_tp_kernel(
                                p2 == q1 || p2 == q2;
             if (touch) continue;  // singular pair (coincident, edge- or vertex-adjacent)
             const float nn[3] = {fr.n.x, fr.n.y, fr.n.z};
+            // corners relative to the test point: y - x = sum_l P_l (y_l - x)
+            const float3 d1 = make_float3(fr.y1.x - x.x, fr.y1.y - x.y, fr.y1.z - x.z),
+                         d2 = make_float3(fr.y2.x - x.x, fr.y2.y - x.y, fr.y2.z - x.z),
+                         d3 = make_float3(fr.y3.x - x.x, fr.y3.y - x.y, fr.y3.z - x.z);
             cf part[3][NC];
 #pragma unroll
             for (int kk = 0; kk < 3; kk++)
@@ -154,38 +158,44 @@ __global__ void __launch_bounds__(gal_max_threads<KIND, BM>(), 1) gal_tp_kernel(
             if (NCB) bm.zero();
             for (int q = 0; q < pt.n; q++) {
                 const float4 P = pt.p[q];
-                const float dx = P.x * fr.y1.x + P.y * fr.y2.x + P.z * fr.y3.x - x.x;
-                const float dy = P.x * fr.y1.y + P.y * fr.y2.y + P.z * fr.y3.y - x.y;
-                const float dz = P.x * fr.y1.z + P.y * fr.y2.z + P.z * fr.y3.z - x.z;
+                const float dx = P.x * d1.x + P.y * d2.x + P.z * d3.x;
+                const float dy = P.x * d1.y + P.y * d2.y + P.z * d3.y;
+                const float dz = P.x * d1.z + P.y * d2.z + P.z * d3.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 const float rinv = rsqrtf(r2);
                 const float r = r2 * rinv;
                 const float rh[3] = {dx * rinv, dy * rinv, dz * rinv};
                 const RadialTerms<float, cf> rt = radial<(NCB > 0)>(r, rinv, k);
+                // the collocation scatter's tensor build: per-row vectors, the common factor
+                // (1/(4 pi rho r) for G, 1/(4 pi r^2) for H) in the weight
                 cf u[NC];
+                float sc;
                 if (KIND == SOD_G) {
                     cf al, be;
-                    g_coeffs(rt, k, rinv, al, be);
+                    g_coeffs_unit(rt, k, al, be);
+                    sc = k.inv4pirho * rinv;
 #pragma unroll
-                    for (int p = 0; p < 3; p++)
+                    for (int p = 0; p < 3; p++) {
+                        const cf ar = cmulr(al, rh[p]);
 #pragma unroll
                         for (int qq = p; qq < 3; qq++)
-                            u[sym_index(p, qq)] = p == qq ? cfmar(al, rh[p] * rh[qq], be) : cmulr(al, rh[p] * rh[qq]);
+                            u[sym_index(p, qq)] = p == qq ? cfmar(ar, rh[qq], be) : cmulr(ar, rh[qq]);
+                    }
                 } else {
                     cf ha, hb, hd;
-                    h_coeffs(rt, k, rinv * rinv, ha, hb, hd);
+                    h_coeffs_unit(rt, k, ha, hb, hd);
+                    sc = k.inv4pi * (rinv * rinv);
                     const float rn = rh[0] * nn[0] + rh[1] * nn[1] + rh[2] * nn[2];
                     const cf hdr = cmulr(hd, rn), hbr = cmulr(hb, rn);
 #pragma unroll
-                    for (int p = 0; p < 3; p++)
+                    for (int p = 0; p < 3; p++) {
+                        const cf dp = cfmar(hdr, rh[p], cmulr(hb, nn[p])), bp = cmulr(ha, rh[p]);
 #pragma unroll
-                        for (int qq = 0; qq < 3; qq++) {
-                            cf v = cfmar(hdr, rh[p] * rh[qq], p == qq ? hbr : mk(0.f, 0.f));
-                            v = cfmar(hb, nn[p] * rh[qq], v);
-                            u[3 * p + qq] = cfmar(ha, rh[p] * nn[qq], v);
-                        }
+                        for (int qq = 0; qq < 3; qq++)
+                            u[3 * p + qq] = cfmar(dp, rh[qq], p == qq ? cfmar(bp, nn[qq], hbr) : cmulr(bp, nn[qq]));
+                    }
                 }
-                const float w = P.w * fr.area;
+                const float w = P.w * fr.area * sc;
                 const float wl[3] = {w * P.x, w * P.y, w * P.z};
 #pragma unroll
                 for (int kk = 0; kk < 3; kk++)
