@@ -119,3 +119,72 @@ def test_face_colouring_is_a_proper_capacity_colouring(sodlib, level, axes):
     bad = np.array([[0, 1, 99]], dtype=np.int32)
     col = np.empty(1, dtype=np.int32)
     assert lib.sod_face_colouring(sodlib.ptr(bad), 1, 3, 32, sodlib.ptr(col), ctypes.byref(n)) == sodlib.SOD_ERR_INVALID_ARG
+
+
+_COLOUR_CASES = ((2, 96), (3, 160), (3, 224), (4, 448))  # (icosphere level, capacity): not used above
+
+_COLOUR_CHILD = r"""
+import ctypes, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from surfaceonlydeformables_gb300 import _lib
+from surfaceonlydeformables_gb300.meshes import make_icosphere_mesh
+lib = _lib.load()
+out = []
+for level, cap in %r:
+    m = make_icosphere_mesh(level, 0.1, seed=5)
+    F = np.ascontiguousarray(m.F, dtype=np.int32)
+    col = np.empty(m.nF, dtype=np.int32)
+    n = ctypes.c_int()
+    assert lib.sod_face_colouring(_lib.ptr(F), m.nF, m.nV, cap, _lib.ptr(col), ctypes.byref(n)) == 0
+    out.append(col)
+np.savez(sys.argv[2], *out)
+"""
+
+
+def test_face_colouring_same_across_processes_and_threads(sodlib, tmp_path):
+    """The scatter's summation order follows the colouring, so it must not depend on the process or
+    on the cache: a fresh process (cold cache) and eight concurrent callers in this one (cache misses
+    racing on the same connectivity, then hits) give the same colours."""
+    import subprocess
+    import sys
+    import threading
+
+    from surfaceonlydeformables_gb300.meshes import make_icosphere_mesh
+
+    out = tmp_path / "colours.npz"
+    subprocess.run([sys.executable, "-c", _COLOUR_CHILD % (_COLOUR_CASES,), ROOT, str(out)], check=True,
+                   timeout=600)
+    ref = np.load(out)
+    ref = [ref[f"arr_{t}"] for t in range(len(_COLOUR_CASES))]
+    lib = sodlib.load()
+    meshes = []
+    for level, cap in _COLOUR_CASES:
+        m = make_icosphere_mesh(level, 0.1, seed=5)
+        meshes.append((np.ascontiguousarray(m.F, dtype=np.int32), m.nF, m.nV, cap))
+    got = [[None] * len(meshes) for _ in range(8)]
+    errors = []
+
+    def worker(w):
+        try:
+            for t in range(len(meshes)):
+                i = (t + w) % len(meshes)  # callers start on different meshes
+                F, nF, nV, cap = meshes[i]
+                col = np.empty(nF, dtype=np.int32)
+                n = ctypes.c_int()
+                rc = lib.sod_face_colouring(sodlib.ptr(F), nF, nV, cap, sodlib.ptr(col), ctypes.byref(n))
+                got[w][i] = (rc, col)
+        except Exception as e:  # reported below, on the test's thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(w,)) for w in range(8)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    for w in range(8):
+        for i in range(len(meshes)):
+            rc, col = got[w][i]
+            assert rc == 0
+            np.testing.assert_array_equal(col, ref[i], err_msg=f"caller {w}, case {_COLOUR_CASES[i]}")
