@@ -121,6 +121,37 @@ def test_face_colouring_is_a_proper_capacity_colouring(sodlib, level, axes):
     assert lib.sod_face_colouring(sodlib.ptr(bad), 1, 3, 32, sodlib.ptr(col), ctypes.byref(n)) == sodlib.SOD_ERR_INVALID_ARG
 
 
+@pytest.mark.parametrize("fixture,keys", [("bunny_mesh.npz", ("V", "F")), ("cube_meshes.npz", ("V_cont", "F_cont")),
+                                          ("cube_meshes.npz", ("V_disc", "F_disc"))])
+def test_face_colouring_on_scene_meshes(sodlib, fixture, keys):
+    """The reference's own scene meshes (irregular valence; the split cube has duplicated vertices
+    along its traction discontinuities): proper capacity colourings, never below the lower bound
+    max(ceil(nF / T), largest vertex valence); the bunny reaches that bound."""
+    d = np.load(os.path.join(ROOT, "tests", "golden", fixture))
+    V, F = d[keys[0]], np.ascontiguousarray(d[keys[1]], dtype=np.int32)
+    nV, nF = len(V), len(F)
+    valence = int(np.bincount(F.ravel(), minlength=nV).max())
+    lib = sodlib.load()
+    for cap in (128, 256, 512):
+        col = np.empty(nF, dtype=np.int32)
+        n = ctypes.c_int()
+        assert lib.sod_face_colouring(sodlib.ptr(F), nF, nV, cap, sodlib.ptr(col), ctypes.byref(n)) == 0
+        k = n.value
+        counts = np.bincount(col, minlength=k)
+        assert col.min() == 0 and col.max() == k - 1 and counts.min() >= 1 and counts.max() <= cap
+        star_of = [[] for _ in range(nV)]
+        for f, tri in enumerate(F):
+            for v in tri:
+                star_of[v].append(f)
+        for v in range(nV):
+            star = col[star_of[v]]
+            assert len(np.unique(star)) == len(star), (cap, v)
+        bound = max(-(-nF // cap), valence)
+        assert k >= bound
+        if fixture == "bunny_mesh.npz":
+            assert k == bound, (cap, k, bound)
+
+
 _COLOUR_CASES = ((2, 96), (3, 160), (3, 224), (4, 448))  # (icosphere level, capacity): not used above
 
 _COLOUR_CHILD = r"""
