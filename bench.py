@@ -162,33 +162,42 @@ def measure_fp32_peak(torch, dev) -> float:
     return best
 
 
-def cpu_sample(objs, threads: int, budget_s: float = 12.0):
-    """Reference CPU path (oracle, reference-mixed precision, OpenMP over field vertices) on a bounded
-    sample of the workload: (object, kind, frequency) calls in workload order until `budget_s` has
-    elapsed; returns entries/s over the calls that ran."""
+def cpu_sample(objs, threads: int, freqs_per_object: int = 3, seed: int = 29):
+    """Reference CPU path (oracle, reference-mixed precision, OpenMP over field vertices) on a bounded,
+    stratified sample of the whole workload: every object and every kind, `freqs_per_object` of the
+    object's frequencies (spread over its list: first, middle and last for three) and a seeded subset of
+    2 x threads field vertices (all of them on smaller meshes).  A stratum's (object, kind) time is
+    scaled by its row and frequency sampling fractions to estimate the CPU time of the whole step (the
+    per-entry cost of a row does not depend on the row or on the frequency); returns the workload's
+    entries / that estimate, the sample's wall time, the cores, a description and the estimate."""
     from oracle import oracle as O
 
     O.build()
     cores = O.set_threads(threads)
+    rng = np.random.default_rng(seed)
     t0 = time.perf_counter()
-    done, calls, seen = 0, 0, set()
-    for k, obj in enumerate(objs):
+    est, total, calls = 0.0, 0, 0
+    for obj in objs:
         m, mat = obj["mesh"], obj["mat"]
         s, R, L = O.cq_frequencies(obj["bdf"], obj["dt"], obj["N"])
-        for sl in s:
-            for kind in KINDS:
-                O.collocation(kind, m, mat, sl, order=obj["order"], subdiv=obj["subdiv"], mode=O.MIXED)
+        if "fsel" in obj:
+            s = s[list(obj["fsel"])]
+        nf = len(s)
+        pick = sorted(set(np.linspace(0, nf - 1, max(1, min(freqs_per_object, nf))).round().astype(int).tolist()))
+        nr = min(m.nV, 2 * cores)
+        rows = np.sort(rng.choice(m.nV, nr, replace=False)).astype(np.int32)
+        for kind in KINDS:
+            total += nf * kind_entries(kind, m.nV)
+            t1 = time.perf_counter()
+            for l in pick:
+                O.collocation(kind, m, mat, s[l], order=obj["order"], subdiv=obj["subdiv"], rows=rows, mode=O.MIXED)
                 calls += 1
-                done += kind_entries(kind, m.nV)
-                seen.add(k)
-            if time.perf_counter() - t0 > budget_s:
-                break
-        if time.perf_counter() - t0 > budget_s:
-            break
+            est += (time.perf_counter() - t1) * (m.nV / nr) * (nf / len(pick))
     dt = time.perf_counter() - t0
-    sample = (f"{calls} (object, kind, frequency) calls over the first {len(seen)} objects of the workload "
-              f"in order, {dt:.1f} s")
-    return done / dt, dt, cores, sample
+    sample = (f"stratified: all {len(objs)} objects x 4 kinds, {freqs_per_object} frequencies per object, "
+              f"{2 * cores} seeded field vertices per object (all on smaller meshes); {calls} calls in "
+              f"{dt:.1f} s; whole-step CPU time estimated from the strata at {est:.0f} s")
+    return total / est, dt, cores, sample, est
 
 
 def check_batched_rows(objs, outs, rows_per_object: int = 2, seed: int = 17) -> dict:
@@ -792,17 +801,23 @@ def run_reference(args):
         return 0
     rates = []
     for it in range(args.warmup + args.steps):
-        r, dt, cores, sample = cpu_sample(objs, threads, budget_s=10.0)
+        r, dt, cores, sample, est = cpu_sample(objs, threads)
         if it >= args.warmup:
-            rates.append((r, dt))
-    value = float(np.mean([r for r, _ in rates]))
-    ms = float(np.mean([d for _, d in rates]) * 1e3)
+            rates.append((r, dt, est))
+    value = float(np.mean([r for r, _, _ in rates]))
+    ms = float(np.mean([d for _, d, _ in rates]) * 1e3)  # the sample's wall time per step
     line = {"metric": "CQBEM Laplace-domain entries/s (mixed-size 24-object set)", "value": value,
             "unit": "entries/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "fp32+fp64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": "mixed-size 24-object collocation set (sampled on CPU)", "objects": 24},
-            "cpu_baseline": {"value": value, "unit": "entries/s", "cores": cores, "kind": "port", "sample": sample},
+            "config": {"workload": "mixed-size 24-object collocation assembly (G,H,B_trans,B_angular, all "
+                                   "Laplace frequencies); reference CPU path (oracle port, reference-mixed "
+                                   "precision, OpenMP over field vertices), stratified sample",
+                       "objects": len(objs), "vertices": [o["mesh"].nV for o in objs],
+                       "frequencies": [len(o["fsel"]) if "fsel" in o else (o["N"] + 1) // 2 + 1 for o in objs],
+                       "quadrature": "7-point (order 5), singular 5x5 FP64"},
+            "cpu_baseline": {"value": value, "unit": "entries/s", "cores": cores, "kind": "port", "sample": sample,
+                             "estimated_step_s": float(np.mean([e for _, _, e in rates]))},
             "e2e": {"value": value, "unit": "entries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -1033,9 +1048,9 @@ def run_gpu(args):
     # ---- CPU baseline (rank 0, N = 1 only) ----
     cpu = None
     if rank == 0 and world == 1 and not (args.no_cpu or args.value_only):
-        r, dtc, cores, sample = cpu_sample(objs, os.cpu_count() or 1)
+        r, dtc, cores, sample, est = cpu_sample(objs, os.cpu_count() or 1)
         cpu = {"value": r, "unit": "entries/s", "cores": cores, "kind": "port", "sample": sample,
-               "seconds": dtc}
+               "seconds": dtc, "estimated_step_s": est}
     paths = {"batched_graph": {"entries_per_s": value, "launches_per_step": launches_per_step}}
     if t_plain:
         paths["per_object_fused"] = {"entries_per_s": total_entries / t_per_object, "ms_per_step": t_per_object * 1e3}
