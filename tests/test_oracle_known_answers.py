@@ -88,6 +88,37 @@ def test_static_limit_of_single_layer(oracle):
     assert abs(gaps[0] / gaps[1] - 2.0) < 0.05 and abs(gaps[1] / gaps[2] - 2.0) < 0.05
 
 
+def test_static_limit_of_double_layer(oracle):
+    """p_hat(s) -> Kelvin p* as s -> 0 (src/elastics_bem_matrix_collection.cpp:48-50 and the static
+    H of :43-385).  Off the diagonal blocks the dynamic H, Guiggiani pass on the faces around the
+    collocation vertex included, converges to the static H quadratically in s (the O(s) terms of the
+    traction kernel cancel).  On the diagonal blocks the dynamic H plus the free term C must approach
+    the static H, whose diagonal blocks the rigid-body identity sets (minus the sum of the row's other
+    blocks): that pins the strongly singular integration and C together, converging as O(h^2)."""
+    mat = Material(1e5, 0.3, 1000.0)
+    errs = []
+    for level in (1, 2):
+        m = make_icosphere_mesh(level, 0.1)
+        n = 3 * m.nV
+        off = np.ones((n, n), dtype=bool)
+        for i in range(m.nV):
+            off[3 * i:3 * i + 3, 3 * i:3 * i + 3] = False
+        Hs = oracle.elastostatic("H", m, mat, galerkin=False)
+        if level == 1:
+            gaps = []
+            for s in (1.6e-2, 8e-3, 4e-3):
+                Hd = oracle.collocation("H", m, mat, s)
+                gaps.append(np.linalg.norm((Hd.real - Hs)[off]) / np.linalg.norm(Hs[off]))
+            assert gaps[-1] < 1e-8
+            assert abs(gaps[0] / gaps[1] - 4.0) < 0.1 and abs(gaps[1] / gaps[2] - 4.0) < 0.1
+        Hd = oracle.collocation("H", m, mat, 2e-3).real
+        Cb = np.asarray(oracle.c_matrix_collocation(m, 0.3)).reshape(m.nV, 3, 3)
+        for i in range(m.nV):
+            Hd[3 * i:3 * i + 3, 3 * i:3 * i + 3] += Cb[i]
+        errs.append(np.linalg.norm((Hd - Hs)[~off]) / np.linalg.norm(Hs[~off]))
+    assert errs[1] < 5e-5 and errs[0] / errs[1] > 3.0, errs
+
+
 def test_galerkin_single_layer_symmetric(oracle):
     m = make_icosphere_mesh(1, 0.1)
     mat = Material(1e5, 0.3, 1000.0)
