@@ -119,6 +119,35 @@ def test_static_limit_of_double_layer(oracle):
     assert errs[1] < 5e-5 and errs[0] / errs[1] > 3.0, errs
 
 
+def test_galerkin_static_limits(oracle):
+    """The Galerkin forms (src/elastodynamics_cqbem_*_galerkin_non_singular.cu and the Sauter-Schwab
+    pairs of src/elastodynamics_cqbem_galerkin_singular.cpp) against the static Galerkin G and H
+    (src/elastics_bem_matrix_collection.cpp:43-385): G converges linearly in s, H plus the Galerkin
+    mass matrix quadratically off the diagonal blocks; on them the static H is set by the rigid-body
+    identity, and the directly integrated coincident pairs approach it as the singular order rises."""
+    m = make_icosphere_mesh(1, 0.1)
+    mat = Material(1e5, 0.3, 1000.0)
+    n = 3 * m.nV
+    off = np.ones((n, n), dtype=bool)
+    for i in range(m.nV):
+        off[3 * i:3 * i + 3, 3 * i:3 * i + 3] = False
+    Gs = oracle.elastostatic("G", m, mat, galerkin=True, order=4, sorder=4)
+    g = [np.linalg.norm(oracle.galerkin("G", m, mat, s, order=4, sorder=4).real - Gs) / np.linalg.norm(Gs)
+         for s in (1.6e-2, 8e-3, 4e-3)]
+    assert g[-1] < 1e-4 and abs(g[0] / g[1] - 2.0) < 0.05 and abs(g[1] / g[2] - 2.0) < 0.05, g
+    M = oracle.c_matrix_galerkin(m)
+    Hs = oracle.elastostatic("H", m, mat, galerkin=True, order=4, sorder=4)
+    h = [np.linalg.norm((oracle.galerkin("H", m, mat, s, order=4, sorder=4).real + M - Hs)[off])
+         / np.linalg.norm(Hs[off]) for s in (1.6e-2, 8e-3, 4e-3)]
+    assert h[-1] < 1e-8 and abs(h[0] / h[1] - 4.0) < 0.1 and abs(h[1] / h[2] - 4.0) < 0.1, h
+    d = []
+    for so in (2, 3, 4):
+        Hs = oracle.elastostatic("H", m, mat, galerkin=True, order=4, sorder=so)
+        Hd = oracle.galerkin("H", m, mat, 2e-3, order=4, sorder=so).real + M
+        d.append(np.linalg.norm((Hd - Hs)[~off]) / np.linalg.norm(Hs[~off]))
+    assert d[0] > 10 * d[1] > 100 * d[2] and d[2] < 5e-5, d
+
+
 def test_galerkin_single_layer_symmetric(oracle):
     m = make_icosphere_mesh(1, 0.1)
     mat = Material(1e5, 0.3, 1000.0)
