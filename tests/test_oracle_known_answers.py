@@ -148,6 +148,70 @@ def test_galerkin_static_limits(oracle):
     assert d[0] > 10 * d[1] > 100 * d[2] and d[2] < 5e-5, d
 
 
+def _ball_moments(x, a, s, mat, n=40):
+    """Moments of the dynamic Kelvin tensor over the ball |y| <= a seen from x on its surface:
+    I0[p, j] = int U_pj(x, y) dV_y and I1[p, j, k] = int U_pj(x, y) (y - x)_k dV_y, in spherical
+    coordinates about x (radius t up to the chord 2 a cos(theta) of direction theta from the
+    inward normal; t^2 U is smooth), Gauss-Legendre in t and theta, trapezoid in phi."""
+    c1, c2, rho = mat.c1, mat.c2, mat.rho
+    w = -x / np.linalg.norm(x)
+    e1 = np.cross(w, [1.0, 0.0, 0.0] if abs(w[0]) < 0.9 else [0.0, 1.0, 0.0])
+    e1 /= np.linalg.norm(e1)
+    e2 = np.cross(w, e1)
+    gx, gw = np.polynomial.legendre.leggauss(n)
+    th, thw = (gx + 1) * np.pi / 4, gw * np.pi / 4
+    ph = np.arange(2 * n) * np.pi / n
+    T, P = np.meshgrid(th, ph, indexing="ij")
+    d = (np.sin(T) * np.cos(P))[..., None] * e1 + (np.sin(T) * np.sin(P))[..., None] * e2 + np.cos(T)[..., None] * w
+    R = 2 * a * np.cos(T)
+    t = (gx + 1)[None, None, :] * R[..., None] / 2  # [theta, phi, t]
+    wt = gw[None, None, :] * R[..., None] / 2
+    z1, z2 = t * s / c1, t * s / c2
+    e1s, e2s = np.exp(-z1), np.exp(-z2)
+    psi = lambda z: ((1 + z) * np.exp(-z) - 1) / (z * z)
+    Y = psi(z1) / c1 ** 2 - psi(z2) / c2 ** 2
+    al = (3 * Y + e1s / c1 ** 2 - e2s / c2 ** 2) / (4 * np.pi * rho * t)
+    be = (e2s / c2 ** 2 - Y) / (4 * np.pi * rho * t)
+    ang = (np.sin(T) * thw[:, None] * (np.pi / n))[..., None]
+    k0, k1 = wt * t ** 2 * ang, wt * t ** 3 * ang
+    dd = d[..., :, None] * d[..., None, :]
+    eye = np.eye(3)
+    I0 = np.einsum("abk,abij->ij", k0 * al, dd) + np.einsum("abk->", k0 * be) * eye
+    I1 = (np.einsum("abk,abij,abl->ijl", k1 * al, dd, d)
+          + np.einsum("abk,abl->l", k1 * be, d)[None, None, :] * eye[:, :, None])
+    return I0, I1
+
+
+def test_b_kernels_are_body_force_integrals(oracle):
+    """B_trans and B_angular are the boundary forms of the body-force integrals of a rigidly
+    accelerating frame (src/elastodynamics_cqbem_B_{trans,angular}_collocation.cu): for a field
+    vertex x on a sphere,
+        B_trans[x]_pj          = -rho int_Omega U_pj(x, y) dV_y
+        B_angular[x]_p,(3j+k)  = -rho int_Omega U_pj(x, y) (y - x)_k dV_y
+    with U the dynamic Kelvin tensor.  The icosphere is a polyhedron inscribed in the ball, so the
+    gap closes as O(h^2): about 4x per subdivision level."""
+    a = 0.1
+    mat = Material(1e5, 0.3, 1000.0)
+    errs = {}
+    for level in (3, 4):
+        m = make_icosphere_mesh(level, a)
+        for s in (40 + 25j, 150 - 60j):
+            rows = np.array([0, 7], dtype=np.int32)
+            Bt = oracle.collocation("B_trans", m, mat, s, rows=rows)
+            Ba = oracle.collocation("B_angular", m, mat, s, rows=rows)
+            for r, i in enumerate(rows):
+                I0, I1 = _ball_moments(m.V[i], a, s, mat)
+                bt, ba = Bt[3 * r:3 * r + 3], Ba[3 * r:3 * r + 3]
+                errs[(level, s, int(i), "t")] = np.linalg.norm(bt + mat.rho * I0) / np.linalg.norm(bt)
+                errs[(level, s, int(i), "a")] = np.linalg.norm(ba + mat.rho * I1.reshape(3, 9)) / np.linalg.norm(ba)
+    for key, e4 in errs.items():
+        if key[0] != 4:
+            continue
+        e3 = errs[(3,) + key[1:]]
+        assert e4 < 4e-3, (key, e4)
+        assert 3.0 < e3 / e4 < 5.0, (key, e3, e4)
+
+
 def test_galerkin_single_layer_symmetric(oracle):
     m = make_icosphere_mesh(1, 0.1)
     mat = Material(1e5, 0.3, 1000.0)
