@@ -9,7 +9,9 @@
  * golden vectors, and cannot be compiled here (its Eigen and libigl submodules are empty and
  * there is no network).  This file restates the reference's algorithms in plain C++ so that
  * they can be checked by known-answer tests (quadrature exactness, closed-form CQ weights,
- * static limits, symmetries, rigid-mode null spaces) instead.
+ * static Kelvin limits of G and H, collocation and Galerkin; the rigid-body identity of H's
+ * diagonal with the free term; B_trans and B_angular as the body-force volume integrals of the
+ * Kelvin tensor; symmetries, rigid-mode null spaces) instead.
  *
  * Precision modes:
  *   mode 0  FP64 everywhere, kernels in their cancellation-free form (the reference's formulas
