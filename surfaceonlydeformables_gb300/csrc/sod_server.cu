@@ -193,7 +193,9 @@ void slot_main(sod_server *s, sod_server::Slot *sl) {
             cudaEventCreateWithFlags(&d.packed, cudaEventDisableTiming);
             cudaEventRecord(d.packed, s->step_ctx->stream);
         }
-        if (tmp) cudaFreeAsync(tmp, rc == SOD_OK ? s->step_ctx->stream : sl->ctx->stream);
+        // once a bank exists its weight copies (on the step stream) read tmp, also when a later copy
+        // failed: free it behind them; otherwise behind the precompute on the slot's stream
+        if (tmp) cudaFreeAsync(tmp, d.bank ? s->step_ctx->stream : sl->ctx->stream);
         if (mesh) sod_mesh_destroy(mesh);
         if (rc != SOD_OK && d.bank) {
             sod_history_destroy(d.bank);
