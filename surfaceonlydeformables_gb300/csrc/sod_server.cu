@@ -280,6 +280,10 @@ void scheduler_main(sod_server *s) {
             } else {
                 auto it = s->objects.find(r->object);
                 if (it != s->objects.end()) {
+                    if ((int)r->p.size() != it->second->n) {
+                        complete(s, r, SOD_ERR_INVALID_ARG);  // p, u must have the object's 3V entries
+                        continue;
+                    }
                     it->second->steps.push_back(r);
                     it->second->pending++;
                 } else if (s->assembling.count(r->object)) {
@@ -320,7 +324,12 @@ void scheduler_main(sod_server *s) {
             o->last_use = Clock::now();
             auto e = s->early.find(r->id);
             if (e != s->early.end()) {
-                o->steps = std::move(e->second);
+                for (Request *q : e->second) {
+                    if ((int)q->p.size() == o->n)
+                        o->steps.push_back(q);
+                    else
+                        complete(s, q, SOD_ERR_INVALID_ARG);  // length other than the object's 3V
+                }
                 o->pending = (int)o->steps.size();
                 s->early.erase(e);
             }
@@ -474,14 +483,9 @@ void scheduler_main(sod_server *s) {
 
 extern "C" {
 
-int sod_server_create(int device, int64_t hbm_cap_bytes, int slots, int max_vertices, sod_server **out) {
-    SOD_REQUIRE(out, "null output pointer");
-    SOD_REQUIRE(hbm_cap_bytes > 0 && slots >= 1 && slots <= 8 && max_vertices >= 3,
-                "need a positive HBM cap, 1..8 assembly slots and max_vertices >= 3");
-    auto s = std::make_unique<sod_server>();
-    s->device = device;
-    s->cap = hbm_cap_bytes;
-    s->vmax_n = 3 * max_vertices;
+// The server's device resources: the step context on the highest-priority stream, the staging
+// ring and one context per assembly slot.  On failure the caller tears down what was made.
+static int server_alloc(sod_server *s, int device, int slots) {
     SOD_TRY(sod_context_create(device, &s->step_ctx));
     {
         // time steps run on the device's highest-priority stream: the block scheduler hands them SMs
@@ -491,8 +495,9 @@ int sod_server_create(int device, int64_t hbm_cap_bytes, int slots, int max_vert
         SOD_CHECK_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
         cudaStream_t hs = nullptr;
         SOD_CHECK_CUDA(cudaStreamCreateWithPriority(&hs, cudaStreamNonBlocking, hi));
-        SOD_CHECK_CUDA(cudaStreamDestroy(s->step_ctx->own_stream));
+        const cudaError_t e = cudaStreamDestroy(s->step_ctx->own_stream);
         s->step_ctx->own_stream = s->step_ctx->stream = hs;
+        SOD_CHECK_CUDA(e);
     }
     constexpr int RING = 6;  // groups in flight
     s->ring.resize(RING);
@@ -505,9 +510,24 @@ int sod_server_create(int device, int64_t hbm_cap_bytes, int slots, int max_vert
         s->free_ring.push_back(k);
     }
     for (int k = 0; k < slots; k++) {
-        auto sl = std::make_unique<sod_server::Slot>();
-        SOD_TRY(sod_context_create(device, &sl->ctx));
-        s->slots.push_back(std::move(sl));
+        s->slots.push_back(std::make_unique<sod_server::Slot>());
+        SOD_TRY(sod_context_create(device, &s->slots.back()->ctx));
+    }
+    return SOD_OK;
+}
+
+int sod_server_create(int device, int64_t hbm_cap_bytes, int slots, int max_vertices, sod_server **out) {
+    SOD_REQUIRE(out, "null output pointer");
+    SOD_REQUIRE(hbm_cap_bytes > 0 && slots >= 1 && slots <= 8 && max_vertices >= 3,
+                "need a positive HBM cap, 1..8 assembly slots and max_vertices >= 3");
+    auto s = std::make_unique<sod_server>();
+    s->device = device;
+    s->cap = hbm_cap_bytes;
+    s->vmax_n = 3 * max_vertices;
+    const int rc = server_alloc(s.get(), device, slots);
+    if (rc != SOD_OK) {  // no thread runs yet: the teardown frees whatever was made
+        sod_server_destroy(s.release());
+        return rc;
     }
     sod_server *raw = s.release();
     for (auto &sl : raw->slots) sl->th = std::thread(slot_main, raw, sl.get());
@@ -633,11 +653,11 @@ int sod_server_destroy(sod_server *s) {
     s->jan_cv.notify_all();
     if (s->janitor.joinable()) s->janitor.join();
     cudaSetDevice(s->device);
-    cudaStreamSynchronize(s->step_ctx->stream);
-    for (auto &st : s->ring) {
-        cudaFreeHost(st.hbuf);
-        cudaFree(st.dbuf);
-        cudaEventDestroy(st.ev);
+    if (s->step_ctx) cudaStreamSynchronize(s->step_ctx->stream);
+    for (auto &st : s->ring) {  // also a partly made server (sod_server_create's failure path)
+        if (st.hbuf) cudaFreeHost(st.hbuf);
+        if (st.dbuf) cudaFree(st.dbuf);
+        if (st.ev) cudaEventDestroy(st.ev);
     }
     for (auto &sl : s->slots) sod_context_destroy(sl->ctx);
     sod_context_destroy(s->step_ctx);

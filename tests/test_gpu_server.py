@@ -99,4 +99,11 @@ def test_server_capacity_and_eviction(gpu_ctx):
     srv.drain(60)
     st = {i: code for i, code, _ in srv.poll()}
     assert st[a] == 0 and st[b] == 0 and st[s] == L.SOD_ERR_INVALID_ARG
+    # a step whose vectors are not the object's 3V long is rejected on the host; the object still steps
+    bad = srv.submit_step(b, np.ones(n - 3), np.zeros(n - 3))
+    good = srv.submit_step(b, np.ones(n), np.zeros(n))
+    srv.drain(60)
+    st = {i: code for i, code, _ in srv.poll()}
+    assert st[bad] == L.SOD_ERR_INVALID_ARG and st[good] == 0
+    assert srv.result(good).shape == (n,)
     srv.close()
