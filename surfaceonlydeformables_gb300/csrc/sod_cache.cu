@@ -79,6 +79,7 @@ int sod_mat_write(sod_context *ctx, const char *path, const void *data, int64_t 
 
 int sod_mat_read(sod_context *ctx, const char *path, void *data, int64_t rows, int64_t cols) {
     SOD_REQUIRE(path && data, "null argument");
+    SOD_REQUIRE(rows >= 0 && cols >= 0, "negative matrix size");
     if (ctx) SOD_CHECK_CUDA(cudaSetDevice(ctx->device));
     FILE *f = fopen(path, "rb");
     if (!f) {
@@ -103,9 +104,11 @@ int sod_mat_read(sod_context *ctx, const char *path, void *data, int64_t rows, i
             return SOD_ERR_INVALID_ARG;
         }
         if (dev) {
-            SOD_CHECK_CUDA(cudaMemcpyAsync(static_cast<double *>(data) + e0, buf.data(), ne * 8, cudaMemcpyHostToDevice,
-                                           ctx->stream));
-            SOD_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+            cudaError_t e = cudaMemcpyAsync(static_cast<double *>(data) + e0, buf.data(), ne * 8,
+                                            cudaMemcpyHostToDevice, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            if (e != cudaSuccess) fclose(f);
+            SOD_CHECK_CUDA(e);
         }
     }
     fclose(f);

@@ -86,6 +86,18 @@ def test_mat_file_format_roundtrip(sodlib, tmp_path):
     assert np.array_equal(api.mat_read(None, p, 7, 5), M.astype(np.float32).astype(np.float64))
     with pytest.raises(sodlib.SodError):
         api.mat_read(None, p, 5, 7)  # wrong dimensions are rejected
+    # a file whose header claims negative sizes, and one cut short, are rejected as well
+    lib = sodlib.load()
+    out = np.empty(35)
+    neg = str(tmp_path / "neg.mat")
+    with open(neg, "wb") as fh:
+        fh.write(np.array([-7, -5], dtype=np.int64).tobytes() + np.zeros(35).tobytes())
+    assert lib.sod_mat_read(None, neg.encode(), sodlib.ptr(out), -7, -5) == sodlib.SOD_ERR_INVALID_ARG
+    cut = str(tmp_path / "cut.mat")
+    with open(cut, "wb") as fh:
+        fh.write(raw[:16 + 8 * 20])
+    assert lib.sod_mat_read(None, cut.encode(), sodlib.ptr(out), 7, 5) == sodlib.SOD_ERR_INVALID_ARG
+    assert b"truncated" in lib.sod_last_error()
 
 
 @pytest.mark.parametrize("level,axes", [(2, (1.0, 1.0, 1.0)), (3, (1.4, 0.8, 1.1)), (4, (1.0, 1.0, 1.0)),
