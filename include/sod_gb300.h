@@ -112,7 +112,8 @@ int64_t sod_context_launch_count(const sod_context *ctx);
 /* ---- mesh: device-resident geometry + precomputed topology -------------------------------- */
 /* Uploads V, F (and N, or computes unit face normals), builds vertex stars, face colourings for
  * the deterministic scatter, and the singular-pair lists.  vmap: vertex_map_inverse of the
- * reference (NULL when traction discontinuity is off). */
+ * reference (NULL when traction discontinuity is off), nV entries in [0, nV).  Face indices outside
+ * [0, nV), non-finite coordinates and zero-area faces are rejected with SOD_ERR_INVALID_ARG. */
 int sod_mesh_create(sod_context *ctx, const double *V, int nV, const int *F, int nF, const double *N,
                     const int *vmap, sod_mesh **mesh);
 int sod_mesh_destroy(sod_mesh *mesh);

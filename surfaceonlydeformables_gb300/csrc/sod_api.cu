@@ -657,7 +657,8 @@ int sod_mesh_create(sod_context *ctx, const double *V, int nV, const int *F, int
     m->has_vmap = vmap != nullptr;
     if (vmap) {
         m->vmap.assign(vmap, vmap + nV);
-        for (int v = 0; v < nV; v++) SOD_REQUIRE(m->vmap[v] >= 0, "negative vertex_map_inverse entry");
+        for (int v = 0; v < nV; v++)
+            SOD_REQUIRE(m->vmap[v] >= 0 && m->vmap[v] < nV, "vertex_map_inverse entry outside [0, nV)");
     }
     auto canon = [&](int v) { return m->has_vmap ? m->vmap[v] : v; };
     // stars: for vertex i, the faces with a corner whose canonical id equals canon(i); singular
