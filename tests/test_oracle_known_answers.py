@@ -212,6 +212,25 @@ def test_b_kernels_are_body_force_integrals(oracle):
         assert 3.0 < e3 / e4 < 5.0, (key, e3, e4)
 
 
+def test_galerkin_b_is_mass_matrix_times_collocation_b(oracle):
+    """B_trans and B_angular are smooth in the field point, so the Galerkin rows (test functions
+    phi_i, src/elastodynamics_cqbem_B_*_galerkin_non_singular.cu and the singular pairs) approach the
+    P1 mass matrix times the collocation rows, M = int phi_i phi_j = 2 x the Galerkin free-term matrix,
+    as O(h^2); with the collocation B tied to the body-force integrals, this pins the Galerkin B."""
+    mat = Material(1e5, 0.3, 1000.0)
+    s = 40 + 25j
+    err = {}
+    for level in (1, 2):
+        m = make_icosphere_mesh(level, 0.1)
+        M = 2 * oracle.c_matrix_galerkin(m)
+        for kind in ("B_trans", "B_angular"):
+            Bg = oracle.galerkin(kind, m, mat, s, order=4, sorder=4)
+            Bc = oracle.collocation(kind, m, mat, s)
+            err[(level, kind)] = np.linalg.norm(Bg - M @ Bc) / np.linalg.norm(Bg)
+    for kind in ("B_trans", "B_angular"):
+        assert err[(2, kind)] < 2.5e-2 and err[(1, kind)] / err[(2, kind)] > 3.0, err
+
+
 def test_galerkin_single_layer_symmetric(oracle):
     m = make_icosphere_mesh(1, 0.1)
     mat = Material(1e5, 0.3, 1000.0)
