@@ -11,7 +11,8 @@
  * they can be checked by known-answer tests (quadrature exactness, closed-form CQ weights,
  * static Kelvin limits of G and H, collocation and Galerkin; the rigid-body identity of H's
  * diagonal with the free term; B_trans and B_angular as the body-force volume integrals of the
- * Kelvin tensor; symmetries, rigid-mode null spaces) instead.
+ * Kelvin tensor, and Galerkin B as the mass matrix times collocation B; symmetries, rigid-mode
+ * null spaces) instead.
  *
  * Precision modes:
  *   mode 0  FP64 everywhere, kernels in their cancellation-free form (the reference's formulas
